@@ -1,0 +1,425 @@
+#!/usr/bin/env python
+"""Benchmark of the exact-GP hot path: conjugate MLL + gradient evaluations per
+second at n = 16384, d = 8, Matern-5/2 ARD (X ~ N(0, I_8), lengthscales
+log-uniform in [0.3, 3], variance 1, noise 1e-2, y drawn from the prior plus
+noise in float64), mixed-precision form against the plain FP64 form.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+One step = one conjugate_mll value + gradient (lengthscales, variance,
+obs_stddev, constant mean) over the whole synthetic dataset.  The exact GP
+does not shard, so N > 1 runs N independent replicas (one per rank, weak
+scaling).  Prints one JSON line on rank 0.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MLL+grad evals/s at n=16k: mixed vs FP64 form on one GB300 @ rel err ≤1e-6"
+WORKLOAD = ("exact GP conjugate_mll + gradient, Matern-5/2 ARD, n=16384, d=8, X~N(0,I8), "
+            "lengthscales log-U[0.3,3], variance 1, noise 1e-2, y = prior sample + noise")
+PEAK_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
+# dram__bytes_read.sum + dram__bytes_write.sum of one adjoint (lauum_grad) launch,
+# from the ncu capture summarised in profiles/ (scaled to n = 16384); None until captured.
+ADJOINT_TRAFFIC_BYTES_N16384 = None
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    p.add_argument("--n", type=int, default=16384)
+    p.add_argument("--d", type=int, default=8)
+    p.add_argument("--fp64-steps", type=int, default=2)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--seed", type=int, default=0)
+    return p.parse_args()
+
+
+def c2_inputs(n, d, seed):
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal((n, d))
+    ls = np.exp(rng.uniform(np.log(0.3), np.log(3.0), d))
+    eps = rng.standard_normal(n)
+    return x, ls, eps
+
+
+def c2_y_device(x, ls, eps, device):
+    """y = chol(K + (1e-6 + 1e-2) I) eps in float64 on the GPU (data generation,
+    through the library's own float64 Gram and Cholesky)."""
+    import torch
+
+    import gpjax_gb300 as gpx
+    X = torch.as_tensor(x, device=device)
+    kern = gpx.kernels.Matern52(lengthscale=ls, variance=1.0)
+    K = kern.gram(X).to_dense()
+    K.diagonal().add_(1e-6 + 1e-2)
+    L, info = gpx.linalg.cholesky_dense(K)
+    del K
+    assert int(info.item()) == 0
+    y = L @ torch.as_tensor(eps, device=device)
+    del L
+    torch.cuda.empty_cache()
+    return y
+
+
+def c2_y_host(x, ls, eps):
+    import scipy.linalg as sla
+    from oracle import gp_oracle as O
+    S = O.gram(O.MATERN52, x, ls, 1.0) + (1e-6 + 1e-2) * np.eye(len(x))
+    return sla.cholesky(S, lower=True) @ eps
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [v.strip() for v in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return json.load(f), "measured"
+    except (OSError, ValueError):
+        return PEAK_FALLBACK, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# CPU leg: the float64 oracle (the reference's op sequence) on the host cores
+# ---------------------------------------------------------------------------
+def cpu_mll_grad_time(n, d, seed, threads):
+    """Seconds for one MLL + gradient of the oracle at size n (LU value and
+    torch float64 autograd gradient, the reference's slogdet/solve path)."""
+    import torch
+    from oracle import gp_oracle as O
+    torch.set_num_threads(threads)
+    x, ls, eps = c2_inputs(n, d, seed)
+    y = c2_y_host(x, ls, eps)
+    t0 = time.perf_counter()
+    O.conjugate_mll_torch(O.MATERN52, x, y[:, None], ls, 1.0, 0.1, 0.0, lu=True)
+    return time.perf_counter() - t0
+
+
+def pick_cpu_sample(n_full, d, seed, threads, budget_s):
+    t_small = cpu_mll_grad_time(1024, d, seed, threads)
+    n_s = 1024
+    for cand in (2048, 3072, 4096, 6144, 8192, 12288, 16384):
+        if cand > n_full:
+            break
+        if t_small * (cand / 1024.0) ** 3 <= budget_s:
+            n_s = cand
+    return n_s
+
+
+def cpu_baseline(n_full, d, seed, budget_s=20.0):
+    threads = os.cpu_count() or 1
+    n_s = pick_cpu_sample(n_full, d, seed, threads, budget_s)
+    t = cpu_mll_grad_time(n_s, d, seed, threads)
+    scale = (n_s / n_full) ** 3
+    return {"value": scale / t, "unit": "evals/s", "cores": threads, "kind": "port",
+            "sample": (f"one float64 MLL+grad of the oracle port (LU slogdet/solve value, torch "
+                       f"float64 autograd gradient) at n={n_s} on the same generator, "
+                       f"{t:.2f} s, scaled by (n/{n_full})^3 to n={n_full}")}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    budget = max(2.0, 150.0 / max(1, args.steps + args.warmup))
+    n_s = pick_cpu_sample(args.n, args.d, args.seed, threads, budget)
+    times = []
+    for i in range(args.warmup + args.steps):
+        t = cpu_mll_grad_time(n_s, args.d, args.seed, threads)
+        if i >= args.warmup:
+            times.append(t)
+    tot = sum(times)
+    scale = (n_s / args.n) ** 3
+    value = scale * args.steps / tot
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "evals/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * tot / args.steps / scale, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n": args.n, "d": args.d, "kernel": "Matern52",
+                   "parallelism": "replicas"},
+        "cpu_baseline": {"value": value, "unit": "evals/s", "cores": threads, "kind": "port",
+                         "sample": (f"each step: one float64 MLL+grad of the oracle port at "
+                                    f"n={n_s} (LU slogdet/solve value, torch float64 autograd "
+                                    f"gradient), scaled by (n/{args.n})^3")},
+        "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU leg
+# ---------------------------------------------------------------------------
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+
+    import gpjax_gb300 as gpx
+    from gpjax_gb300 import _lib
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    lib = _lib.lib()
+    n, d = args.n, args.d
+
+    # CPU baseline first (rank 0 at N = 1), before any process pool or GPU work
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(n, d, args.seed)
+
+    x, ls, eps = c2_inputs(n, d, args.seed)
+    X = torch.as_tensor(x, device=dev)
+    y = c2_y_device(x, ls, eps, dev)
+    theta = torch.tensor(list(ls) + [1.0, 0.1, 0.0], dtype=torch.float64, device=dev)
+    out = torch.zeros(1, dtype=torch.float64, device=dev)
+    grad = torch.zeros(d + 3, dtype=torch.float64, device=dev)
+    info = torch.zeros(1, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def make_ws(prec):
+        return _lib.workspace(lib.gpk_conjugate_mll_workspace_bytes(n, d, prec), dev)
+
+    def step(prec, ws):
+        _lib.call("gpk_conjugate_mll", _lib.MATERN52, n, d, X.data_ptr(), d, y.data_ptr(),
+                  theta.data_ptr(), d, 1e-6, prec, 1, out.data_ptr(), grad.data_ptr(),
+                  info.data_ptr(), ws.data_ptr(), ws.numel(), stream.cuda_stream)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    def max_over_ranks(v):
+        if world == 1:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- plain FP64 form (reference precision) ----
+    fp64 = None
+    mll64 = g64 = None
+    if args.fp64_steps > 0:
+        ws64 = make_ws(_lib.PREC_FP64)
+        step(_lib.PREC_FP64, ws64)
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.fp64_steps):
+            step(_lib.PREC_FP64, ws64)
+        e1.record(stream)
+        barrier()
+        t64 = max_over_ranks(e0.elapsed_time(e1) / 1000.0)
+        mll64, g64 = float(out.item()), grad.cpu().numpy().copy()
+        fp64 = {"evals_per_s": world * args.fp64_steps / t64,
+                "ms_per_step": 1000.0 * t64 / args.fp64_steps, "steps": args.fp64_steps}
+        del ws64
+        torch.cuda.empty_cache()
+
+    # ---- mixed form, device-resident inputs (value) ----
+    ws = make_ws(_lib.PREC_MIXED)
+    for _ in range(args.warmup):
+        step(_lib.PREC_MIXED, ws)
+    barrier()
+    nph = 7
+    ph = [[torch.cuda.Event(enable_timing=True) for _ in range(nph)] for _ in range(args.steps)]
+    ev_arrays = [ctypes_void_array(nph) for _ in range(args.steps)]
+    for s in range(args.steps):
+        for k in range(nph):
+            ph[s][k].record(stream)  # torch creates the CUDA event on first record
+            ev_arrays[s][k] = ph[s][k].cuda_event
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = lib.gpk_launch_count()
+    with ClockSampler(local) as clk:
+        barrier()
+        e0.record(stream)
+        for s in range(args.steps):
+            lib.gpk_set_profile_events(ev_arrays[s], nph)
+            step(_lib.PREC_MIXED, ws)
+        e1.record(stream)
+        barrier()
+    lib.gpk_set_profile_events(None, 0)
+    launches = lib.gpk_launch_count() - launches0
+    t_dev = max_over_ranks(e0.elapsed_time(e1) / 1000.0)
+    mll_mixed, g_mixed = float(out.item()), grad.cpu().numpy().copy()
+    phase_names = ["gram", "cholesky", "trtri", "solve_refine", "adjoint", "finalize"]
+    phases = {nm: float(np.mean([ph[s][k].elapsed_time(ph[s][k + 1]) for s in range(args.steps)]))
+              for k, nm in enumerate(phase_names)}
+
+    # ---- e2e through the public API with host buffers ----
+    Xh = torch.as_tensor(x).pin_memory()
+    yh = y.cpu().pin_memory()
+    kern = gpx.kernels.Matern52(lengthscale=ls, variance=1.0)
+    post = gpx.gps.Prior(kernel=kern) * gpx.likelihoods.Gaussian(n, obs_stddev=0.1)
+    for p in (kern.lengthscale, kern.variance, post.likelihood.obs_stddev):
+        p.to(dev).requires_grad_(True)
+
+    def e2e_step():
+        Xd = Xh.to(dev, non_blocking=True)
+        yd = yh.to(dev, non_blocking=True)
+        data = gpx.Dataset(X=Xd, y=yd, device=dev)
+        for p in (kern.lengthscale, kern.variance, post.likelihood.obs_stddev):
+            p.value.grad = None
+        val = gpx.objectives.conjugate_mll(post, data, precision="mixed")
+        val.backward()
+        res = torch.cat([val.detach().reshape(1), kern.lengthscale.value.grad,
+                         kern.variance.value.grad.reshape(1),
+                         post.likelihood.obs_stddev.value.grad.reshape(1)])
+        return res.cpu()
+
+    for _ in range(2):
+        e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r = e2e_step()
+    barrier()
+    t_e2e = max_over_ranks(time.perf_counter() - t0)
+    h2d = Xh.numel() * 8 + yh.numel() * 8
+    d2h = r.numel() * 8
+
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+
+    peaks, peak_kind = measured_peaks()
+    flops_adjoint = n ** 3 / 3.0  # W = V V^T over the lower triangle
+    t_adj = phases["adjoint"] / 1000.0
+    achieved = flops_adjoint / t_adj / 1e12
+    peak = float(peaks.get("bf16_tflops", PEAK_FALLBACK["bf16_tflops"]))
+    rel_mll = abs(mll_mixed - mll64) / abs(mll64) if mll64 is not None else None
+    rel_grad = (float(np.linalg.norm(g_mixed - g64) / np.linalg.norm(g64))
+                if g64 is not None else None)
+    grad_comp = ({"names": [f"lengthscale[{k}]" for k in range(d)] +
+                  ["variance", "obs_stddev", "constant"],
+                  "fp64": [float(v) for v in g64],
+                  "rel_err": [float(abs(a - b) / max(abs(b), 1e-300))
+                              for a, b in zip(g_mixed, g64)]}
+                 if g64 is not None else None)
+    value = world * args.steps / t_dev
+    line = {
+        "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 Gram + f32/tf32x3 factor + f64 refinement/accumulation",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n": n, "d": d, "kernel": "Matern52",
+                   "precision": "mixed", "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "working set (3 x n^2 float32 = 3.2 GB) larger than L2; no flush"},
+        "roofline": {"bound": "tensor", "kernel": "lauum_grad (fused inverse product + adjoint)",
+                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "peak_kind": f"{peak_kind} bf16 dense",
+                     "traffic": ADJOINT_TRAFFIC_BYTES_N16384,
+                     "algorithmic_flops_per_launch": flops_adjoint},
+        "phases_ms": phases,
+        "fp64_form": fp64,
+        "speedup_vs_fp64": (value / fp64["evals_per_s"]) if fp64 else None,
+        "rel_err_mll_vs_fp64": rel_mll, "rel_err_grad_vs_fp64": rel_grad,
+        "grad_components": grad_comp,
+        "mll": mll_mixed,
+        "e2e": {"value": world * args.steps / t_e2e, "unit": "evals/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "path": "gpjax_gb300.objectives.conjugate_mll(...).backward() from pinned host X, y"},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def ctypes_void_array(k):
+    import ctypes
+    return (ctypes.c_void_p * k)()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

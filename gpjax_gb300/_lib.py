@@ -1,0 +1,118 @@
+"""ctypes binding of the C ABI declared in include/gpk.h.
+
+The shared library is loaded from the package directory.  There is no
+fallback: every computation in this package runs through libgpk.so on a CUDA
+device, and a missing library or device raises immediately.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import torch
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libgpk.so")
+
+# enums (include/gpk.h)
+RBF, MATERN32, MATERN52 = 0, 1, 2
+F64, F32 = 0, 1
+PREC_FP64, PREC_MIXED = 0, 1
+
+_c_i64 = ctypes.c_int64
+_c_int = ctypes.c_int
+_c_dbl = ctypes.c_double
+_c_ptr = ctypes.c_void_p
+_c_size = ctypes.c_size_t
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "gpk_version": (_c_int, []),
+    "gpk_status_string": (ctypes.c_char_p, [_c_int]),
+    "gpk_launch_count": (ctypes.c_longlong, []),
+    "gpk_set_profile_events": (None, [ctypes.POINTER(ctypes.c_void_p), _c_int]),
+    "gpk_cross_covariance": (_c_int, [_c_int, _c_i64, _c_i64, _c_int, _c_ptr, _c_i64, _c_ptr,
+                                      _c_i64, _c_ptr, _c_int, _c_int, _c_ptr, _c_i64, _c_ptr]),
+    "gpk_gram": (_c_int, [_c_int, _c_i64, _c_int, _c_ptr, _c_i64, _c_ptr, _c_int, _c_int, _c_ptr,
+                          _c_i64, _c_ptr]),
+    "gpk_diagonal": (_c_int, [_c_int, _c_i64, _c_int, _c_ptr, _c_i64, _c_ptr, _c_int, _c_ptr,
+                              _c_ptr]),
+    "gpk_lower_cholesky": (_c_int, [_c_i64, _c_int, _c_ptr, _c_i64, _c_ptr, _c_ptr, _c_ptr]),
+    "gpk_solve_triangular_workspace_bytes": (_c_size, [_c_i64, _c_i64, _c_int]),
+    "gpk_solve_triangular": (_c_int, [_c_i64, _c_i64, _c_int, _c_ptr, _c_i64, _c_ptr, _c_i64,
+                                      _c_ptr, _c_size, _c_ptr]),
+    "gpk_logdet_triangular": (_c_int, [_c_i64, _c_int, _c_ptr, _c_i64, _c_ptr, _c_ptr]),
+    "gpk_conjugate_mll_workspace_bytes": (_c_size, [_c_i64, _c_int, _c_int]),
+    "gpk_conjugate_mll": (_c_int, [_c_int, _c_i64, _c_int, _c_ptr, _c_i64, _c_ptr, _c_ptr, _c_int,
+                                   _c_dbl, _c_int, _c_int, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_size,
+                                   _c_ptr]),
+    "gpk_collapsed_elbo_workspace_bytes": (_c_size, [_c_i64, _c_i64, _c_int, _c_int]),
+    "gpk_collapsed_elbo": (_c_int, [_c_int, _c_i64, _c_i64, _c_int, _c_ptr, _c_i64, _c_ptr,
+                                    _c_ptr, _c_i64, _c_ptr, _c_int, _c_dbl, _c_int, _c_int,
+                                    _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_size, _c_ptr]),
+    "gpk_predict_workspace_bytes": (_c_size, [_c_i64, _c_i64, _c_int, _c_int]),
+    "gpk_predict": (_c_int, [_c_int, _c_i64, _c_i64, _c_int, _c_ptr, _c_i64, _c_ptr, _c_ptr,
+                             _c_i64, _c_ptr, _c_int, _c_dbl, _c_dbl, _c_int, _c_ptr, _c_ptr,
+                             _c_ptr, _c_i64, _c_ptr, _c_ptr, _c_size, _c_ptr]),
+}
+
+_LIB = None
+
+
+class GPKError(RuntimeError):
+    """A non-zero gpk_status from the C ABI."""
+
+    def __init__(self, fn: str, status: int):
+        msg = lib().gpk_status_string(status).decode()
+        super().__init__(f"{fn} failed: {msg} (status {status})")
+        self.status = status
+
+
+def lib() -> ctypes.CDLL:
+    """Loads libgpk.so once and declares every exported signature."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                f"{LIB_PATH} is missing; build it with `python -m gpjax_gb300._build` "
+                "(nvcc, sm_103a).  There is no CPU fallback.")
+        handle = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(handle, name, None)
+            if fn is None:
+                continue  # call() raises for an entry point this build lacks
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = handle
+    return _LIB
+
+
+def call(name: str, *args) -> None:
+    """Calls a gpk_* entry point and raises GPKError on a non-zero status."""
+    fn = getattr(lib(), name, None)
+    if fn is None:
+        raise RuntimeError(f"{name} is not exported by {LIB_PATH}")
+    st = fn(*args)
+    if st != 0:
+        raise GPKError(name, st)
+
+
+def require_cuda(*tensors: torch.Tensor) -> torch.device:
+    if not torch.cuda.is_available():
+        raise RuntimeError("gpjax_gb300 needs a CUDA device (GB300, sm_103a); none is visible")
+    for t in tensors:
+        if t is not None and not t.is_cuda:
+            raise ValueError("expected CUDA tensors")
+    return tensors[0].device if tensors else torch.device("cuda")
+
+
+def stream_ptr(device: torch.device | None = None) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def ptr(t: torch.Tensor | None) -> int | None:
+    return None if t is None else t.data_ptr()
+
+
+def workspace(nbytes: int, device: torch.device) -> torch.Tensor:
+    """Caller-owned workspace for one call (the library never allocates)."""
+    return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)

@@ -1,0 +1,111 @@
+// Shared device helpers for the gpk library: pointwise stationary kernels and
+// their derivatives, status handling and small reductions.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <math.h>
+#include "gpk.h"
+
+#define GPK_MAX_D 32  // largest input dimension handled by the register paths
+
+namespace gpk {
+
+// ---------------------------------------------------------------------------
+// Pointwise stationary kernels on the scaled squared distance
+//   sq = sum_d ((x_d - y_d) / l_d)^2
+// RBF       k = s2 exp(-sq/2)                          (kernels/stationary/rbf.py:40-44)
+// Matern32  k = s2 (1 + sqrt3 t) exp(-sqrt3 t)         (matern32.py:41-54)
+// Matern52  k = s2 (1 + sqrt5 t + 5/3 t^2) exp(-sqrt5 t) (matern52.py:42-53)
+// with t = sqrt(max(sq, 1e-36)) (stationary/utils.py:56-67).
+//
+// dcoef(sq) returns c with dk/dl_d = c * (x_d - y_d)^2 / l_d^3 and
+// dk/dx_d = -c * (x_d - y_d) / l_d^2; the 1e-36 floor has zero derivative,
+// which matches differentiating max(sq, 1e-36) below the floor.
+// ---------------------------------------------------------------------------
+template <typename T> struct Consts;
+template <> struct Consts<double> {
+  static __device__ __forceinline__ double floor_() { return 1e-36; }
+};
+template <> struct Consts<float> {
+  // 1e-36 is a normal float (FLT_MIN ~ 1.18e-38), so the same floor applies.
+  static __device__ __forceinline__ float floor_() { return 1e-36f; }
+};
+
+__device__ __forceinline__ double d_exp(double x) { return exp(x); }
+__device__ __forceinline__ float d_exp(float x) { return expf(x); }
+__device__ __forceinline__ double d_sqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float d_sqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double d_log(double x) { return log(x); }
+__device__ __forceinline__ float d_log(float x) { return logf(x); }
+
+template <typename T>
+__device__ __forceinline__ T kval(int kind, T sq, T s2) {
+  if (kind == GPK_RBF) return s2 * d_exp(T(-0.5) * sq);
+  T t = d_sqrt(sq > Consts<T>::floor_() ? sq : Consts<T>::floor_());
+  if (kind == GPK_MATERN32) {
+    const T r3 = T(1.7320508075688772);
+    return s2 * (T(1) + r3 * t) * d_exp(-r3 * t);
+  }
+  const T r5 = T(2.23606797749979);
+  return s2 * (T(1) + r5 * t + T(5.0 / 3.0) * (t * t)) * d_exp(-r5 * t);
+}
+
+// value and derivative coefficient together (one exp)
+template <typename T>
+__device__ __forceinline__ void kval_dcoef(int kind, T sq, T s2, T& k, T& c) {
+  if (kind == GPK_RBF) {
+    k = s2 * d_exp(T(-0.5) * sq);
+    c = k;
+    return;
+  }
+  T t = d_sqrt(sq > Consts<T>::floor_() ? sq : Consts<T>::floor_());
+  if (kind == GPK_MATERN32) {
+    const T r3 = T(1.7320508075688772);
+    T e = s2 * d_exp(-r3 * t);
+    k = (T(1) + r3 * t) * e;
+    c = T(3) * e;
+    return;
+  }
+  const T r5 = T(2.23606797749979);
+  T e = s2 * d_exp(-r5 * t);
+  k = (T(1) + r5 * t + T(5.0 / 3.0) * (t * t)) * e;
+  c = T(5.0 / 3.0) * (T(1) + r5 * t) * e;
+}
+
+// warp / block reductions
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Sums v over the block into *out with one atomicAdd per warp.
+__device__ __forceinline__ void block_atomic_add(double* out, double v) {
+  v = warp_sum(v);
+  if ((threadIdx.x & 31) == 0) atomicAdd(out, v);
+}
+
+__host__ __device__ inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Counts kernel launches made by the library (reported by gpk_launch_count);
+// every launch site reads its status through launch_status().
+void count_launch();
+inline cudaError_t launch_status() {
+  count_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace gpk
+
+#define GPK_CUDA_TRY(...)                                    \
+  do {                                                       \
+    cudaError_t _e = (__VA_ARGS__);                          \
+    if (_e != cudaSuccess) return GPK_ERR_CUDA;              \
+  } while (0)
+
+#define GPK_LAUNCH_CHECK()                                   \
+  do {                                                       \
+    cudaError_t _e = gpk::launch_status();                   \
+    if (_e != cudaSuccess) return GPK_ERR_CUDA;              \
+  } while (0)

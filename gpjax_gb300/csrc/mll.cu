@@ -1,0 +1,430 @@
+// Exact-GP marginal log-likelihood with its adjoint, plus the dense
+// linear-algebra entry points of the C ABI.
+//
+// Reference op sequence (gpjax/objectives.py:93-107):
+//   obs_noise = obs_stddev^2 ; mx = constant
+//   Sigma = (K(x, x) + I*jitter) + I*obs_noise
+//   mll = -1/2 (n log 2pi + logdet(Sigma) + diff^T solve(Sigma, diff))
+// where logdet and solve are two LU factorisations (linalg/operations.py:
+// 111,164).  Here one Cholesky factor L serves both: log|Sigma| = 2 sum log L_ii
+// and alpha = Sigma^-1 diff = V (M diff) with M = L^-1, V = M^T, refined
+// against residuals accumulated in float64.  The gradient is the fused
+// inverse-product/kernel-derivative reduction of adjoint.cu.
+#include <atomic>
+#include <climits>
+#include <cmath>
+#include "gpk_internal.cuh"
+
+namespace gpk {
+
+static std::atomic<long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+// Optional phase events (benchmark instrumentation), see gpk_set_profile_events.
+static cudaEvent_t g_prof_events[8];
+static int g_prof_count = 0;
+static inline void prof_mark(int k, cudaStream_t s) {
+  if (k < g_prof_count && g_prof_events[k]) cudaEventRecord(g_prof_events[k], s);
+}
+
+// Carves caller-provided workspace into 256-byte aligned regions.
+struct Arena {
+  char* base;
+  size_t off = 0;
+  explicit Arena(void* b) : base(static_cast<char*>(b)) {}
+  template <typename U>
+  U* take(size_t count) {
+    off = (off + 255) & ~size_t(255);
+    U* p = base ? reinterpret_cast<U*>(base + off) : nullptr;
+    off += count * sizeof(U);
+    return p;
+  }
+};
+
+inline int64_t pad_ld(int64_t n) { return ((n + 63) / 64) * 64; }
+
+template <typename T>
+struct MllBuffers {
+  int64_t ld;
+  T *A, *M, *V, *scratch, *xs;
+  double *diff, *z, *alpha, *r, *logdiag, *rpart, *gpart, *dtrack;
+};
+
+template <typename T>
+static size_t mll_layout(int64_t n, int d, void* ws, MllBuffers<T>& b) {
+  Arena a(ws);
+  b.ld = pad_ld(n);
+  const size_t nn = (size_t)n * b.ld;
+  b.A = a.take<T>(nn);
+  b.M = a.take<T>(nn);
+  b.V = a.take<T>(nn);
+  b.scratch = a.take<T>((size_t)n * n / 2 + 64);
+  b.xs = a.take<T>((size_t)n * d);
+  b.diff = a.take<double>(n);
+  b.z = a.take<double>(n);
+  b.alpha = a.take<double>(n);
+  b.r = a.take<double>(n);
+  b.logdiag = a.take<double>(n);
+  b.dtrack = a.take<double>(n);
+  b.rpart = a.take<double>(residual_scratch_doubles((int)n));
+  b.gpart = a.take<double>((size_t)lauum_grad_tiles<T>((int)n) * (d + 2));
+  return a.off + 256;
+}
+
+__global__ void init_info_kernel(int* info) { *info = INT_MAX; }
+
+__global__ void diff_kernel(int n, const double* __restrict__ y, const double* __restrict__ theta,
+                            int n_ls, double* __restrict__ diff) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) diff[i] = y[i] - theta[n_ls + 2];
+}
+
+__global__ void axpy_kernel(int n, const double* __restrict__ x, double* __restrict__ y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] += x[i];
+}
+
+// Neumaier-compensated block sum of f(i) over i < n (one block).
+template <typename F>
+__device__ double block_ksum(int n, F f) {
+  __shared__ double s_sum[32], s_c[32];
+  double sum = 0.0, c = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double v = f(i);
+    const double t = sum + v;
+    c += (fabs(sum) >= fabs(v)) ? (sum - t) + v : (v - t) + sum;
+    sum = t;
+  }
+  // combine the (sum, c) pairs: warp then block, compensating each addition
+  for (int o = 16; o > 0; o >>= 1) {
+    const double os = __shfl_xor_sync(0xffffffffu, sum, o);
+    const double oc = __shfl_xor_sync(0xffffffffu, c, o);
+    const double t = sum + os;
+    c += oc + ((fabs(sum) >= fabs(os)) ? (sum - t) + os : (os - t) + sum);
+    sum = t;
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) {
+    s_sum[w] = sum;
+    s_c[w] = c;
+  }
+  __syncthreads();
+  double tot = 0.0, tc = 0.0;
+  if (threadIdx.x == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    for (int k = 0; k < nw; ++k) {
+      const double v = s_sum[k];
+      const double t = tot + v;
+      tc += s_c[k] + ((fabs(tot) >= fabs(v)) ? (tot - t) + v : (v - t) + tot);
+      tot = t;
+    }
+  }
+  __syncthreads();
+  return tot + tc;  // valid on thread 0
+}
+
+__global__ void __launch_bounds__(256)
+    mll_finalize_kernel(int n, int d, const double* __restrict__ theta, int n_ls,
+                        const double* __restrict__ logdiag, const double* __restrict__ diff,
+                        const double* __restrict__ alpha, const double* __restrict__ gpart,
+                        int ntiles, int want_grad, double jitter, int* __restrict__ info,
+                        double* __restrict__ out_mll, double* __restrict__ out_grad) {
+  const double logdet = 2.0 * block_ksum(n, [&](int i) { return logdiag[i]; });
+  const double quad = block_ksum(n, [&](int i) { return diff[i] * alpha[i]; });
+  const double asum = block_ksum(n, [&](int i) { return alpha[i]; });
+  const int slots = d + 2;
+  __shared__ double sg[GPK_MAX_D + 2];
+  if (want_grad) {
+    // one warp per slot, tiles summed in a fixed strided order
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    for (int s = w; s < slots; s += blockDim.x >> 5) {
+      double acc = 0.0;
+      for (int t = l; t < ntiles; t += 32) acc += gpart[(int64_t)t * slots + s];
+      acc = warp_sum(acc);
+      if (l == 0) sg[s] = acc;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  int inf = *info;
+  if (inf == INT_MAX) inf = 0;
+  *info = inf;
+  const double nan = __longlong_as_double(0x7ff8000000000000ULL);
+  const double mll = -0.5 * ((double)n * log(2.0 * 3.141592653589793) + logdet + quad);
+  *out_mll = inf ? nan : mll;
+  if (!want_grad) return;
+  const double s2 = theta[n_ls];
+  const double sd = theta[n_ls + 1];
+  if (n_ls == 1) {
+    double a = 0.0;
+    for (int k = 0; k < d; ++k) a += sg[k];
+    out_grad[0] = inf ? nan : 0.5 * s2 * a / theta[0];
+  } else {
+    for (int k = 0; k < d; ++k) out_grad[k] = inf ? nan : 0.5 * s2 * sg[k] / theta[k];
+  }
+  // d/d variance: 1/2 sum (alpha alpha^T - W) o K / s2.  With Sigma = K + s I
+  // (s = jitter + obs_stddev^2), W = Sigma^-1 and Sigma alpha = diff this is
+  // exactly 1/2 (diff^T alpha - n - s (alpha^T alpha - tr W)) / s2, which needs
+  // only the refined alpha and the noise sum instead of n^2 cancelling terms.
+  const double snoise = jitter + sd * sd;
+  const double gvar = (s2 > 0.0) ? 0.5 * (quad - (double)n - snoise * sg[d + 1]) / s2
+                                 : 0.5 * sg[d];
+  out_grad[n_ls] = inf ? nan : gvar;
+  out_grad[n_ls + 1] = inf ? nan : sd * sg[d + 1];
+  out_grad[n_ls + 2] = inf ? nan : asum;
+}
+
+__global__ void finish_info_kernel(int* info) {
+  if (*info == INT_MAX) *info = 0;
+}
+
+__global__ void zero_outputs_kernel(double* out_mll, double* out_grad, int ng, int* info) {
+  if (out_mll) *out_mll = 0.0;
+  if (out_grad)
+    for (int k = 0; k < ng; ++k) out_grad[k] = 0.0;
+  if (info) *info = 0;
+}
+
+template <typename T>
+static gpk_status mll_run(int kind, int n, int d, const double* x, int64_t ldx, const double* y,
+                          const double* theta, int n_ls, double jitter, int refine, int want_grad,
+                          double* out_mll, double* out_grad, int* info, void* ws,
+                          cudaStream_t s) {
+  MllBuffers<T> b;
+  mll_layout<T>(n, d, ws, b);
+  prof_mark(0, s);
+  init_info_kernel<<<1, 1, 0, s>>>(info);
+  GPK_LAUNCH_CHECK();
+  GPK_CUDA_TRY(scale_inputs<T>(x, ldx, n, d, theta, n_ls, b.xs, s));
+  diff_kernel<<<(int)cdiv(n, 256), 256, 0, s>>>(n, y, theta, n_ls, b.diff);
+  GPK_LAUNCH_CHECK();
+  GPK_CUDA_TRY(cross_cov_scaled<T, T>(kind, n, n, d, b.xs, b.xs, theta, n_ls, 1, jitter, b.A,
+                                      b.ld, s));
+  GPK_CUDA_TRY(sigma_diag_init(kind, n, theta, n_ls, jitter, b.dtrack, s));
+  prof_mark(1, s);
+  GPK_CUDA_TRY(potrf_lower<T>(b.A, b.ld, n, b.logdiag, info, b.dtrack, false, s));
+  prof_mark(2, s);
+  GPK_CUDA_TRY(trtri_lower<T>(b.A, b.ld, n, b.M, b.ld, b.V, b.ld, b.scratch, s));
+  prof_mark(3, s);
+  GPK_CUDA_TRY(gemv_tri<T>(b.M, b.ld, n, true, b.diff, b.z, 1.0, false, s));
+  GPK_CUDA_TRY(gemv_tri<T>(b.V, b.ld, n, false, b.z, b.alpha, 1.0, false, s));
+  for (int it = 0; it < refine; ++it) {
+    GPK_CUDA_TRY(residual<T>(kind, n, d, b.xs, theta, n_ls, jitter, b.diff, b.alpha, b.r, b.rpart,
+                             s));
+    GPK_CUDA_TRY(gemv_tri<T>(b.M, b.ld, n, true, b.r, b.z, 1.0, false, s));
+    GPK_CUDA_TRY(gemv_tri<T>(b.V, b.ld, n, false, b.z, b.alpha, 1.0, true, s));
+  }
+  prof_mark(4, s);
+  if (want_grad)
+    GPK_CUDA_TRY(lauum_grad<T>(kind, b.V, b.ld, n, d, b.xs, theta, n_ls, b.alpha, b.gpart, s));
+  prof_mark(5, s);
+  mll_finalize_kernel<<<1, 256, 0, s>>>(n, d, theta, n_ls, b.logdiag, b.diff, b.alpha, b.gpart,
+                                        lauum_grad_tiles<T>(n), want_grad, jitter, info,
+                                        out_mll, out_grad);
+  GPK_LAUNCH_CHECK();
+  prof_mark(6, s);
+  return GPK_OK;
+}
+
+}  // namespace gpk
+
+using namespace gpk;
+
+extern "C" int gpk_version(void) { return 100; }
+
+extern "C" long long gpk_launch_count(void) { return g_launches.load(); }
+
+extern "C" void gpk_set_profile_events(void* const* events, int count) {
+  g_prof_count = 0;
+  if (!events || count <= 0) return;
+  const int m = count < 8 ? count : 8;
+  for (int k = 0; k < m; ++k) g_prof_events[k] = static_cast<cudaEvent_t>(events[k]);
+  g_prof_count = m;
+}
+
+extern "C" const char* gpk_status_string(int status) {
+  switch (status) {
+    case GPK_OK: return "ok";
+    case GPK_ERR_BAD_ARG: return "invalid argument";
+    case GPK_ERR_NOT_PD: return "matrix is not positive definite";
+    case GPK_ERR_WORKSPACE: return "workspace too small";
+    case GPK_ERR_CUDA: return "CUDA error";
+    case GPK_ERR_TIMEOUT: return "device wait timed out";
+    case GPK_ERR_UNSUPPORTED: return "unsupported configuration";
+    default: return "unknown status";
+  }
+}
+
+static bool mll_args_ok(int kind, int64_t n, int d, int64_t ldx, int n_ls, int precision) {
+  if (kind < GPK_RBF || kind > GPK_MATERN52) return false;
+  if (n < 0 || n > (1 << 20)) return false;
+  if (d <= 0 || d > GPK_MAX_D || ldx < d) return false;
+  if (!(n_ls == 1 || n_ls == d)) return false;
+  if (precision != GPK_PREC_FP64 && precision != GPK_PREC_MIXED) return false;
+  return true;
+}
+
+extern "C" size_t gpk_conjugate_mll_workspace_bytes(int64_t n, int d, int precision) {
+  if (n <= 0 || d <= 0) return 256;
+  if (precision == GPK_PREC_FP64) {
+    MllBuffers<double> b;
+    return mll_layout<double>(n, d, nullptr, b);
+  }
+  MllBuffers<float> b;
+  return mll_layout<float>(n, d, nullptr, b);
+}
+
+extern "C" gpk_status gpk_conjugate_mll(int kind, int64_t n, int d, const double* x, int64_t ldx,
+                                        const double* y, const double* theta, int n_ls,
+                                        double jitter, int precision, int want_grad,
+                                        double* out_mll, double* out_grad, int* info,
+                                        void* workspace, size_t workspace_bytes,
+                                        cudaStream_t stream) {
+  if (!mll_args_ok(kind, n, d, ldx, n_ls, precision)) return GPK_ERR_BAD_ARG;
+  if (!out_mll || !info || !theta || (want_grad && !out_grad)) return GPK_ERR_BAD_ARG;
+  if (n == 0) {
+    zero_outputs_kernel<<<1, 1, 0, stream>>>(out_mll, want_grad ? out_grad : nullptr, n_ls + 3,
+                                             info);
+    GPK_LAUNCH_CHECK();
+    return GPK_OK;
+  }
+  if (!x || !y || !workspace) return GPK_ERR_BAD_ARG;
+  if (workspace_bytes < gpk_conjugate_mll_workspace_bytes(n, d, precision))
+    return GPK_ERR_WORKSPACE;
+  if (precision == GPK_PREC_FP64)
+    return mll_run<double>(kind, (int)n, d, x, ldx, y, theta, n_ls, jitter, 1, want_grad, out_mll,
+                           out_grad, info, workspace, stream);
+  return mll_run<float>(kind, (int)n, d, x, ldx, y, theta, n_ls, jitter, 2, want_grad, out_mll,
+                        out_grad, info, workspace, stream);
+}
+
+extern "C" gpk_status gpk_lower_cholesky(int64_t n, int dtype, void* A, int64_t lda,
+                                         double* logdiag, int* info, cudaStream_t stream) {
+  if (n < 0 || n > (1 << 20) || lda < n || !info) return GPK_ERR_BAD_ARG;
+  if (n == 0) {
+    zero_outputs_kernel<<<1, 1, 0, stream>>>(nullptr, nullptr, 0, info);
+    GPK_LAUNCH_CHECK();
+    return GPK_OK;
+  }
+  if (!A) return GPK_ERR_BAD_ARG;
+  init_info_kernel<<<1, 1, 0, stream>>>(info);
+  GPK_LAUNCH_CHECK();
+  if (dtype == GPK_F64)
+    GPK_CUDA_TRY(potrf_lower<double>((double*)A, lda, (int)n, logdiag, info, nullptr, true, stream));
+  else if (dtype == GPK_F32)
+    GPK_CUDA_TRY(potrf_lower<float>((float*)A, lda, (int)n, logdiag, info, nullptr, true, stream));
+  else
+    return GPK_ERR_BAD_ARG;
+  finish_info_kernel<<<1, 1, 0, stream>>>(info);
+  GPK_LAUNCH_CHECK();
+  return GPK_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Triangular solve L X = B through the triangular inverse:
+// X^T = B^T M^T, one NT GEMM with the transposed store landing in B.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void transpose_kernel(int rows, int cols, const T* __restrict__ src, int64_t lds,
+                                 T* __restrict__ dst, int64_t ldd) {
+  __shared__ T tile[32][33];
+  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int r = by + k, c = bx + threadIdx.x;
+    tile[k][threadIdx.x] = (r < rows && c < cols) ? src[(int64_t)r * lds + c] : T(0);
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int r = bx + k, c = by + threadIdx.x;  // dst is cols x rows
+    if (r < cols && c < rows) dst[(int64_t)r * ldd + c] = tile[threadIdx.x][k];
+  }
+}
+
+template <typename T>
+static size_t solve_layout(int64_t n, int64_t nrhs, void* ws, T** M, T** V, T** scr, T** BT,
+                           int64_t* ld) {
+  Arena a(ws);
+  *ld = pad_ld(n);
+  *M = a.take<T>((size_t)n * *ld);
+  *V = a.take<T>((size_t)n * *ld);
+  *scr = a.take<T>((size_t)n * n / 2 + 64);
+  *BT = a.take<T>((size_t)nrhs * *ld);
+  return a.off + 256;
+}
+
+extern "C" size_t gpk_solve_triangular_workspace_bytes(int64_t n, int64_t nrhs, int dtype) {
+  int64_t ld;
+  if (dtype == GPK_F64) {
+    double *M, *V, *S, *B;
+    return solve_layout<double>(n, nrhs, nullptr, &M, &V, &S, &B, &ld);
+  }
+  float *M, *V, *S, *B;
+  return solve_layout<float>(n, nrhs, nullptr, &M, &V, &S, &B, &ld);
+}
+
+template <typename T>
+static gpk_status solve_run(int n, int nrhs, const T* L, int64_t lda, T* B, int64_t ldb, void* ws,
+                            cudaStream_t s) {
+  T *M, *V, *scr, *BT;
+  int64_t ld;
+  solve_layout<T>(n, nrhs, ws, &M, &V, &scr, &BT, &ld);
+  GPK_CUDA_TRY(trtri_lower<T>(L, lda, n, M, ld, V, ld, scr, s));
+  dim3 tb(32, 8);
+  dim3 grid((unsigned)cdiv(nrhs, 32), (unsigned)cdiv(n, 32));
+  transpose_kernel<T><<<grid, tb, 0, s>>>(n, nrhs, B, ldb, BT, ld);
+  GPK_LAUNCH_CHECK();
+  GemmProb<T> p{};
+  p.A = BT;
+  p.lda = ld;
+  p.M = nrhs;
+  p.B = M;
+  p.ldb = ld;
+  p.b_tri = TRI_LOWER;
+  p.N = n;
+  p.K = n;
+  p.C = nullptr;
+  p.Ct = B;
+  p.ldct = ldb;
+  p.alpha = T(1);
+  p.beta = T(0);
+  GPK_CUDA_TRY(gemm_nt<T>(p, 1, s));
+  return GPK_OK;
+}
+
+extern "C" gpk_status gpk_solve_triangular(int64_t n, int64_t nrhs, int dtype, const void* L,
+                                           int64_t lda, void* B, int64_t ldb, void* workspace,
+                                           size_t workspace_bytes, cudaStream_t stream) {
+  if (n < 0 || nrhs < 0 || n > (1 << 20) || lda < n || ldb < nrhs) return GPK_ERR_BAD_ARG;
+  if (n == 0 || nrhs == 0) return GPK_OK;
+  if (!L || !B || !workspace) return GPK_ERR_BAD_ARG;
+  if (workspace_bytes < gpk_solve_triangular_workspace_bytes(n, nrhs, dtype))
+    return GPK_ERR_WORKSPACE;
+  if (dtype == GPK_F64)
+    return solve_run<double>((int)n, (int)nrhs, (const double*)L, lda, (double*)B, ldb, workspace,
+                             stream);
+  if (dtype == GPK_F32)
+    return solve_run<float>((int)n, (int)nrhs, (const float*)L, lda, (float*)B, ldb, workspace,
+                            stream);
+  return GPK_ERR_BAD_ARG;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+    logdet_tri_kernel(int n, const T* __restrict__ L, int64_t lda, double* out) {
+  const double v = block_ksum(n, [&](int i) { return log((double)L[(int64_t)i * lda + i]); });
+  if (threadIdx.x == 0) *out = v;
+}
+
+extern "C" gpk_status gpk_logdet_triangular(int64_t n, int dtype, const void* L, int64_t lda,
+                                            double* out, cudaStream_t stream) {
+  if (n < 0 || lda < n || !out || (n > 0 && !L)) return GPK_ERR_BAD_ARG;
+  if (dtype == GPK_F64)
+    logdet_tri_kernel<double><<<1, 256, 0, stream>>>((int)n, (const double*)L, lda, out);
+  else if (dtype == GPK_F32)
+    logdet_tri_kernel<float><<<1, 256, 0, stream>>>((int)n, (const float*)L, lda, out);
+  else
+    return GPK_ERR_BAD_ARG;
+  GPK_LAUNCH_CHECK();
+  return GPK_OK;
+}

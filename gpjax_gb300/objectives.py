@@ -1,0 +1,91 @@
+"""Objectives on the GPU: conjugate_mll and collapsed_elbo
+(mirrors gpjax/objectives.py:33-416).
+
+Each objective is a ``torch.autograd.Function``: one call of the C ABI returns
+the value together with its gradient in the reference's constrained
+coordinates (lengthscale, variance, obs_stddev, constant mean and, for the
+collapsed ELBO, the inducing inputs); ``backward`` only scales the stored
+gradient by the incoming cotangent.  This is the counterpart of the
+reference's ``jax.value_and_grad`` over the objective (fit.py:160,233).
+"""
+from __future__ import annotations
+
+import torch
+
+from . import _lib
+from .config import precision_code
+from .gps import _mean_constant
+
+
+class _ConjugateMLL(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, theta, x, y, kind, n_ls, jitter, prec):
+        dev = _lib.require_cuda(x, y, theta)
+        n, d = x.shape
+        want_grad = bool(ctx.needs_input_grad[0])
+        th = theta.detach().contiguous()
+        xc, yc = x.detach().contiguous(), y.detach().reshape(-1).contiguous()
+        out = torch.empty(1, dtype=torch.float64, device=dev)
+        grad = torch.zeros(n_ls + 3, dtype=torch.float64, device=dev)
+        info = torch.zeros(1, dtype=torch.int32, device=dev)
+        nbytes = _lib.lib().gpk_conjugate_mll_workspace_bytes(n, d, prec)
+        ws = _lib.workspace(nbytes, dev)
+        _lib.call("gpk_conjugate_mll", kind, n, d, xc.data_ptr(), d, yc.data_ptr(), th.data_ptr(),
+                  n_ls, float(jitter), prec, int(want_grad), out.data_ptr(), grad.data_ptr(),
+                  info.data_ptr(), ws.data_ptr(), ws.numel(), _lib.stream_ptr(dev))
+        ctx.save_for_backward(grad)
+        ctx.info = info
+        return out[0]
+
+    @staticmethod
+    def backward(ctx, g):
+        (grad,) = ctx.saved_tensors
+        return g * grad, None, None, None, None, None, None
+
+
+def conjugate_mll(posterior, data, precision: str | None = None) -> torch.Tensor:
+    """Marginal log-likelihood of a conjugate GP (objectives.py:36-107).
+
+    Sigma = (K(x, x) + I*prior.jitter) + I*obs_stddev^2;
+    returns log N(y; m(x), Sigma) as a 0-d float64 tensor that is
+    differentiable w.r.t. the kernel, likelihood and mean parameters.
+    """
+    kernel = posterior.prior.kernel
+    x = kernel.slice_input(data.X)
+    dev = _lib.require_cuda(x)
+    const = _mean_constant(posterior.prior.mean_function, dev)
+    theta = kernel.theta_vector(dev, posterior.likelihood.obs_stddev.value, const)
+    return _ConjugateMLL.apply(theta, x, data.y, kernel.kind, kernel.n_ls,
+                               float(posterior.prior.jitter), precision_code(precision))
+
+
+def value_and_grad(objective, model, data, **kw):
+    """(value, {name: grad}) of an objective, like jax.value_and_grad over the
+    model's parameters (fit.py:160)."""
+    params = named_parameters(model)
+    for p in params.values():
+        p.requires_grad_(True)
+    val = objective(model, data, **kw)
+    grads = torch.autograd.grad(val, [p.value for p in params.values()], allow_unused=True)
+    out = {k: (g if g is not None else torch.zeros_like(p.value))
+           for (k, p), g in zip(params.items(), grads)}
+    return val.detach(), out
+
+
+def named_parameters(model) -> dict:
+    """The trainable Parameters of a posterior / variational family by dotted name."""
+    from .parameters import Parameter
+    found = {}
+
+    def walk(obj, prefix, seen):
+        if id(obj) in seen:
+            return
+        seen.add(id(obj))
+        for k, v in vars(obj).items():
+            name = f"{prefix}{k}"
+            if isinstance(v, Parameter):
+                found[name] = v
+            elif hasattr(v, "__dict__") and not isinstance(v, (torch.Tensor, type)):
+                walk(v, name + ".", seen)
+    walk(model, "", set())
+    return found

@@ -1,0 +1,173 @@
+/*
+ * gpk.h -- C ABI of the GB300 (sm_103a) exact/sparse Gaussian-process library.
+ *
+ * Plain C types only: device pointers, sizes, a CUDA stream.  Every device
+ * buffer is owned by the caller (torch tensors, XLA buffers under jax.ffi);
+ * the library never allocates.  Scratch memory comes from the caller through
+ * the matching *_workspace_bytes() query.  All calls are asynchronous on the
+ * given stream and do not synchronise the host.
+ *
+ * Hyperparameters live on the device as a float64 vector
+ *     theta = [ lengthscale[0..n_ls), variance, obs_stddev, mean_constant ]
+ * with n_ls = 1 (isotropic) or d (ARD), in the reference's constrained
+ * coordinates (kernels/stationary/base.py:54-95, likelihoods.py:129-152,
+ * mean_functions.py:131-153).  Gradients use the same layout.
+ *
+ * Errors: a gpk_status is returned for argument/launch errors.  A factorised
+ * matrix that is not positive definite is reported on the device through
+ * *info (0 = ok, k > 0 = the leading minor of order k is not positive
+ * definite, LAPACK convention); outputs are then NaN, which is what the
+ * reference's jnp.linalg.cholesky produces (linalg/operations.py:54-55).
+ */
+#ifndef GPK_H_
+#define GPK_H_
+
+#include <stddef.h>
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  GPK_OK = 0,
+  GPK_ERR_BAD_ARG = 1,
+  GPK_ERR_NOT_PD = 2,
+  GPK_ERR_WORKSPACE = 3,
+  GPK_ERR_CUDA = 4,
+  GPK_ERR_TIMEOUT = 5,
+  GPK_ERR_UNSUPPORTED = 6
+} gpk_status;
+
+/* stationary kernels: kernels/stationary/{rbf,matern32,matern52}.py */
+typedef enum { GPK_RBF = 0, GPK_MATERN32 = 1, GPK_MATERN52 = 2 } gpk_kernel_kind;
+
+typedef enum { GPK_F64 = 0, GPK_F32 = 1 } gpk_dtype;
+
+/* GPK_PREC_FP64: every step in float64.
+ * GPK_PREC_MIXED: float32 Gram, split-TF32 tensor-core factorisation and
+ * inversion with float32 accumulation, float64 residual refinement of
+ * alpha = Sigma^-1 (y - m), float64 log-det and gradient accumulation. */
+typedef enum { GPK_PREC_FP64 = 0, GPK_PREC_MIXED = 1 } gpk_precision;
+
+/* Library version as major*10000 + minor*100 + patch. */
+int gpk_version(void);
+
+/* Human-readable name of a status code (static string). */
+const char* gpk_status_string(int status);
+
+/* Instrumentation (no counterpart in the reference).
+ * gpk_launch_count: kernel launches issued by the library since it was loaded.
+ * gpk_set_profile_events: when given >= 7 cudaEvent_t handles, each
+ * gpk_conjugate_mll call records them on its stream at its phase boundaries
+ * (0 start, 1 Gram built, 2 Cholesky done, 3 triangular inverse done,
+ * 4 alpha solved and refined, 5 adjoint done, 6 end); NULL disables.
+ * Process-global and not thread-safe: meant for benchmarks. */
+long long gpk_launch_count(void);
+void gpk_set_profile_events(void* const* events, int count);
+
+/* ---------------------------------------------------------------------------
+ * Kernel computations
+ * Replaces AbstractKernelComputation.cross_covariance / gram / diagonal
+ * (gpjax/kernels/computations/base.py:56-109) and
+ * DenseKernelComputation._cross_covariance (computations/dense.py:32-36).
+ * x [n, d] and y [m, d] are row-major float64 with leading dims ldx, ldy;
+ * out [n, m] is row-major with leading dim ldo in out_dtype.
+ * ------------------------------------------------------------------------- */
+gpk_status gpk_cross_covariance(int kind, int64_t n, int64_t m, int d,
+                                const double* x, int64_t ldx,
+                                const double* y, int64_t ldy,
+                                const double* theta, int n_ls,
+                                int out_dtype, void* out, int64_t ldo,
+                                cudaStream_t stream);
+
+/* Full-square Gram K(x, x) (computations/base.py:56-72). */
+gpk_status gpk_gram(int kind, int64_t n, int d, const double* x, int64_t ldx,
+                    const double* theta, int n_ls, int out_dtype, void* out,
+                    int64_t ldo, cudaStream_t stream);
+
+/* diag k(x_i, x_i) as float64 [n] (computations/base.py:95-109). */
+gpk_status gpk_diagonal(int kind, int64_t n, int d, const double* x, int64_t ldx,
+                        const double* theta, int n_ls, double* out,
+                        cudaStream_t stream);
+
+/* ---------------------------------------------------------------------------
+ * Linear algebra on dense row-major matrices
+ * ------------------------------------------------------------------------- */
+/* In-place lower Cholesky of the SPD matrix A [n, n] (only the lower triangle
+ * is read; the strict upper triangle is zeroed on return).
+ * Replaces lower_cholesky's Dense branch (linalg/operations.py:54-55).
+ * logdiag (optional, float64 [n]) receives log L_ii. */
+gpk_status gpk_lower_cholesky(int64_t n, int dtype, void* A, int64_t lda,
+                              double* logdiag, int* info, cudaStream_t stream);
+
+/* Solves L X = B in place for lower-triangular L [n, n] and B [n, nrhs]
+ * (row-major, ldb >= nrhs).  Replaces solve's Triangular branch
+ * (linalg/operations.py:105-107, jsp.linalg.solve_triangular lower=True).
+ * workspace: gpk_solve_triangular_workspace_bytes(). */
+size_t gpk_solve_triangular_workspace_bytes(int64_t n, int64_t nrhs, int dtype);
+gpk_status gpk_solve_triangular(int64_t n, int64_t nrhs, int dtype,
+                                const void* L, int64_t lda, void* B, int64_t ldb,
+                                void* workspace, size_t workspace_bytes,
+                                cudaStream_t stream);
+
+/* sum_i log L_ii in float64 (compensated), the Triangular branch of logdet
+ * (linalg/operations.py:142-144); out is one device double. */
+gpk_status gpk_logdet_triangular(int64_t n, int dtype, const void* L, int64_t lda,
+                                 double* out, cudaStream_t stream);
+
+/* ---------------------------------------------------------------------------
+ * Objectives
+ * ------------------------------------------------------------------------- */
+/* Exact-GP marginal log-likelihood and its gradient
+ * (conjugate_mll, gpjax/objectives.py:36-107, through
+ * GaussianDistribution.log_prob, gpjax/distributions.py:115-134).
+ *   Sigma = K(x, x) + I*jitter + I*obs_stddev^2, diff = y - mean_constant,
+ *   mll   = -1/2 (n log 2pi + log|Sigma| + diff^T Sigma^-1 diff).
+ * x [n, d] float64 row-major, y [n] float64; out_mll: 1 device double;
+ * out_grad (if want_grad): device double [n_ls + 3] in theta's layout;
+ * info: device int (0 or first non-PD order).  jitter is posterior.prior.jitter. */
+size_t gpk_conjugate_mll_workspace_bytes(int64_t n, int d, int precision);
+gpk_status gpk_conjugate_mll(int kind, int64_t n, int d,
+                             const double* x, int64_t ldx, const double* y,
+                             const double* theta, int n_ls, double jitter,
+                             int precision, int want_grad,
+                             double* out_mll, double* out_grad, int* info,
+                             void* workspace, size_t workspace_bytes,
+                             cudaStream_t stream);
+
+/* SGPR collapsed ELBO and its gradient (collapsed_elbo,
+ * gpjax/objectives.py:321-416), including d/dZ for the inducing inputs.
+ * z [m, d] float64; out_grad: theta layout [n_ls + 3]; out_grad_z [m, d]. */
+size_t gpk_collapsed_elbo_workspace_bytes(int64_t n, int64_t m, int d, int precision);
+gpk_status gpk_collapsed_elbo(int kind, int64_t n, int64_t m, int d,
+                              const double* x, int64_t ldx, const double* y,
+                              const double* z, int64_t ldz,
+                              const double* theta, int n_ls, double jitter,
+                              int precision, int want_grad,
+                              double* out_elbo, double* out_grad, double* out_grad_z,
+                              int* info, void* workspace, size_t workspace_bytes,
+                              cudaStream_t stream);
+
+/* ---------------------------------------------------------------------------
+ * Prediction: ConjugatePosterior.predict (gpjax/gps.py:443-526).
+ * mean [t] and var [t] float64 (var = diag of the predictive covariance,
+ * GaussianDistribution.variance, distributions.py:79-81); cov [t, t] float64
+ * row-major only when cov != NULL.  jitter is the posterior's (added to Kxx),
+ * prior_jitter the prior's (added to the predictive covariance).
+ * ------------------------------------------------------------------------- */
+size_t gpk_predict_workspace_bytes(int64_t n, int64_t t, int d, int precision);
+gpk_status gpk_predict(int kind, int64_t n, int64_t t, int d,
+                       const double* x, int64_t ldx, const double* y,
+                       const double* xt, int64_t ldxt,
+                       const double* theta, int n_ls,
+                       double jitter, double prior_jitter, int precision,
+                       double* mean, double* var, double* cov, int64_t ldcov,
+                       int* info, void* workspace, size_t workspace_bytes,
+                       cudaStream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GPK_H_ */

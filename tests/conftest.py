@@ -1,0 +1,28 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+@pytest.fixture(scope="session")
+def built_lib():
+    """Path of libgpk.so, building it in-tree when missing (nvcc cross-compiles)."""
+    from gpjax_gb300 import _build
+    return _build.build()
+
+
+@pytest.fixture(scope="session")
+def cuda_lib(built_lib):
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from gpjax_gb300 import _lib
+    return _lib.lib()

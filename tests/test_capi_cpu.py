@@ -1,0 +1,104 @@
+"""CPU: the C-ABI library loads, exports every entry point that include/gpk.h
+declares, and its host-only paths (workspace queries, argument validation)
+behave.  No compute call is made, so no GPU is needed."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if h.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", h)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names |= set(re.findall(r"\b(gpk_[a-z0-9_]+)\s*\(", src))
+    return sorted(names)
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for required in ("gpk_conjugate_mll", "gpk_gram", "gpk_cross_covariance",
+                     "gpk_lower_cholesky", "gpk_solve_triangular", "gpk_predict"):
+        assert required in names
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    lib = ctypes.CDLL(built_lib)
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, f"not exported: {missing}"
+
+
+def test_python_binding_covers_header(built_lib):
+    from gpjax_gb300 import _lib
+    assert set(declared_functions()) <= set(_lib.SIGNATURES)
+
+
+def test_version_and_status_strings(built_lib):
+    from gpjax_gb300 import _lib
+    lib = _lib.lib()
+    assert lib.gpk_version() >= 100
+    assert lib.gpk_status_string(0) == b"ok"
+    assert b"workspace" in lib.gpk_status_string(3)
+
+
+def test_workspace_queries(built_lib):
+    from gpjax_gb300 import _lib
+    lib = _lib.lib()
+    a = lib.gpk_conjugate_mll_workspace_bytes(16384, 8, _lib.PREC_MIXED)
+    b = lib.gpk_conjugate_mll_workspace_bytes(16384, 8, _lib.PREC_FP64)
+    # three n x n panels (factor, inverse, transposed inverse) plus scratch
+    assert 3 * 16384 * 16384 * 4 < a < 5 * 16384 * 16384 * 4
+    assert 3 * 16384 * 16384 * 8 < b < 5 * 16384 * 16384 * 8
+    assert lib.gpk_predict_workspace_bytes(2048, 512, 4, _lib.PREC_FP64) > 0
+    assert lib.gpk_solve_triangular_workspace_bytes(100, 3, _lib.F64) > 0
+
+
+@pytest.mark.parametrize("kind,n,d,n_ls,prec", [
+    (7, 10, 2, 1, 0),      # unknown kernel
+    (0, -1, 2, 1, 0),      # negative n
+    (0, 10, 0, 1, 0),      # d = 0
+    (0, 10, 3, 2, 0),      # n_ls neither 1 nor d
+    (0, 10, 3, 3, 9),      # unknown precision
+    (0, 10, 99, 1, 0),     # d above the register limit
+])
+def test_mll_rejects_bad_arguments(built_lib, kind, n, d, n_ls, prec):
+    from gpjax_gb300 import _lib
+    lib = _lib.lib()
+    st = lib.gpk_conjugate_mll(kind, n, d, None, max(d, 1), None, None, n_ls, 1e-6, prec, 1,
+                               None, None, None, None, 0, None)
+    assert st == 1  # GPK_ERR_BAD_ARG, returned before any device work
+
+
+def test_mll_rejects_small_workspace(built_lib):
+    from gpjax_gb300 import _lib
+    lib = _lib.lib()
+    fake = ctypes.c_void_p(0x1000)  # never dereferenced: the size check fails first
+    st = lib.gpk_conjugate_mll(0, 100, 2, fake, 2, fake, fake, 1, 1e-6, 0, 1, fake, fake, fake,
+                               fake, 16, None)
+    assert st == 3  # GPK_ERR_WORKSPACE
+
+
+def test_cross_covariance_rejects_bad_arguments(built_lib):
+    from gpjax_gb300 import _lib
+    lib = _lib.lib()
+    assert lib.gpk_cross_covariance(5, 3, 3, 2, None, 2, None, 2, None, 1, 0, None, 3, None) == 1
+    assert lib.gpk_cross_covariance(0, 3, 3, 2, None, 1, None, 2, None, 1, 0, None, 3, None) == 1
+
+
+def test_product_has_no_cpu_fallback():
+    """The package never imports the oracle, and fails loudly without CUDA."""
+    import subprocess
+    import sys
+    code = ("import sys, gpjax_gb300, torch\n"
+            "assert not any(m.startswith('oracle') for m in sys.modules)\n")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    pkg = os.path.join(ROOT, "gpjax_gb300")
+    for f in os.listdir(pkg):
+        if f.endswith(".py"):
+            assert "oracle" not in open(os.path.join(pkg, f)).read().replace("oracle is", ""), f

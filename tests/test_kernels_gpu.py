@@ -1,0 +1,78 @@
+"""GPU parity of Gram / cross-covariance / diagonal and of the linear-algebra
+operations against the float64 oracle and numpy."""
+import numpy as np
+import pytest
+import torch
+
+import gpjax_gb300 as gpx
+from gpjax_gb300 import kernels as K
+from gpjax_gb300 import linalg as LA
+from oracle import gp_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("cls,kind", [(K.RBF, O.RBF), (K.Matern32, O.MATERN32),
+                                      (K.Matern52, O.MATERN52)])
+@pytest.mark.parametrize("n,m,d", [(1, 1, 1), (7, 3, 2), (65, 130, 8), (200, 33, 16)])
+def test_cross_covariance_parity(cuda_lib, cls, kind, n, m, d):
+    rng = np.random.default_rng(n + m + d)
+    x, y = rng.standard_normal((n, d)), rng.standard_normal((m, d))
+    ls = np.exp(rng.uniform(-1, 1, d))
+    k = cls(lengthscale=ls, variance=0.7)
+    out = k.cross_covariance(torch.as_tensor(x, device="cuda"),
+                             torch.as_tensor(y, device="cuda")).cpu().numpy()
+    ref = O.cross_covariance(kind, x, y, ls, 0.7)
+    assert np.allclose(out, ref, rtol=1e-13, atol=1e-14)
+    G = k.gram(torch.as_tensor(x, device="cuda")).to_dense().cpu().numpy()
+    assert np.allclose(G, O.gram(kind, x, ls, 0.7), rtol=1e-13, atol=1e-14)
+    dg = k.diagonal(torch.as_tensor(x, device="cuda")).diagonal.cpu().numpy()
+    assert np.allclose(dg, O.diagonal(kind, x, ls, 0.7))
+
+
+def test_compute_engine_swap_keeps_diagonal(cuda_lib):
+    # tests/test_kernels/test_computation.py:43-81 of the reference
+    x = torch.randn(20, 3, dtype=torch.float64, device="cuda")
+    k = K.RBF(lengthscale=np.array([0.5, 1.0, 2.0]), variance=1.5)
+    d1 = torch.diagonal(k.gram(x).to_dense())
+    k.compute_engine = gpx.computations.DiagonalKernelComputation()
+    d2 = k.gram(x).diagonal
+    assert torch.allclose(d1, d2)
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-11), (torch.float32, 2e-4)])
+@pytest.mark.parametrize("n", [1, 2, 3, 64, 65, 127, 128, 129, 300, 700])
+def test_cholesky_solve_logdet(cuda_lib, dtype, tol, n):
+    rng = np.random.default_rng(n)
+    A = rng.standard_normal((n, n))
+    A = A @ A.T / n + np.eye(n)
+    At = torch.as_tensor(A, device="cuda", dtype=dtype)
+    L = LA.lower_cholesky(LA.Dense(At)).to_dense().double().cpu().numpy()
+    Lref = np.linalg.cholesky(A)
+    assert np.allclose(L, Lref, rtol=tol, atol=tol)
+    B = rng.standard_normal((n, 5))
+    X = LA.solve(LA.Triangular(torch.as_tensor(Lref, device="cuda", dtype=dtype)),
+                 torch.as_tensor(B, device="cuda", dtype=dtype)).double().cpu().numpy()
+    assert np.allclose(Lref @ X, B, rtol=tol * 10, atol=tol * 10)
+    ld = float(LA.logdet(LA.Dense(At)))
+    assert np.isclose(ld, np.linalg.slogdet(A)[1], rtol=tol, atol=tol * n)
+
+
+def test_linalg_known_answers(cuda_lib):
+    # tests/test_linalg.py:237-396 of the reference
+    A = torch.tensor([[2.0, 1.0], [1.0, 3.0]], dtype=torch.float64, device="cuda")
+    b = torch.tensor([1.0, 2.0], dtype=torch.float64, device="cuda")
+    x = LA.solve(LA.Dense(A), b)
+    assert torch.allclose(A @ x, b)
+    assert np.isclose(float(LA.logdet(LA.Dense(A))), np.log(5.0))
+    L = torch.tensor([[2.0, 0.0], [1.0, 3.0]], dtype=torch.float64, device="cuda")
+    xt = LA.solve(LA.Triangular(L), torch.tensor([2.0, 7.0], dtype=torch.float64, device="cuda"))
+    assert torch.allclose(L @ xt, torch.tensor([2.0, 7.0], dtype=torch.float64, device="cuda"))
+    assert np.isclose(float(LA.logdet(LA.Triangular(L))), np.log(6.0))
+
+
+def test_cholesky_not_pd_reports_info(cuda_lib):
+    A = torch.tensor([[1.0, 2.0], [2.0, 1.0]], dtype=torch.float64, device="cuda")
+    L, info = LA.cholesky_dense(A)
+    assert int(info.item()) == 2
+    assert torch.isnan(L[1, 1])

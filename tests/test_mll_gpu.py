@@ -1,0 +1,112 @@
+"""GPU parity of conjugate_mll and its gradient against the float64 oracle
+(LU-based value as in the reference, torch float64 autograd gradients).
+
+Tolerances: plain FP64 form 1e-10 relative on the MLL, 1e-7 on gradients;
+mixed form 1e-6 relative on the MLL and 1e-4 relative (to the gradient norm
+and per component with a small absolute floor) on gradients."""
+import numpy as np
+import pytest
+import torch
+
+import gpjax_gb300 as gpx
+from oracle import gp_oracle as O
+from tests._gpu_helpers import c2_like, grads_of, make_posterior, to_cuda_params
+
+pytestmark = pytest.mark.gpu
+
+
+def run(kind, x, y, ls, var, sd, c, precision):
+    post = to_cuda_params(make_posterior(kind, ls, var, sd, c))
+    data = gpx.Dataset(X=x, y=y)
+    val = gpx.objectives.conjugate_mll(post, data, precision=precision)
+    val.backward()
+    return float(val), grads_of(post)
+
+
+def oracle(kind, x, y, ls, var, sd, c):
+    val = O.conjugate_mll(kind, x, y, ls, var, sd, c)
+    _, g = O.conjugate_mll_torch(kind, x, y, ls, var, sd, c, lu=False)
+    return val, np.concatenate([np.atleast_1d(g["lengthscale"]),
+                                [g["variance"], g["obs_stddev"], g["constant"]]])
+
+
+CASES = [(0, 1, 1), (1, 2, 2), (2, 3, 1), (0, 17, 3), (2, 63, 8), (1, 65, 4), (2, 127, 8),
+         (0, 129, 2), (2, 300, 8), (1, 555, 5), (2, 1000, 8), (0, 1100, 16)]
+
+
+@pytest.mark.parametrize("kind,n,d", CASES)
+@pytest.mark.parametrize("ard", [True, False])
+def test_mll_fp64_parity(cuda_lib, kind, n, d, ard):
+    rng = np.random.default_rng(n * 7 + d)
+    x = rng.uniform(-2, 2, size=(n, d))
+    y = np.sin(x).sum(1, keepdims=True) + 0.1 * rng.standard_normal((n, 1))
+    ls = np.exp(rng.uniform(np.log(0.5), np.log(2.0), d)) if ard else np.array(1.3)
+    var, sd, c = 1.2, 0.3, 0.1
+    val, g = run(kind, x, y, ls, var, sd, c, "fp64")
+    ref, gref = oracle(kind, x, y, ls, var, sd, c)
+    assert abs(val - ref) <= 1e-10 * max(1.0, abs(ref)), (val, ref)
+    assert np.allclose(g, gref, rtol=1e-7, atol=1e-8 * max(1.0, np.abs(gref).max())), (g, gref)
+
+
+def _mixed_check(val, g, ref, gref, tol_scale, gtol=1e-4):
+    """MLL within 1e-6 of tol_scale; gradient within gtol relative to its norm
+    (the mixed form's factor carries float32 backward error, which bounds the
+    trace term of the noise gradient; each component is also held to 1e-3)."""
+    err = np.abs(g - gref)
+    assert abs(val - ref) <= 1e-6 * tol_scale, (val, ref, abs(val - ref) / tol_scale)
+    assert np.linalg.norm(err) <= gtol * np.linalg.norm(gref), (g, gref)
+    assert np.all(err <= 1e-3 * np.abs(gref) + gtol * 0.1 * np.linalg.norm(gref)), (g, gref)
+
+
+@pytest.mark.parametrize("n", [700, 2048, 3000])
+def test_mll_mixed_parity_c2(cuda_lib, n):
+    """Matern-5/2 ARD, d = 8, X ~ N(0, I), noise 1e-2: |dMLL|/|MLL| <= 1e-6."""
+    x, y, ls = c2_like(n, 8, seed=n, kind=2)
+    val, g = run(2, x, y, ls, 1.0, 0.1, 0.0, "mixed")
+    ref, gref = oracle(2, x, y, ls, 1.0, 0.1, 0.0)
+    _mixed_check(val, g, ref, gref, abs(ref))
+
+
+@pytest.mark.parametrize("kind,n,d", [(0, 1024, 4), (1, 1500, 6), (0, 555, 16)])
+def test_mll_mixed_parity_other_kernels(cuda_lib, kind, n, d):
+    """Other kernels: MLL error relative to the size of its terms
+    (|log det| + |quad| + n log 2pi) / 2, which stays meaningful when the MLL
+    itself is near zero; gradients within 5e-4 of their norm (the RBF Gram is
+    an order of magnitude worse conditioned than the Matern-5/2 one)."""
+    x, y, ls = c2_like(n, d, seed=n, kind=kind)
+    val, g = run(kind, x, y, ls, 1.0, 0.1, 0.0, "mixed")
+    ref, gref = oracle(kind, x, y, ls, 1.0, 0.1, 0.0)
+    S = O.gram(kind, x, ls, 1.0) + (1e-6 + 1e-2) * np.eye(n)
+    ld = np.linalg.slogdet(S)[1]
+    quad = float(y[:, 0] @ np.linalg.solve(S, y[:, 0]))
+    _mixed_check(val, g, ref, gref, 0.5 * (abs(ld) + abs(quad) + n * np.log(2 * np.pi)),
+                 gtol=5e-4)
+
+
+def test_mll_matches_finite_differences(cuda_lib):
+    x, y, ls = c2_like(200, 3, seed=5)
+    var, sd, c = 0.9, 0.2, 0.05
+    _, g = run(2, x, y, ls, var, sd, c, "fp64")
+    vec = np.concatenate([ls, [var, sd, c]])
+
+    def f(v):
+        post = make_posterior(2, v[:3], v[3], v[4], v[5])
+        return float(gpx.objectives.conjugate_mll(post, gpx.Dataset(X=x, y=y), precision="fp64"))
+    fd = O.central_fd(f, vec, 1e-6)
+    assert np.allclose(g, fd, rtol=1e-5, atol=1e-5), (g, fd)
+
+
+def test_mll_not_pd_gives_nan_and_info(cuda_lib):
+    # duplicate inputs with zero noise and zero jitter: singular Sigma
+    x = np.zeros((5, 2))
+    y = np.ones((5, 1))
+    post = make_posterior(0, [1.0, 1.0], 1.0, 0.0, 0.0, jitter=0.0)
+    val = gpx.objectives.conjugate_mll(post, gpx.Dataset(X=x, y=y), precision="fp64")
+    assert np.isnan(float(val))
+
+
+def test_mll_deterministic(cuda_lib):
+    x, y, ls = c2_like(600, 8, seed=11)
+    a, ga = run(2, x, y, ls, 1.0, 0.1, 0.0, "mixed")
+    b, gb = run(2, x, y, ls, 1.0, 0.1, 0.0, "mixed")
+    assert a == b and np.array_equal(ga, gb)

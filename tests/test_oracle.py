@@ -1,0 +1,114 @@
+"""CPU: the float64 oracle against the reference's own known answers and
+identities (the oracle is the checker for every GPU parity test)."""
+import numpy as np
+import pytest
+import scipy.stats
+
+from oracle import gp_oracle as O
+
+
+def _data(n, d, seed):
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(-2.0, 2.0, size=(n, d))
+    y = np.sin(x[:, :1]) + 0.1 * rng.standard_normal((n, 1))
+    return x, y
+
+
+def test_linalg_known_answers():
+    # tests/test_linalg.py:330-348 and :380-396 of the reference
+    A = np.array([[2.0, 1.0], [1.0, 3.0]])
+    b = np.array([1.0, 2.0])
+    assert np.allclose(A @ O.solve_dense(A, b), b)
+    assert np.isclose(O.logdet_dense(A), np.log(5.0))
+    L = np.array([[2.0, 0.0], [1.0, 3.0]])
+    assert np.isclose(np.sum(np.log(np.diag(L))), np.log(6.0))
+    Lc = np.linalg.cholesky(A)
+    assert np.allclose(Lc @ Lc.T, A, atol=1e-6)
+
+
+@pytest.mark.parametrize("n", [1, 2, 5, 100])
+def test_log_prob_matches_mvn(n):
+    # tests/test_gaussian_distribution.py:102-123: Dense log_prob == MVN log_prob
+    rng = np.random.default_rng(n)
+    mean = rng.uniform(size=n)
+    sq = rng.uniform(size=(n, n))
+    cov = sq @ sq.T + 1e-3 * np.eye(n)
+    y = rng.uniform(size=n)
+    ref = scipy.stats.multivariate_normal(mean, cov).logpdf(y)
+    assert np.isclose(O.gaussian_log_prob(mean, cov, y), ref, rtol=1e-10, atol=1e-10)
+
+
+@pytest.mark.parametrize("n_points", [10, 20])
+@pytest.mark.parametrize("n_dims", [1, 2, 3])
+@pytest.mark.parametrize("seed", [123, 42])
+def test_collapsed_elbo_equals_mll_when_z_is_x(n_points, n_dims, seed):
+    # tests/test_objectives.py:193-199: with Z = X the bound is tight
+    x, y = _data(n_points, n_dims, seed)
+    mll = O.conjugate_mll(O.RBF, x, y, 1.0, 1.0, 1.0, 0.0)
+    elbo = O.collapsed_elbo(O.RBF, x, y, x, 1.0, 1.0, 1.0, 0.0)
+    assert abs(elbo - mll) / abs(mll) < 1e-6
+
+
+@pytest.mark.parametrize("kind", [O.RBF, O.MATERN32, O.MATERN52])
+def test_lu_and_cholesky_forms_agree(kind):
+    x, y = _data(50, 3, 0)
+    ls = np.array([0.5, 1.0, 2.0])
+    a = O.conjugate_mll(kind, x, y, ls, 1.3, 0.2, 0.1)
+    b = O.conjugate_mll_cholesky(kind, x, y, ls, 1.3, 0.2, 0.1)
+    assert abs(a - b) <= 1e-10 * abs(a)
+
+
+@pytest.mark.parametrize("kind", [O.RBF, O.MATERN32, O.MATERN52])
+def test_mll_gradient_vs_finite_differences(kind):
+    x, y = _data(30, 2, 1)
+    ls, var, sd, c = np.array([0.7, 1.4]), 1.2, 0.3, 0.05
+    val, g = O.conjugate_mll_torch(kind, x, y, ls, var, sd, c)
+    assert np.isclose(val, O.conjugate_mll(kind, x, y, ls, var, sd, c), rtol=1e-12)
+    _, g_chol = O.conjugate_mll_torch(kind, x, y, ls, var, sd, c, lu=False)
+    vec = np.concatenate([ls, [var, sd, c]])
+
+    def f(v):
+        return O.conjugate_mll(kind, x, y, v[:2], v[2], v[3], v[4])
+    fd = O.central_fd(f, vec, 1e-6)
+    ad = np.concatenate([g["lengthscale"], [g["variance"], g["obs_stddev"], g["constant"]]])
+    adc = np.concatenate([g_chol["lengthscale"],
+                          [g_chol["variance"], g_chol["obs_stddev"], g_chol["constant"]]])
+    assert np.allclose(ad, fd, rtol=1e-5, atol=1e-6)
+    assert np.allclose(ad, adc, rtol=1e-10, atol=1e-10)
+
+
+def test_elbo_gradient_vs_finite_differences():
+    rng = np.random.default_rng(3)
+    x, y = _data(40, 2, 3)
+    z = rng.uniform(-2, 2, size=(7, 2))
+    ls, var, sd = np.array([0.8, 1.1]), 0.9, 0.25
+    val, g = O.collapsed_elbo_torch(O.RBF, x, y, z, ls, var, sd, 0.0)
+    assert np.isclose(val, O.collapsed_elbo(O.RBF, x, y, z, ls, var, sd, 0.0), rtol=1e-12)
+    fz = O.central_fd(lambda zz: O.collapsed_elbo(O.RBF, x, y, zz.reshape(7, 2), ls, var, sd),
+                      z.reshape(-1), 1e-6)
+    assert np.allclose(g["inducing_inputs"].reshape(-1), fz, rtol=1e-4, atol=1e-6)
+
+
+def test_predict_matches_direct_formula():
+    x, y = _data(40, 2, 5)
+    t = np.random.default_rng(9).uniform(-2, 2, size=(11, 2))
+    mean, cov = O.predict(O.MATERN52, x, y, t, 0.9, 1.1, 0.3, 0.2)
+    S = O.gram(O.MATERN52, x, 0.9, 1.1) + (1e-6 + 0.09) * np.eye(40)
+    Kxt = O.cross_covariance(O.MATERN52, x, t, 0.9, 1.1)
+    mean2 = 0.2 + Kxt.T @ np.linalg.solve(S, y[:, 0] - 0.2)
+    cov2 = O.gram(O.MATERN52, t, 0.9, 1.1) - Kxt.T @ np.linalg.solve(S, Kxt) + 1e-6 * np.eye(11)
+    assert np.allclose(mean, mean2, rtol=1e-10, atol=1e-10)
+    assert np.allclose(cov, cov2, rtol=1e-9, atol=1e-10)
+
+
+def test_golden_fixtures_reproduce():
+    """The committed fixtures (tests/golden) still match the oracle."""
+    import os
+    path = os.path.join(os.path.dirname(__file__), "golden", "golden_small.npz")
+    g = np.load(path)
+    for case in range(int(g["ncases"])):
+        p = lambda k: g[f"c{case}_{k}"]  # noqa: E731
+        kind = int(p("kind"))
+        val = O.conjugate_mll(kind, p("x"), p("y"), p("ls"), float(p("var")), float(p("sd")),
+                              float(p("c")))
+        assert np.isclose(val, float(p("mll")), rtol=1e-12, atol=1e-12)
