@@ -320,7 +320,9 @@ def run_gpu(args):
     launches = lib.gpk_launch_count() - launches0
     t_dev = max_over_ranks(e0.elapsed_time(e1) / 1000.0)
     mll_mixed, g_mixed = float(out.item()), grad.cpu().numpy().copy()
-    phase_names = ["gram", "cholesky", "trtri", "solve_refine", "adjoint", "finalize"]
+    # mixed form: "factor" is the recursive Cholesky that also forms L^-1, so
+    # "inverse" is empty; float64 form: the blocked Cholesky then the inverse
+    phase_names = ["gram", "factor", "inverse", "solve_refine", "adjoint", "finalize"]
     phases = {nm: float(np.mean([ph[s][k].elapsed_time(ph[s][k + 1]) for s in range(args.steps)]))
               for k, nm in enumerate(phase_names)}
 
@@ -385,7 +387,8 @@ def run_gpu(args):
         "config": {"workload": WORKLOAD, "n": n, "d": d, "kernel": "Matern52",
                    "precision": "mixed", "parallelism": "replicas" if world > 1 else "single",
                    "l2": "working set (3 x n^2 float32 = 3.2 GB) larger than L2; no flush"},
-        "roofline": {"bound": "tensor", "kernel": "lauum_grad (fused inverse product + adjoint)",
+        "roofline": {"bound": "tensor",
+                     "kernel": "tc_gemm_kernel<MODE_GRAD> (fused L^-T L^-1 product + adjoint)",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "peak_kind": f"{peak_kind} bf16 dense",
                      "traffic": ADJOINT_TRAFFIC_BYTES_N16384,

@@ -93,7 +93,8 @@ __global__ void __launch_bounds__(512) potrf_diag_kernel(T* A, int64_t lda, int 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int LD = NB + 1;
   double* Dd = reinterpret_cast<double*>(smem_raw);  // float64 diagonal of the block
-  T* S = reinterpret_cast<T*>(Dd + NB);
+  double* Pv = Dd + NB;                              // float64 pivots
+  T* S = reinterpret_cast<T*>(Pv + NB);
   T* col = S + NB * LD;
   T* dl = col + NB;
   const int nb = min(NB, n - k0);
@@ -107,7 +108,9 @@ __global__ void __launch_bounds__(512) potrf_diag_kernel(T* A, int64_t lda, int 
   __syncthreads();
   for (int j = 0; j < nb; ++j) {
     const double pivd = Dd[j];
-    const T ljj = (T)sqrt(pivd);  // NaN when the pivot is negative, as in the reference
+    // NaN when the pivot is negative, as in the reference; float64 square
+    // root only when the factor itself is float64
+    const T ljj = sizeof(T) == 8 ? (T)sqrt(pivd) : (T)sqrtf((float)pivd);
     for (int i = j + 1 + threadIdx.x; i < nb; i += blockDim.x) {
       T v = S[i * LD + j] / ljj;
       S[i * LD + j] = v;
@@ -115,8 +118,7 @@ __global__ void __launch_bounds__(512) potrf_diag_kernel(T* A, int64_t lda, int 
     }
     if (threadIdx.x == 0) {
       dl[j] = ljj;
-      if (logdiag) logdiag[k0 + j] = 0.5 * log(pivd);
-      if (!(pivd > 0.0)) atomicMin(info, k0 + j + 1);
+      Pv[j] = pivd;
     }
     __syncthreads();
     for (int i = j + 1 + warp; i < nb; i += nwarps) {
@@ -128,6 +130,10 @@ __global__ void __launch_bounds__(512) potrf_diag_kernel(T* A, int64_t lda, int 
       Dd[i] -= c * c;
     }
     __syncthreads();
+  }
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    if (logdiag) logdiag[k0 + i] = 0.5 * log(Pv[i]);
+    if (!(Pv[i] > 0.0)) atomicMin(info, k0 + i + 1);
   }
   for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
     int i = e / nb, j = e % nb;
@@ -213,7 +219,7 @@ template <typename T>
 cudaError_t potrf_lower(T* A, int64_t lda, int n, double* logdiag, int* info, double* dtrack,
                         bool zero_upper, cudaStream_t s) {
   constexpr int NB = Blk<T>::NB;
-  const size_t smem_diag = (size_t)(NB * (NB + 1) + 2 * NB) * sizeof(T) + NB * sizeof(double);
+  const size_t smem_diag = (size_t)(NB * (NB + 1) + 2 * NB) * sizeof(T) + 2 * NB * sizeof(double);
   const size_t smem_trsm = (size_t)(NB * (NB + 1) + 128 * (NB + 1) + NB) * sizeof(T);
   cudaFuncSetAttribute(potrf_diag_kernel<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)smem_diag);

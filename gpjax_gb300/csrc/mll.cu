@@ -23,9 +23,16 @@ void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 // Optional phase events (benchmark instrumentation), see gpk_set_profile_events.
 static cudaEvent_t g_prof_events[8];
 static int g_prof_count = 0;
-static inline void prof_mark(int k, cudaStream_t s) {
+void prof_mark(int k, cudaStream_t s) {
   if (k < g_prof_count && g_prof_events[k]) cudaEventRecord(g_prof_events[k], s);
 }
+
+// mixed_tc.cu
+size_t mll_tc_workspace_bytes(int64_t n, int d);
+bool mll_tc_supported(int d);
+gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, const double* y,
+                      const double* theta, int n_ls, double jitter, int refine, int want_grad,
+                      double* out_mll, double* out_grad, int* info, void* ws, cudaStream_t s);
 
 // Carves caller-provided workspace into 256-byte aligned regions.
 struct Arena {
@@ -175,6 +182,15 @@ __global__ void __launch_bounds__(256)
   out_grad[n_ls + 2] = inf ? nan : asum;
 }
 
+cudaError_t mll_finalize_launch(int n, int d, const double* theta, int n_ls, const double* logdiag,
+                                const double* diff, const double* alpha, const double* gpart,
+                                int ntiles, int want_grad, double jitter, int* info,
+                                double* out_mll, double* out_grad, cudaStream_t s) {
+  mll_finalize_kernel<<<1, 256, 0, s>>>(n, d, theta, n_ls, logdiag, diff, alpha, gpart, ntiles,
+                                        want_grad, jitter, info, out_mll, out_grad);
+  return launch_status();
+}
+
 __global__ void finish_info_kernel(int* info) {
   if (*info == INT_MAX) *info = 0;
 }
@@ -271,6 +287,7 @@ extern "C" size_t gpk_conjugate_mll_workspace_bytes(int64_t n, int d, int precis
     MllBuffers<double> b;
     return mll_layout<double>(n, d, nullptr, b);
   }
+  if (mll_tc_supported(d)) return mll_tc_workspace_bytes(n, d);
   MllBuffers<float> b;
   return mll_layout<float>(n, d, nullptr, b);
 }
@@ -295,6 +312,9 @@ extern "C" gpk_status gpk_conjugate_mll(int kind, int64_t n, int d, const double
   if (precision == GPK_PREC_FP64)
     return mll_run<double>(kind, (int)n, d, x, ldx, y, theta, n_ls, jitter, 1, want_grad, out_mll,
                            out_grad, info, workspace, stream);
+  if (mll_tc_supported(d))
+    return mll_run_tc(kind, (int)n, d, x, ldx, y, theta, n_ls, jitter, 2, want_grad, out_mll,
+                      out_grad, info, workspace, stream);
   return mll_run<float>(kind, (int)n, d, x, ldx, y, theta, n_ls, jitter, 2, want_grad, out_mll,
                         out_grad, info, workspace, stream);
 }

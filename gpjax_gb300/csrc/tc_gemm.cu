@@ -1,0 +1,673 @@
+// tcgen05 split-TF32 NT GEMM: kernel, tensor-map encoding and launch helpers.
+// See tc_gemm.cuh for the arithmetic.
+#include <mutex>
+#include "tc_gemm.cuh"
+
+namespace gpk {
+namespace tc {
+
+// ---------------------------------------------------------------------------
+// PTX wrappers (sm_100+ family)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: about two seconds of SM clock, or until another thread of the
+// CTA has given up (abort flag).  Returns false on timeout / abort.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+                                          int* err) {
+  const long long t0 = clock64();
+  for (uint32_t it = 0;; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((it & 255u) == 255u) {
+      if (*abort_flag) return false;
+      if (clock64() - t0 > 4000000000LL) {
+        *abort_flag = 1;
+        if (err) atomicExch(err, 1);
+        return false;
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// 128B-swizzled K-major shared-memory descriptor: rows of 128 B, 8-row groups
+// 1024 B apart (SBO), version bits 46..48 = 1, swizzle mode 2 (128B).
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)(16u >> 4) << 16;
+  d |= (uint64_t)(1024u >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
+// kind::tf32, float32 accumulate, K-major A and B, M = 128, N = 128
+__host__ __device__ constexpr uint32_t idesc_tf32(int m, int n) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+__device__ __forceinline__ float tf32_rna(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+__device__ __forceinline__ void split_tf32(float x, float& hi, float& lo) {
+  hi = tf32_rna(x);
+  lo = tf32_rna(x - hi);
+}
+
+// ---------------------------------------------------------------------------
+// The kernel
+// ---------------------------------------------------------------------------
+struct SmemCtl {
+  uint64_t full[STAGES];
+  uint64_t empty[STAGES];
+  uint64_t tfull[4];   // accumulator segment ready (MMA -> epilogue)
+  uint64_t tempty[4];  // accumulator segment drained (epilogue -> MMA)
+  uint32_t tmem;
+  int abort_flag;
+};
+
+// The tensor-core float32 accumulator rounds less carefully than an FMA, so
+// each accumulator only sums SEG_CHUNKS x 32 K-elements (12 MMA steps per
+// chunk); the epilogue warps drain finished segments into round-to-nearest
+// float32 registers while the MMA thread fills the next of NBUF TMEM buffers.
+constexpr int SEG_CHUNKS = 1;
+constexpr int NBUF = 4;
+constexpr int TLD = BN + 4;    // staged output tile row stride (floats)
+
+template <int MODE>
+__global__ void __launch_bounds__(NUM_THREADS, 1)
+    tc_gemm_kernel(const __grid_constant__ CUtensorMap ta_hi, const __grid_constant__ CUtensorMap ta_lo,
+                   const __grid_constant__ CUtensorMap tb_hi, const __grid_constant__ CUtensorMap tb_lo,
+                   const __grid_constant__ TcParams p) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* tiles = reinterpret_cast<uint8_t*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  SmemCtl* ctl = reinterpret_cast<SmemCtl*>(tiles + STAGES * STAGE_BYTES);
+  float* gx = reinterpret_cast<float*>(ctl + 1);  // MODE_GRAD: column points and alphas
+  float* ga = gx + BN * GRAD_DMAX;
+  double* gred = reinterpret_cast<double*>(ga + BN);
+  float* otile = reinterpret_cast<float*>(tiles);  // output tile, reuses the operand ring
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int z = blockIdx.z;
+  int I, J;
+  if (p.c_lower) {
+    const int t = blockIdx.x;
+    int i = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while (i * (i + 1) / 2 > t) --i;
+    while ((i + 1) * (i + 2) / 2 <= t) ++i;
+    I = i;
+    J = t - i * (i + 1) / 2;
+  } else {
+    I = blockIdx.x / p.tiles_n;
+    J = blockIdx.x % p.tiles_n;
+  }
+  const int i0 = I * BM, j0 = J * BN;
+  int klo = 0, khi = p.K;
+  if (p.a_tri == TRI_LOWER) khi = min(khi, i0 + BM);
+  if (p.a_tri == TRI_UPPER) klo = max(klo, i0);
+  if (p.b_tri == TRI_LOWER) khi = min(khi, j0 + BN);
+  if (p.b_tri == TRI_UPPER) klo = max(klo, j0);
+  klo = (klo / BK) * BK;
+  const int nk = khi > klo ? (khi - klo + BK - 1) / BK : 0;
+  const int nseg = (nk + SEG_CHUNKS - 1) / SEG_CHUNKS;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&ctl->full[s], 1);
+      mbar_init(&ctl->empty[s], 1);
+    }
+    for (int b = 0; b < NBUF; ++b) {
+      mbar_init(&ctl->tfull[b], 1);
+      mbar_init(&ctl->tempty[b], 4);  // one arrival per epilogue warp
+    }
+    ctl->abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&ctl->tmem)),
+                 "r"(NBUF * BN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = ctl->tmem;
+  volatile int* abort_flag = &ctl->abort_flag;
+
+  if (warp == 0) {
+    if (lane == 0 && nk > 0) {
+      const int ay = i0 + p.a_row0 + z * p.a_zrow, ax0 = p.a_col0 + z * p.a_zcol;
+      const int by = j0 + p.b_row0 + z * p.b_zrow, bx0 = p.b_col0 + z * p.b_zcol;
+      int issued = 0;
+      for (int kc = 0; kc < nk; ++kc) {
+        const int s = kc % STAGES;
+        if (kc >= STAGES) {
+          if (!mbar_wait(&ctl->empty[s], ((kc / STAGES) - 1) & 1, abort_flag, p.err)) break;
+        }
+        uint8_t* st = tiles + s * STAGE_BYTES;
+        const int k = klo + kc * BK;
+        mbar_expect_tx(&ctl->full[s], STAGE_BYTES);
+        tma_load_2d(st + 0 * TILE_BYTES, &ta_hi, ax0 + k, ay, &ctl->full[s]);
+        tma_load_2d(st + 1 * TILE_BYTES, &ta_lo, ax0 + k, ay, &ctl->full[s]);
+        tma_load_2d(st + 2 * TILE_BYTES, &tb_hi, bx0 + k, by, &ctl->full[s]);
+        tma_load_2d(st + 3 * TILE_BYTES, &tb_lo, bx0 + k, by, &ctl->full[s]);
+        ++issued;
+      }
+      if (*abort_flag) {
+        // drain the copies this thread issued before returning
+        for (int kc = max(0, issued - STAGES); kc < issued; ++kc)
+          mbar_wait(&ctl->full[kc % STAGES], (kc / STAGES) & 1, abort_flag, nullptr);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = idesc_tf32(BM, BN);
+      bool ok = true;
+      for (int kc = 0; kc < nk && ok; ++kc) {
+        const int seg = kc / SEG_CHUNKS, b = seg % NBUF;
+        const uint32_t tacc = tmem + (uint32_t)(b * BN);
+        if (kc % SEG_CHUNKS == 0 && seg >= NBUF) {
+          ok = mbar_wait(&ctl->tempty[b], ((seg / NBUF) - 1) & 1, abort_flag, p.err);
+          if (!ok) break;
+          tc_fence_after();
+        }
+        const int s = kc % STAGES;
+        ok = mbar_wait(&ctl->full[s], (kc / STAGES) & 1, abort_flag, p.err);
+        if (!ok) break;
+        tc_fence_after();
+        const uint32_t sb = smem_u32(tiles + s * STAGE_BYTES);
+        const uint64_t ahi = sdesc(sb), alo = sdesc(sb + TILE_BYTES);
+        const uint64_t bhi = sdesc(sb + 2 * TILE_BYTES), blo = sdesc(sb + 3 * TILE_BYTES);
+        const bool first = (kc % SEG_CHUNKS) == 0;
+#pragma unroll
+        for (int k4 = 0; k4 < BK / 8; ++k4) {
+          const uint64_t off = (uint64_t)((k4 * 32) >> 4);  // 32 bytes per K = 8 step
+          mma_tf32(tacc, alo + off, bhi + off, idesc, (first && k4 == 0) ? 0u : 1u);
+          mma_tf32(tacc, ahi + off, blo + off, idesc, 1u);
+          mma_tf32(tacc, ahi + off, bhi + off, idesc, 1u);
+        }
+        mma_commit(&ctl->empty[s]);
+        if (kc % SEG_CHUNKS == SEG_CHUNKS - 1 || kc == nk - 1) mma_commit(&ctl->tfull[b]);
+      }
+    }
+    __syncwarp();
+  } else {
+    // ---------------- epilogue warps 2..5 ----------------
+    const int q = warp & 3;  // TMEM lane quarter this warp may access
+    const int ew = warp - 2;
+    const int r = q * 32 + lane;
+    const int gi = i0 + r;  // row within the problem
+    const int et = threadIdx.x - 64;
+    if (MODE == MODE_GRAD) {
+      for (int e = et; e < BN * GRAD_DMAX; e += 128) {
+        const int c = e / GRAD_DMAX, k = e % GRAD_DMAX;
+        const int gj = j0 + c;
+        gx[e] = (gj < p.n_true && k < p.d) ? p.xs[(int64_t)gj * p.d + k] : 0.f;
+      }
+      for (int c = et; c < BN; c += 128) {
+        const int gj = j0 + c;
+        ga[c] = gj < p.n_true ? (float)p.avec[gj] : 0.f;
+      }
+    }
+    // drain the accumulator segments into float32 registers (round to nearest)
+    float acc[BN];
+#pragma unroll
+    for (int c = 0; c < BN; ++c) acc[c] = 0.f;
+    bool have = true;
+    for (int seg = 0; seg < nseg; ++seg) {
+      const int b = seg % NBUF;
+      have = __all_sync(0xffffffffu, mbar_wait(&ctl->tfull[b], (seg / NBUF) & 1, abort_flag, p.err));
+      if (!have) break;
+      tc_fence_after();
+      const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN);
+#pragma unroll
+      for (int cb = 0; cb < BN / 32; ++cb) {
+        float v[32];
+        tmem_ld32(tb + cb * 32, v);
+#pragma unroll
+        for (int k = 0; k < 32; ++k) acc[cb * 32 + k] += v[k];
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(
+                                      smem_u32(&ctl->tempty[b]))
+                                  : "memory");
+    }
+    if (MODE == MODE_ADD_F32 || MODE == MODE_STORE_SPLIT) {
+      // dtrack: sum of squares of this row's outputs (float64)
+      if (MODE == MODE_STORE_SPLIT && p.dtrack && have && gi < p.M) {
+        double dsum = 0.0;
+#pragma unroll
+        for (int c = 0; c < BN; ++c) {
+          const float w = p.alpha * acc[c];
+          if (j0 + c < p.N) dsum += (double)w * (double)w;
+        }
+        atomicAdd(&p.dtrack[p.c_row0 + (int64_t)z * p.c_zrow + gi], -dsum);
+      }
+      // stage the tile, then write whole rows (coalesced, 4 floats per lane)
+      asm volatile("bar.sync 1, 128;" ::: "memory");  // all segments drained: ring is free
+#pragma unroll
+      for (int c = 0; c < BN; c += 4)
+        *reinterpret_cast<float4*>(&otile[r * TLD + c]) =
+            have ? make_float4(p.alpha * acc[c], p.alpha * acc[c + 1], p.alpha * acc[c + 2],
+                               p.alpha * acc[c + 3])
+                 : make_float4(0.f, 0.f, 0.f, 0.f);
+      asm volatile("bar.sync 1, 128;" ::: "memory");
+      if (have) {
+        const int64_t crow0 = p.c_row0 + (int64_t)z * p.c_zrow + i0;
+        const int64_t ccol = p.c_col0 + (int64_t)z * p.c_zcol + j0;
+        const int c4 = lane * 4;
+        if (p.c0) {
+          for (int rr = ew; rr < BM; rr += 4) {
+            const int grow = i0 + rr;
+            if (grow >= p.M) break;
+            const float4 w4 = *reinterpret_cast<const float4*>(&otile[rr * TLD + c4]);
+            const float wv[4] = {w4.x, w4.y, w4.z, w4.w};
+            const int64_t base = (crow0 + rr) * p.ldc + ccol + c4;
+            const bool full4 = (j0 + c4 + 3 < p.N) && !(p.c_lower && j0 + c4 + 3 > grow) &&
+                               ((base & 3) == 0);
+            if (MODE == MODE_ADD_F32) {
+              if (full4) {
+                float4 cv = *reinterpret_cast<float4*>(p.c0 + base);
+                cv.x += wv[0];
+                cv.y += wv[1];
+                cv.z += wv[2];
+                cv.w += wv[3];
+                *reinterpret_cast<float4*>(p.c0 + base) = cv;
+              } else {
+                for (int k = 0; k < 4; ++k) {
+                  const int gj = j0 + c4 + k;
+                  if (gj < p.N && !(p.c_lower && gj > grow)) p.c0[base + k] += wv[k];
+                }
+              }
+            } else {
+              float hv[4], lv[4];
+#pragma unroll
+              for (int k = 0; k < 4; ++k) split_tf32(wv[k], hv[k], lv[k]);
+              if (full4) {
+                *reinterpret_cast<float4*>(p.c0 + base) = make_float4(hv[0], hv[1], hv[2], hv[3]);
+                *reinterpret_cast<float4*>(p.c1 + base) = make_float4(lv[0], lv[1], lv[2], lv[3]);
+              } else {
+                for (int k = 0; k < 4; ++k) {
+                  const int gj = j0 + c4 + k;
+                  if (gj < p.N && !(p.c_lower && gj > grow)) {
+                    p.c0[base + k] = hv[k];
+                    p.c1[base + k] = lv[k];
+                  }
+                }
+              }
+            }
+          }
+        }
+        if (MODE == MODE_STORE_SPLIT && p.t0) {
+          // transposed: output row = tile column j, lanes over tile rows i
+          const int64_t trow0 = p.t_row0 + (int64_t)z * p.t_zrow + j0;
+          const int64_t tcol = p.t_col0 + (int64_t)z * p.t_zcol + i0;
+          for (int cc = ew; cc < BN; cc += 4) {
+            if (j0 + cc >= p.N) break;
+            const int64_t base = (trow0 + cc) * p.ldt + tcol;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              const int ii = lane + 32 * k;  // 32 consecutive rows -> one coalesced line
+              if (i0 + ii < p.M) {
+                float hv, lv;
+                split_tf32(otile[ii * TLD + cc], hv, lv);
+                p.t0[base + ii] = hv;
+                p.t1[base + ii] = lv;
+              }
+            }
+          }
+        }
+      }
+    }
+    if (MODE == MODE_GRAD) {
+      asm volatile("bar.sync 1, 128;" ::: "memory");  // gx / ga staged
+      // W tile -> reduction against dK/dtheta (unit variance); an aborted wait
+      // contributes zeros but still joins the reduction barrier
+      float xi[GRAD_DMAX];
+#pragma unroll
+      for (int k = 0; k < GRAD_DMAX; ++k)
+        xi[k] = (gi < p.n_true && k < p.d) ? p.xs[(int64_t)gi * p.d + k] : 0.f;
+      const float ai = gi < p.n_true ? (float)p.avec[gi] : 0.f;
+      double gl[GRAD_DMAX];
+#pragma unroll
+      for (int k = 0; k < GRAD_DMAX; ++k) gl[k] = 0.0;
+      double gnoise = 0.0, gvar = 0.0;
+#pragma unroll
+      for (int cb = 0; cb < BN / 32; ++cb) {
+        float pl[GRAD_DMAX];
+#pragma unroll
+        for (int k = 0; k < GRAD_DMAX; ++k) pl[k] = 0.f;
+        float pvar = 0.f;
+#pragma unroll
+        for (int k = 0; k < 32; ++k) {
+          const int c = cb * 32 + k;
+          const int gj = j0 + c;
+          if (!have || gi >= p.n_true || gj >= p.n_true || gj > gi) continue;
+          const float w = acc[c];
+          const float f = (gi == gj) ? 1.f : 2.f;
+          const float coef = f * (ai * ga[c] - w);
+          float dsq[GRAD_DMAX];
+          float sq = 0.f;
+#pragma unroll
+          for (int kk = 0; kk < GRAD_DMAX; ++kk) {
+            const float df = xi[kk] - gx[c * GRAD_DMAX + kk];
+            dsq[kk] = df * df;
+            sq += dsq[kk];
+          }
+          float k1, c1;
+          kval_dcoef<float>(p.kind, sq, 1.f, k1, c1);
+          pvar = fmaf(coef, k1, pvar);
+          const float cc = coef * c1;
+#pragma unroll
+          for (int kk = 0; kk < GRAD_DMAX; ++kk) pl[kk] = fmaf(cc, dsq[kk], pl[kk]);
+          if (gi == gj) gnoise += (double)ai * (double)ai - (double)w;
+        }
+#pragma unroll
+        for (int kk = 0; kk < GRAD_DMAX; ++kk) gl[kk] += (double)pl[kk];
+        gvar += (double)pvar;
+      }
+      // reduce over the 4 epilogue warps into gpart[tile]
+      const int slots = p.d + 2;
+      for (int sidx = 0; sidx < slots; ++sidx) {
+        double val;
+        if (sidx < p.d) {
+          val = 0.0;
+#pragma unroll
+          for (int kk = 0; kk < GRAD_DMAX; ++kk)
+            if (kk == sidx) val = gl[kk];
+        } else if (sidx == p.d) {
+          val = gvar;
+        } else {
+          val = gnoise;
+        }
+        val = warp_sum(val);
+        if (lane == 0) gred[sidx * 4 + ew] = val;
+      }
+      asm volatile("bar.sync 1, 128;" ::: "memory");
+      const int tile_id = blockIdx.x + (int)gridDim.x * z;
+      for (int sidx = et; sidx < slots; sidx += 128) {
+        const double tot =
+            ((gred[sidx * 4] + gred[sidx * 4 + 1]) + gred[sidx * 4 + 2]) + gred[sidx * 4 + 3];
+        p.gpart[(int64_t)tile_id * slots + sidx] = tot;
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(NBUF * BN)
+                 : "memory");
+  }
+}
+
+// ---------------------------------------------------------------------------
+// TF32 split of a float32 matrix
+// ---------------------------------------------------------------------------
+__global__ void tf32_split_kernel(const float* __restrict__ src, int64_t lds, int rows, int cols,
+                                  float* __restrict__ hi, float* __restrict__ lo, int64_t ldo) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (int64_t)rows * cols) return;
+  const int r = (int)(e / cols), c = (int)(e % cols);
+  float h, l;
+  split_tf32(src[(int64_t)r * lds + c], h, l);
+  hi[(int64_t)r * ldo + c] = h;
+  lo[(int64_t)r * ldo + c] = l;
+}
+
+}  // namespace tc
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(f);
+  });
+  return fn;
+}
+
+// float32 row-major [rows, cols] with leading dimension ld; box 32 x 128, 128B swizzle
+static bool make_map(CUtensorMap* m, const float* base, int64_t rows, int64_t cols, int64_t ld) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  if ((reinterpret_cast<uintptr_t>(base) & 15u) != 0 || ((ld * 4) & 15) != 0) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)(ld * 4)};
+  cuuint32_t box[2] = {(cuuint32_t)tc::BK, (cuuint32_t)tc::BM};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides,
+                  box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+static size_t tc_smem_bytes() {
+  return 1024 + (size_t)tc::STAGES * tc::STAGE_BYTES + sizeof(tc::SmemCtl) +
+         (size_t)tc::BN * tc::GRAD_DMAX * 4 + tc::BN * 4 + 64 * sizeof(double) + 64;
+}
+
+bool tc_make_map(TcMap* m, const float* hi, const float* lo, int64_t rows, int64_t cols,
+                 int64_t ld) {
+  return make_map(&m->hi, hi, rows, cols, ld) && make_map(&m->lo, lo, rows, cols, ld);
+}
+
+cudaError_t tc_gemm_run(int mode, const TcMap& A, const TcMap& B, const tc::TcParams& p0,
+                        int batch, cudaStream_t s) {
+  if (p0.M <= 0 || p0.N <= 0 || batch <= 0) return cudaSuccess;
+  tc::TcParams p = p0;
+  p.tiles_m = (p.M + tc::BM - 1) / tc::BM;
+  p.tiles_n = (p.N + tc::BN - 1) / tc::BN;
+  const int tiles = p.c_lower ? p.tiles_m * (p.tiles_m + 1) / 2 : p.tiles_m * p.tiles_n;
+  dim3 grid(tiles, 1, batch);
+  const size_t smem = tc_smem_bytes();
+  switch (mode) {
+    case tc::MODE_ADD_F32:
+      cudaFuncSetAttribute(tc::tc_gemm_kernel<tc::MODE_ADD_F32>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      tc::tc_gemm_kernel<tc::MODE_ADD_F32><<<grid, tc::NUM_THREADS, smem, s>>>(A.hi, A.lo, B.hi,
+                                                                             B.lo, p);
+      break;
+    case tc::MODE_STORE_SPLIT:
+      cudaFuncSetAttribute(tc::tc_gemm_kernel<tc::MODE_STORE_SPLIT>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      tc::tc_gemm_kernel<tc::MODE_STORE_SPLIT><<<grid, tc::NUM_THREADS, smem, s>>>(A.hi, A.lo,
+                                                                                 B.hi, B.lo, p);
+      break;
+    case tc::MODE_GRAD:
+      cudaFuncSetAttribute(tc::tc_gemm_kernel<tc::MODE_GRAD>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      tc::tc_gemm_kernel<tc::MODE_GRAD><<<grid, tc::NUM_THREADS, smem, s>>>(A.hi, A.lo, B.hi, B.lo,
+                                                                          p);
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
+  return launch_status();
+}
+
+cudaError_t tc_gemm_launch(int mode, const TcMat& A, const TcMat& B, const tc::TcParams& p,
+                           int batch, cudaStream_t s) {
+  TcMap ma, mb;
+  if (!tc_make_map(&ma, A.hi, A.lo, A.rows, A.cols, A.ld) ||
+      !tc_make_map(&mb, B.hi, B.lo, B.rows, B.cols, B.ld))
+    return cudaErrorInvalidValue;
+  return tc_gemm_run(mode, ma, mb, p, batch, s);
+}
+
+cudaError_t tf32_split(const float* src, int64_t lds, int rows, int cols, float* hi, float* lo,
+                       int64_t ldo, cudaStream_t s) {
+  const int64_t total = (int64_t)rows * cols;
+  if (total <= 0) return cudaSuccess;
+  tc::tf32_split_kernel<<<(int)cdiv(total, 256), 256, 0, s>>>(src, lds, rows, cols, hi, lo, ldo);
+  return launch_status();
+}
+
+}  // namespace gpk
+
+// ---------------------------------------------------------------------------
+// C ABI: standalone split-TF32 GEMM, C = beta*C + alpha * A B^T
+// ---------------------------------------------------------------------------
+using namespace gpk;
+
+static size_t gemm_ws_layout(int64_t M, int64_t N, int64_t K, void* ws, float** ahi, float** alo,
+                             float** bhi, float** blo, int64_t* ldk) {
+  const int64_t ld = ((K + 31) / 32) * 32;
+  *ldk = ld;
+  char* b = static_cast<char*>(ws);
+  size_t off = 0;
+  auto take = [&](int64_t rows) {
+    off = (off + 255) & ~size_t(255);
+    float* p = b ? reinterpret_cast<float*>(b + off) : nullptr;
+    off += (size_t)rows * ld * 4;
+    return p;
+  };
+  *ahi = take(M);
+  *alo = take(M);
+  *bhi = take(N);
+  *blo = take(N);
+  return off + 256;
+}
+
+extern "C" size_t gpk_gemm_tf32x3_workspace_bytes(int64_t M, int64_t N, int64_t K) {
+  float *a, *b, *c, *d;
+  int64_t ld;
+  return gemm_ws_layout(M, N, K, nullptr, &a, &b, &c, &d, &ld);
+}
+
+__global__ void scale_matrix_kernel(float* C, int64_t ldc, int M, int N, float beta) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (int64_t)M * N) return;
+  float* p = C + (e / N) * ldc + (e % N);
+  *p = beta == 0.f ? 0.f : beta * *p;
+}
+
+extern "C" gpk_status gpk_gemm_tf32x3(int64_t M, int64_t N, int64_t K, float alpha,
+                                      const float* A, int64_t lda, const float* B, int64_t ldb,
+                                      float beta, float* C, int64_t ldc, int lower_only,
+                                      int* err_flag, void* workspace, size_t workspace_bytes,
+                                      cudaStream_t stream) {
+  if (M < 0 || N < 0 || K < 0 || lda < K || ldb < K || ldc < N) return GPK_ERR_BAD_ARG;
+  if (M > (1 << 24) || N > (1 << 24) || K > (1 << 24)) return GPK_ERR_BAD_ARG;
+  if (lower_only && M != N) return GPK_ERR_BAD_ARG;
+  if (M == 0 || N == 0) return GPK_OK;
+  if (!A || !B || !C || !workspace) return GPK_ERR_BAD_ARG;
+  if (workspace_bytes < gpk_gemm_tf32x3_workspace_bytes(M, N, K)) return GPK_ERR_WORKSPACE;
+  float *ahi, *alo, *bhi, *blo;
+  int64_t ld;
+  gemm_ws_layout(M, N, K, workspace, &ahi, &alo, &bhi, &blo, &ld);
+  if (beta != 1.f) {
+    scale_matrix_kernel<<<(int)cdiv(M * N, 256), 256, 0, stream>>>(C, ldc, (int)M, (int)N, beta);
+    GPK_LAUNCH_CHECK();
+  }
+  if (K == 0) return GPK_OK;
+  GPK_CUDA_TRY(tf32_split(A, lda, (int)M, (int)K, ahi, alo, ld, stream));
+  GPK_CUDA_TRY(tf32_split(B, ldb, (int)N, (int)K, bhi, blo, ld, stream));
+  tc::TcParams p{};
+  p.M = (int)M;
+  p.N = (int)N;
+  p.K = (int)K;
+  p.c_lower = lower_only ? 1 : 0;
+  p.c0 = C;
+  p.ldc = ldc;
+  p.alpha = alpha;
+  p.err = err_flag;
+  TcMat a{ahi, alo, M, K, ld}, b{bhi, blo, N, K, ld};
+  GPK_CUDA_TRY(tc_gemm_launch(tc::MODE_ADD_F32, a, b, p, 1, stream));
+  return GPK_OK;
+}

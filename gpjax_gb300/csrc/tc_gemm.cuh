@@ -1,0 +1,79 @@
+// Split-TF32 NT GEMM on the 5th-generation tensor cores (tcgen05, sm_103a).
+//
+//   acc[i, j] = sum_k A[i, k] B[j, k],  A = A_hi + A_lo, B = B_hi + B_lo
+//   computed as A_lo B_hi + A_hi B_lo + A_hi B_hi
+// where *_hi is the operand rounded to TF32 and *_lo the TF32 rounding of the
+// remainder (both stored as float32 bit patterns with zero low 13 bits), which
+// recovers float32-class products on the TF32 pipe.  Operands are staged by
+// TMA (128B swizzle) into a 3-stage shared-memory ring, one elected thread
+// issues tcgen05.mma into a 128x128 float32 accumulator in tensor memory, and
+// four epilogue warps read it back with tcgen05.ld and apply a fused epilogue
+// (trailing update, split store with optional transpose, or the MLL adjoint
+// reduction).  Every mbarrier wait is bounded: on timeout the CTA sets an
+// error flag, drains its own copies and returns.
+#pragma once
+#include <cuda.h>
+#include "gpk_internal.cuh"
+
+namespace gpk {
+namespace tc {
+
+constexpr int BM = 128, BN = 128, BK = 32;
+constexpr int STAGES = 3;
+constexpr int TILE_BYTES = BM * BK * 4;        // 16 KB: 128 rows x 128 B
+constexpr int STAGE_BYTES = 4 * TILE_BYTES;    // A_hi, A_lo, B_hi, B_lo
+constexpr int NUM_THREADS = 192;               // w0 TMA, w1 MMA + TMEM, w2..w5 epilogue
+constexpr int GRAD_DMAX = 16;                  // largest input dimension of the adjoint epilogue
+
+enum Mode { MODE_ADD_F32 = 0, MODE_STORE_SPLIT = 1, MODE_GRAD = 2 };
+
+struct TcParams {
+  int M, N, K;
+  int a_row0, a_col0, b_row0, b_col0;   // origin of A and B inside their tensor maps
+  int a_zrow, a_zcol, b_zrow, b_zcol;   // per-batch (blockIdx.z) origin increments
+  int a_tri, b_tri, c_lower;
+  int tiles_m, tiles_n;
+  // outputs (MODE_ADD_F32: c0 += alpha*acc; MODE_STORE_SPLIT: hi/lo of alpha*acc
+  // into c0/c1 at (i, j) and t0/t1 at (j, i))
+  float *c0, *c1, *t0, *t1;
+  int64_t ldc, ldt;
+  int64_t c_row0, c_col0, c_zrow, c_zcol;
+  int64_t t_row0, t_col0, t_zrow, t_zcol;
+  float alpha;
+  double* dtrack;  // optional: dtrack[c_row0 + i] -= sum_j (alpha*acc)^2
+  // adjoint epilogue
+  int n_true, d, kind;
+  const float* xs;
+  const double* avec;
+  double* gpart;
+  int* err;
+};
+
+}  // namespace tc
+
+// Host helpers (tc_gemm.cu).
+struct TcMat {
+  const float* hi;
+  const float* lo;
+  int64_t rows, cols, ld;  // extent of the whole array the tensor map covers
+};
+
+// Launches one (batched) split-TF32 NT GEMM; maps are encoded from A and B.
+cudaError_t tc_gemm_launch(int mode, const TcMat& A, const TcMat& B, const tc::TcParams& p,
+                           int batch, cudaStream_t s);
+
+// Pre-encoded hi/lo tensor maps of one split operand array (encode once per
+// call, reuse for every GEMM that reads the array at some origin).
+struct TcMap {
+  CUtensorMap hi, lo;
+};
+bool tc_make_map(TcMap* m, const float* hi, const float* lo, int64_t rows, int64_t cols,
+                 int64_t ld);
+cudaError_t tc_gemm_run(int mode, const TcMap& A, const TcMap& B, const tc::TcParams& p,
+                        int batch, cudaStream_t s);
+
+// hi/lo TF32 split of a float32 matrix (rows x cols, ld) into hi/lo (ldo).
+cudaError_t tf32_split(const float* src, int64_t lds, int rows, int cols, float* hi, float* lo,
+                       int64_t ldo, cudaStream_t s);
+
+}  // namespace gpk

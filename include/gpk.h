@@ -167,6 +167,21 @@ gpk_status gpk_predict(int kind, int64_t n, int64_t t, int d,
                        int* info, void* workspace, size_t workspace_bytes,
                        cudaStream_t stream);
 
+/* ---------------------------------------------------------------------------
+ * Split-TF32 tensor-core GEMM (no counterpart in the reference; the building
+ * block of the mixed form).  C = beta*C + alpha * A B^T with A [M, K],
+ * B [N, K], C [M, N] float32 row-major, computed on tcgen05 as
+ * A_lo B_hi + A_hi B_lo + A_hi B_hi with float32 accumulation.  lower_only
+ * (M == N) updates only i >= j.  err_flag (optional device int) is set to 1
+ * if a device-side wait timed out.  workspace: gpk_gemm_tf32x3_workspace_bytes.
+ * ------------------------------------------------------------------------- */
+size_t gpk_gemm_tf32x3_workspace_bytes(int64_t M, int64_t N, int64_t K);
+gpk_status gpk_gemm_tf32x3(int64_t M, int64_t N, int64_t K, float alpha,
+                           const float* A, int64_t lda, const float* B, int64_t ldb,
+                           float beta, float* C, int64_t ldc, int lower_only,
+                           int* err_flag, void* workspace, size_t workspace_bytes,
+                           cudaStream_t stream);
+
 #ifdef __cplusplus
 }
 #endif
