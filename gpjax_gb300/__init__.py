@@ -6,11 +6,12 @@ variational_families, Dataset.  All arithmetic runs in libgpk.so (CUDA,
 sm_103a) through its C ABI (include/gpk.h).
 """
 from . import (computations, config, distributions, gps, kernels, likelihoods, linalg,
-               mean_functions, objectives, parameters)
+               mean_functions, objectives, parameters, variational_families)
 from ._lib import GPKError
 from .dataset import Dataset
 
 __version__ = "0.1.0"
 
 __all__ = ["Dataset", "GPKError", "computations", "config", "distributions", "gps", "kernels",
-           "likelihoods", "linalg", "mean_functions", "objectives", "parameters"]
+           "likelihoods", "linalg", "mean_functions", "objectives", "parameters",
+           "variational_families"]

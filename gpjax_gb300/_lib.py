@@ -34,6 +34,10 @@ SIGNATURES = {
                                       _c_i64, _c_ptr, _c_int, _c_int, _c_ptr, _c_i64, _c_ptr]),
     "gpk_gram": (_c_int, [_c_int, _c_i64, _c_int, _c_ptr, _c_i64, _c_ptr, _c_int, _c_int, _c_ptr,
                           _c_i64, _c_ptr]),
+    "gpk_cross_covariance_vjp_workspace_bytes": (_c_size, [_c_i64, _c_i64, _c_int]),
+    "gpk_cross_covariance_vjp": (_c_int, [_c_int, _c_i64, _c_i64, _c_int, _c_ptr, _c_i64, _c_ptr,
+                                          _c_i64, _c_ptr, _c_int, _c_ptr, _c_i64, _c_ptr, _c_ptr,
+                                          _c_ptr, _c_ptr, _c_size, _c_ptr]),
     "gpk_diagonal": (_c_int, [_c_int, _c_i64, _c_int, _c_ptr, _c_i64, _c_ptr, _c_int, _c_ptr,
                               _c_ptr]),
     "gpk_lower_cholesky": (_c_int, [_c_i64, _c_int, _c_ptr, _c_i64, _c_ptr, _c_ptr, _c_ptr]),

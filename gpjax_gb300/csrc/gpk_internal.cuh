@@ -67,7 +67,8 @@ cudaError_t scale_inputs(const double* x, int64_t ldx, int n, int d, const doubl
                          T* xs, cudaStream_t s);
 
 // Gram/cross-covariance from scaled inputs.  mode 0: out = K(xs, ys) full;
-// mode 1: lower triangle of K(xs, xs) + diag_add*I with zeros above the diagonal.
+// mode 1: lower triangle of (K(xs, xs) + jitter I) + obs_stddev^2 I with zeros
+// above the diagonal; mode 2: the same without the noise term.
 template <typename T, typename TO>
 cudaError_t cross_cov_scaled(int kind, int n, int m, int d, const T* xs, const T* ys,
                              const double* theta, int n_ls, int mode, double diag_add, TO* out,

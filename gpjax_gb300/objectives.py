@@ -89,3 +89,64 @@ def named_parameters(model) -> dict:
                 walk(v, name + ".", seen)
     walk(model, "", set())
     return found
+
+
+class _CollapsedELBO(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, theta, z, x, y, kind, n_ls, jitter, prec):
+        dev = _lib.require_cuda(x, y, theta, z)
+        n, d = x.shape
+        m = z.shape[0]
+        want = bool(ctx.needs_input_grad[0] or ctx.needs_input_grad[1])
+        th = theta.detach().contiguous()
+        xc, yc = x.detach().contiguous(), y.detach().reshape(-1).contiguous()
+        zc = z.detach().to(torch.float64).contiguous()
+        out = torch.empty(1, dtype=torch.float64, device=dev)
+        grad = torch.zeros(n_ls + 3, dtype=torch.float64, device=dev)
+        gz = torch.zeros((m, d), dtype=torch.float64, device=dev)
+        info = torch.zeros(1, dtype=torch.int32, device=dev)
+        nbytes = _lib.lib().gpk_collapsed_elbo_workspace_bytes(n, m, d, prec)
+        ws = _lib.workspace(nbytes, dev)
+        _lib.call("gpk_collapsed_elbo", kind, n, m, d, xc.data_ptr(), d, yc.data_ptr(),
+                  zc.data_ptr(), d, th.data_ptr(), n_ls, float(jitter), prec, int(want),
+                  out.data_ptr(), grad.data_ptr(), gz.data_ptr(), info.data_ptr(), ws.data_ptr(),
+                  ws.numel(), _lib.stream_ptr(dev))
+        ctx.save_for_backward(grad, gz)
+        ctx.info = info
+        return out[0]
+
+    @staticmethod
+    def backward(ctx, g):
+        grad, gz = ctx.saved_tensors
+        return g * grad, g * gz, None, None, None, None, None, None
+
+
+def collapsed_elbo(variational_family, data, precision: str | None = None) -> torch.Tensor:
+    """SGPR collapsed evidence lower bound (objectives.py:321-416), differentiable
+    w.r.t. the kernel, likelihood and mean parameters and the inducing inputs."""
+    q = variational_family
+    post = q.posterior
+    kernel = post.prior.kernel
+    x = kernel.slice_input(data.X)
+    dev = _lib.require_cuda(x)
+    z = kernel.slice_input(q.inducing_inputs.value.to(dev))
+    const = _mean_constant(post.prior.mean_function, dev)
+    theta = kernel.theta_vector(dev, post.likelihood.obs_stddev.value, const)
+    return _CollapsedELBO.apply(theta, z, x, data.y, kernel.kind, kernel.n_ls, float(q.jitter),
+                                precision_code(precision))
+
+
+def cross_covariance_vjp(kind, n_ls, theta, x, y, G, need_x=False, need_y=False):
+    """Cotangent of K(x, y) -> (d theta [n_ls + 3], d x, d y) through gpk_cross_covariance_vjp."""
+    dev = _lib.require_cuda(x, y, G)
+    n, m, d = x.shape[0], y.shape[0], x.shape[1]
+    gth = torch.zeros(n_ls + 3, dtype=torch.float64, device=dev)
+    gx = torch.zeros((n, d), dtype=torch.float64, device=dev) if need_x else None
+    gy = torch.zeros((m, d), dtype=torch.float64, device=dev) if need_y else None
+    Gc = G.detach().to(torch.float64).contiguous()
+    nbytes = _lib.lib().gpk_cross_covariance_vjp_workspace_bytes(n, m, d)
+    ws = _lib.workspace(nbytes, dev)
+    _lib.call("gpk_cross_covariance_vjp", kind, n, m, d, x.data_ptr(), d, y.data_ptr(), d,
+              theta.data_ptr(), n_ls, Gc.data_ptr(), m, gth.data_ptr(), _lib.ptr(gx),
+              _lib.ptr(gy), ws.data_ptr(), ws.numel(), _lib.stream_ptr(dev))
+    return gth, gx, gy

@@ -87,6 +87,22 @@ gpk_status gpk_gram(int kind, int64_t n, int d, const double* x, int64_t ldx,
                     const double* theta, int n_ls, int out_dtype, void* out,
                     int64_t ldo, cudaStream_t stream);
 
+/* Reverse-mode derivative of gpk_cross_covariance: given the cotangent
+ * G [n, m] (float64, leading dim ldg) of K(x, y), writes grad_theta
+ * [n_ls + 3] (lengthscales, variance; the obs_stddev and mean slots are 0)
+ * and, when non-NULL, grad_x [n, d] and grad_y [m, d].  Counterpart of JAX
+ * differentiating DenseKernelComputation.cross_covariance
+ * (computations/dense.py:32-36).  workspace: gpk_cross_covariance_vjp_workspace_bytes. */
+size_t gpk_cross_covariance_vjp_workspace_bytes(int64_t n, int64_t m, int d);
+gpk_status gpk_cross_covariance_vjp(int kind, int64_t n, int64_t m, int d,
+                                    const double* x, int64_t ldx,
+                                    const double* y, int64_t ldy,
+                                    const double* theta, int n_ls,
+                                    const double* G, int64_t ldg,
+                                    double* grad_theta, double* grad_x, double* grad_y,
+                                    void* workspace, size_t workspace_bytes,
+                                    cudaStream_t stream);
+
 /* diag k(x_i, x_i) as float64 [n] (computations/base.py:95-109). */
 gpk_status gpk_diagonal(int kind, int64_t n, int d, const double* x, int64_t ldx,
                         const double* theta, int n_ls, double* out,

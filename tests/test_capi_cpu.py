@@ -51,8 +51,9 @@ def test_workspace_queries(built_lib):
     lib = _lib.lib()
     a = lib.gpk_conjugate_mll_workspace_bytes(16384, 8, _lib.PREC_MIXED)
     b = lib.gpk_conjugate_mll_workspace_bytes(16384, 8, _lib.PREC_FP64)
-    # three n x n panels (factor, inverse, transposed inverse) plus scratch
-    assert 3 * 16384 * 16384 * 4 < a < 5 * 16384 * 16384 * 4
+    # mixed: the float32 input plus TF32 hi/lo pairs of L, L^-1 and L^-T (7 n x n)
+    assert 7 * 16384 * 16384 * 4 < a < 9 * 16384 * 16384 * 4
+    # float64: factor, inverse and transposed inverse plus scratch
     assert 3 * 16384 * 16384 * 8 < b < 5 * 16384 * 16384 * 8
     assert lib.gpk_predict_workspace_bytes(2048, 512, 4, _lib.PREC_FP64) > 0
     assert lib.gpk_solve_triangular_workspace_bytes(100, 3, _lib.F64) > 0

@@ -1,0 +1,133 @@
+"""GPU parity of collapsed_elbo (value, gradients w.r.t. kernel, likelihood and
+mean parameters and the inducing inputs), of the cross-covariance cotangent and
+of the SGPR predictive, against the float64 oracle / torch float64 autograd."""
+import numpy as np
+import pytest
+import torch
+
+import gpjax_gb300 as gpx
+from oracle import gp_oracle as O
+from tests._gpu_helpers import KINDS
+
+pytestmark = pytest.mark.gpu
+
+
+def _family(kind, Z, ls, var, sd, c, jitter=1e-6):
+    kern = KINDS[kind](lengthscale=np.asarray(ls, np.float64), variance=var)
+    prior = gpx.gps.Prior(kernel=kern, mean_function=gpx.mean_functions.Constant(
+        gpx.parameters.Real(c)))
+    post = prior * gpx.likelihoods.Gaussian(num_datapoints=1, obs_stddev=sd)
+    q = gpx.variational_families.CollapsedVariationalGaussian(post, Z, jitter=jitter)
+    for p in (kern.lengthscale, kern.variance, post.likelihood.obs_stddev,
+              prior.mean_function.constant, q.inducing_inputs):
+        p.to("cuda").requires_grad_(True)
+    return q
+
+
+def _run(kind, x, y, Z, ls, var, sd, c, precision="fp64"):
+    q = _family(kind, Z, ls, var, sd, c)
+    val = gpx.objectives.collapsed_elbo(q, gpx.Dataset(X=x, y=y), precision=precision)
+    val.backward()
+    k = q.posterior.prior.kernel
+    g = np.concatenate([np.atleast_1d(k.lengthscale.value.grad.cpu().numpy()),
+                        [float(k.variance.value.grad),
+                         float(q.posterior.likelihood.obs_stddev.value.grad),
+                         float(q.posterior.prior.mean_function.constant.value.grad)]])
+    return float(val.detach()), g, q.inducing_inputs.value.grad.cpu().numpy()
+
+
+def _oracle(kind, x, y, Z, ls, var, sd, c):
+    val, g = O.collapsed_elbo_torch(kind, x, y, Z, ls, var, sd, c)
+    gv = np.concatenate([np.atleast_1d(g["lengthscale"]),
+                         [g["variance"], g["obs_stddev"], g["constant"]]])
+    return val, gv, g["inducing_inputs"]
+
+
+@pytest.mark.parametrize("kind,n,m,d,ard", [(0, 50, 7, 1, False), (1, 300, 20, 2, True),
+                                            (2, 1000, 64, 3, True), (0, 9000, 100, 8, True),
+                                            (2, 700, 130, 5, False)])
+def test_collapsed_elbo_fp64(cuda_lib, kind, n, m, d, ard):
+    rng = np.random.default_rng(n + m)
+    x = rng.uniform(-2, 2, size=(n, d))
+    y = np.sin(x).sum(1, keepdims=True) + 0.1 * rng.standard_normal((n, 1))
+    Z = x[rng.choice(n, m, replace=False)] + 0.05 * rng.standard_normal((m, d))
+    ls = np.exp(rng.uniform(np.log(0.5), np.log(2.0), d)) if ard else np.array(1.1)
+    val, g, gz = _run(kind, x, y, Z, ls, 1.2, 0.3, 0.1)
+    ref, gref, gzref = _oracle(kind, x, y, Z, ls, 1.2, 0.3, 0.1)
+    assert abs(val - ref) <= 1e-9 * abs(ref), (val, ref)
+    assert np.allclose(g, gref, rtol=1e-6, atol=1e-7 * np.abs(gref).max()), (g, gref)
+    assert np.allclose(gz, gzref, rtol=1e-6, atol=1e-7 * np.abs(gzref).max())
+
+
+@pytest.mark.parametrize("n_points", [10, 20])
+@pytest.mark.parametrize("n_dims", [1, 2, 3])
+def test_collapsed_elbo_equals_mll_when_z_is_x(cuda_lib, n_points, n_dims):
+    # tests/test_objectives.py:193-199 of the reference
+    rng = np.random.default_rng(n_points * 10 + n_dims)
+    x = rng.uniform(-2, 2, size=(n_points, n_dims))
+    y = np.sin(x[:, :1]) + 0.1 * rng.standard_normal((n_points, 1))
+    q = _family(0, x, np.ones(n_dims), 1.0, 1.0, 0.0)
+    elbo = float(gpx.objectives.collapsed_elbo(q, gpx.Dataset(X=x, y=y), precision="fp64"))
+    mll = float(gpx.objectives.conjugate_mll(q.posterior, gpx.Dataset(X=x, y=y), precision="fp64"))
+    assert abs(elbo - mll) / abs(mll) < 1e-6
+
+
+def test_collapsed_elbo_mixed(cuda_lib):
+    """Mixed form (float32 Phi, float64 m x m algebra) on a mixture-of-Gaussians
+    input like the SGPR workload, at reduced n; errors are reported."""
+    rng = np.random.default_rng(5)
+    n, m, d = 20000, 128, 8
+    means = rng.uniform(-5, 5, size=(16, d))
+    x = means[rng.integers(0, 16, n)] + 0.5 * rng.standard_normal((n, d))
+    y = np.sin(x).sum(1, keepdims=True) + 0.1 * rng.standard_normal((n, 1))
+    Z = x[rng.choice(n, m, replace=False)]
+    ls = np.exp(rng.uniform(np.log(0.5), np.log(2.0), d))
+    v64, g64, z64 = _run(0, x, y, Z, ls, 1.0, 0.1, 0.0, "fp64")
+    vm, gm, zm = _run(0, x, y, Z, ls, 1.0, 0.1, 0.0, "mixed")
+    ref = O.collapsed_elbo(0, x, y, Z, ls, 1.0, 0.1, 0.0)
+    print(f"SGPR n={n} m={m}: fp64 rel {abs(v64 - ref) / abs(ref):.2e}, "
+          f"mixed rel {abs(vm - ref) / abs(ref):.2e}, "
+          f"mixed grad rel {np.linalg.norm(gm - g64) / np.linalg.norm(g64):.2e}")
+    assert abs(v64 - ref) <= 1e-9 * abs(ref)
+    assert abs(vm - ref) <= 1e-4 * abs(ref)
+    assert np.linalg.norm(gm - g64) <= 1e-2 * np.linalg.norm(g64)
+
+
+@pytest.mark.parametrize("kind", [0, 1, 2])
+@pytest.mark.parametrize("ard", [True, False])
+def test_cross_covariance_vjp(cuda_lib, kind, ard):
+    rng = np.random.default_rng(kind)
+    n, m, d = 37, 29, 3
+    x, y = rng.standard_normal((n, d)), rng.standard_normal((m, d)) + 0.3
+    W = rng.standard_normal((n, m))
+    ls = np.array([0.6, 1.1, 1.7]) if ard else np.array(0.9)
+    k = KINDS[kind](lengthscale=ls, variance=1.3)
+    k.lengthscale.to("cuda").requires_grad_(True)
+    k.variance.to("cuda").requires_grad_(True)
+    X = torch.tensor(x, device="cuda", requires_grad=True)
+    Y = torch.tensor(y, device="cuda", requires_grad=True)
+    (k.cross_covariance(X, Y) * torch.as_tensor(W, device="cuda")).sum().backward()
+    # torch float64 autograd of the oracle kernel
+    lt = torch.tensor(ls, requires_grad=True)
+    vt = torch.tensor(1.3, dtype=torch.float64, requires_grad=True)
+    xt = torch.tensor(x, requires_grad=True)
+    yt = torch.tensor(y, requires_grad=True)
+    (O._t_kernel(kind, xt, yt, lt, vt) * torch.as_tensor(W)).sum().backward()
+    assert np.allclose(k.lengthscale.value.grad.cpu().numpy(), lt.grad.numpy(), rtol=1e-10)
+    assert np.isclose(float(k.variance.value.grad), float(vt.grad), rtol=1e-10)
+    assert np.allclose(X.grad.cpu().numpy(), xt.grad.numpy(), rtol=1e-9, atol=1e-12)
+    assert np.allclose(Y.grad.cpu().numpy(), yt.grad.numpy(), rtol=1e-9, atol=1e-12)
+
+
+def test_sgpr_predict(cuda_lib):
+    rng = np.random.default_rng(2)
+    n, m, t, d = 400, 30, 25, 2
+    x = rng.uniform(-2, 2, size=(n, d))
+    y = np.sin(x).sum(1, keepdims=True) + 0.1 * rng.standard_normal((n, 1))
+    Z = x[:m].copy()
+    T = rng.uniform(-2, 2, size=(t, d))
+    q = _family(2, Z, np.array([0.8, 1.2]), 1.1, 0.2, 0.05)
+    dist = q.predict(torch.as_tensor(T, device="cuda"), gpx.Dataset(X=x, y=y))
+    mean, cov = O.sgpr_predict(2, x, y, Z, T, np.array([0.8, 1.2]), 1.1, 0.2, 0.05)
+    assert np.allclose(dist.mean.cpu().numpy(), mean, rtol=1e-8, atol=1e-9)
+    assert np.allclose(dist.covariance().cpu().numpy(), cov, rtol=1e-7, atol=1e-9)
