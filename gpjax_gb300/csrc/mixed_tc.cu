@@ -45,59 +45,94 @@ __global__ void __launch_bounds__(512)
   double* Pv = Dd + N;                            // float64 pivots
   float* S = reinterpret_cast<float*>(Pv + N);   // L
   float* Ms = S + N * LD;                         // L^-1
-  float* Tt = Ms + N * LD;                        // merge temporary, 64 x 65
-  float* col = Tt + 64 * 65;
+  float* Tt = Ms + N * LD;                        // panel / merge temporary, 96 x 33 >= 64 x 65
+  float* col = Tt + 96 * 65;
   float* dl = col + N;
   const int tid = threadIdx.x, nt = blockDim.x;
   const int warp = tid >> 5, lane = tid & 31, nwarps = nt >> 5;
   for (int e = tid; e < N * N; e += nt) {
     const int i = e / N, j = e % N;
-    S[i * LD + j] = (j <= i) ? A[(int64_t)(o + i) * lda + o + j] : 0.f;
+    S[i * LD + j] = 0.f;
     Ms[i * LD + j] = 0.f;
   }
   for (int i = tid; i < N; i += nt) Dd[i] = dtrack[o + i];
+  // ---- Cholesky: each thread owns SLOTS strictly-lower entries in registers,
+  //      numbered column by column; one pivot step = scale column j, barrier,
+  //      rank-1 update of the owned entries right of column j, barrier ----
+  constexpr int NLOW = N * (N - 1) / 2;                 // 8128
+  constexpr int SLOTS = (NLOW + 511) / 512;             // 16 (blockDim.x == 512)
+  float val[SLOTS];
+  int sik[SLOTS];  // (row << 8) | column; an unused slot holds (0, 0)
+#pragma unroll
+  for (int q = 0; q < SLOTS; ++q) {
+    const int e = tid + 512 * q;
+    sik[q] = 0;
+    val[q] = 0.f;
+    if (e < NLOW) {
+      // column-major strictly-lower numbering: column k starts at k*(2N-1-k)/2
+      // float32 estimate (exact after the integer corrections; no float64 here:
+      // float64 throughput on this part is a small fraction of float32)
+      int k = (int)((2.f * N - 1.f - sqrtf((2.f * N - 1.f) * (2.f * N - 1.f) - 8.f * (float)e)) * 0.5f);
+      k = k < 0 ? 0 : (k > N - 2 ? N - 2 : k);
+      while (k > 0 && k * (2 * N - 1 - k) / 2 > e) --k;
+      while ((k + 1) * (2 * N - 2 - k) / 2 <= e) ++k;
+      const int i = k + 1 + (e - k * (2 * N - 1 - k) / 2);
+      sik[q] = (i << 8) | k;
+      val[q] = A[(int64_t)(o + i) * lda + o + k];
+    }
+  }
   __syncthreads();
-  // ---- Cholesky, right-looking, float64 diagonal ----
   for (int j = 0; j < N; ++j) {
-    // the pivot carries float64 history; its square root is only needed in
-    // float32 (every thread takes it, so no float64 transcendental here)
     const double piv = Dd[j];
-    const float ljj = sqrtf((float)piv);
-    for (int i = j + 1 + tid; i < N; i += nt) {
-      const float v = S[i * LD + j] / ljj;
-      S[i * LD + j] = v;
-      col[i] = v;
+    const float ljj = sqrtf((float)piv);  // float64 pivot history, float32 root
+    const float rl = 1.f / ljj;
+#pragma unroll
+    for (int q = 0; q < SLOTS; ++q) {
+      if ((sik[q] & 255) == j && sik[q] != 0) {
+        val[q] *= rl;
+        col[sik[q] >> 8] = val[q];
+      }
     }
     if (tid == 0) {
       dl[j] = ljj;
       Pv[j] = piv;
     }
     __syncthreads();
-    for (int i = j + 1 + warp; i < N; i += nwarps) {
-      const float ci = col[i];
-      for (int k = j + 1 + lane; k < i; k += 32) S[i * LD + k] -= ci * col[k];
+#pragma unroll
+    for (int q = 0; q < SLOTS; ++q) {
+      const int k = sik[q] & 255;
+      if (k > j) val[q] = fmaf(-col[sik[q] >> 8], col[k], val[q]);
     }
-    for (int i = j + 1 + tid; i < N; i += nt) {
-      const double c = (double)col[i];
-      Dd[i] -= c * c;
+    if (tid > j && tid < N) {
+      const double c = (double)col[tid];
+      Dd[tid] -= c * c;
     }
     __syncthreads();
   }
+  // L into shared memory for the inverse
+#pragma unroll
+  for (int q = 0; q < SLOTS; ++q)
+    if ((sik[q] >> 8) > (sik[q] & 255)) S[(sik[q] >> 8) * LD + (sik[q] & 255)] = val[q];
   for (int i = tid; i < N; i += nt) {
     S[i * LD + i] = dl[i];
     logdiag[o + i] = 0.5 * log(Pv[i]);
     if (!(Pv[i] > 0.0)) atomicMin(info, o + i + 1);
   }
   __syncthreads();
-  // ---- inverse: 32 x 32 diagonal blocks by column substitution ----
+  // ---- inverse: 32 x 32 diagonal blocks (lane = column, registers) ----
   if (warp < 4) {
-    const int b = warp * 32, c = lane;
-    Ms[(b + c) * LD + b + c] = 1.f / S[(b + c) * LD + b + c];
-    for (int i = c + 1; i < 32; ++i) {
-      float s = 0.f;
-      for (int k = c; k < i; ++k) s = fmaf(S[(b + i) * LD + b + k], Ms[(b + k) * LD + b + c], s);
-      Ms[(b + i) * LD + b + c] = -s / S[(b + i) * LD + b + i];
+    const int b0 = warp * 32, c = lane;
+    float mc[32];
+#pragma unroll
+    for (int i = 0; i < 32; ++i) {
+      float sacc = 0.f;
+#pragma unroll
+      for (int k = 0; k < i; ++k) sacc = fmaf(S[(b0 + i) * LD + b0 + k], mc[k], sacc);
+      const float dii = S[(b0 + i) * LD + b0 + i];
+      mc[i] = (i < c) ? 0.f : ((i == c) ? 1.f / dii : -sacc / dii);
     }
+#pragma unroll
+    for (int i = 0; i < 32; ++i) Ms[(b0 + i) * LD + b0 + c] = mc[i];
   }
   __syncthreads();
   // ---- doubling merges: M21 = -M22 (L21 M11) for half sizes 32 then 64 ----
@@ -139,7 +174,7 @@ __global__ void __launch_bounds__(512)
 }
 
 size_t leaf_smem_bytes() {
-  return 2 * LEAF * sizeof(double) + (size_t)(2 * LEAF * (LEAF + 1) + 64 * 65 + 2 * LEAF) * 4;
+  return 2 * LEAF * sizeof(double) + (size_t)(2 * LEAF * (LEAF + 1) + 96 * 65 + 2 * LEAF) * 4;
 }
 
 // y = op(Th + Tl) x over a triangle, float64 accumulation, one warp per row.

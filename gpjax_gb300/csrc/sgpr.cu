@@ -204,13 +204,15 @@ __global__ void __launch_bounds__(256)
   }
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   for (int k = 0; k < 2 * d + 1; ++k) {
-    double v = k < d ? al[0] : 0.0;
+    // slot k: [0, d) lengthscale terms, [d, 2d) Z terms, 2d variance term
+    double v = av;
+    if (k < 2 * d) {
+      const int idx = k < d ? k : k - d;
+      v = 0.0;
 #pragma unroll
-    for (int q = 0; q < DMAXS; ++q) {
-      if (k == q) v = al[q];
-      if (k == d + q) v = az[q];
+      for (int q = 0; q < DMAXS; ++q)
+        if (q == idx) v = (k < d) ? al[q] : az[q];
     }
-    if (k == 2 * d) v = av;
     v = warp_sum(v);
     if (l == 0) red[k * 8 + w] = v;
   }
@@ -351,10 +353,14 @@ __global__ void __launch_bounds__(256)
   // theta partials of this block
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   for (int k = 0; k <= d; ++k) {
-    double v = (k < d) ? 0.0 : av;
+    // slot k: [0, d) lengthscale terms, d variance term
+    double v = av;
+    if (k < d) {
+      v = 0.0;
 #pragma unroll
-    for (int q = 0; q < DMAXS; ++q)
-      if (k == q) v = al[q];
+      for (int q = 0; q < DMAXS; ++q)
+        if (q == k) v = al[q];
+    }
     v = warp_sum(v);
     if (l == 0) sred[w][k] = v;
   }

@@ -122,6 +122,20 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
   for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
 }
 
+// two of these then one tcgen05.wait::ld keep two TMEM loads in flight
+__device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+}
+
 __device__ __forceinline__ float tf32_rna(float x) {
   uint32_t r;
   asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
@@ -152,6 +166,9 @@ struct SmemCtl {
 constexpr int SEG_CHUNKS = 1;
 constexpr int NBUF = 4;
 constexpr int TLD = BN + 4;    // staged output tile row stride (floats)
+constexpr int EPI_WARPS = 8;   // epilogue warps: two per TMEM lane quarter
+constexpr int EPI_THREADS = EPI_WARPS * 32;
+constexpr int HC = BN / 2;     // accumulator columns owned by one epilogue thread
 
 template <int MODE>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
@@ -198,7 +215,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     }
     for (int b = 0; b < NBUF; ++b) {
       mbar_init(&ctl->tfull[b], 1);
-      mbar_init(&ctl->tempty[b], 4);  // one arrival per epilogue warp
+      mbar_init(&ctl->tempty[b], EPI_WARPS);  // one arrival per epilogue warp
     }
     ctl->abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -274,40 +291,46 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     }
     __syncwarp();
   } else {
-    // ---------------- epilogue warps 2..5 ----------------
+    // ---------------- epilogue warps 2..9 ----------------
+    // two warps per TMEM lane quarter; each owns one row and HC columns of it
     const int q = warp & 3;  // TMEM lane quarter this warp may access
     const int ew = warp - 2;
+    const int hcol = (ew >> 2) * HC;  // first tile column this thread owns
     const int r = q * 32 + lane;
     const int gi = i0 + r;  // row within the problem
     const int et = threadIdx.x - 64;
     if (MODE == MODE_GRAD) {
-      for (int e = et; e < BN * GRAD_DMAX; e += 128) {
+      for (int e = et; e < BN * GRAD_DMAX; e += EPI_THREADS) {
         const int c = e / GRAD_DMAX, k = e % GRAD_DMAX;
         const int gj = j0 + c;
         gx[e] = (gj < p.n_true && k < p.d) ? p.xs[(int64_t)gj * p.d + k] : 0.f;
       }
-      for (int c = et; c < BN; c += 128) {
+      for (int c = et; c < BN; c += EPI_THREADS) {
         const int gj = j0 + c;
         ga[c] = gj < p.n_true ? (float)p.avec[gj] : 0.f;
       }
     }
     // drain the accumulator segments into float32 registers (round to nearest)
-    float acc[BN];
+    float acc[HC];
 #pragma unroll
-    for (int c = 0; c < BN; ++c) acc[c] = 0.f;
+    for (int c = 0; c < HC; ++c) acc[c] = 0.f;
     bool have = true;
     for (int seg = 0; seg < nseg; ++seg) {
       const int b = seg % NBUF;
       have = __all_sync(0xffffffffu, mbar_wait(&ctl->tfull[b], (seg / NBUF) & 1, abort_flag, p.err));
       if (!have) break;
       tc_fence_after();
-      const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN);
+      const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN + hcol);
+      {
+        uint32_t v0[32], v1[32];
+        tmem_ld32_nowait(tb, v0);
+        tmem_ld32_nowait(tb + 32, v1);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-      for (int cb = 0; cb < BN / 32; ++cb) {
-        float v[32];
-        tmem_ld32(tb + cb * 32, v);
-#pragma unroll
-        for (int k = 0; k < 32; ++k) acc[cb * 32 + k] += v[k];
+        for (int k = 0; k < 32; ++k) {
+          acc[k] += __uint_as_float(v0[k]);
+          acc[32 + k] += __uint_as_float(v1[k]);
+        }
       }
       tc_fence_before();
       __syncwarp();
@@ -320,27 +343,27 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       if (MODE == MODE_STORE_SPLIT && p.dtrack && have && gi < p.M) {
         double dsum = 0.0;
 #pragma unroll
-        for (int c = 0; c < BN; ++c) {
+        for (int c = 0; c < HC; ++c) {
           const float w = p.alpha * acc[c];
-          if (j0 + c < p.N) dsum += (double)w * (double)w;
+          if (j0 + hcol + c < p.N) dsum += (double)w * (double)w;
         }
         atomicAdd(&p.dtrack[p.c_row0 + (int64_t)z * p.c_zrow + gi], -dsum);
       }
       // stage the tile, then write whole rows (coalesced, 4 floats per lane)
-      asm volatile("bar.sync 1, 128;" ::: "memory");  // all segments drained: ring is free
+      asm volatile("bar.sync 1, %0;" ::"r"(EPI_THREADS) : "memory");  // ring is free
 #pragma unroll
-      for (int c = 0; c < BN; c += 4)
-        *reinterpret_cast<float4*>(&otile[r * TLD + c]) =
+      for (int c = 0; c < HC; c += 4)
+        *reinterpret_cast<float4*>(&otile[r * TLD + hcol + c]) =
             have ? make_float4(p.alpha * acc[c], p.alpha * acc[c + 1], p.alpha * acc[c + 2],
                                p.alpha * acc[c + 3])
                  : make_float4(0.f, 0.f, 0.f, 0.f);
-      asm volatile("bar.sync 1, 128;" ::: "memory");
+      asm volatile("bar.sync 1, %0;" ::"r"(EPI_THREADS) : "memory");
       if (have) {
         const int64_t crow0 = p.c_row0 + (int64_t)z * p.c_zrow + i0;
         const int64_t ccol = p.c_col0 + (int64_t)z * p.c_zcol + j0;
         const int c4 = lane * 4;
         if (p.c0) {
-          for (int rr = ew; rr < BM; rr += 4) {
+          for (int rr = ew; rr < BM; rr += EPI_WARPS) {
             const int grow = i0 + rr;
             if (grow >= p.M) break;
             const float4 w4 = *reinterpret_cast<const float4*>(&otile[rr * TLD + c4]);
@@ -385,7 +408,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
           // transposed: output row = tile column j, lanes over tile rows i
           const int64_t trow0 = p.t_row0 + (int64_t)z * p.t_zrow + j0;
           const int64_t tcol = p.t_col0 + (int64_t)z * p.t_zcol + i0;
-          for (int cc = ew; cc < BN; cc += 4) {
+          for (int cc = ew; cc < BN; cc += EPI_WARPS) {
             if (j0 + cc >= p.N) break;
             const int64_t base = (trow0 + cc) * p.ldt + tcol;
 #pragma unroll
@@ -403,7 +426,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       }
     }
     if (MODE == MODE_GRAD) {
-      asm volatile("bar.sync 1, 128;" ::: "memory");  // gx / ga staged
+      asm volatile("bar.sync 1, %0;" ::"r"(EPI_THREADS) : "memory");  // gx / ga staged
       // W tile -> reduction against dK/dtheta (unit variance); an aborted wait
       // contributes zeros but still joins the reduction barrier
       float xi[GRAD_DMAX];
@@ -416,17 +439,17 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       for (int k = 0; k < GRAD_DMAX; ++k) gl[k] = 0.0;
       double gnoise = 0.0, gvar = 0.0;
 #pragma unroll
-      for (int cb = 0; cb < BN / 32; ++cb) {
+      for (int cb = 0; cb < HC / 32; ++cb) {
         float pl[GRAD_DMAX];
 #pragma unroll
         for (int k = 0; k < GRAD_DMAX; ++k) pl[k] = 0.f;
         float pvar = 0.f;
 #pragma unroll
         for (int k = 0; k < 32; ++k) {
-          const int c = cb * 32 + k;
+          const int c = hcol + cb * 32 + k;
           const int gj = j0 + c;
           if (!have || gi >= p.n_true || gj >= p.n_true || gj > gi) continue;
-          const float w = acc[c];
+          const float w = acc[cb * 32 + k];
           const float f = (gi == gj) ? 1.f : 2.f;
           const float coef = f * (ai * ga[c] - w);
           float dsq[GRAD_DMAX];
@@ -464,13 +487,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
           val = gnoise;
         }
         val = warp_sum(val);
-        if (lane == 0) gred[sidx * 4 + ew] = val;
+        if (lane == 0) gred[sidx * EPI_WARPS + ew] = val;
       }
-      asm volatile("bar.sync 1, 128;" ::: "memory");
+      asm volatile("bar.sync 1, %0;" ::"r"(EPI_THREADS) : "memory");
       const int tile_id = blockIdx.x + (int)gridDim.x * z;
-      for (int sidx = et; sidx < slots; sidx += 128) {
-        const double tot =
-            ((gred[sidx * 4] + gred[sidx * 4 + 1]) + gred[sidx * 4 + 2]) + gred[sidx * 4 + 3];
+      for (int sidx = et; sidx < slots; sidx += EPI_THREADS) {
+        double tot = 0.0;
+        for (int w8 = 0; w8 < EPI_WARPS; ++w8) tot += gred[sidx * EPI_WARPS + w8];
         p.gpart[(int64_t)tile_id * slots + sidx] = tot;
       }
     }
@@ -539,7 +562,8 @@ static bool make_map(CUtensorMap* m, const float* base, int64_t rows, int64_t co
 
 static size_t tc_smem_bytes() {
   return 1024 + (size_t)tc::STAGES * tc::STAGE_BYTES + sizeof(tc::SmemCtl) +
-         (size_t)tc::BN * tc::GRAD_DMAX * 4 + tc::BN * 4 + 64 * sizeof(double) + 64;
+         (size_t)tc::BN * tc::GRAD_DMAX * 4 + tc::BN * 4 +
+         (size_t)(tc::GRAD_DMAX + 2) * 8 * sizeof(double) + 64;
 }
 
 bool tc_make_map(TcMap* m, const float* hi, const float* lo, int64_t rows, int64_t cols,

@@ -22,7 +22,7 @@ constexpr int BM = 128, BN = 128, BK = 32;
 constexpr int STAGES = 3;
 constexpr int TILE_BYTES = BM * BK * 4;        // 16 KB: 128 rows x 128 B
 constexpr int STAGE_BYTES = 4 * TILE_BYTES;    // A_hi, A_lo, B_hi, B_lo
-constexpr int NUM_THREADS = 192;               // w0 TMA, w1 MMA + TMEM, w2..w5 epilogue
+constexpr int NUM_THREADS = 320;               // w0 TMA, w1 MMA + TMEM, w2..w9 epilogue
 constexpr int GRAD_DMAX = 16;                  // largest input dimension of the adjoint epilogue
 
 enum Mode { MODE_ADD_F32 = 0, MODE_STORE_SPLIT = 1, MODE_GRAD = 2 };
