@@ -13,6 +13,7 @@
 #include <atomic>
 #include <climits>
 #include <cmath>
+#include <mutex>
 #include "gpk_internal.cuh"
 
 namespace gpk {
@@ -447,4 +448,77 @@ extern "C" gpk_status gpk_logdet_triangular(int64_t n, int dtype, const void* L,
     return GPK_ERR_BAD_ARG;
   GPK_LAUNCH_CHECK();
   return GPK_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free float64 marginal log-likelihood for small problems.
+//
+// Callers that cannot allocate device memory (code running inside CUDA stream
+// capture, where cudaMalloc would break the capture; host frameworks that
+// hand a custom call no workspace; embedded or real-time hosts that forbid
+// allocation after start-up) use this entry point instead of
+// gpk_conjugate_mll: its scratch is a file-scope device array, so the call
+// allocates nothing.  The array holds GPK_NOALLOC_SCRATCH_BYTES, enough for
+// n <= GPK_NOALLOC_MAX_N and d <= GPK_NOALLOC_MAX_D; every GPU that loads the
+// library keeps it until the process exits.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNoallocBytes = (size_t)8 << 20;  // 8 MiB
+constexpr int kNoallocMaxN = 512;
+constexpr int kNoallocMaxD = 32;
+constexpr int kMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
+
+// Device address of g_noalloc_scratch per device.  In host code the array's
+// name is only a host-side stand-in, so the address comes from
+// cudaGetSymbolAddress, taken once per device with that device current.
+static void* g_noalloc_ptr[kMaxDevices];
+static std::mutex g_noalloc_mutex;
+
+gpk_status noalloc_scratch(void** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return GPK_ERR_CUDA;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return GPK_ERR_CUDA;
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return GPK_OK;
+}
+
+}  // namespace
+
+extern "C" size_t gpk_conjugate_mll_noalloc_max_n(void) { return kNoallocMaxN; }
+
+extern "C" gpk_status gpk_conjugate_mll_noalloc(int kind, int64_t n, int d, const double* x,
+                                                int64_t ldx, const double* y,
+                                                const double* theta, int n_ls, double jitter,
+                                                int want_grad, double* out_mll,
+                                                double* out_grad, int* info,
+                                                cudaStream_t stream) {
+  if (!mll_args_ok(kind, n, d, ldx, n_ls, GPK_PREC_FP64)) return GPK_ERR_BAD_ARG;
+  // sizes beyond the static scratch are refused, never truncated
+  if (n > kNoallocMaxN || d > kNoallocMaxD) return GPK_ERR_UNSUPPORTED;
+  if (!out_mll || !info || !theta || (want_grad && !out_grad)) return GPK_ERR_BAD_ARG;
+  if (n == 0) {
+    zero_outputs_kernel<<<1, 1, 0, stream>>>(out_mll, want_grad ? out_grad : nullptr, n_ls + 3,
+                                             info);
+    GPK_LAUNCH_CHECK();
+    return GPK_OK;
+  }
+  if (!x || !y) return GPK_ERR_BAD_ARG;
+  MllBuffers<double> b;
+  if (mll_layout<double>(n, d, nullptr, b) > kNoallocBytes) return GPK_ERR_UNSUPPORTED;
+  void* ws = nullptr;
+  const gpk_status st = noalloc_scratch(&ws);
+  if (st != GPK_OK) return st;
+  // Every region of the layout is written before it is read within one
+  // call (Gram, factor, inverse, solves, per-tile partials), so nothing left
+  // by an earlier call has to be cleared.
+  return mll_run<double>(kind, (int)n, d, x, ldx, y, theta, n_ls, jitter, 1, want_grad, out_mll,
+                         out_grad, info, ws, stream);
 }

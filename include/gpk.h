@@ -153,6 +153,26 @@ gpk_status gpk_conjugate_mll(int kind, int64_t n, int d,
                              void* workspace, size_t workspace_bytes,
                              cudaStream_t stream);
 
+/* Allocation-free variant of gpk_conjugate_mll, float64 form only.
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory -- code running inside CUDA stream capture (cudaMalloc would break
+ * the capture), host frameworks that pass a custom call no workspace, hosts
+ * that forbid allocation after start-up -- the scratch is a static device
+ * array of 8 MiB inside the library, which bounds the problem to
+ * n <= gpk_conjugate_mll_noalloc_max_n() (512) and d <= 32; larger sizes return
+ * GPK_ERR_UNSUPPORTED.  Every GPU that loads the library holds the array until
+ * the process exits.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress); make that first call before any stream
+ * capture.  All calls share the one array: calls that overlap on the GPU
+ * (different streams, or different host threads on the same device) race;
+ * serialise them.  Arguments and results are those of gpk_conjugate_mll. */
+size_t gpk_conjugate_mll_noalloc_max_n(void);
+gpk_status gpk_conjugate_mll_noalloc(int kind, int64_t n, int d,
+                                     const double* x, int64_t ldx, const double* y,
+                                     const double* theta, int n_ls, double jitter,
+                                     int want_grad, double* out_mll, double* out_grad,
+                                     int* info, cudaStream_t stream);
+
 /* SGPR collapsed ELBO and its gradient (collapsed_elbo,
  * gpjax/objectives.py:321-416), including d/dZ for the inducing inputs.
  * z [m, d] float64; out_grad: theta layout [n_ls + 3]; out_grad_z [m, d]. */

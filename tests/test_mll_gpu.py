@@ -48,14 +48,14 @@ def test_mll_fp64_parity(cuda_lib, kind, n, d, ard):
     assert np.allclose(g, gref, rtol=1e-7, atol=1e-8 * max(1.0, np.abs(gref).max())), (g, gref)
 
 
-def _mixed_check(val, g, ref, gref, tol_scale, gtol=1e-4, vtol=1e-6):
+def _mixed_check(val, g, ref, gref, tol_scale, gtol=1e-4, vtol=1e-6, ptol=1e-3):
     """MLL within 1e-6 of tol_scale; gradient within gtol relative to its norm
     (the mixed form's factor carries float32 backward error, which bounds the
-    trace term of the noise gradient; each component is also held to 1e-3)."""
+    trace term of the noise gradient; each component is also held to ptol)."""
     err = np.abs(g - gref)
     assert abs(val - ref) <= vtol * tol_scale, (val, ref, abs(val - ref) / tol_scale)
     assert np.linalg.norm(err) <= gtol * np.linalg.norm(gref), (g, gref)
-    assert np.all(err <= 1e-3 * np.abs(gref) + gtol * 0.1 * np.linalg.norm(gref)), (g, gref)
+    assert np.all(err <= ptol * np.abs(gref) + gtol * 0.1 * np.linalg.norm(gref)), (g, gref)
 
 
 @pytest.mark.parametrize("n", [700, 2048, 3000])
@@ -82,7 +82,7 @@ def test_mll_mixed_parity_other_kernels(cuda_lib, kind, n, d):
     ld = np.linalg.slogdet(S)[1]
     quad = float(y[:, 0] @ np.linalg.solve(S, y[:, 0]))
     _mixed_check(val, g, ref, gref, 0.5 * (abs(ld) + abs(quad) + n * np.log(2 * np.pi)),
-                 gtol=2e-3, vtol=1e-5)
+                 gtol=2e-3, vtol=1e-5, ptol=5e-3)
 
 
 def test_mll_matches_finite_differences(cuda_lib):
