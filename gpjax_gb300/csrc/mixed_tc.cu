@@ -41,8 +41,8 @@ __global__ void __launch_bounds__(512)
                          float* __restrict__ Vh, float* __restrict__ Vl, int64_t ldm) {
   constexpr int N = LEAF, LD = LEAF + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  double* Dd = reinterpret_cast<double*>(smem_raw);
-  double* Pv = Dd + N;                            // float64 pivots
+  double* Dd = reinterpret_cast<double*>(smem_raw);  // diagonal track (as float pairs below)
+  double* Pv = Dd + N;                            // pivots (as float pairs below)
   float* S = reinterpret_cast<float*>(Pv + N);   // L
   float* Ms = S + N * LD;                         // L^-1
   float* Tt = Ms + N * LD;                        // panel / merge temporary, 96 x 33 >= 64 x 65
@@ -55,68 +55,84 @@ __global__ void __launch_bounds__(512)
     S[i * LD + j] = 0.f;
     Ms[i * LD + j] = 0.f;
   }
-  for (int i = tid; i < N; i += nt) Dd[i] = dtrack[o + i];
-  // ---- Cholesky: each thread owns SLOTS strictly-lower entries in registers,
-  //      numbered column by column; one pivot step = scale column j, barrier,
-  //      rank-1 update of the owned entries right of column j, barrier ----
-  constexpr int NLOW = N * (N - 1) / 2;                 // 8128
-  constexpr int SLOTS = (NLOW + 511) / 512;             // 16 (blockDim.x == 512)
-  float val[SLOTS];
-  int sik[SLOTS];  // (row << 8) | column; an unused slot holds (0, 0)
-#pragma unroll
-  for (int q = 0; q < SLOTS; ++q) {
-    const int e = tid + 512 * q;
-    sik[q] = 0;
-    val[q] = 0.f;
-    if (e < NLOW) {
-      // column-major strictly-lower numbering: column k starts at k*(2N-1-k)/2
-      // float32 estimate (exact after the integer corrections; no float64 here:
-      // float64 throughput on this part is a small fraction of float32)
-      int k = (int)((2.f * N - 1.f - sqrtf((2.f * N - 1.f) * (2.f * N - 1.f) - 8.f * (float)e)) * 0.5f);
-      k = k < 0 ? 0 : (k > N - 2 ? N - 2 : k);
-      while (k > 0 && k * (2 * N - 1 - k) / 2 > e) --k;
-      while ((k + 1) * (2 * N - 2 - k) / 2 <= e) ++k;
-      const int i = k + 1 + (e - k * (2 * N - 1 - k) / 2);
-      sik[q] = (i << 8) | k;
-      val[q] = A[(int64_t)(o + i) * lda + o + k];
-    }
+  __syncthreads();
+  for (int e = tid; e < N * N; e += nt) {
+    const int i = e / N, j = e % N;
+    if (j < i) S[i * LD + j] = A[(int64_t)(o + i) * lda + o + j];
+  }
+  // float-float copy (hi + lo, ~48 bits) of the float64 diagonal track: the
+  // pivot history keeps float64-class accuracy with float32 arithmetic only
+  // (float64 throughput on this part is a small fraction of float32)
+  float* Dh = reinterpret_cast<float*>(Dd);
+  float* Dlo = Dh + N;
+  float* Ph = reinterpret_cast<float*>(Pv);  // pivots as float-float pairs
+  float* Pl = Ph + N;
+  for (int i = tid; i < N; i += nt) {
+    const double dv = dtrack[o + i];
+    const float hi = (float)dv;
+    Dh[i] = hi;
+    Dlo[i] = (float)(dv - (double)hi);
   }
   __syncthreads();
-  for (int j = 0; j < N; ++j) {
-    const double piv = Dd[j];
-    const float ljj = sqrtf((float)piv);  // float64 pivot history, float32 root
-    const float rl = 1.f / ljj;
-#pragma unroll
-    for (int q = 0; q < SLOTS; ++q) {
-      if ((sik[q] & 255) == j && sik[q] != 0) {
-        val[q] *= rl;
-        col[sik[q] >> 8] = val[q];
+  // ---- Cholesky by 32-wide panels: inside a panel each pivot step touches
+  //      only the panel's columns (warps over rows, lanes over columns); the
+  //      columns right of the panel get one rank-32 update per panel ----
+  for (int c0 = 0; c0 < N; c0 += 32) {
+    const int pend = c0 + 31;
+    for (int j = c0; j <= pend; ++j) {
+      const float ph = Dh[j], pl = Dlo[j];
+      const float ljj = sqrtf(ph + pl);
+      const float rl = 1.f / ljj;
+      for (int i = j + 1 + tid; i < N; i += nt) {
+        const float v = S[i * LD + j] * rl;
+        S[i * LD + j] = v;
+        col[i] = v;
       }
+      if (tid == 0) {
+        dl[j] = ljj;
+        Ph[j] = ph;  // no float64 work inside the loop: every warp waits on this one
+        Pl[j] = pl;
+      }
+      __syncthreads();
+      const int k = j + 1 + lane;  // panel column updated by this lane
+      if (k <= pend) {
+        const float ck = col[k];
+        for (int i = k + 1 + warp; i < N; i += nwarps) S[i * LD + k] = fmaf(-col[i], ck, S[i * LD + k]);
+      }
+      if (tid > j && tid < N) {
+        // (Dh, Dlo) -= c^2 exactly to ~2^-48: product error by FMA, TwoSum,
+        // then renormalisation
+        const float c = col[tid];
+        const float p = c * c, pe = fmaf(c, c, -p);
+        const float a = Dh[tid];
+        const float s1 = a - p, bb = s1 - a;
+        const float err = (a - (s1 - bb)) + (-p - bb);
+        const float lo = (Dlo[tid] - pe) + err;
+        const float hi = s1 + lo;
+        Dlo[tid] = lo - (hi - s1);
+        Dh[tid] = hi;
+      }
+      __syncthreads();
     }
-    if (tid == 0) {
-      dl[j] = ljj;
-      Pv[j] = piv;
+    // rank-32 update of the strictly lower part right of the panel
+    const int r0 = pend + 1, nr = N - r0;
+    if (nr > 1) {
+      for (int e = tid; e < nr * nr; e += nt) {
+        const int r = e / nr, q = e % nr;
+        if (q >= r) continue;
+        float sacc = 0.f;
+#pragma unroll 8
+        for (int c = c0; c <= pend; ++c) sacc = fmaf(S[(r0 + r) * LD + c], S[(r0 + q) * LD + c], sacc);
+        S[(r0 + r) * LD + r0 + q] -= sacc;
+      }
+      __syncthreads();
     }
-    __syncthreads();
-#pragma unroll
-    for (int q = 0; q < SLOTS; ++q) {
-      const int k = sik[q] & 255;
-      if (k > j) val[q] = fmaf(-col[sik[q] >> 8], col[k], val[q]);
-    }
-    if (tid > j && tid < N) {
-      const double c = (double)col[tid];
-      Dd[tid] -= c * c;
-    }
-    __syncthreads();
   }
-  // L into shared memory for the inverse
-#pragma unroll
-  for (int q = 0; q < SLOTS; ++q)
-    if ((sik[q] >> 8) > (sik[q] & 255)) S[(sik[q] >> 8) * LD + (sik[q] & 255)] = val[q];
   for (int i = tid; i < N; i += nt) {
     S[i * LD + i] = dl[i];
-    logdiag[o + i] = 0.5 * log(Pv[i]);
-    if (!(Pv[i] > 0.0)) atomicMin(info, o + i + 1);
+    const double pv = (double)Ph[i] + (double)Pl[i];
+    logdiag[o + i] = 0.5 * log(pv);
+    if (!(pv > 0.0)) atomicMin(info, o + i + 1);
   }
   __syncthreads();
   // ---- inverse: 32 x 32 diagonal blocks (lane = column, registers) ----
@@ -135,26 +151,52 @@ __global__ void __launch_bounds__(512)
     for (int i = 0; i < 32; ++i) Ms[(b0 + i) * LD + b0 + c] = mc[i];
   }
   __syncthreads();
-  // ---- doubling merges: M21 = -M22 (L21 M11) for half sizes 32 then 64 ----
+  // ---- doubling merges: M21 = -M22 (L21 M11) for half sizes 32 then 64,
+  //      each thread computing a 2 x 4 output block ----
   for (int h = 32; h < N; h *= 2) {
     const int pairs = N / (2 * h);
+    const int nblk = (h / 2) * (h / 4);  // 2 x 4 blocks per h x h product
     for (int pr = 0; pr < pairs; ++pr) {
       const int ob = pr * 2 * h;
-      // T = L21 M11   (h x h), M11 lower
-      for (int e = tid; e < h * h; e += nt) {
-        const int i = e / h, j = e % h;
-        float s = 0.f;
-        for (int c = j; c < h; ++c)
-          s = fmaf(S[(ob + h + i) * LD + ob + c], Ms[(ob + c) * LD + ob + j], s);
-        Tt[i * 65 + j] = s;
+      // T = L21 M11 (M11 lower: M11[c][j] = 0 for c < j)
+      for (int bidx = tid; bidx < nblk; bidx += nt) {
+        const int i2 = (bidx / (h / 4)) * 2, j4 = (bidx % (h / 4)) * 4;
+        float a0[4] = {0.f, 0.f, 0.f, 0.f}, a1[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int c = j4; c < h; ++c) {
+          const float l0 = S[(ob + h + i2) * LD + ob + c], l1 = S[(ob + h + i2 + 1) * LD + ob + c];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const float m = Ms[(ob + c) * LD + ob + j4 + q];
+            a0[q] = fmaf(l0, m, a0[q]);
+            a1[q] = fmaf(l1, m, a1[q]);
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          Tt[i2 * 65 + j4 + q] = a0[q];
+          Tt[(i2 + 1) * 65 + j4 + q] = a1[q];
+        }
       }
       __syncthreads();
-      // M21 = -M22 T   (M22 lower)
-      for (int e = tid; e < h * h; e += nt) {
-        const int i = e / h, j = e % h;
-        float s = 0.f;
-        for (int c = 0; c <= i; ++c) s = fmaf(Ms[(ob + h + i) * LD + ob + h + c], Tt[c * 65 + j], s);
-        Ms[(ob + h + i) * LD + ob + j] = -s;
+      // M21 = -M22 T (M22 lower: M22[i][c] = 0 for c > i)
+      for (int bidx = tid; bidx < nblk; bidx += nt) {
+        const int i2 = (bidx / (h / 4)) * 2, j4 = (bidx % (h / 4)) * 4;
+        float a0[4] = {0.f, 0.f, 0.f, 0.f}, a1[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int c = 0; c <= i2 + 1; ++c) {
+          const float m0 = Ms[(ob + h + i2) * LD + ob + h + c];  // zero when c > i2
+          const float m1 = Ms[(ob + h + i2 + 1) * LD + ob + h + c];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const float t = Tt[c * 65 + j4 + q];
+            a0[q] = fmaf(m0, t, a0[q]);
+            a1[q] = fmaf(m1, t, a1[q]);
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          Ms[(ob + h + i2) * LD + ob + j4 + q] = -a0[q];
+          Ms[(ob + h + i2 + 1) * LD + ob + j4 + q] = -a1[q];
+        }
       }
       __syncthreads();
     }
