@@ -13,8 +13,9 @@
 // Every product is one split-TF32 NT GEMM (tc_gemm.cu) reading K-contiguous
 // operands: L (rows), M = L^-1 and V = M^T are each kept row-major as TF32
 // hi/lo pairs.  Recursion leaves are 128 x 128 diagonal blocks factored and
-// inverted by one CTA in float32 with float64 pivots (the float64 diagonal
-// track is decremented by every L21 product).  n is padded to a multiple of
+// inverted by one CTA in float32, with pivots from a float64 diagonal track
+// (decremented by every L21 product; carried as float-float pairs inside the
+// leaf).  n is padded to a multiple of
 // 128 with an identity block, which leaves the factor, the inverse, the
 // log-determinant and alpha of the original system unchanged.
 #include <climits>
@@ -24,6 +25,12 @@ namespace gpk {
 namespace {
 
 constexpr int LEAF = 128;
+constexpr int LEAF_NT = 512;  // threads of the leaf kernel
+
+constexpr int LEAF_LD = LEAF + 1;   // S / Ms row stride: odd, so column walks are conflict-free
+constexpr int LEAF_PB = 32;         // panel width
+constexpr int LEAF_PTLD = LEAF + 4; // k-major panel copy: 16-byte rows
+constexpr int LEAF_LTLD = LEAF_PB + 4;
 
 __device__ __forceinline__ float tf32_rna_f(float x) {
   uint32_t r;
@@ -31,192 +38,283 @@ __device__ __forceinline__ float tf32_rna_f(float x) {
   return __uint_as_float(r);
 }
 
-// One CTA: Cholesky of the 128 x 128 diagonal block at (o, o) with float64
-// pivots from dtrack, then its inverse by 32-wide blocks and two doubling
-// merges; writes M (hi/lo) and V = M^T (hi/lo) diagonal blocks.
-__global__ void __launch_bounds__(512)
+// (hi, lo) -= c * c, exact to ~2^-48 of the result: the product error comes
+// from one FMA, the sum error from TwoSum, then a renormalisation.  The _rn
+// intrinsics keep the compiler from contracting the steps into FMAs.
+__device__ __forceinline__ void ff_sub_sq(float& hi, float& lo, float c) {
+  const float p = __fmul_rn(c, c);
+  const float pe = fmaf(c, c, -p);
+  const float s1 = __fsub_rn(hi, p);
+  const float bb = __fsub_rn(s1, hi);
+  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s1, bb)), __fsub_rn(-p, bb));
+  const float l2 = __fadd_rn(__fsub_rn(lo, pe), err);
+  const float h2 = __fadd_rn(s1, l2);
+  lo = __fsub_rn(l2, __fsub_rn(h2, s1));
+  hi = h2;
+}
+
+// One CTA: Cholesky of the 128 x 128 diagonal block at (o, o) by 32-wide
+// panels (a warp-level register factor of the diagonal block, row substitution
+// below it, a rank-32 trailing update), pivots from the float64 diagonal track
+// carried as float-float pairs; the inverse from the four 32 x 32 diagonal
+// inverses and two doubling merges.  Writes the M (hi/lo) and V = M^T (hi/lo)
+// diagonal blocks and half the log of each pivot.
+__global__ void __launch_bounds__(LEAF_NT)
     leaf_chol_inv_kernel(const float* __restrict__ A, int64_t lda, int o,
                          const double* __restrict__ dtrack, double* __restrict__ logdiag,
                          int* __restrict__ info, float* __restrict__ Mh, float* __restrict__ Ml,
                          float* __restrict__ Vh, float* __restrict__ Vl, int64_t ldm) {
-  constexpr int N = LEAF, LD = LEAF + 1;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  double* Dd = reinterpret_cast<double*>(smem_raw);  // diagonal track (as float pairs below)
-  double* Pv = Dd + N;                            // pivots (as float pairs below)
-  float* S = reinterpret_cast<float*>(Pv + N);   // L
-  float* Ms = S + N * LD;                         // L^-1
-  float* Tt = Ms + N * LD;                        // panel / merge temporary, 96 x 33 >= 64 x 65
-  float* col = Tt + 96 * 65;
-  float* dl = col + N;
-  const int tid = threadIdx.x, nt = blockDim.x;
-  const int warp = tid >> 5, lane = tid & 31, nwarps = nt >> 5;
-  for (int e = tid; e < N * N; e += nt) {
-    const int i = e / N, j = e % N;
-    S[i * LD + j] = 0.f;
-    Ms[i * LD + j] = 0.f;
-  }
-  __syncthreads();
-  for (int e = tid; e < N * N; e += nt) {
-    const int i = e / N, j = e % N;
-    if (j < i) S[i * LD + j] = A[(int64_t)(o + i) * lda + o + j];
-  }
-  // float-float copy (hi + lo, ~48 bits) of the float64 diagonal track: the
-  // pivot history keeps float64-class accuracy with float32 arithmetic only
-  // (float64 throughput on this part is a small fraction of float32)
-  float* Dh = reinterpret_cast<float*>(Dd);
+  constexpr int N = LEAF, LD = LEAF_LD, NT = LEAF_NT, PB = LEAF_PB;
+  static_assert(N == 128 && NT == 512, "tile maps below assume a 128-wide leaf and 512 threads");
+  extern __shared__ __align__(16) float leaf_smem[];
+  float* Pt = leaf_smem;              // [PB][PTLD]  rows below the panel, k-major
+  float* Lt = Pt + PB * LEAF_PTLD;    // [PB][LTLD]  diagonal block of the panel, transposed
+  float* S = Lt + PB * LEAF_LTLD;     // [N][LD]     A -> L (strictly lower part)
+  float* Ms = S + N * LD;             // [N][LD]     M = L^-1
+  float* Tt = Ms + N * LD;            // [64 * 65]   merge products
+  float* Dh = Tt + 64 * 65;           // float-float diagonal track
   float* Dlo = Dh + N;
-  float* Ph = reinterpret_cast<float*>(Pv);  // pivots as float-float pairs
+  float* Ph = Dlo + N;                // float-float pivots
   float* Pl = Ph + N;
-  for (int i = tid; i < N; i += nt) {
-    const double dv = dtrack[o + i];
+  float* Rl = Pl + N;                 // 1 / diag(L)
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  // ---- load the block (32 coalesced loads in flight per thread), zero M ----
+  {
+    float v[N * N / NT];
+#pragma unroll
+    for (int u = 0; u < N * N / NT; ++u) {
+      const int e = tid + u * NT;
+      v[u] = A[(int64_t)(o + e / N) * lda + o + e % N];
+    }
+#pragma unroll
+    for (int u = 0; u < N * N / NT; ++u) {
+      const int e = tid + u * NT;
+      S[(e / N) * LD + e % N] = v[u];
+    }
+  }
+  for (int e = tid; e < N * LD; e += NT) Ms[e] = 0.f;
+  if (tid < N) {
+    const double dv = dtrack[o + tid];
     const float hi = (float)dv;
-    Dh[i] = hi;
-    Dlo[i] = (float)(dv - (double)hi);
+    Dh[tid] = hi;
+    Dlo[tid] = (float)(dv - (double)hi);
   }
   __syncthreads();
-  // ---- Cholesky by 32-wide panels: inside a panel each pivot step touches
-  //      only the panel's columns (warps over rows, lanes over columns); the
-  //      columns right of the panel get one rank-32 update per panel ----
-  for (int c0 = 0; c0 < N; c0 += 32) {
-    const int pend = c0 + 31;
-    for (int j = c0; j <= pend; ++j) {
-      const float ph = Dh[j], pl = Dlo[j];
-      const float ljj = sqrtf(ph + pl);
-      const float rl = 1.f / ljj;
-      for (int i = j + 1 + tid; i < N; i += nt) {
-        const float v = S[i * LD + j] * rl;
-        S[i * LD + j] = v;
-        col[i] = v;
+
+  // ---- blocked right-looking Cholesky, 32-wide panels ----
+  for (int p = 0; p < N / PB; ++p) {
+    const int c0 = p * PB;
+    // P1: one warp factors the diagonal block in registers (lane = row).  The
+    // pivot for the next column comes from a float32 candidate one FMA away,
+    // while the float-float track is updated off that dependency chain.
+    if (warp == 0) {
+      const int row = c0 + lane;
+      float r[PB];
+#pragma unroll
+      for (int k = 0; k < PB; ++k) r[k] = S[row * LD + c0 + k];
+      float dh = Dh[row], dlo = Dlo[row];
+      float pf = dh + dlo;
+#pragma unroll
+      for (int j = 0; j < PB; ++j) {
+        const float piv = __shfl_sync(0xffffffffu, pf, j);
+        const float rl = rsqrtf(piv);
+        const float lij = r[j] * rl;  // meaningful for lane > j
+        if (lane == j) {
+          Ph[row] = dh;
+          Pl[row] = dlo;
+          Rl[row] = rl;
+        }
+        if (lane > j) {
+          r[j] = lij;
+          pf = fmaf(-lij, lij, dh) + dlo;
+          ff_sub_sq(dh, dlo, lij);
+        }
+#pragma unroll
+        for (int k = j + 1; k < PB; ++k) r[k] = fmaf(-lij, __shfl_sync(0xffffffffu, lij, k), r[k]);
       }
-      if (tid == 0) {
-        dl[j] = ljj;
-        Ph[j] = ph;  // no float64 work inside the loop: every warp waits on this one
-        Pl[j] = pl;
+#pragma unroll
+      for (int k = 0; k < PB; ++k) {
+        if (k < lane) S[row * LD + c0 + k] = r[k];
+        Lt[k * LEAF_LTLD + lane] = (k < lane) ? r[k] : 0.f;  // Lt[k][i] = L[i][k]
       }
-      __syncthreads();
-      const int k = j + 1 + lane;  // panel column updated by this lane
-      if (k <= pend) {
-        const float ck = col[k];
-        for (int i = k + 1 + warp; i < N; i += nwarps) S[i * LD + k] = fmaf(-col[i], ck, S[i * LD + k]);
-      }
-      if (tid > j && tid < N) {
-        // (Dh, Dlo) -= c^2 exactly to ~2^-48: product error by FMA, TwoSum,
-        // then renormalisation
-        const float c = col[tid];
-        const float p = c * c, pe = fmaf(c, c, -p);
-        const float a = Dh[tid];
-        const float s1 = a - p, bb = s1 - a;
-        const float err = (a - (s1 - bb)) + (-p - bb);
-        const float lo = (Dlo[tid] - pe) + err;
-        const float hi = s1 + lo;
-        Dlo[tid] = lo - (hi - s1);
-        Dh[tid] = hi;
-      }
-      __syncthreads();
     }
-    // rank-32 update of the strictly lower part right of the panel
-    const int r0 = pend + 1, nr = N - r0;
-    if (nr > 1) {
-      for (int e = tid; e < nr * nr; e += nt) {
-        const int r = e / nr, q = e % nr;
-        if (q >= r) continue;
-        float sacc = 0.f;
+    __syncthreads();
+    // P2: rows below the panel by substitution, one thread per row; one warp
+    // meanwhile inverts the diagonal block (lane = column).
+    const int r0 = c0 + PB, R = N - r0;
+    if (tid < R) {
+      const int row = r0 + tid;
+      float a[PB], rl[PB];
+#pragma unroll
+      for (int k = 0; k < PB; ++k) a[k] = S[row * LD + c0 + k];
+#pragma unroll
+      for (int g = 0; g < PB / 4; ++g) {
+        const float4 t = *reinterpret_cast<const float4*>(Rl + c0 + 4 * g);
+        rl[4 * g] = t.x;
+        rl[4 * g + 1] = t.y;
+        rl[4 * g + 2] = t.z;
+        rl[4 * g + 3] = t.w;
+      }
+#pragma unroll
+      for (int m = 0; m < PB; ++m) {
+        const float x = a[m] * rl[m];
+        a[m] = x;
+#pragma unroll
+        for (int g = 0; g < PB / 4; ++g) {
+          if (4 * g + 3 > m) {
+            const float4 l = *reinterpret_cast<const float4*>(Lt + m * LEAF_LTLD + 4 * g);
+            if (4 * g + 0 > m) a[4 * g + 0] = fmaf(-x, l.x, a[4 * g + 0]);
+            if (4 * g + 1 > m) a[4 * g + 1] = fmaf(-x, l.y, a[4 * g + 1]);
+            if (4 * g + 2 > m) a[4 * g + 2] = fmaf(-x, l.z, a[4 * g + 2]);
+            a[4 * g + 3] = fmaf(-x, l.w, a[4 * g + 3]);
+          }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < PB; ++k) {
+        S[row * LD + c0 + k] = a[k];
+        Pt[k * LEAF_PTLD + row] = a[k];
+      }
+    }
+    if (warp == 8) {
+      const int cc = lane;
+      float mc[PB];
+#pragma unroll
+      for (int i = 0; i < PB; ++i) {
+        float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+        for (int k = 0; k < i; ++k) {
+          const float l = Lt[k * LEAF_LTLD + i];  // L[i][k], the same for every lane
+          if (k & 1)
+            s1 = fmaf(l, mc[k], s1);
+          else
+            s0 = fmaf(l, mc[k], s0);
+        }
+        const float rli = Rl[c0 + i];
+        mc[i] = (i < cc) ? 0.f : ((i == cc) ? rli : -rli * (s0 + s1));
+      }
+#pragma unroll
+      for (int i = 0; i < PB; ++i) Ms[(c0 + i) * LD + c0 + cc] = mc[i];
+    }
+    __syncthreads();
+    // P3: rank-32 update of the strictly lower trailing part from the k-major
+    // copy (4 x 4 tiles, float4 operands); the float-float diagonal track
+    // loses the squares of the new rows on other threads.
+    if (R > 0) {
+      const int T = R / 4, ntiles = T * (T + 1) / 2;
+      for (int t = tid; t < ntiles; t += NT) {
+        int tr = (int)((sqrtf(8.f * (float)t + 1.f) - 1.f) * 0.5f);
+        while (tr * (tr + 1) / 2 > t) --tr;
+        while ((tr + 1) * (tr + 2) / 2 <= t) ++tr;
+        const int tc = t - tr * (tr + 1) / 2;
+        const int R0 = r0 + 4 * tr, C0 = r0 + 4 * tc;
+        float acc[4][4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
 #pragma unroll 8
-        for (int c = c0; c <= pend; ++c) sacc = fmaf(S[(r0 + r) * LD + c], S[(r0 + q) * LD + c], sacc);
-        S[(r0 + r) * LD + r0 + q] -= sacc;
+        for (int k = 0; k < PB; ++k) {
+          const float4 a4 = *reinterpret_cast<const float4*>(Pt + k * LEAF_PTLD + R0);
+          const float4 b4 = *reinterpret_cast<const float4*>(Pt + k * LEAF_PTLD + C0);
+          const float av[4] = {a4.x, a4.y, a4.z, a4.w}, bv[4] = {b4.x, b4.y, b4.z, b4.w};
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(av[u], bv[v], acc[u][v]);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int v = 0; v < 4; ++v)
+            if (R0 + u > C0 + v) S[(R0 + u) * LD + C0 + v] -= acc[u][v];
+      }
+      if (tid >= NT - R) {
+        const int row = r0 + tid - (NT - R);
+        float dh = Dh[row], dlo = Dlo[row];
+#pragma unroll
+        for (int k = 0; k < PB; ++k) ff_sub_sq(dh, dlo, Pt[k * LEAF_PTLD + row]);
+        Dh[row] = dh;
+        Dlo[row] = dlo;
       }
       __syncthreads();
     }
   }
-  for (int i = tid; i < N; i += nt) {
-    S[i * LD + i] = dl[i];
-    const double pv = (double)Ph[i] + (double)Pl[i];
-    logdiag[o + i] = 0.5 * log(pv);
-    if (!(pv > 0.0)) atomicMin(info, o + i + 1);
+  if (tid < N) {
+    const double pv = (double)Ph[tid] + (double)Pl[tid];
+    logdiag[o + tid] = 0.5 * log(pv);
+    if (!(pv > 0.0)) atomicMin(info, o + tid + 1);
   }
-  __syncthreads();
-  // ---- inverse: 32 x 32 diagonal blocks (lane = column, registers) ----
-  if (warp < 4) {
-    const int b0 = warp * 32, c = lane;
-    float mc[32];
-#pragma unroll
-    for (int i = 0; i < 32; ++i) {
-      float sacc = 0.f;
-#pragma unroll
-      for (int k = 0; k < i; ++k) sacc = fmaf(S[(b0 + i) * LD + b0 + k], mc[k], sacc);
-      const float dii = S[(b0 + i) * LD + b0 + i];
-      mc[i] = (i < c) ? 0.f : ((i == c) ? 1.f / dii : -sacc / dii);
-    }
-#pragma unroll
-    for (int i = 0; i < 32; ++i) Ms[(b0 + i) * LD + b0 + c] = mc[i];
-  }
-  __syncthreads();
-  // ---- doubling merges: M21 = -M22 (L21 M11) for half sizes 32 then 64,
-  //      each thread computing a 2 x 4 output block ----
-  for (int h = 32; h < N; h *= 2) {
-    const int pairs = N / (2 * h);
-    const int nblk = (h / 2) * (h / 4);  // 2 x 4 blocks per h x h product
-    for (int pr = 0; pr < pairs; ++pr) {
-      const int ob = pr * 2 * h;
-      // T = L21 M11 (M11 lower: M11[c][j] = 0 for c < j)
-      for (int bidx = tid; bidx < nblk; bidx += nt) {
-        const int i2 = (bidx / (h / 4)) * 2, j4 = (bidx % (h / 4)) * 4;
-        float a0[4] = {0.f, 0.f, 0.f, 0.f}, a1[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int c = j4; c < h; ++c) {
-          const float l0 = S[(ob + h + i2) * LD + ob + c], l1 = S[(ob + h + i2 + 1) * LD + ob + c];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const float m = Ms[(ob + c) * LD + ob + j4 + q];
-            a0[q] = fmaf(l0, m, a0[q]);
-            a1[q] = fmaf(l1, m, a1[q]);
-          }
-        }
+  // ---- off-diagonal blocks of M by doubling merges, M21 = -M22 (L21 M11):
+  //      both 32-wide pairs in one pass, then the 64-wide one; 2 x 4 tiles ----
+  for (int h = PB; h < N; h *= 2) {
+    const int pairs = N / (2 * h), per = (h / 2) * (h / 4), tl = h + 1;
+    for (int job = tid; job < pairs * per; job += NT) {
+      const int pr = job / per, b = job % per, ob = pr * 2 * h;
+      const int i2 = (b / (h / 4)) * 2, j4 = (b % (h / 4)) * 4;
+      float* T = Tt + pr * h * tl;
+      float a0[4] = {0.f, 0.f, 0.f, 0.f}, a1[4] = {0.f, 0.f, 0.f, 0.f};
+      for (int c = j4; c < h; ++c) {  // M11[c][j] = 0 for c < j
+        const float l0 = S[(ob + h + i2) * LD + ob + c], l1 = S[(ob + h + i2 + 1) * LD + ob + c];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-          Tt[i2 * 65 + j4 + q] = a0[q];
-          Tt[(i2 + 1) * 65 + j4 + q] = a1[q];
+          const float m = Ms[(ob + c) * LD + ob + j4 + q];
+          a0[q] = fmaf(l0, m, a0[q]);
+          a1[q] = fmaf(l1, m, a1[q]);
         }
       }
-      __syncthreads();
-      // M21 = -M22 T (M22 lower: M22[i][c] = 0 for c > i)
-      for (int bidx = tid; bidx < nblk; bidx += nt) {
-        const int i2 = (bidx / (h / 4)) * 2, j4 = (bidx % (h / 4)) * 4;
-        float a0[4] = {0.f, 0.f, 0.f, 0.f}, a1[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int c = 0; c <= i2 + 1; ++c) {
-          const float m0 = Ms[(ob + h + i2) * LD + ob + h + c];  // zero when c > i2
-          const float m1 = Ms[(ob + h + i2 + 1) * LD + ob + h + c];
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const float t = Tt[c * 65 + j4 + q];
-            a0[q] = fmaf(m0, t, a0[q]);
-            a1[q] = fmaf(m1, t, a1[q]);
-          }
-        }
+      for (int q = 0; q < 4; ++q) {
+        T[i2 * tl + j4 + q] = a0[q];
+        T[(i2 + 1) * tl + j4 + q] = a1[q];
+      }
+    }
+    __syncthreads();
+    for (int job = tid; job < pairs * per; job += NT) {
+      const int pr = job / per, b = job % per, ob = pr * 2 * h;
+      const int i2 = (b / (h / 4)) * 2, j4 = (b % (h / 4)) * 4;
+      const float* T = Tt + pr * h * tl;
+      float a0[4] = {0.f, 0.f, 0.f, 0.f}, a1[4] = {0.f, 0.f, 0.f, 0.f};
+      for (int c = 0; c <= i2 + 1; ++c) {  // M22[i][c] = 0 for c > i
+        const float m0 = Ms[(ob + h + i2) * LD + ob + h + c];
+        const float m1 = Ms[(ob + h + i2 + 1) * LD + ob + h + c];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-          Ms[(ob + h + i2) * LD + ob + j4 + q] = -a0[q];
-          Ms[(ob + h + i2 + 1) * LD + ob + j4 + q] = -a1[q];
+          const float t = T[c * tl + j4 + q];
+          a0[q] = fmaf(m0, t, a0[q]);
+          a1[q] = fmaf(m1, t, a1[q]);
         }
       }
-      __syncthreads();
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        Ms[(ob + h + i2) * LD + ob + j4 + q] = -a0[q];
+        Ms[(ob + h + i2 + 1) * LD + ob + j4 + q] = -a1[q];
+      }
     }
+    __syncthreads();
   }
-  // ---- write M and V = M^T as TF32 hi/lo ----
-  for (int e = tid; e < N * N; e += nt) {
-    const int i = e / N, j = e % N;
-    const float m = Ms[i * LD + j];
-    const float hi = tf32_rna_f(m), lo = tf32_rna_f(m - hi);
-    Mh[(int64_t)(o + i) * ldm + o + j] = hi;
-    Ml[(int64_t)(o + i) * ldm + o + j] = lo;
-    const float mt = Ms[j * LD + i];
-    const float hit = tf32_rna_f(mt), lot = tf32_rna_f(mt - hit);
-    Vh[(int64_t)(o + i) * ldm + o + j] = hit;
-    Vl[(int64_t)(o + i) * ldm + o + j] = lot;
+  // ---- write M and V = M^T as TF32 hi/lo: one warp per 32 x 32 block,
+  //      lane = column (coalesced rows, conflict-free shared reads) ----
+  {
+    const int bi = warp >> 2, bj = warp & 3;
+    const int col = bj * PB + lane;
+    for (int i = 0; i < PB; ++i) {
+      const int row = bi * PB + i;
+      const int64_t off = (int64_t)(o + row) * ldm + o + col;
+      const float m = (bj <= bi) ? Ms[row * LD + col] : 0.f;
+      const float mt = (bj >= bi) ? Ms[col * LD + row] : 0.f;
+      const float hi = tf32_rna_f(m), hit = tf32_rna_f(mt);
+      Mh[off] = hi;
+      Ml[off] = tf32_rna_f(m - hi);
+      Vh[off] = hit;
+      Vl[off] = tf32_rna_f(mt - hit);
+    }
   }
 }
 
 size_t leaf_smem_bytes() {
-  return 2 * LEAF * sizeof(double) + (size_t)(2 * LEAF * (LEAF + 1) + 96 * 65 + 2 * LEAF) * 4;
+  return (size_t)(LEAF_PB * LEAF_PTLD + LEAF_PB * LEAF_LTLD + 2 * LEAF * LEAF_LD + 64 * 65 + 5 * LEAF) * 4;
 }
 
 // y = op(Th + Tl) x over a triangle, float64 accumulation, one warp per row.
@@ -282,7 +380,7 @@ struct TcChol {
 
 cudaError_t chol_inv_rec(TcChol& c, int o, int sz) {
   if (sz == LEAF) {
-    leaf_chol_inv_kernel<<<1, 512, leaf_smem_bytes(), c.s>>>(c.A, c.ld, o, c.dtrack, c.logdiag,
+    leaf_chol_inv_kernel<<<1, LEAF_NT, leaf_smem_bytes(), c.s>>>(c.A, c.ld, o, c.dtrack, c.logdiag,
                                                              c.info, c.Mh, c.Ml, c.Vh, c.Vl, c.ld);
     return launch_status();
   }
