@@ -27,10 +27,10 @@ namespace {
 constexpr int LEAF = 128;
 constexpr int LEAF_NT = 512;  // threads of the leaf kernel
 
-constexpr int LEAF_LD = LEAF + 1;   // S / Ms row stride: odd, so column walks are conflict-free
-constexpr int LEAF_PB = 32;         // panel width
-constexpr int LEAF_PTLD = LEAF + 4; // k-major panel copy: 16-byte rows
-constexpr int LEAF_LTLD = LEAF_PB + 4;
+constexpr int LEAF_PB = 32;             // panel width
+constexpr int LEAF_LDT = LEAF + 4;      // k-major L and row-major M: 16-byte rows
+constexpr int LEAF_TLD = 64 + 4;        // merge product rows
+constexpr int LEAF_WNT = LEAF_NT - 32;  // panel-loop threads; the last warp inverts diagonal blocks
 
 __device__ __forceinline__ float tf32_rna_f(float x) {
   uint32_t r;
@@ -53,47 +53,117 @@ __device__ __forceinline__ void ff_sub_sq(float& hi, float& lo, float c) {
   hi = h2;
 }
 
-// One CTA: Cholesky of the 128 x 128 diagonal block at (o, o) by 32-wide
-// panels (a warp-level register factor of the diagonal block, row substitution
-// below it, a rank-32 trailing update), pivots from the float64 diagonal track
-// carried as float-float pairs; the inverse from the four 32 x 32 diagonal
-// inverses and two doubling merges.  Writes the M (hi/lo) and V = M^T (hi/lo)
-// diagonal blocks and half the log of each pivot.
+__device__ __forceinline__ void bar_sync_n(int id, int n) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+__device__ __forceinline__ void bar_arrive_n(int id, int n) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+
+__device__ __forceinline__ void fma4x4(float (&acc)[4][4], const float4 a, const float4 b) {
+  const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(av[u], bv[v], acc[u][v]);
+}
+
+// M rows [r0, r0+nr) x columns [c0, c0+nc) to global as TF32 hi/lo (float4 rows)
+__device__ __forceinline__ void leaf_put_m(const float* Ms, int r0, int nr, int c0, int nc, int o,
+                                           int64_t ldm, float* Mh, float* Ml, int t, int nth) {
+  const int q4 = nc / 4;
+  for (int e = t; e < nr * q4; e += nth) {
+    const int i = r0 + e / q4, c = c0 + 4 * (e % q4);
+    const float4 m = *reinterpret_cast<const float4*>(Ms + i * LEAF_LDT + c);
+    const float4 hi = make_float4(tf32_rna_f(m.x), tf32_rna_f(m.y), tf32_rna_f(m.z), tf32_rna_f(m.w));
+    const float4 lo = make_float4(tf32_rna_f(m.x - hi.x), tf32_rna_f(m.y - hi.y),
+                                  tf32_rna_f(m.z - hi.z), tf32_rna_f(m.w - hi.w));
+    const int64_t off = (int64_t)(o + i) * ldm + o + c;
+    *reinterpret_cast<float4*>(Mh + off) = hi;
+    *reinterpret_cast<float4*>(Ml + off) = lo;
+  }
+}
+
+// V = M^T rows [vr0, vr0+nvr) x columns [vc0, vc0+nvc): lane = V column
+// (coalesced stores), float4 reads along M rows (conflict-free)
+__device__ __forceinline__ void leaf_put_v(const float* Ms, int vr0, int nvr, int vc0, int nvc,
+                                           int o, int64_t ldm, float* Vh, float* Vl, int t, int nth) {
+  for (int e = t; e < (nvr / 4) * nvc; e += nth) {
+    const int vc = vc0 + e % nvc, vr = vr0 + 4 * (e / nvc);
+    const float4 m = *reinterpret_cast<const float4*>(Ms + vc * LEAF_LDT + vr);  // M[vc][vr..]
+    const float mv[4] = {m.x, m.y, m.z, m.w};
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int64_t off = (int64_t)(o + vr + u) * ldm + o + vc;
+      const float hi = tf32_rna_f(mv[u]);
+      Vh[off] = hi;
+      Vl[off] = tf32_rna_f(mv[u] - hi);
+    }
+  }
+}
+
+// Columns [k0, k0+nk) of the block into k-major L (lane = row: conflict-free)
+__device__ __forceinline__ void leaf_load_cols(const float* __restrict__ A, int64_t lda, int o,
+                                               float* LT, int k0, int nk, int t, int nth) {
+  constexpr int N = LEAF, CH = 8;  // float4 loads in flight per thread
+  const int total = N * (nk / 4);
+  for (int base = t; base < total; base += CH * nth) {
+    float4 v[CH];
+#pragma unroll
+    for (int u = 0; u < CH; ++u) {
+      const int e = base + u * nth;
+      if (e < total)
+        v[u] = *reinterpret_cast<const float4*>(A + (int64_t)(o + e % N) * lda + o + k0 + 4 * (e / N));
+    }
+#pragma unroll
+    for (int u = 0; u < CH; ++u) {
+      const int e = base + u * nth;
+      if (e < total) {
+        const int i = e % N, k = k0 + 4 * (e / N);
+        LT[(k + 0) * LEAF_LDT + i] = v[u].x;
+        LT[(k + 1) * LEAF_LDT + i] = v[u].y;
+        LT[(k + 2) * LEAF_LDT + i] = v[u].z;
+        LT[(k + 3) * LEAF_LDT + i] = v[u].w;
+      }
+    }
+  }
+}
+
+// One CTA: Cholesky of the 128 x 128 diagonal block at (o, o) and its inverse.
+// Pivots come from the float64 diagonal track, carried as float-float pairs.
+//  * blocked right-looking factor over 32-wide panels (warps 0..14): one warp
+//    factors the diagonal block in registers, one thread per row substitutes
+//    the rows below it, then a rank-32 update of the lower trailing part from
+//    the k-major L (4 x 4 tiles, float4 operands);
+//  * the last warp inverts each 32 x 32 diagonal block as soon as it is
+//    factored (handed over through a named barrier) and writes it out;
+//  * two doubling merges M21 = -M22 (L21 M11) fill the rest of M.
+// Writes the lower blocks of M (hi/lo), the upper blocks of V = M^T (hi/lo)
+// and half the log of each pivot; the zero blocks of M and V come from
+// leaf_zero_kernel.
 __global__ void __launch_bounds__(LEAF_NT)
     leaf_chol_inv_kernel(const float* __restrict__ A, int64_t lda, int o,
                          const double* __restrict__ dtrack, double* __restrict__ logdiag,
                          int* __restrict__ info, float* __restrict__ Mh, float* __restrict__ Ml,
                          float* __restrict__ Vh, float* __restrict__ Vl, int64_t ldm) {
-  constexpr int N = LEAF, LD = LEAF_LD, NT = LEAF_NT, PB = LEAF_PB;
+  constexpr int N = LEAF, NT = LEAF_NT, PB = LEAF_PB, LDT = LEAF_LDT, TLD = LEAF_TLD,
+                WNT = LEAF_WNT;
   static_assert(N == 128 && NT == 512, "tile maps below assume a 128-wide leaf and 512 threads");
   extern __shared__ __align__(16) float leaf_smem[];
-  float* Pt = leaf_smem;              // [PB][PTLD]  rows below the panel, k-major
-  float* Lt = Pt + PB * LEAF_PTLD;    // [PB][LTLD]  diagonal block of the panel, transposed
-  float* S = Lt + PB * LEAF_LTLD;     // [N][LD]     A -> L (strictly lower part)
-  float* Ms = S + N * LD;             // [N][LD]     M = L^-1
-  float* Tt = Ms + N * LD;            // [64 * 65]   merge products
-  float* Dh = Tt + 64 * 65;           // float-float diagonal track
+  float* LT = leaf_smem;      // [N][LDT]  LT[k][i] = L[i][k]
+  float* Ms = LT + N * LDT;   // [N][LDT]  M = L^-1, row-major
+  float* Tt = Ms + N * LDT;   // [64][TLD] merge products; column buffer of the diagonal factor
+  float* Dh = Tt + 64 * TLD;  // float-float diagonal track
   float* Dlo = Dh + N;
-  float* Ph = Dlo + N;                // float-float pivots
+  float* Ph = Dlo + N;        // float-float pivots
   float* Pl = Ph + N;
-  float* Rl = Pl + N;                 // 1 / diag(L)
+  float* Rl = Pl + N;         // 1 / diag(L)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-  // ---- load the block (32 coalesced loads in flight per thread), zero M ----
-  {
-    float v[N * N / NT];
-#pragma unroll
-    for (int u = 0; u < N * N / NT; ++u) {
-      const int e = tid + u * NT;
-      v[u] = A[(int64_t)(o + e / N) * lda + o + e % N];
-    }
-#pragma unroll
-    for (int u = 0; u < N * N / NT; ++u) {
-      const int e = tid + u * NT;
-      S[(e / N) * LD + e % N] = v[u];
-    }
-  }
-  for (int e = tid; e < N * LD; e += NT) Ms[e] = 0.f;
+  // ---- the block into k-major L, the diagonal track, M = 0 ----
+  leaf_load_cols(A, lda, o, LT, 0, N, tid, NT);
+  for (int e = tid; e < N * LDT / 4; e += NT)
+    reinterpret_cast<float4*>(Ms)[e] = make_float4(0.f, 0.f, 0.f, 0.f);
   if (tid < N) {
     const double dv = dtrack[o + tid];
     const float hi = (float)dv;
@@ -102,219 +172,283 @@ __global__ void __launch_bounds__(LEAF_NT)
   }
   __syncthreads();
 
-  // ---- blocked right-looking Cholesky, 32-wide panels ----
-  for (int p = 0; p < N / PB; ++p) {
-    const int c0 = p * PB;
-    // P1: one warp factors the diagonal block in registers (lane = row).  The
-    // pivot for the next column comes from a float32 candidate one FMA away,
-    // while the float-float track is updated off that dependency chain.
-    if (warp == 0) {
-      const int row = c0 + lane;
-      float r[PB];
+  if (warp < WNT / 32) {
+    // ---- blocked right-looking Cholesky over 32-wide panels (warps 0..14) ----
+    for (int p = 0; p < N / PB; ++p) {
+      const int c0 = p * PB;
+      if (warp == 0) {
+        // P1: the diagonal block in registers, lane = row; the next pivot
+        // comes from a float32 candidate one FMA away while the float-float
+        // track is updated off that dependency chain; the new column is
+        // broadcast through a double-buffered shared row
+        const int row = c0 + lane;
+        float r[PB];
 #pragma unroll
-      for (int k = 0; k < PB; ++k) r[k] = S[row * LD + c0 + k];
-      float dh = Dh[row], dlo = Dlo[row];
-      float pf = dh + dlo;
+        for (int k = 0; k < PB; ++k) r[k] = LT[(c0 + k) * LDT + row];
+        float dh = Dh[row], dlo = Dlo[row];
+        float pf = dh + dlo;
 #pragma unroll
-      for (int j = 0; j < PB; ++j) {
-        const float piv = __shfl_sync(0xffffffffu, pf, j);
-        const float rl = rsqrtf(piv);
-        const float lij = r[j] * rl;  // meaningful for lane > j
-        if (lane == j) {
-          Ph[row] = dh;
-          Pl[row] = dlo;
-          Rl[row] = rl;
+        for (int j = 0; j < PB; ++j) {
+          const float piv = __shfl_sync(0xffffffffu, pf, j);
+          const float rl = rsqrtf(piv);
+          const float lij = r[j] * rl;  // meaningful for lane > j
+          if (lane == j) {
+            Ph[row] = dh;
+            Pl[row] = dlo;
+            Rl[row] = rl;
+          }
+          const bool below = lane > j;
+          const float npf = fmaf(-lij, lij, dh) + dlo;
+          float nh = dh, nl = dlo;
+          ff_sub_sq(nh, nl, lij);
+          r[j] = below ? lij : r[j];
+          pf = below ? npf : pf;
+          dh = below ? nh : dh;
+          dlo = below ? nl : dlo;
+          float* colb = Tt + (j & 1) * PB;  // double-buffered column
+          colb[lane] = lij;
+          __syncwarp();
+#pragma unroll
+          for (int g = (j + 1) / 4; g < PB / 4; ++g) {
+            const float4 c4 = *reinterpret_cast<const float4*>(colb + 4 * g);
+            if (4 * g + 0 > j) r[4 * g + 0] = fmaf(-lij, c4.x, r[4 * g + 0]);
+            if (4 * g + 1 > j) r[4 * g + 1] = fmaf(-lij, c4.y, r[4 * g + 1]);
+            if (4 * g + 2 > j) r[4 * g + 2] = fmaf(-lij, c4.z, r[4 * g + 2]);
+            if (4 * g + 3 > j) r[4 * g + 3] = fmaf(-lij, c4.w, r[4 * g + 3]);
+          }
         }
-        if (lane > j) {
-          r[j] = lij;
-          pf = fmaf(-lij, lij, dh) + dlo;
-          ff_sub_sq(dh, dlo, lij);
-        }
 #pragma unroll
-        for (int k = j + 1; k < PB; ++k) r[k] = fmaf(-lij, __shfl_sync(0xffffffffu, lij, k), r[k]);
+        for (int k = 0; k < PB; ++k) LT[(c0 + k) * LDT + row] = (k < lane) ? r[k] : 0.f;
+        bar_arrive_n(2 + p, 64);  // diagonal block p is final: hand it to the inverting warp
       }
+      bar_sync_n(1, WNT);
+      // P2: rows below the panel by substitution, one thread per row
+      const int r0 = c0 + PB, R = N - r0;
+      if (tid < R) {
+        const int row = r0 + tid;
+        float a[PB], rl[PB];
 #pragma unroll
-      for (int k = 0; k < PB; ++k) {
-        if (k < lane) S[row * LD + c0 + k] = r[k];
-        Lt[k * LEAF_LTLD + lane] = (k < lane) ? r[k] : 0.f;  // Lt[k][i] = L[i][k]
-      }
-    }
-    __syncthreads();
-    // P2: rows below the panel by substitution, one thread per row; one warp
-    // meanwhile inverts the diagonal block (lane = column).
-    const int r0 = c0 + PB, R = N - r0;
-    if (tid < R) {
-      const int row = r0 + tid;
-      float a[PB], rl[PB];
-#pragma unroll
-      for (int k = 0; k < PB; ++k) a[k] = S[row * LD + c0 + k];
-#pragma unroll
-      for (int g = 0; g < PB / 4; ++g) {
-        const float4 t = *reinterpret_cast<const float4*>(Rl + c0 + 4 * g);
-        rl[4 * g] = t.x;
-        rl[4 * g + 1] = t.y;
-        rl[4 * g + 2] = t.z;
-        rl[4 * g + 3] = t.w;
-      }
-#pragma unroll
-      for (int m = 0; m < PB; ++m) {
-        const float x = a[m] * rl[m];
-        a[m] = x;
+        for (int k = 0; k < PB; ++k) a[k] = LT[(c0 + k) * LDT + row];
 #pragma unroll
         for (int g = 0; g < PB / 4; ++g) {
-          if (4 * g + 3 > m) {
-            const float4 l = *reinterpret_cast<const float4*>(Lt + m * LEAF_LTLD + 4 * g);
-            if (4 * g + 0 > m) a[4 * g + 0] = fmaf(-x, l.x, a[4 * g + 0]);
-            if (4 * g + 1 > m) a[4 * g + 1] = fmaf(-x, l.y, a[4 * g + 1]);
-            if (4 * g + 2 > m) a[4 * g + 2] = fmaf(-x, l.z, a[4 * g + 2]);
-            a[4 * g + 3] = fmaf(-x, l.w, a[4 * g + 3]);
+          const float4 t = *reinterpret_cast<const float4*>(Rl + c0 + 4 * g);
+          rl[4 * g] = t.x;
+          rl[4 * g + 1] = t.y;
+          rl[4 * g + 2] = t.z;
+          rl[4 * g + 3] = t.w;
+        }
+#pragma unroll
+        for (int m = 0; m < PB; ++m) {
+          const float x = a[m] * rl[m];
+          a[m] = x;
+#pragma unroll
+          for (int g = 0; g < PB / 4; ++g) {
+            if (4 * g + 3 > m) {  // column m of the diagonal block: zeros on and above it
+              const float4 l = *reinterpret_cast<const float4*>(LT + (c0 + m) * LDT + c0 + 4 * g);
+              if (4 * g + 0 > m) a[4 * g + 0] = fmaf(-x, l.x, a[4 * g + 0]);
+              if (4 * g + 1 > m) a[4 * g + 1] = fmaf(-x, l.y, a[4 * g + 1]);
+              if (4 * g + 2 > m) a[4 * g + 2] = fmaf(-x, l.z, a[4 * g + 2]);
+              a[4 * g + 3] = fmaf(-x, l.w, a[4 * g + 3]);
+            }
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < PB; ++k) LT[(c0 + k) * LDT + row] = a[k];
+      }
+      bar_sync_n(1, WNT);
+      // P3: rank-32 update of the lower trailing part, 4 x 4 tiles enumerated
+      // by tile column (a warp's lanes share the column and walk the rows);
+      // other threads take the squares off the float-float diagonal track
+      if (R > 0) {
+        const int T = R / 4, ntiles = T * (T + 1) / 2;
+        for (int t = tid; t < ntiles; t += WNT) {
+          int tc = 0, rem = t;
+          while (rem >= T - tc) {
+            rem -= T - tc;
+            ++tc;
+          }
+          const int R0 = r0 + 4 * (tc + rem), C0 = r0 + 4 * tc;
+          float acc[4][4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
+#pragma unroll 8
+          for (int k = 0; k < PB; ++k)
+            fma4x4(acc, *reinterpret_cast<const float4*>(LT + (c0 + k) * LDT + R0),
+                   *reinterpret_cast<const float4*>(LT + (c0 + k) * LDT + C0));
+#pragma unroll
+          for (int v = 0; v < 4; ++v) {
+            float4* d = reinterpret_cast<float4*>(LT + (C0 + v) * LDT + R0);
+            float4 x = *d;
+            x.x -= acc[0][v];
+            x.y -= acc[1][v];
+            x.z -= acc[2][v];
+            x.w -= acc[3][v];
+            *d = x;
+          }
+        }
+        if (tid >= WNT - R) {
+          const int row = r0 + tid - (WNT - R);
+          float dh = Dh[row], dlo = Dlo[row];
+#pragma unroll
+          for (int k = 0; k < PB; ++k) ff_sub_sq(dh, dlo, LT[(c0 + k) * LDT + row]);
+          Dh[row] = dh;
+          Dlo[row] = dlo;
+        }
+        bar_sync_n(1, WNT);
+      }
+    }
+  } else {
+    // ---- last warp: invert each diagonal block as soon as it is factored
+    //      (lane = column; right-looking, float4 reads down L's columns) and
+    //      write it out, M and V = M^T ----
+    for (int p = 0; p < N / PB; ++p) {
+      const int c0 = p * PB, cc = lane;
+      bar_sync_n(2 + p, 64);
+      float acc[PB], mc[PB];
+#pragma unroll
+      for (int i = 0; i < PB; ++i) acc[i] = 0.f;
+#pragma unroll
+      for (int k = 0; k < PB; ++k) {
+        const float rlk = Rl[c0 + k];
+        mc[k] = rlk * ((k == cc) ? 1.f - acc[k] : -acc[k]);  // zero for k < cc
+#pragma unroll
+        for (int g = 0; g < PB / 4; ++g) {
+          if (4 * g + 3 > k) {
+            const float4 l = *reinterpret_cast<const float4*>(LT + (c0 + k) * LDT + c0 + 4 * g);
+            if (4 * g + 0 > k) acc[4 * g + 0] = fmaf(l.x, mc[k], acc[4 * g + 0]);
+            if (4 * g + 1 > k) acc[4 * g + 1] = fmaf(l.y, mc[k], acc[4 * g + 1]);
+            if (4 * g + 2 > k) acc[4 * g + 2] = fmaf(l.z, mc[k], acc[4 * g + 2]);
+            acc[4 * g + 3] = fmaf(l.w, mc[k], acc[4 * g + 3]);
           }
         }
       }
 #pragma unroll
-      for (int k = 0; k < PB; ++k) {
-        S[row * LD + c0 + k] = a[k];
-        Pt[k * LEAF_PTLD + row] = a[k];
-      }
-    }
-    if (warp == 8) {
-      const int cc = lane;
-      float mc[PB];
-#pragma unroll
-      for (int i = 0; i < PB; ++i) {
-        float s0 = 0.f, s1 = 0.f;
-#pragma unroll
-        for (int k = 0; k < i; ++k) {
-          const float l = Lt[k * LEAF_LTLD + i];  // L[i][k], the same for every lane
-          if (k & 1)
-            s1 = fmaf(l, mc[k], s1);
-          else
-            s0 = fmaf(l, mc[k], s0);
-        }
-        const float rli = Rl[c0 + i];
-        mc[i] = (i < cc) ? 0.f : ((i == cc) ? rli : -rli * (s0 + s1));
-      }
-#pragma unroll
-      for (int i = 0; i < PB; ++i) Ms[(c0 + i) * LD + c0 + cc] = mc[i];
-    }
-    __syncthreads();
-    // P3: rank-32 update of the strictly lower trailing part from the k-major
-    // copy (4 x 4 tiles, float4 operands); the float-float diagonal track
-    // loses the squares of the new rows on other threads.
-    if (R > 0) {
-      const int T = R / 4, ntiles = T * (T + 1) / 2;
-      for (int t = tid; t < ntiles; t += NT) {
-        int tr = (int)((sqrtf(8.f * (float)t + 1.f) - 1.f) * 0.5f);
-        while (tr * (tr + 1) / 2 > t) --tr;
-        while ((tr + 1) * (tr + 2) / 2 <= t) ++tr;
-        const int tc = t - tr * (tr + 1) / 2;
-        const int R0 = r0 + 4 * tr, C0 = r0 + 4 * tc;
-        float acc[4][4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-#pragma unroll
-          for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
-#pragma unroll 8
-        for (int k = 0; k < PB; ++k) {
-          const float4 a4 = *reinterpret_cast<const float4*>(Pt + k * LEAF_PTLD + R0);
-          const float4 b4 = *reinterpret_cast<const float4*>(Pt + k * LEAF_PTLD + C0);
-          const float av[4] = {a4.x, a4.y, a4.z, a4.w}, bv[4] = {b4.x, b4.y, b4.z, b4.w};
-#pragma unroll
-          for (int u = 0; u < 4; ++u)
-#pragma unroll
-            for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(av[u], bv[v], acc[u][v]);
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-#pragma unroll
-          for (int v = 0; v < 4; ++v)
-            if (R0 + u > C0 + v) S[(R0 + u) * LD + C0 + v] -= acc[u][v];
-      }
-      if (tid >= NT - R) {
-        const int row = r0 + tid - (NT - R);
-        float dh = Dh[row], dlo = Dlo[row];
-#pragma unroll
-        for (int k = 0; k < PB; ++k) ff_sub_sq(dh, dlo, Pt[k * LEAF_PTLD + row]);
-        Dh[row] = dh;
-        Dlo[row] = dlo;
-      }
-      __syncthreads();
+      for (int i = 0; i < PB; ++i) Ms[(c0 + i) * LDT + c0 + cc] = mc[i];
+      __syncwarp();
+      leaf_put_m(Ms, c0, PB, c0, PB, o, ldm, Mh, Ml, lane, 32);
+      leaf_put_v(Ms, c0, PB, c0, PB, o, ldm, Vh, Vl, lane, 32);
     }
   }
-  if (tid < N) {
-    const double pv = (double)Ph[tid] + (double)Pl[tid];
-    logdiag[o + tid] = 0.5 * log(pv);
-    if (!(pv > 0.0)) atomicMin(info, o + tid + 1);
+  __syncthreads();
+  if (tid >= 384) {  // idle during every merge phase below
+    const int i = tid - 384;
+    const double pv = (double)Ph[i] + (double)Pl[i];
+    logdiag[o + i] = 0.5 * log(pv);
+    if (!(pv > 0.0)) atomicMin(info, o + i + 1);
   }
-  // ---- off-diagonal blocks of M by doubling merges, M21 = -M22 (L21 M11):
-  //      both 32-wide pairs in one pass, then the 64-wide one; 2 x 4 tiles ----
-  for (int h = PB; h < N; h *= 2) {
-    const int pairs = N / (2 * h), per = (h / 2) * (h / 4), tl = h + 1;
-    for (int job = tid; job < pairs * per; job += NT) {
-      const int pr = job / per, b = job % per, ob = pr * 2 * h;
-      const int i2 = (b / (h / 4)) * 2, j4 = (b % (h / 4)) * 4;
-      float* T = Tt + pr * h * tl;
-      float a0[4] = {0.f, 0.f, 0.f, 0.f}, a1[4] = {0.f, 0.f, 0.f, 0.f};
-      for (int c = j4; c < h; ++c) {  // M11[c][j] = 0 for c < j
-        const float l0 = S[(ob + h + i2) * LD + ob + c], l1 = S[(ob + h + i2 + 1) * LD + ob + c];
+  // ---- off-diagonal blocks of M by doubling merges, M21 = -M22 (L21 M11),
+  //      4 x 4 tiles with float4 operands: both 32-wide pairs, then 64 ----
+  if (tid < 128) {  // T = L21 M11 for the pairs at 0 and 64 (lanes walk rows)
+    const int pr = tid >> 6, b = tid & 63, ob = pr * 64;
+    const int i0 = (b & 7) * 4, j0 = (b >> 3) * 4;
+    float acc[4][4] = {};
+#pragma unroll 4
+    for (int c = j0; c < PB; ++c)  // M11[c][j] = 0 for c < j
+      fma4x4(acc, *reinterpret_cast<const float4*>(LT + (ob + c) * LDT + ob + PB + i0),
+             *reinterpret_cast<const float4*>(Ms + (ob + c) * LDT + ob + j0));
+    float* T = Tt + pr * PB * TLD;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const float m = Ms[(ob + c) * LD + ob + j4 + q];
-          a0[q] = fmaf(l0, m, a0[q]);
-          a1[q] = fmaf(l1, m, a1[q]);
-        }
-      }
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        T[i2 * tl + j4 + q] = a0[q];
-        T[(i2 + 1) * tl + j4 + q] = a1[q];
-      }
-    }
-    __syncthreads();
-    for (int job = tid; job < pairs * per; job += NT) {
-      const int pr = job / per, b = job % per, ob = pr * 2 * h;
-      const int i2 = (b / (h / 4)) * 2, j4 = (b % (h / 4)) * 4;
-      const float* T = Tt + pr * h * tl;
-      float a0[4] = {0.f, 0.f, 0.f, 0.f}, a1[4] = {0.f, 0.f, 0.f, 0.f};
-      for (int c = 0; c <= i2 + 1; ++c) {  // M22[i][c] = 0 for c > i
-        const float m0 = Ms[(ob + h + i2) * LD + ob + h + c];
-        const float m1 = Ms[(ob + h + i2 + 1) * LD + ob + h + c];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const float t = T[c * tl + j4 + q];
-          a0[q] = fmaf(m0, t, a0[q]);
-          a1[q] = fmaf(m1, t, a1[q]);
-        }
-      }
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        Ms[(ob + h + i2) * LD + ob + j4 + q] = -a0[q];
-        Ms[(ob + h + i2 + 1) * LD + ob + j4 + q] = -a1[q];
-      }
-    }
-    __syncthreads();
+    for (int u = 0; u < 4; ++u)
+      *reinterpret_cast<float4*>(T + (i0 + u) * TLD + j0) =
+          make_float4(acc[u][0], acc[u][1], acc[u][2], acc[u][3]);
   }
-  // ---- write M and V = M^T as TF32 hi/lo: one warp per 32 x 32 block,
-  //      lane = column (coalesced rows, conflict-free shared reads) ----
-  {
-    const int bi = warp >> 2, bj = warp & 3;
-    const int col = bj * PB + lane;
-    for (int i = 0; i < PB; ++i) {
-      const int row = bi * PB + i;
-      const int64_t off = (int64_t)(o + row) * ldm + o + col;
-      const float m = (bj <= bi) ? Ms[row * LD + col] : 0.f;
-      const float mt = (bj >= bi) ? Ms[col * LD + row] : 0.f;
-      const float hi = tf32_rna_f(m), hit = tf32_rna_f(mt);
-      Mh[off] = hi;
-      Ml[off] = tf32_rna_f(m - hi);
-      Vh[off] = hit;
-      Vl[off] = tf32_rna_f(mt - hit);
+  __syncthreads();
+  if (tid < 128) {  // M21 = -M22 T
+    const int pr = tid >> 6, b = tid & 63, ob = pr * 64;
+    const int i0 = (b >> 3) * 4, j0 = (b & 7) * 4;
+    const float* T = Tt + pr * PB * TLD;
+    float acc[4][4] = {};
+#pragma unroll 2
+    for (int c4 = 0; c4 <= i0 / 4; ++c4) {  // M22[i][c] = 0 for c > i
+      float4 mrow[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        mrow[u] = *reinterpret_cast<const float4*>(Ms + (ob + PB + i0 + u) * LDT + ob + PB + 4 * c4);
+      fma4x4(acc, make_float4(mrow[0].x, mrow[1].x, mrow[2].x, mrow[3].x),
+             *reinterpret_cast<const float4*>(T + (4 * c4 + 0) * TLD + j0));
+      fma4x4(acc, make_float4(mrow[0].y, mrow[1].y, mrow[2].y, mrow[3].y),
+             *reinterpret_cast<const float4*>(T + (4 * c4 + 1) * TLD + j0));
+      fma4x4(acc, make_float4(mrow[0].z, mrow[1].z, mrow[2].z, mrow[3].z),
+             *reinterpret_cast<const float4*>(T + (4 * c4 + 2) * TLD + j0));
+      fma4x4(acc, make_float4(mrow[0].w, mrow[1].w, mrow[2].w, mrow[3].w),
+             *reinterpret_cast<const float4*>(T + (4 * c4 + 3) * TLD + j0));
     }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      *reinterpret_cast<float4*>(Ms + (ob + PB + i0 + u) * LDT + ob + j0) =
+          make_float4(-acc[u][0], -acc[u][1], -acc[u][2], -acc[u][3]);
+  }
+  __syncthreads();
+  if (tid < 256) {  // T = L21 M11 for the 64-wide halves (lanes walk rows)
+    const int i0 = (tid & 15) * 4, j0 = (tid >> 4) * 4;
+    float acc[4][4] = {};
+#pragma unroll 4
+    for (int c = j0; c < 64; ++c)
+      fma4x4(acc, *reinterpret_cast<const float4*>(LT + c * LDT + 64 + i0),
+             *reinterpret_cast<const float4*>(Ms + c * LDT + j0));
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      *reinterpret_cast<float4*>(Tt + (i0 + u) * TLD + j0) =
+          make_float4(acc[u][0], acc[u][1], acc[u][2], acc[u][3]);
+  } else if (tid < 384) {  // the 32-wide merge results are final: write them out
+    leaf_put_m(Ms, PB, PB, 0, PB, o, ldm, Mh, Ml, tid - 256, 128);
+    leaf_put_m(Ms, 3 * PB, PB, 2 * PB, PB, o, ldm, Mh, Ml, tid - 256, 128);
+    leaf_put_v(Ms, 0, PB, PB, PB, o, ldm, Vh, Vl, tid - 256, 128);
+    leaf_put_v(Ms, 2 * PB, PB, 3 * PB, PB, o, ldm, Vh, Vl, tid - 256, 128);
+  }
+  __syncthreads();
+  if (tid < 256) {  // M21 = -M22 T
+    const int i0 = (tid >> 4) * 4, j0 = (tid & 15) * 4;
+    float acc[4][4] = {};
+#pragma unroll 2
+    for (int c4 = 0; c4 <= i0 / 4; ++c4) {
+      float4 mrow[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        mrow[u] = *reinterpret_cast<const float4*>(Ms + (64 + i0 + u) * LDT + 64 + 4 * c4);
+      fma4x4(acc, make_float4(mrow[0].x, mrow[1].x, mrow[2].x, mrow[3].x),
+             *reinterpret_cast<const float4*>(Tt + (4 * c4 + 0) * TLD + j0));
+      fma4x4(acc, make_float4(mrow[0].y, mrow[1].y, mrow[2].y, mrow[3].y),
+             *reinterpret_cast<const float4*>(Tt + (4 * c4 + 1) * TLD + j0));
+      fma4x4(acc, make_float4(mrow[0].z, mrow[1].z, mrow[2].z, mrow[3].z),
+             *reinterpret_cast<const float4*>(Tt + (4 * c4 + 2) * TLD + j0));
+      fma4x4(acc, make_float4(mrow[0].w, mrow[1].w, mrow[2].w, mrow[3].w),
+             *reinterpret_cast<const float4*>(Tt + (4 * c4 + 3) * TLD + j0));
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      *reinterpret_cast<float4*>(Ms + (64 + i0 + u) * LDT + j0) =
+          make_float4(-acc[u][0], -acc[u][1], -acc[u][2], -acc[u][3]);
+  }
+  __syncthreads();
+  // ---- the 64-wide merge result: M rows 64.., columns ..63 and its transpose ----
+  leaf_put_m(Ms, 64, 64, 0, 64, o, ldm, Mh, Ml, tid, NT);
+  leaf_put_v(Ms, 0, 64, 64, 64, o, ldm, Vh, Vl, tid, NT);
+}
+
+
+// Zeros of the outputs inside every 128 x 128 diagonal block: M above and
+// V = M^T below the 32-wide diagonal blocks (the leaves write the rest).
+__global__ void leaf_zero_kernel(float* Mh, float* Ml, float* Vh, float* Vl, int64_t ldm) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;  // (row, float4) of one block
+  if (e >= LEAF * 24) return;
+  const int o = blockIdx.y * LEAF, i = e / 24, q = e % 24, bi = i / LEAF_PB;
+  const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (q < 24 - 8 * bi) {
+    const int64_t off = (int64_t)(o + i) * ldm + o + LEAF_PB * (bi + 1) + 4 * q;
+    *reinterpret_cast<float4*>(Mh + off) = z;
+    *reinterpret_cast<float4*>(Ml + off) = z;
+  } else {
+    const int64_t off = (int64_t)(o + i) * ldm + o + 4 * (q - (24 - 8 * bi));
+    *reinterpret_cast<float4*>(Vh + off) = z;
+    *reinterpret_cast<float4*>(Vl + off) = z;
   }
 }
 
 size_t leaf_smem_bytes() {
-  return (size_t)(LEAF_PB * LEAF_PTLD + LEAF_PB * LEAF_LTLD + 2 * LEAF * LEAF_LD + 64 * 65 + 5 * LEAF) * 4;
+  return (size_t)(2 * LEAF * LEAF_LDT + 64 * LEAF_TLD + 5 * LEAF) * sizeof(float);
 }
 
 // y = op(Th + Tl) x over a triangle, float64 accumulation, one warp per row.
@@ -586,6 +720,9 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
     return GPK_ERR_UNSUPPORTED;
   cudaFuncSetAttribute(leaf_chol_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)leaf_smem_bytes());
+  leaf_zero_kernel<<<dim3(cdiv(LEAF * 24, 256), np / LEAF), 256, 0, s>>>(b.Mh, b.Ml, b.Vh, b.Vl,
+                                                                          b.ld);
+  GPK_LAUNCH_CHECK();
   GPK_CUDA_TRY(chol_inv_rec(c, 0, np));
   prof_mark(2, s);
   prof_mark(3, s);
