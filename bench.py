@@ -320,9 +320,12 @@ def run_gpu(args):
     launches = lib.gpk_launch_count() - launches0
     t_dev = max_over_ranks(e0.elapsed_time(e1) / 1000.0)
     mll_mixed, g_mixed = float(out.item()), grad.cpu().numpy().copy()
-    # mixed form: "factor" is the recursive Cholesky that also forms L^-1, so
-    # "inverse" is empty; float64 form: the blocked Cholesky then the inverse
-    phase_names = ["gram", "factor", "inverse", "solve_refine", "adjoint", "finalize"]
+    # mixed form, caller's stream: Gram; recursive Cholesky that also forms
+    # L^-1 (with the T^T products overlapped on the library's side stream);
+    # the fork to the side stream (alpha solve + refinement + alpha terms of
+    # the gradient); the adjoint GEMM (-W terms); the wait for the side work
+    # still running after it; the float64 finalisation
+    phase_names = ["gram", "factor", "fork", "adjoint", "side_tail", "finalize"]
     phases = {nm: float(np.mean([ph[s][k].elapsed_time(ph[s][k + 1]) for s in range(args.steps)]))
               for k, nm in enumerate(phase_names)}
 

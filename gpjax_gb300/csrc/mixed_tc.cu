@@ -19,6 +19,7 @@
 // 128 with an identity block, which leaves the factor, the inverse, the
 // log-determinant and alpha of the original system unchanged.
 #include <climits>
+#include <mutex>
 #include "tc_gemm.cuh"
 
 namespace gpk {
@@ -501,18 +502,115 @@ __global__ void tc_diff_kernel(int n, const double* __restrict__ y, const double
   if (i < n) diff[i] = y[i] - theta[n_ls + 2];
 }
 
+// alpha alpha^T contracted against dK/dtheta (unit variance) over the lower
+// triangle, one 128 x 128 tile per CTA and one row per thread: the alpha part
+// of the MLL gradient, which the finalisation adds to the adjoint GEMM's -W
+// part.  Per element in float32 as in the GEMM epilogue, 32-column partials,
+// float64 accumulation.  Sized (128 threads, DMAX-bounded registers) to fit
+// beside a resident GEMM CTA.
+constexpr int AG_THREADS = LEAF;
+template <int DMAX>
+__global__ void __launch_bounds__(AG_THREADS)
+    alpha_grad_kernel(int kind, int n, int d, const float* __restrict__ xs,
+                      const double* __restrict__ alpha, double* __restrict__ gpart) {
+  constexpr int T = LEAF, NW = AG_THREADS / 32;
+  __shared__ float gx[T * DMAX];
+  __shared__ float ga[T];
+  __shared__ double red[(DMAX + 2) * NW];
+  const int t = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  int I = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+  while (I * (I + 1) / 2 > t) --I;
+  while ((I + 1) * (I + 2) / 2 <= t) ++I;
+  const int i0 = I * T, j0 = (t - I * (I + 1) / 2) * T;
+  for (int e = tid; e < T * DMAX; e += AG_THREADS) {
+    const int c = e / DMAX, k = e % DMAX, gj = j0 + c;
+    gx[e] = (gj < n && k < d) ? xs[(int64_t)gj * d + k] : 0.f;
+  }
+  for (int c = tid; c < T; c += AG_THREADS) ga[c] = (j0 + c < n) ? (float)alpha[j0 + c] : 0.f;
+  __syncthreads();
+  const int gi = i0 + tid;
+  double gl[DMAX];
+#pragma unroll
+  for (int k = 0; k < DMAX; ++k) gl[k] = 0.0;
+  double gvar = 0.0, gnoise = 0.0;
+  if (gi < n) {
+    float xi[DMAX];
+#pragma unroll
+    for (int k = 0; k < DMAX; ++k) xi[k] = k < d ? xs[(int64_t)gi * d + k] : 0.f;
+    const float ai = (float)alpha[gi];
+    for (int cb = 0; cb < T; cb += 32) {
+      float pl[DMAX];
+#pragma unroll
+      for (int k = 0; k < DMAX; ++k) pl[k] = 0.f;
+      float pvar = 0.f;
+      for (int q = 0; q < 32; ++q) {
+        const int c = cb + q, gj = j0 + c;
+        if (gj >= n || gj > gi) continue;
+        const float coef = ((gi == gj) ? 1.f : 2.f) * ai * ga[c];
+        float sq = 0.f;
+#pragma unroll
+        for (int k = 0; k < DMAX; ++k) {
+          const float df = xi[k] - gx[c * DMAX + k];
+          sq = fmaf(df, df, sq);
+        }
+        float k1, c1;
+        kval_dcoef<float>(kind, sq, 1.f, k1, c1);
+        pvar = fmaf(coef, k1, pvar);
+        const float cc = coef * c1;
+#pragma unroll
+        for (int k = 0; k < DMAX; ++k) {
+          const float df = xi[k] - gx[c * DMAX + k];
+          pl[k] = fmaf(cc, df * df, pl[k]);
+        }
+        if (gi == gj) gnoise += (double)ai * (double)ai;
+      }
+#pragma unroll
+      for (int k = 0; k < DMAX; ++k) gl[k] += (double)pl[k];
+      gvar += (double)pvar;
+    }
+  }
+  const int slots = d + 2;
+  for (int sidx = 0; sidx < slots; ++sidx) {
+    double val = (sidx == d) ? gvar : gnoise;
+    if (sidx < d) {
+#pragma unroll
+      for (int k = 0; k < DMAX; ++k)
+        if (k == sidx) val = gl[k];
+    }
+    val = warp_sum(val);
+    if (lane == 0) red[sidx * NW + warp] = val;
+  }
+  __syncthreads();
+  for (int sidx = tid; sidx < slots; sidx += AG_THREADS) {
+    double tot = 0.0;
+    for (int w = 0; w < NW; ++w) tot += red[sidx * NW + w];
+    gpart[(int64_t)t * slots + sidx] = tot;
+  }
+}
+
+constexpr int kMaxDepth = 24;  // recursion depth bound (n_pad < 128 * 2^23)
+
 struct TcChol {
   float* A;
   int64_t ld;
-  float *Lh, *Ll, *Mh, *Ml, *Vh, *Vl, *SAh, *SAl, *TTh, *TTl;
+  float *Lh, *Ll, *Mh, *Ml, *Vh, *Vl, *SAh, *SAl;
   int64_t ldsa;
-  TcMap mL, mM, mV, mSA, mTT;
+  TcMap mL, mM, mV, mSA;
+  TcMap mTT[kMaxDepth];  // T^T scratch, one per depth: TT(node) lives until M21(node)
+  float *TTh[kMaxDepth], *TTl[kMaxDepth];
+  int64_t ldtt[kMaxDepth];
   double *dtrack, *logdiag;
   int *info, *err;
-  cudaStream_t s;
+  cudaStream_t s;     // the caller's stream: the factor's critical path
+  cudaStream_t side;  // T^T = (L21 M11)^T products, overlapped with the right subtree
+  cudaEvent_t efork, ejoin;
 };
 
-cudaError_t chol_inv_rec(TcChol& c, int o, int sz) {
+// A node of size sz at depth `depth`: [L11, M11] = chol_inv(A11) (left, size h),
+// L21 = A21 M11^T, A22 -= L21 L21^T, [L22, M22] = chol_inv(A22) (right), and
+// M21 = -M22 T with T = L21 M11.  T^T only needs L21 and the left child, so it
+// runs on the side stream while the right subtree is factored; M21 waits for it.
+cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
   if (sz == LEAF) {
     leaf_chol_inv_kernel<<<1, LEAF_NT, leaf_smem_bytes(), c.s>>>(c.A, c.ld, o, c.dtrack, c.logdiag,
                                                              c.info, c.Mh, c.Ml, c.Vh, c.Vl, c.ld);
@@ -520,7 +618,7 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz) {
   }
   const int h = ((sz / 2 + LEAF - 1) / LEAF) * LEAF;
   const int h2 = sz - h;
-  cudaError_t e = chol_inv_rec(c, o, h);
+  cudaError_t e = chol_inv_rec(c, o, h, depth + 1);
   if (e != cudaSuccess) return e;
   // A21 -> split scratch
   e = tf32_split(c.A + (int64_t)(o + h) * c.ld + o, c.ld, h2, h, c.SAh, c.SAl, c.ldsa, c.s);
@@ -544,6 +642,28 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz) {
     e = tc_gemm_run(tc::MODE_STORE_SPLIT, c.mSA, c.mM, p, 1, c.s);
     if (e != cudaSuccess) return e;
   }
+  {  // T^T = (L21 M11)^T on the side stream; T[i, j] = sum_c L21[i, c] V11[j, c]
+    e = cudaEventRecord(c.efork, c.s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c.side, c.efork, 0);
+    if (e != cudaSuccess) return e;
+    tc::TcParams p{};
+    p.M = h2;
+    p.N = h;
+    p.K = h;
+    p.a_row0 = o + h;
+    p.a_col0 = o;
+    p.b_row0 = o;
+    p.b_col0 = o;
+    p.b_tri = TRI_UPPER;
+    p.t0 = c.TTh[depth];
+    p.t1 = c.TTl[depth];
+    p.ldt = c.ldtt[depth];
+    p.alpha = 1.f;
+    p.err = c.err;
+    e = tc_gemm_run(tc::MODE_STORE_SPLIT, c.mL, c.mV, p, 1, c.side);
+    if (e == cudaSuccess) e = cudaEventRecord(c.ejoin, c.side);
+    if (e != cudaSuccess) return e;
+  }
   {  // A22 -= L21 L21^T (lower tiles)
     tc::TcParams p{};
     p.M = h2;
@@ -563,26 +683,12 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz) {
     e = tc_gemm_run(tc::MODE_ADD_F32, c.mL, c.mL, p, 1, c.s);
     if (e != cudaSuccess) return e;
   }
-  e = chol_inv_rec(c, o + h, h2);
+  e = chol_inv_rec(c, o + h, h2, depth + 1);
   if (e != cudaSuccess) return e;
-  {  // T^T = (L21 M11)^T ; T[i, j] = sum_c L21[i, c] V11[j, c]
-    tc::TcParams p{};
-    p.M = h2;
-    p.N = h;
-    p.K = h;
-    p.a_row0 = o + h;
-    p.a_col0 = o;
-    p.b_row0 = o;
-    p.b_col0 = o;
-    p.b_tri = TRI_UPPER;
-    p.t0 = c.TTh;
-    p.t1 = c.TTl;
-    p.ldt = c.ldsa;
-    p.alpha = 1.f;
-    p.err = c.err;
-    e = tc_gemm_run(tc::MODE_STORE_SPLIT, c.mL, c.mV, p, 1, c.s);
-    if (e != cudaSuccess) return e;
-  }
+  // the latest T^T on the side stream is this node's or a later one: either
+  // way this node's is complete when it is
+  e = cudaStreamWaitEvent(c.s, c.ejoin, 0);
+  if (e != cudaSuccess) return e;
   {  // M21 = -M22 T ; M21[i, j] = sum_c M22[i, c] TT[j, c]; V12 = M21^T
     tc::TcParams p{};
     p.M = h2;
@@ -603,7 +709,7 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz) {
     p.t_col0 = o + h;
     p.alpha = -1.f;
     p.err = c.err;
-    e = tc_gemm_run(tc::MODE_STORE_SPLIT, c.mM, c.mTT, p, 1, c.s);
+    e = tc_gemm_run(tc::MODE_STORE_SPLIT, c.mM, c.mTT[depth], p, 1, c.s);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -612,7 +718,10 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz) {
 struct TcBuffers {
   int npad;
   int64_t ld, ldsa;
-  float *A, *Lh, *Ll, *Mh, *Ml, *Vh, *Vl, *SAh, *SAl, *TTh, *TTl, *xs;
+  float *A, *Lh, *Ll, *Mh, *Ml, *Vh, *Vl, *SAh, *SAl, *xs;
+  float *TTh[kMaxDepth], *TTl[kMaxDepth];
+  int64_t ldtt[kMaxDepth];
+  int ndepth;
   double *diff, *z, *alpha, *r, *logdiag, *dtrack, *rpart, *gpart;
   int* err;
 };
@@ -641,8 +750,14 @@ size_t tc_layout(int64_t n, int d, void* ws, TcBuffers& b) {
   b.Vl = (float*)take(nn);
   b.SAh = (float*)take(hh);
   b.SAl = (float*)take(hh);
-  b.TTh = (float*)take(hh);
-  b.TTl = (float*)take(hh);
+  // T^T at depth k is at most s_{k+1} x s_{k+1}, s_0 = n_pad, s_{k+1} = ceil128(s_k / 2)
+  b.ndepth = 0;
+  for (int64_t sk = b.npad; sk > LEAF && b.ndepth < kMaxDepth; ++b.ndepth) {
+    sk = ((sk / 2 + LEAF - 1) / LEAF) * LEAF;
+    b.ldtt[b.ndepth] = sk;
+    b.TTh[b.ndepth] = (float*)take((size_t)sk * sk * 4);
+    b.TTl[b.ndepth] = (float*)take((size_t)sk * sk * 4);
+  }
   b.xs = (float*)take((size_t)n * d * 4);
   b.diff = (double*)take((size_t)b.npad * 8);
   b.z = (double*)take((size_t)b.npad * 8);
@@ -652,7 +767,7 @@ size_t tc_layout(int64_t n, int d, void* ws, TcBuffers& b) {
   b.dtrack = (double*)take((size_t)b.npad * 8);
   b.rpart = (double*)take(residual_scratch_doubles((int)n) * 8);
   const size_t tm = (size_t)b.npad / LEAF;
-  b.gpart = (double*)take(tm * (tm + 1) / 2 * (d + 2) * 8);
+  b.gpart = (double*)take(2 * (tm * (tm + 1) / 2) * (d + 2) * 8);  // adjoint tiles, alpha tiles
   b.err = (int*)take(64);
   return off + 1024;
 }
@@ -665,6 +780,40 @@ cudaError_t mll_finalize_launch(int n, int d, const double* theta, int n_ls, con
                                 int ntiles, int want_grad, double jitter, int* info,
                                 double* out_mll, double* out_grad, cudaStream_t s);
 void prof_mark(int k, cudaStream_t s);
+
+namespace {
+struct SideCtx {
+  cudaStream_t hp = nullptr;    // highest priority: the critical path
+  cudaStream_t side = nullptr;  // lowest priority: work that fills idle SMs
+  cudaEvent_t estart = nullptr, efork = nullptr, ejoin = nullptr, edone = nullptr;
+};
+constexpr int kMaxDevices = 64;
+std::mutex g_side_mu;
+SideCtx g_side[kMaxDevices];
+
+// Created once per device and kept: two non-blocking streams at the ends of
+// the device's priority range (pending blocks of the high-priority stream are
+// dispatched first as SMs free up, so overlapped work only fills what the
+// critical path leaves idle) and the fork / join events (timing disabled).
+cudaError_t side_ctx(SideCtx** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  SideCtx& sc = g_side[dev];
+  if (!sc.side) {
+    int least = 0, greatest = 0;
+    e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&sc.hp, cudaStreamNonBlocking, greatest);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&sc.side, cudaStreamNonBlocking, least);
+    for (cudaEvent_t* ev : {&sc.estart, &sc.efork, &sc.ejoin, &sc.edone})
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) return e;
+  }
+  *out = &sc;
+  return cudaSuccess;
+}
+}  // namespace
 
 size_t mll_tc_workspace_bytes(int64_t n, int d) {
   TcBuffers b;
@@ -705,43 +854,79 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
   c.Vl = b.Vl;
   c.SAh = b.SAh;
   c.SAl = b.SAl;
-  c.TTh = b.TTh;
-  c.TTl = b.TTl;
   c.ldsa = b.ldsa;
   c.dtrack = b.dtrack;
   c.logdiag = b.logdiag;
   c.info = info;
   c.err = b.err;
-  c.s = s;
   if (!tc_make_map(&c.mL, b.Lh, b.Ll, np, np, b.ld) || !tc_make_map(&c.mM, b.Mh, b.Ml, np, np, b.ld) ||
       !tc_make_map(&c.mV, b.Vh, b.Vl, np, np, b.ld) ||
-      !tc_make_map(&c.mSA, b.SAh, b.SAl, b.ldsa, b.ldsa, b.ldsa) ||
-      !tc_make_map(&c.mTT, b.TTh, b.TTl, b.ldsa, b.ldsa, b.ldsa))
+      !tc_make_map(&c.mSA, b.SAh, b.SAl, b.ldsa, b.ldsa, b.ldsa))
     return GPK_ERR_UNSUPPORTED;
+  for (int k = 0; k < b.ndepth; ++k) {
+    c.TTh[k] = b.TTh[k];
+    c.TTl[k] = b.TTl[k];
+    c.ldtt[k] = b.ldtt[k];
+    if (!tc_make_map(&c.mTT[k], b.TTh[k], b.TTl[k], b.ldtt[k], b.ldtt[k], b.ldtt[k]))
+      return GPK_ERR_UNSUPPORTED;
+  }
   cudaFuncSetAttribute(leaf_chol_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)leaf_smem_bytes());
-  leaf_zero_kernel<<<dim3(cdiv(LEAF * 24, 256), np / LEAF), 256, 0, s>>>(b.Mh, b.Ml, b.Vh, b.Vl,
-                                                                          b.ld);
+  // The factor and the adjoint GEMM run on the library's high-priority stream
+  // (hs), the T^T products, the alpha solve and the alpha terms on its
+  // low-priority side stream; both fork from and join back into the caller's
+  // stream s.  The streams and events are per device; the host-side enqueue
+  // of one evaluation holds them.
+  std::lock_guard<std::mutex> lock(g_side_mu);
+  SideCtx* sc = nullptr;
+  GPK_CUDA_TRY(side_ctx(&sc));
+  cudaStream_t hs = sc->hp;
+  c.s = hs;
+  c.side = sc->side;
+  c.efork = sc->efork;
+  c.ejoin = sc->ejoin;
+  GPK_CUDA_TRY(cudaEventRecord(sc->estart, s));
+  GPK_CUDA_TRY(cudaStreamWaitEvent(hs, sc->estart, 0));
+  leaf_zero_kernel<<<dim3(cdiv(LEAF * 24, 256), np / LEAF), 256, 0, hs>>>(b.Mh, b.Ml, b.Vh, b.Vl,
+                                                                           b.ld);
   GPK_LAUNCH_CHECK();
-  GPK_CUDA_TRY(chol_inv_rec(c, 0, np));
-  prof_mark(2, s);
-  prof_mark(3, s);
+  GPK_CUDA_TRY(chol_inv_rec(c, 0, np, 0));
+  prof_mark(2, hs);
+  const int tm = np / LEAF;
+  const int ntiles = tm * (tm + 1) / 2;
+  // alpha = Sigma^-1 (y - m), refined against float64 residuals.  With a
+  // gradient it runs on the side stream next to the adjoint GEMM (which then
+  // contracts only -W), followed there by the alpha alpha^T terms.
+  cudaStream_t sv = hs;
+  if (want_grad) {
+    GPK_CUDA_TRY(cudaEventRecord(c.efork, hs));
+    GPK_CUDA_TRY(cudaStreamWaitEvent(c.side, c.efork, 0));
+    sv = c.side;
+  }
   const int gb = (int)cdiv((int64_t)np * 32, 256);
-  gemv_split_kernel<<<gb, 256, 0, s>>>(b.Mh, b.Ml, b.ld, np, 1, b.diff, b.z, 0);
+  gemv_split_kernel<<<gb, 256, 0, sv>>>(b.Mh, b.Ml, b.ld, np, 1, b.diff, b.z, 0);
   GPK_LAUNCH_CHECK();
-  gemv_split_kernel<<<gb, 256, 0, s>>>(b.Vh, b.Vl, b.ld, np, 0, b.z, b.alpha, 0);
+  gemv_split_kernel<<<gb, 256, 0, sv>>>(b.Vh, b.Vl, b.ld, np, 0, b.z, b.alpha, 0);
   GPK_LAUNCH_CHECK();
   for (int it = 0; it < refine; ++it) {
     GPK_CUDA_TRY(residual<float>(kind, n, d, b.xs, theta, n_ls, jitter, b.diff, b.alpha, b.r,
-                                 b.rpart, s));
-    gemv_split_kernel<<<gb, 256, 0, s>>>(b.Mh, b.Ml, b.ld, np, 1, b.r, b.z, 0);
+                                 b.rpart, sv));
+    gemv_split_kernel<<<gb, 256, 0, sv>>>(b.Mh, b.Ml, b.ld, np, 1, b.r, b.z, 0);
     GPK_LAUNCH_CHECK();
-    gemv_split_kernel<<<gb, 256, 0, s>>>(b.Vh, b.Vl, b.ld, np, 0, b.z, b.alpha, 1);
+    gemv_split_kernel<<<gb, 256, 0, sv>>>(b.Vh, b.Vl, b.ld, np, 0, b.z, b.alpha, 1);
     GPK_LAUNCH_CHECK();
   }
-  prof_mark(4, s);
-  const int tm = np / LEAF;
-  const int ntiles = tm * (tm + 1) / 2;
+  if (want_grad) {
+    double* gp_alpha = b.gpart + (int64_t)ntiles * (d + 2);
+    if (d <= 8)
+      alpha_grad_kernel<8><<<ntiles, AG_THREADS, 0, sv>>>(kind, n, d, b.xs, b.alpha, gp_alpha);
+    else
+      alpha_grad_kernel<tc::GRAD_DMAX><<<ntiles, AG_THREADS, 0, sv>>>(kind, n, d, b.xs, b.alpha,
+                                                                     gp_alpha);
+    GPK_LAUNCH_CHECK();
+    GPK_CUDA_TRY(cudaEventRecord(c.ejoin, sv));
+  }
+  prof_mark(3, hs);
   if (want_grad) {
     tc::TcParams p{};
     p.M = np;
@@ -754,16 +939,21 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
     p.d = d;
     p.kind = kind;
     p.xs = b.xs;
-    p.avec = b.alpha;
+    p.avec = nullptr;  // the alpha terms come from alpha_grad_kernel
     p.gpart = b.gpart;
     p.err = b.err;
-    GPK_CUDA_TRY(tc_gemm_run(tc::MODE_GRAD, c.mV, c.mV, p, 1, s));
+    GPK_CUDA_TRY(tc_gemm_run(tc::MODE_GRAD, c.mV, c.mV, p, 1, hs));
   }
-  prof_mark(5, s);
+  prof_mark(4, hs);
+  if (want_grad) GPK_CUDA_TRY(cudaStreamWaitEvent(hs, c.ejoin, 0));
+  prof_mark(5, hs);
+  GPK_CUDA_TRY(cudaEventRecord(sc->edone, hs));
+  GPK_CUDA_TRY(cudaStreamWaitEvent(s, sc->edone, 0));
   tc_check_err<<<1, 1, 0, s>>>(b.err, info);
   GPK_LAUNCH_CHECK();
-  GPK_CUDA_TRY(mll_finalize_launch(n, d, theta, n_ls, b.logdiag, b.diff, b.alpha, b.gpart, ntiles,
-                                   want_grad, jitter, info, out_mll, out_grad, s));
+  GPK_CUDA_TRY(mll_finalize_launch(n, d, theta, n_ls, b.logdiag, b.diff, b.alpha, b.gpart,
+                                   want_grad ? 2 * ntiles : ntiles, want_grad, jitter, info,
+                                   out_mll, out_grad, s));
   prof_mark(6, s);
   return GPK_OK;
 }

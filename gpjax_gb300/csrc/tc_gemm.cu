@@ -170,6 +170,45 @@ constexpr int EPI_WARPS = 8;   // epilogue warps: two per TMEM lane quarter
 constexpr int EPI_THREADS = EPI_WARPS * 32;
 constexpr int HC = BN / 2;     // accumulator columns owned by one epilogue thread
 
+// Launch index -> output tile (I, J), grouped so that the CTAs resident at
+// one time share operand panels in L2: groups of TILE_GROUP tile rows, walked
+// column by column (consecutive CTAs take consecutive rows of one column).
+// For c_lower only tiles with J <= I exist.
+constexpr int TILE_GROUP = 8;
+__device__ __forceinline__ void tile_of(int t, int c_lower, int tiles_m, int tiles_n, int& I,
+                                        int& J) {
+  constexpr int G = TILE_GROUP;
+  if (!c_lower) {
+    const int g = t / (G * tiles_n), l = t % (G * tiles_n);
+    const int rows = min(G, tiles_m - g * G);
+    J = l / rows;
+    I = g * G + l % rows;
+    return;
+  }
+  int g = 0, base = 0;
+  for (;; ++g) {
+    const int rows = min(G, tiles_m - g * G);
+    const int cnt = g * G * rows + rows * (rows + 1) / 2;
+    if (t < base + cnt) break;
+    base += cnt;
+  }
+  const int rows = min(G, tiles_m - g * G);
+  int l = t - base;
+  if (l < g * G * rows) {  // columns left of the group's diagonal block
+    J = l / rows;
+    I = g * G + l % rows;
+    return;
+  }
+  l -= g * G * rows;  // the diagonal block: column j holds rows j..rows-1
+  int j = 0;
+  while (l >= rows - j) {
+    l -= rows - j;
+    ++j;
+  }
+  J = g * G + j;
+  I = J + l;
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap ta_hi, const __grid_constant__ CUtensorMap ta_lo,
@@ -187,17 +226,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int z = blockIdx.z;
   int I, J;
-  if (p.c_lower) {
-    const int t = blockIdx.x;
-    int i = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
-    while (i * (i + 1) / 2 > t) --i;
-    while ((i + 1) * (i + 2) / 2 <= t) ++i;
-    I = i;
-    J = t - i * (i + 1) / 2;
-  } else {
-    I = blockIdx.x / p.tiles_n;
-    J = blockIdx.x % p.tiles_n;
-  }
+  tile_of(blockIdx.x, p.c_lower, p.tiles_m, p.tiles_n, I, J);
   const int i0 = I * BM, j0 = J * BN;
   int klo = 0, khi = p.K;
   if (p.a_tri == TRI_LOWER) khi = min(khi, i0 + BM);
@@ -307,7 +336,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       }
       for (int c = et; c < BN; c += EPI_THREADS) {
         const int gj = j0 + c;
-        ga[c] = gj < p.n_true ? (float)p.avec[gj] : 0.f;
+        ga[c] = (p.avec && gj < p.n_true) ? (float)p.avec[gj] : 0.f;
       }
     }
     // drain the accumulator segments into float32 registers (round to nearest)
@@ -433,7 +462,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 #pragma unroll
       for (int k = 0; k < GRAD_DMAX; ++k)
         xi[k] = (gi < p.n_true && k < p.d) ? p.xs[(int64_t)gi * p.d + k] : 0.f;
-      const float ai = gi < p.n_true ? (float)p.avec[gi] : 0.f;
+      const float ai = (p.avec && gi < p.n_true) ? (float)p.avec[gi] : 0.f;  // null: -W terms only
       double gl[GRAD_DMAX];
 #pragma unroll
       for (int k = 0; k < GRAD_DMAX; ++k) gl[k] = 0.0;
