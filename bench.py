@@ -31,9 +31,13 @@ METRIC = "MLL+grad evals/s at n=16k: mixed vs FP64 form on one GB300 @ rel err â
 WORKLOAD = ("exact GP conjugate_mll + gradient, Matern-5/2 ARD, n=16384, d=8, X~N(0,I8), "
             "lengthscales log-U[0.3,3], variance 1, noise 1e-2, y = prior sample + noise")
 PEAK_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
-# dram__bytes_read.sum + dram__bytes_write.sum of one adjoint (lauum_grad) launch,
-# from the ncu capture summarised in profiles/ (scaled to n = 16384); None until captured.
-ADJOINT_TRAFFIC_BYTES_N16384 = None
+# dram__bytes_read.sum + dram__bytes_write.sum of one adjoint GEMM launch
+# (tc_gemm_kernel<MODE_GRAD>) on this workload at full size, n = 16384: 8.98 GB
+# read + 4.54 MB written, from a one-pass ncu capture summarised in
+# profiles/tc_gemm_grad_dram_n16384.txt.  The algorithmic operand volume is
+# 1.07 GB (the upper triangle of V in TF32 hi/lo): tiles of one L2-resident
+# group share panels, the groups re-read them.
+ADJOINT_TRAFFIC_BYTES_N16384 = 8.98e9 + 4.54e6
 
 
 def parse_args():
@@ -391,7 +395,7 @@ def run_gpu(args):
                    "precision": "mixed", "parallelism": "replicas" if world > 1 else "single",
                    "l2": "working set (3 x n^2 float32 = 3.2 GB) larger than L2; no flush"},
         "roofline": {"bound": "tensor",
-                     "kernel": "tc_gemm_kernel<MODE_GRAD> (fused L^-T L^-1 product + adjoint)",
+                     "kernel": "tc_gemm_kernel<MODE_GRAD> (W = L^-T L^-1 tiles contracted with dK/dtheta)",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "peak_kind": f"{peak_kind} bf16 dense",
                      "traffic": ADJOINT_TRAFFIC_BYTES_N16384,
