@@ -893,7 +893,22 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
   GPK_CUDA_TRY(chol_inv_rec(c, 0, np, 0));
   prof_mark(2, hs);
   const int tm = np / LEAF;
-  const int ntiles = tm * (tm + 1) / 2;
+  const int ntiles = tm * (tm + 1) / 2;  // alpha_grad_kernel tiles
+  tc::TcParams pg{};                      // the adjoint GEMM (launched below)
+  pg.M = np;
+  pg.N = np;
+  pg.K = np;
+  pg.a_tri = TRI_UPPER;
+  pg.b_tri = TRI_UPPER;
+  pg.c_lower = 1;
+  pg.n_true = n;
+  pg.d = d;
+  pg.kind = kind;
+  pg.xs = b.xs;
+  pg.avec = nullptr;  // the alpha terms come from alpha_grad_kernel
+  pg.gpart = b.gpart;
+  pg.err = b.err;
+  const int ntiles_adj = tc_gemm_tiles(tc::MODE_GRAD, pg);  // gpart rows of the adjoint
   // alpha = Sigma^-1 (y - m), refined against float64 residuals.  With a
   // gradient it runs on the side stream next to the adjoint GEMM (which then
   // contracts only -W), followed there by the alpha alpha^T terms.
@@ -917,7 +932,7 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
     GPK_LAUNCH_CHECK();
   }
   if (want_grad) {
-    double* gp_alpha = b.gpart + (int64_t)ntiles * (d + 2);
+    double* gp_alpha = b.gpart + (int64_t)ntiles_adj * (d + 2);
     if (d <= 8)
       alpha_grad_kernel<8><<<ntiles, AG_THREADS, 0, sv>>>(kind, n, d, b.xs, b.alpha, gp_alpha);
     else
@@ -927,23 +942,7 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
     GPK_CUDA_TRY(cudaEventRecord(c.ejoin, sv));
   }
   prof_mark(3, hs);
-  if (want_grad) {
-    tc::TcParams p{};
-    p.M = np;
-    p.N = np;
-    p.K = np;
-    p.a_tri = TRI_UPPER;
-    p.b_tri = TRI_UPPER;
-    p.c_lower = 1;
-    p.n_true = n;
-    p.d = d;
-    p.kind = kind;
-    p.xs = b.xs;
-    p.avec = nullptr;  // the alpha terms come from alpha_grad_kernel
-    p.gpart = b.gpart;
-    p.err = b.err;
-    GPK_CUDA_TRY(tc_gemm_run(tc::MODE_GRAD, c.mV, c.mV, p, 1, hs));
-  }
+  if (want_grad) GPK_CUDA_TRY(tc_gemm_run(tc::MODE_GRAD, c.mV, c.mV, pg, 1, hs));
   prof_mark(4, hs);
   if (want_grad) GPK_CUDA_TRY(cudaStreamWaitEvent(hs, c.ejoin, 0));
   prof_mark(5, hs);
@@ -952,7 +951,7 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
   tc_check_err<<<1, 1, 0, s>>>(b.err, info);
   GPK_LAUNCH_CHECK();
   GPK_CUDA_TRY(mll_finalize_launch(n, d, theta, n_ls, b.logdiag, b.diff, b.alpha, b.gpart,
-                                   want_grad ? 2 * ntiles : ntiles, want_grad, jitter, info,
+                                   want_grad ? ntiles_adj + ntiles : 0, want_grad, jitter, info,
                                    out_mll, out_grad, s));
   prof_mark(6, s);
   return GPK_OK;

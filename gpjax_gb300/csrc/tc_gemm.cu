@@ -70,19 +70,22 @@ __device__ __forceinline__ void tc_fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
-// 128B-swizzled K-major shared-memory descriptor: rows of 128 B, 8-row groups
-// 1024 B apart (SBO), version bits 46..48 = 1, swizzle mode 2 (128B).
+// Swizzled K-major shared-memory descriptor: rows of SWZ bytes (one K slice
+// of the tile), 8-row groups 8 * SWZ bytes apart (SBO), version bits 46..48 =
+// 1, swizzle mode 2 (128B) or 4 (64B).
+template <int SWZ>
 __device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
+  static_assert(SWZ == 128 || SWZ == 64, "128B or 64B swizzle");
   uint64_t d = 0;
   d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
   d |= (uint64_t)(16u >> 4) << 16;
-  d |= (uint64_t)(1024u >> 4) << 32;
+  d |= (uint64_t)((8u * SWZ) >> 4) << 32;
   d |= (uint64_t)1 << 46;
-  d |= (uint64_t)2 << 61;
+  d |= (uint64_t)(SWZ == 128 ? 2 : 4) << 61;
   return d;
 }
 
-// kind::tf32, float32 accumulate, K-major A and B, M = 128, N = 128
+// kind::tf32, float32 accumulate, K-major A and B, M x N
 __host__ __device__ constexpr uint32_t idesc_tf32(int m, int n) {
   return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) |
          ((uint32_t)(m >> 4) << 24);
@@ -150,9 +153,29 @@ __device__ __forceinline__ void split_tf32(float x, float& hi, float& lo) {
 // ---------------------------------------------------------------------------
 // The kernel
 // ---------------------------------------------------------------------------
+// Two tile shapes.  Narrow: 128 x 128 outputs, 32-wide K slices in 128B
+// swizzle, 3 stages of 64 KB, 4 accumulator buffers of 128 TMEM columns.
+// Wide (large GEMMs): 128 x 256 outputs, 16-wide K slices in 64B swizzle, 4
+// stages of 48 KB, 2 buffers of 256 columns: a quarter fewer operand bytes,
+// both from L2 and from shared memory, per multiply-add.
+template <bool WIDE>
+struct Tile {
+  static constexpr int BN = WIDE ? 256 : 128;
+  static constexpr int BK = WIDE ? 16 : 32;
+  static constexpr int STAGES = WIDE ? 4 : 3;
+  static constexpr int SWZ = BK * 4;  // bytes of one K slice row
+  static constexpr int A_BYTES = BM * BK * 4;
+  static constexpr int B_BYTES = BN * BK * 4;
+  static constexpr int STAGE_BYTES = 2 * (A_BYTES + B_BYTES);  // A_hi, A_lo, B_hi, B_lo
+  static constexpr int NBUF = 512 / BN;                        // TMEM accumulator buffers
+  static constexpr int HC = BN / 2;  // accumulator columns owned by one epilogue thread
+  static constexpr int TLD = BN + 4; // staged output tile row stride (floats)
+};
+
+template <int STAGES_>
 struct SmemCtl {
-  uint64_t full[STAGES];
-  uint64_t empty[STAGES];
+  uint64_t full[STAGES_];
+  uint64_t empty[STAGES_];
   uint64_t tfull[4];   // accumulator segment ready (MMA -> epilogue)
   uint64_t tempty[4];  // accumulator segment drained (epilogue -> MMA)
   uint32_t tmem;
@@ -160,23 +183,21 @@ struct SmemCtl {
 };
 
 // The tensor-core float32 accumulator rounds less carefully than an FMA, so
-// each accumulator only sums SEG_CHUNKS x 32 K-elements (12 MMA steps per
-// chunk); the epilogue warps drain finished segments into round-to-nearest
-// float32 registers while the MMA thread fills the next of NBUF TMEM buffers.
+// each accumulator only sums one K slice (BK elements, 3 MMAs per 8); the
+// epilogue warps drain finished segments into round-to-nearest float32
+// registers while the MMA thread fills the next of NBUF TMEM buffers.
 constexpr int SEG_CHUNKS = 1;
-constexpr int NBUF = 4;
-constexpr int TLD = BN + 4;    // staged output tile row stride (floats)
 constexpr int EPI_WARPS = 8;   // epilogue warps: two per TMEM lane quarter
 constexpr int EPI_THREADS = EPI_WARPS * 32;
-constexpr int HC = BN / 2;     // accumulator columns owned by one epilogue thread
 
 // Launch index -> output tile (I, J), grouped so that the CTAs resident at
 // one time share operand panels in L2: groups of TILE_GROUP tile rows, walked
 // column by column (consecutive CTAs take consecutive rows of one column).
-// For c_lower only tiles with J <= I exist.
+// Column tiles are `ratio` row tiles wide; for c_lower only tiles holding
+// elements on or below the diagonal exist (J <= I / ratio).
 constexpr int TILE_GROUP = 8;
-__device__ __forceinline__ void tile_of(int t, int c_lower, int tiles_m, int tiles_n, int& I,
-                                        int& J) {
+__host__ __device__ inline void tile_of(int t, int c_lower, int tiles_m, int tiles_n, int ratio,
+                                        int& I, int& J) {
   constexpr int G = TILE_GROUP;
   if (!c_lower) {
     const int g = t / (G * tiles_n), l = t % (G * tiles_n);
@@ -185,48 +206,65 @@ __device__ __forceinline__ void tile_of(int t, int c_lower, int tiles_m, int til
     I = g * G + l % rows;
     return;
   }
-  int g = 0, base = 0;
+  int g = 0, base = 0, rows = 0;
   for (;; ++g) {
-    const int rows = min(G, tiles_m - g * G);
-    const int cnt = g * G * rows + rows * (rows + 1) / 2;
+    rows = min(G, tiles_m - g * G);
+    int cnt = 0;
+    for (int r = 0; r < rows; ++r) cnt += (g * G + r) / ratio + 1;
     if (t < base + cnt) break;
     base += cnt;
   }
-  const int rows = min(G, tiles_m - g * G);
   int l = t - base;
-  if (l < g * G * rows) {  // columns left of the group's diagonal block
+  const int full_cols = (g * G) / ratio;  // columns every row of the group reaches
+  if (l < full_cols * rows) {
     J = l / rows;
     I = g * G + l % rows;
     return;
   }
-  l -= g * G * rows;  // the diagonal block: column j holds rows j..rows-1
-  int j = 0;
-  while (l >= rows - j) {
-    l -= rows - j;
-    ++j;
+  l -= full_cols * rows;
+  for (J = full_cols;; ++J) {  // column J holds the group's rows I >= ratio * J
+    const int r0 = max(g * G, ratio * J);
+    const int cnt = g * G + rows - r0;
+    if (l < cnt) {
+      I = r0 + l;
+      return;
+    }
+    l -= cnt;
   }
-  J = g * G + j;
-  I = J + l;
 }
 
-template <int MODE>
+// Number of launch indices tile_of maps (the grid of one GEMM).
+__host__ __device__ inline int tile_count(int c_lower, int tiles_m, int tiles_n, int ratio) {
+  if (!c_lower) return tiles_m * tiles_n;
+  int cnt = 0;
+  for (int I = 0; I < tiles_m; ++I) cnt += I / ratio + 1;
+  return cnt;
+}
+
+// MODE: epilogue.  WIDE: tile shape (Tile<WIDE>).  DM: bound on the input
+// dimension of the MODE_GRAD epilogue (registers scale with it).
+template <int MODE, bool WIDE, int DM>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap ta_hi, const __grid_constant__ CUtensorMap ta_lo,
                    const __grid_constant__ CUtensorMap tb_hi, const __grid_constant__ CUtensorMap tb_lo,
                    const __grid_constant__ TcParams p) {
+  using TL = Tile<WIDE>;
+  constexpr int BN = TL::BN, BK = TL::BK, STAGES = TL::STAGES, NBUF = TL::NBUF, HC = TL::HC,
+                TLD = TL::TLD, STAGE_BYTES = TL::STAGE_BYTES, A_BYTES = TL::A_BYTES,
+                B_BYTES = TL::B_BYTES;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* tiles = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
-  SmemCtl* ctl = reinterpret_cast<SmemCtl*>(tiles + STAGES * STAGE_BYTES);
+  SmemCtl<STAGES>* ctl = reinterpret_cast<SmemCtl<STAGES>*>(tiles + STAGES * STAGE_BYTES);
   float* gx = reinterpret_cast<float*>(ctl + 1);  // MODE_GRAD: column points and alphas
-  float* ga = gx + BN * GRAD_DMAX;
+  float* ga = gx + BN * DM;
   double* gred = reinterpret_cast<double*>(ga + BN);
   float* otile = reinterpret_cast<float*>(tiles);  // output tile, reuses the operand ring
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int z = blockIdx.z;
   int I, J;
-  tile_of(blockIdx.x, p.c_lower, p.tiles_m, p.tiles_n, I, J);
+  tile_of(blockIdx.x, p.c_lower, p.tiles_m, p.tiles_n, BN / BM, I, J);
   const int i0 = I * BM, j0 = J * BN;
   int klo = 0, khi = p.K;
   if (p.a_tri == TRI_LOWER) khi = min(khi, i0 + BM);
@@ -275,10 +313,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         uint8_t* st = tiles + s * STAGE_BYTES;
         const int k = klo + kc * BK;
         mbar_expect_tx(&ctl->full[s], STAGE_BYTES);
-        tma_load_2d(st + 0 * TILE_BYTES, &ta_hi, ax0 + k, ay, &ctl->full[s]);
-        tma_load_2d(st + 1 * TILE_BYTES, &ta_lo, ax0 + k, ay, &ctl->full[s]);
-        tma_load_2d(st + 2 * TILE_BYTES, &tb_hi, bx0 + k, by, &ctl->full[s]);
-        tma_load_2d(st + 3 * TILE_BYTES, &tb_lo, bx0 + k, by, &ctl->full[s]);
+        tma_load_2d(st, &ta_hi, ax0 + k, ay, &ctl->full[s]);
+        tma_load_2d(st + A_BYTES, &ta_lo, ax0 + k, ay, &ctl->full[s]);
+        tma_load_2d(st + 2 * A_BYTES, &tb_hi, bx0 + k, by, &ctl->full[s]);
+        tma_load_2d(st + 2 * A_BYTES + B_BYTES, &tb_lo, bx0 + k, by, &ctl->full[s]);
         ++issued;
       }
       if (*abort_flag) {
@@ -304,8 +342,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         if (!ok) break;
         tc_fence_after();
         const uint32_t sb = smem_u32(tiles + s * STAGE_BYTES);
-        const uint64_t ahi = sdesc(sb), alo = sdesc(sb + TILE_BYTES);
-        const uint64_t bhi = sdesc(sb + 2 * TILE_BYTES), blo = sdesc(sb + 3 * TILE_BYTES);
+        const uint64_t ahi = sdesc<TL::SWZ>(sb), alo = sdesc<TL::SWZ>(sb + A_BYTES);
+        const uint64_t bhi = sdesc<TL::SWZ>(sb + 2 * A_BYTES);
+        const uint64_t blo = sdesc<TL::SWZ>(sb + 2 * A_BYTES + B_BYTES);
         const bool first = (kc % SEG_CHUNKS) == 0;
 #pragma unroll
         for (int k4 = 0; k4 < BK / 8; ++k4) {
@@ -329,8 +368,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     const int gi = i0 + r;  // row within the problem
     const int et = threadIdx.x - 64;
     if (MODE == MODE_GRAD) {
-      for (int e = et; e < BN * GRAD_DMAX; e += EPI_THREADS) {
-        const int c = e / GRAD_DMAX, k = e % GRAD_DMAX;
+      for (int e = et; e < BN * DM; e += EPI_THREADS) {
+        const int c = e / DM, k = e % DM;
         const int gj = j0 + c;
         gx[e] = (gj < p.n_true && k < p.d) ? p.xs[(int64_t)gj * p.d + k] : 0.f;
       }
@@ -350,7 +389,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       if (!have) break;
       tc_fence_after();
       const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN + hcol);
-      {
+      if (HC == 64) {
         uint32_t v0[32], v1[32];
         tmem_ld32_nowait(tb, v0);
         tmem_ld32_nowait(tb + 32, v1);
@@ -359,6 +398,15 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         for (int k = 0; k < 32; ++k) {
           acc[k] += __uint_as_float(v0[k]);
           acc[32 + k] += __uint_as_float(v1[k]);
+        }
+      } else {
+#pragma unroll
+        for (int cc = 0; cc < HC; cc += 32) {
+          uint32_t v0[32];
+          tmem_ld32_nowait(tb + cc, v0);
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int k = 0; k < 32; ++k) acc[cc + k] += __uint_as_float(v0[k]);
         }
       }
       tc_fence_before();
@@ -390,11 +438,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       if (have) {
         const int64_t crow0 = p.c_row0 + (int64_t)z * p.c_zrow + i0;
         const int64_t ccol = p.c_col0 + (int64_t)z * p.c_zcol + j0;
-        const int c4 = lane * 4;
         if (p.c0) {
-          for (int rr = ew; rr < BM; rr += EPI_WARPS) {
+          for (int rc = ew; rc < BM * (BN / 128); rc += EPI_WARPS) {
+            const int rr = rc % BM, c4 = (rc / BM) * 128 + lane * 4;
             const int grow = i0 + rr;
-            if (grow >= p.M) break;
+            if (grow >= p.M) continue;
             const float4 w4 = *reinterpret_cast<const float4*>(&otile[rr * TLD + c4]);
             const float wv[4] = {w4.x, w4.y, w4.z, w4.w};
             const int64_t base = (crow0 + rr) * p.ldc + ccol + c4;
@@ -458,20 +506,20 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       asm volatile("bar.sync 1, %0;" ::"r"(EPI_THREADS) : "memory");  // gx / ga staged
       // W tile -> reduction against dK/dtheta (unit variance); an aborted wait
       // contributes zeros but still joins the reduction barrier
-      float xi[GRAD_DMAX];
+      float xi[DM];
 #pragma unroll
-      for (int k = 0; k < GRAD_DMAX; ++k)
+      for (int k = 0; k < DM; ++k)
         xi[k] = (gi < p.n_true && k < p.d) ? p.xs[(int64_t)gi * p.d + k] : 0.f;
       const float ai = (p.avec && gi < p.n_true) ? (float)p.avec[gi] : 0.f;  // null: -W terms only
-      double gl[GRAD_DMAX];
+      double gl[DM];
 #pragma unroll
-      for (int k = 0; k < GRAD_DMAX; ++k) gl[k] = 0.0;
+      for (int k = 0; k < DM; ++k) gl[k] = 0.0;
       double gnoise = 0.0, gvar = 0.0;
 #pragma unroll
       for (int cb = 0; cb < HC / 32; ++cb) {
-        float pl[GRAD_DMAX];
+        float pl[DM];
 #pragma unroll
-        for (int k = 0; k < GRAD_DMAX; ++k) pl[k] = 0.f;
+        for (int k = 0; k < DM; ++k) pl[k] = 0.f;
         float pvar = 0.f;
 #pragma unroll
         for (int k = 0; k < 32; ++k) {
@@ -481,24 +529,25 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
           const float w = acc[cb * 32 + k];
           const float f = (gi == gj) ? 1.f : 2.f;
           const float coef = f * (ai * ga[c] - w);
-          float dsq[GRAD_DMAX];
           float sq = 0.f;
 #pragma unroll
-          for (int kk = 0; kk < GRAD_DMAX; ++kk) {
-            const float df = xi[kk] - gx[c * GRAD_DMAX + kk];
-            dsq[kk] = df * df;
-            sq += dsq[kk];
+          for (int kk = 0; kk < DM; ++kk) {
+            const float df = xi[kk] - gx[c * DM + kk];
+            sq = fmaf(df, df, sq);
           }
           float k1, c1;
           kval_dcoef<float>(p.kind, sq, 1.f, k1, c1);
           pvar = fmaf(coef, k1, pvar);
           const float cc = coef * c1;
 #pragma unroll
-          for (int kk = 0; kk < GRAD_DMAX; ++kk) pl[kk] = fmaf(cc, dsq[kk], pl[kk]);
+          for (int kk = 0; kk < DM; ++kk) {
+            const float df = xi[kk] - gx[c * DM + kk];
+            pl[kk] = fmaf(cc, df * df, pl[kk]);
+          }
           if (gi == gj) gnoise += (double)ai * (double)ai - (double)w;
         }
 #pragma unroll
-        for (int kk = 0; kk < GRAD_DMAX; ++kk) gl[kk] += (double)pl[kk];
+        for (int kk = 0; kk < DM; ++kk) gl[kk] += (double)pl[kk];
         gvar += (double)pvar;
       }
       // reduce over the 4 epilogue warps into gpart[tile]
@@ -508,7 +557,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         if (sidx < p.d) {
           val = 0.0;
 #pragma unroll
-          for (int kk = 0; kk < GRAD_DMAX; ++kk)
+          for (int kk = 0; kk < DM; ++kk)
             if (kk == sidx) val = gl[kk];
         } else if (sidx == p.d) {
           val = gvar;
@@ -574,59 +623,99 @@ static EncodeTiledFn encode_fn() {
   return fn;
 }
 
-// float32 row-major [rows, cols] with leading dimension ld; box 32 x 128, 128B swizzle
-static bool make_map(CUtensorMap* m, const float* base, int64_t rows, int64_t cols, int64_t ld) {
+// float32 row-major [rows, cols] with leading dimension ld; box bk x box_rows
+// (bk = 32: 128B swizzle, bk = 16: 64B swizzle; one K slice row per box row)
+static bool make_map(CUtensorMap* m, const float* base, int64_t rows, int64_t cols, int64_t ld,
+                     int bk, int box_rows) {
   EncodeTiledFn fn = encode_fn();
   if (!fn) return false;
   if ((reinterpret_cast<uintptr_t>(base) & 15u) != 0 || ((ld * 4) & 15) != 0) return false;
   cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)(ld * 4)};
-  cuuint32_t box[2] = {(cuuint32_t)tc::BK, (cuuint32_t)tc::BM};
+  cuuint32_t box[2] = {(cuuint32_t)bk, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides,
-                  box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  bk == 32 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
 }
 
+template <bool WIDE>
 static size_t tc_smem_bytes() {
-  return 1024 + (size_t)tc::STAGES * tc::STAGE_BYTES + sizeof(tc::SmemCtl) +
-         (size_t)tc::BN * tc::GRAD_DMAX * 4 + tc::BN * 4 +
+  using TL = tc::Tile<WIDE>;
+  return 1024 + (size_t)TL::STAGES * TL::STAGE_BYTES + sizeof(tc::SmemCtl<TL::STAGES>) +
+         (size_t)TL::BN * tc::GRAD_DMAX * 4 + TL::BN * 4 +
          (size_t)(tc::GRAD_DMAX + 2) * 8 * sizeof(double) + 64;
 }
 
 bool tc_make_map(TcMap* m, const float* hi, const float* lo, int64_t rows, int64_t cols,
                  int64_t ld) {
-  return make_map(&m->hi, hi, rows, cols, ld) && make_map(&m->lo, lo, rows, cols, ld);
+  using N = tc::Tile<false>;
+  using W = tc::Tile<true>;
+  return make_map(&m->hi, hi, rows, cols, ld, N::BK, tc::BM) &&
+         make_map(&m->lo, lo, rows, cols, ld, N::BK, tc::BM) &&
+         make_map(&m->wa_hi, hi, rows, cols, ld, W::BK, tc::BM) &&
+         make_map(&m->wa_lo, lo, rows, cols, ld, W::BK, tc::BM) &&
+         make_map(&m->wb_hi, hi, rows, cols, ld, W::BK, W::BN) &&
+         make_map(&m->wb_lo, lo, rows, cols, ld, W::BK, W::BN);
 }
 
-cudaError_t tc_gemm_run(int mode, const TcMap& A, const TcMap& B, const tc::TcParams& p0,
-                        int batch, cudaStream_t s) {
-  if (p0.M <= 0 || p0.N <= 0 || batch <= 0) return cudaSuccess;
+// The wide tile pays off once a GEMM has several waves of tiles; the adjoint
+// epilogue keeps 128 accumulator columns per thread only with DM = 8.
+static bool use_wide(int mode, const tc::TcParams& p) {
+  if (p.M < 2048 || p.N < 2048) return false;
+  return mode != tc::MODE_GRAD || p.d <= 8;
+}
+
+int tc_gemm_tiles(int mode, const tc::TcParams& p) {
+  const bool wide = use_wide(mode, p);
+  const int bn = wide ? tc::Tile<true>::BN : tc::Tile<false>::BN;
+  const int tm = (p.M + tc::BM - 1) / tc::BM, tn = (p.N + bn - 1) / bn;
+  return tc::tile_count(p.c_lower, tm, tn, bn / tc::BM);
+}
+
+template <int MODE, bool WIDE, int DM>
+static void launch_one(const TcMap& A, const TcMap& B, const tc::TcParams& p0, int batch,
+                       cudaStream_t s) {
+  using TL = tc::Tile<WIDE>;
   tc::TcParams p = p0;
   p.tiles_m = (p.M + tc::BM - 1) / tc::BM;
-  p.tiles_n = (p.N + tc::BN - 1) / tc::BN;
-  const int tiles = p.c_lower ? p.tiles_m * (p.tiles_m + 1) / 2 : p.tiles_m * p.tiles_n;
-  dim3 grid(tiles, 1, batch);
-  const size_t smem = tc_smem_bytes();
+  p.tiles_n = (p.N + TL::BN - 1) / TL::BN;
+  dim3 grid(tc::tile_count(p.c_lower, p.tiles_m, p.tiles_n, TL::BN / tc::BM), 1, batch);
+  const size_t smem = tc_smem_bytes<WIDE>();
+  cudaFuncSetAttribute(tc::tc_gemm_kernel<MODE, WIDE, DM>,
+                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (WIDE)
+    tc::tc_gemm_kernel<MODE, WIDE, DM><<<grid, tc::NUM_THREADS, smem, s>>>(A.wa_hi, A.wa_lo,
+                                                                           B.wb_hi, B.wb_lo, p);
+  else
+    tc::tc_gemm_kernel<MODE, WIDE, DM><<<grid, tc::NUM_THREADS, smem, s>>>(A.hi, A.lo, B.hi,
+                                                                           B.lo, p);
+}
+
+cudaError_t tc_gemm_run(int mode, const TcMap& A, const TcMap& B, const tc::TcParams& p,
+                        int batch, cudaStream_t s) {
+  if (p.M <= 0 || p.N <= 0 || batch <= 0) return cudaSuccess;
+  const bool wide = use_wide(mode, p);
   switch (mode) {
     case tc::MODE_ADD_F32:
-      cudaFuncSetAttribute(tc::tc_gemm_kernel<tc::MODE_ADD_F32>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      tc::tc_gemm_kernel<tc::MODE_ADD_F32><<<grid, tc::NUM_THREADS, smem, s>>>(A.hi, A.lo, B.hi,
-                                                                             B.lo, p);
+      if (wide)
+        launch_one<tc::MODE_ADD_F32, true, tc::GRAD_DMAX>(A, B, p, batch, s);
+      else
+        launch_one<tc::MODE_ADD_F32, false, tc::GRAD_DMAX>(A, B, p, batch, s);
       break;
     case tc::MODE_STORE_SPLIT:
-      cudaFuncSetAttribute(tc::tc_gemm_kernel<tc::MODE_STORE_SPLIT>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      tc::tc_gemm_kernel<tc::MODE_STORE_SPLIT><<<grid, tc::NUM_THREADS, smem, s>>>(A.hi, A.lo,
-                                                                                 B.hi, B.lo, p);
+      if (wide)
+        launch_one<tc::MODE_STORE_SPLIT, true, tc::GRAD_DMAX>(A, B, p, batch, s);
+      else
+        launch_one<tc::MODE_STORE_SPLIT, false, tc::GRAD_DMAX>(A, B, p, batch, s);
       break;
     case tc::MODE_GRAD:
-      cudaFuncSetAttribute(tc::tc_gemm_kernel<tc::MODE_GRAD>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      tc::tc_gemm_kernel<tc::MODE_GRAD><<<grid, tc::NUM_THREADS, smem, s>>>(A.hi, A.lo, B.hi, B.lo,
-                                                                          p);
+      if (wide)
+        launch_one<tc::MODE_GRAD, true, 8>(A, B, p, batch, s);
+      else
+        launch_one<tc::MODE_GRAD, false, tc::GRAD_DMAX>(A, B, p, batch, s);
       break;
     default:
       return cudaErrorInvalidValue;

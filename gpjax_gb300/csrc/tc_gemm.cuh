@@ -5,12 +5,13 @@
 // where *_hi is the operand rounded to TF32 and *_lo the TF32 rounding of the
 // remainder (both stored as float32 bit patterns with zero low 13 bits), which
 // recovers float32-class products on the TF32 pipe.  Operands are staged by
-// TMA (128B swizzle) into a 3-stage shared-memory ring, one elected thread
-// issues tcgen05.mma into a 128x128 float32 accumulator in tensor memory, and
-// four epilogue warps read it back with tcgen05.ld and apply a fused epilogue
-// (trailing update, split store with optional transpose, or the MLL adjoint
-// reduction).  Every mbarrier wait is bounded: on timeout the CTA sets an
-// error flag, drains its own copies and returns.
+// TMA (swizzled) into a shared-memory ring, one elected thread issues
+// tcgen05.mma into float32 accumulators in tensor memory, and eight epilogue
+// warps read them back with tcgen05.ld and apply a fused epilogue (trailing
+// update, split store with optional transpose, or the MLL adjoint reduction).
+// Two tile shapes (128 x 128, and 128 x 256 for large problems) share the
+// code.  Every mbarrier wait is bounded: on timeout the CTA sets an error
+// flag, drains its own copies and returns.
 #pragma once
 #include <cuda.h>
 #include "gpk_internal.cuh"
@@ -18,10 +19,7 @@
 namespace gpk {
 namespace tc {
 
-constexpr int BM = 128, BN = 128, BK = 32;
-constexpr int STAGES = 3;
-constexpr int TILE_BYTES = BM * BK * 4;        // 16 KB: 128 rows x 128 B
-constexpr int STAGE_BYTES = 4 * TILE_BYTES;    // A_hi, A_lo, B_hi, B_lo
+constexpr int BM = 128;                        // output tile rows (TMEM lanes)
 constexpr int NUM_THREADS = 320;               // w0 TMA, w1 MMA + TMEM, w2..w9 epilogue
 constexpr int GRAD_DMAX = 16;                  // largest input dimension of the adjoint epilogue
 
@@ -65,12 +63,17 @@ cudaError_t tc_gemm_launch(int mode, const TcMat& A, const TcMat& B, const tc::T
 // Pre-encoded hi/lo tensor maps of one split operand array (encode once per
 // call, reuse for every GEMM that reads the array at some origin).
 struct TcMap {
-  CUtensorMap hi, lo;
+  CUtensorMap hi, lo;        // narrow tile: box 32 x 128
+  CUtensorMap wa_hi, wa_lo;  // wide tile, A side: box 16 x 128
+  CUtensorMap wb_hi, wb_lo;  // wide tile, B side: box 16 x 256
 };
 bool tc_make_map(TcMap* m, const float* hi, const float* lo, int64_t rows, int64_t cols,
                  int64_t ld);
 cudaError_t tc_gemm_run(int mode, const TcMap& A, const TcMap& B, const tc::TcParams& p,
                         int batch, cudaStream_t s);
+// Grid size (output tiles) tc_gemm_run launches for this mode and problem; the
+// MODE_GRAD epilogue writes one gpart row per tile.
+int tc_gemm_tiles(int mode, const tc::TcParams& p);
 
 // hi/lo TF32 split of a float32 matrix (rows x cols, ld) into hi/lo (ldo).
 cudaError_t tf32_split(const float* src, int64_t lds, int rows, int cols, float* hi, float* lo,

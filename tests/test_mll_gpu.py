@@ -58,7 +58,8 @@ def _mixed_check(val, g, ref, gref, tol_scale, gtol=1e-4, vtol=1e-6, ptol=1e-3):
     assert np.all(err <= ptol * np.abs(gref) + gtol * 0.1 * np.linalg.norm(gref)), (g, gref)
 
 
-@pytest.mark.parametrize("n", [700, 2048, 3000])
+# n = 4500 puts 2304-wide nodes at the top of the recursion (128 x 256 GEMM tiles)
+@pytest.mark.parametrize("n", [700, 2048, 3000, 4500])
 def test_mll_mixed_parity_c2(cuda_lib, n):
     """Matern-5/2 ARD, d = 8, X ~ N(0, I), noise 1e-2: |dMLL|/|MLL| <= 1e-6."""
     x, y, ls = c2_like(n, 8, seed=n, kind=2)

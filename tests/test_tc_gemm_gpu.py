@@ -24,8 +24,10 @@ def gemm(A, B, C, alpha=1.0, beta=0.0, lower=False):
     return C
 
 
+# sizes from 2048 up use the 128 x 256 tile (ragged edges included)
 @pytest.mark.parametrize("M,N,K", [(128, 128, 128), (256, 384, 96), (1000, 777, 513),
-                                   (129, 130, 31), (2048, 2048, 2048), (64, 512, 4096)])
+                                   (129, 130, 31), (2048, 2048, 2048), (64, 512, 4096),
+                                   (2176, 2304, 1000), (2300, 2050, 77)])
 def test_split_tf32_gemm(cuda_lib, M, N, K):
     g = torch.Generator(device="cuda").manual_seed(M + N + K)
     A = torch.randn(M, K, device="cuda", generator=g)
@@ -39,9 +41,9 @@ def test_split_tf32_gemm(cuda_lib, M, N, K):
     assert bool(torch.all(err <= 2e-5 * bound + 1e-6)), float((err / (bound + 1e-30)).max())
 
 
-def test_split_tf32_gemm_lower_only(cuda_lib):
-    n, K = 640, 256
-    g = torch.Generator(device="cuda").manual_seed(7)
+@pytest.mark.parametrize("n,K", [(640, 256), (2304, 512), (2200, 96)])
+def test_split_tf32_gemm_lower_only(cuda_lib, n, K):
+    g = torch.Generator(device="cuda").manual_seed(7 + n)
     P = torch.randn(n, K, device="cuda", generator=g)
     C = torch.zeros(n, n, device="cuda")
     gemm(P, P, C, alpha=1.0, beta=0.0, lower=True)
