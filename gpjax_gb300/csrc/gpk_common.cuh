@@ -104,6 +104,23 @@ inline cudaError_t launch_status() {
     if (_e != cudaSuccess) return GPK_ERR_CUDA;              \
   } while (0)
 
+// Programmatic dependent launch.  A kernel launched with the attribute may
+// start while its predecessor in the stream is finishing: it does its
+// input-independent set-up, then pdl_wait() blocks until the predecessor has
+// completed and its writes are visible; pdl_trigger() lets this kernel's own
+// successor launch.  Both are no-ops for a kernel launched without it.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+struct PdlAttr {
+  cudaLaunchAttribute a[1];
+  explicit PdlAttr(bool on) {
+    a[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    a[0].val.programmaticStreamSerializationAllowed = on ? 1 : 0;
+  }
+};
+
 #define GPK_LAUNCH_CHECK()                                   \
   do {                                                       \
     cudaError_t _e = gpk::launch_status();                   \

@@ -160,6 +160,8 @@ __global__ void __launch_bounds__(LEAF_NT)
   float* Pl = Ph + N;
   float* Rl = Pl + N;         // 1 / diag(L)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  pdl_wait();
+  pdl_trigger();
 
   // ---- the block into k-major L, the diagonal track, M = 0 ----
   leaf_load_cols(A, lda, o, LT, 0, N, tid, NT);
@@ -601,9 +603,10 @@ struct TcChol {
   int64_t ldtt[kMaxDepth];
   double *dtrack, *logdiag;
   int *info, *err;
-  cudaStream_t s;     // the caller's stream: the factor's critical path
+  cudaStream_t s;     // the factor's critical path
   cudaStream_t side;  // T^T = (L21 M11)^T products, overlapped with the right subtree
   cudaEvent_t efork, ejoin;
+  bool prev_kernel;   // the last operation enqueued on s was a kernel launch (PDL allowed)
 };
 
 // A node of size sz at depth `depth`: [L11, M11] = chol_inv(A11) (left, size h),
@@ -612,8 +615,17 @@ struct TcChol {
 // runs on the side stream while the right subtree is factored; M21 waits for it.
 cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
   if (sz == LEAF) {
-    leaf_chol_inv_kernel<<<1, LEAF_NT, leaf_smem_bytes(), c.s>>>(c.A, c.ld, o, c.dtrack, c.logdiag,
-                                                             c.info, c.Mh, c.Ml, c.Vh, c.Vl, c.ld);
+    PdlAttr attr(c.prev_kernel);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(1);
+    cfg.blockDim = dim3(LEAF_NT);
+    cfg.dynamicSmemBytes = leaf_smem_bytes();
+    cfg.stream = c.s;
+    cfg.attrs = attr.a;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, leaf_chol_inv_kernel, (const float*)c.A, c.ld, o,
+                       (const double*)c.dtrack, c.logdiag, c.info, c.Mh, c.Ml, c.Vh, c.Vl, c.ld);
+    c.prev_kernel = true;
     return launch_status();
   }
   const int h = ((sz / 2 + LEAF - 1) / LEAF) * LEAF;
@@ -621,7 +633,8 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
   cudaError_t e = chol_inv_rec(c, o, h, depth + 1);
   if (e != cudaSuccess) return e;
   // A21 -> split scratch
-  e = tf32_split(c.A + (int64_t)(o + h) * c.ld + o, c.ld, h2, h, c.SAh, c.SAl, c.ldsa, c.s);
+  e = tf32_split(c.A + (int64_t)(o + h) * c.ld + o, c.ld, h2, h, c.SAh, c.SAl, c.ldsa, c.s,
+                 c.prev_kernel);
   if (e != cudaSuccess) return e;
   {  // L21 = A21 M11^T, float64 diagonal track of A22
     tc::TcParams p{};
@@ -639,11 +652,12 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
     p.alpha = 1.f;
     p.dtrack = c.dtrack;
     p.err = c.err;
-    e = tc_gemm_run(tc::MODE_STORE_SPLIT, c.mSA, c.mM, p, 1, c.s);
+    e = tc_gemm_run(tc::MODE_STORE_SPLIT, c.mSA, c.mM, p, 1, c.s, true);  // after the split
     if (e != cudaSuccess) return e;
   }
   {  // T^T = (L21 M11)^T on the side stream; T[i, j] = sum_c L21[i, c] V11[j, c]
     e = cudaEventRecord(c.efork, c.s);
+    c.prev_kernel = false;
     if (e == cudaSuccess) e = cudaStreamWaitEvent(c.side, c.efork, 0);
     if (e != cudaSuccess) return e;
     tc::TcParams p{};
@@ -680,7 +694,8 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
     p.c_col0 = o + h;
     p.alpha = -1.f;
     p.err = c.err;
-    e = tc_gemm_run(tc::MODE_ADD_F32, c.mL, c.mL, p, 1, c.s);
+    e = tc_gemm_run(tc::MODE_ADD_F32, c.mL, c.mL, p, 1, c.s, c.prev_kernel);
+    c.prev_kernel = true;
     if (e != cudaSuccess) return e;
   }
   e = chol_inv_rec(c, o + h, h2, depth + 1);
@@ -688,6 +703,7 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
   // the latest T^T on the side stream is this node's or a later one: either
   // way this node's is complete when it is
   e = cudaStreamWaitEvent(c.s, c.ejoin, 0);
+  c.prev_kernel = false;
   if (e != cudaSuccess) return e;
   {  // M21 = -M22 T ; M21[i, j] = sum_c M22[i, c] TT[j, c]; V12 = M21^T
     tc::TcParams p{};
@@ -709,7 +725,8 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
     p.t_col0 = o + h;
     p.alpha = -1.f;
     p.err = c.err;
-    e = tc_gemm_run(tc::MODE_STORE_SPLIT, c.mM, c.mTT[depth], p, 1, c.s);
+    e = tc_gemm_run(tc::MODE_STORE_SPLIT, c.mM, c.mTT[depth], p, 1, c.s, c.prev_kernel);
+    c.prev_kernel = true;
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -890,6 +907,7 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
   leaf_zero_kernel<<<dim3(cdiv(LEAF * 24, 256), np / LEAF), 256, 0, hs>>>(b.Mh, b.Ml, b.Vh, b.Vl,
                                                                            b.ld);
   GPK_LAUNCH_CHECK();
+  c.prev_kernel = true;
   GPK_CUDA_TRY(chol_inv_rec(c, 0, np, 0));
   prof_mark(2, hs);
   const int tm = np / LEAF;

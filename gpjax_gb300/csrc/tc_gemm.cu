@@ -297,6 +297,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
+  pdl_wait();  // everything above touched no input of the previous kernel
+  pdl_trigger();
   const uint32_t tmem = ctl->tmem;
   volatile int* abort_flag = &ctl->abort_flag;
 
@@ -590,6 +592,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 // ---------------------------------------------------------------------------
 __global__ void tf32_split_kernel(const float* __restrict__ src, int64_t lds, int rows, int cols,
                                   float* __restrict__ hi, float* __restrict__ lo, int64_t ldo) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= (int64_t)rows * cols) return;
   const int r = (int)(e / cols), c = (int)(e % cols);
@@ -677,7 +681,7 @@ int tc_gemm_tiles(int mode, const tc::TcParams& p) {
 
 template <int MODE, bool WIDE, int DM>
 static void launch_one(const TcMap& A, const TcMap& B, const tc::TcParams& p0, int batch,
-                       cudaStream_t s) {
+                       cudaStream_t s, bool pdl) {
   using TL = tc::Tile<WIDE>;
   tc::TcParams p = p0;
   p.tiles_m = (p.M + tc::BM - 1) / tc::BM;
@@ -686,36 +690,43 @@ static void launch_one(const TcMap& A, const TcMap& B, const tc::TcParams& p0, i
   const size_t smem = tc_smem_bytes<WIDE>();
   cudaFuncSetAttribute(tc::tc_gemm_kernel<MODE, WIDE, DM>,
                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  PdlAttr attr(pdl);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(tc::NUM_THREADS);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = attr.a;
+  cfg.numAttrs = 1;
   if (WIDE)
-    tc::tc_gemm_kernel<MODE, WIDE, DM><<<grid, tc::NUM_THREADS, smem, s>>>(A.wa_hi, A.wa_lo,
-                                                                           B.wb_hi, B.wb_lo, p);
+    cudaLaunchKernelEx(&cfg, tc::tc_gemm_kernel<MODE, WIDE, DM>, A.wa_hi, A.wa_lo, B.wb_hi,
+                       B.wb_lo, p);
   else
-    tc::tc_gemm_kernel<MODE, WIDE, DM><<<grid, tc::NUM_THREADS, smem, s>>>(A.hi, A.lo, B.hi,
-                                                                           B.lo, p);
+    cudaLaunchKernelEx(&cfg, tc::tc_gemm_kernel<MODE, WIDE, DM>, A.hi, A.lo, B.hi, B.lo, p);
 }
 
 cudaError_t tc_gemm_run(int mode, const TcMap& A, const TcMap& B, const tc::TcParams& p,
-                        int batch, cudaStream_t s) {
+                        int batch, cudaStream_t s, bool pdl) {
   if (p.M <= 0 || p.N <= 0 || batch <= 0) return cudaSuccess;
   const bool wide = use_wide(mode, p);
   switch (mode) {
     case tc::MODE_ADD_F32:
       if (wide)
-        launch_one<tc::MODE_ADD_F32, true, tc::GRAD_DMAX>(A, B, p, batch, s);
+        launch_one<tc::MODE_ADD_F32, true, tc::GRAD_DMAX>(A, B, p, batch, s, pdl);
       else
-        launch_one<tc::MODE_ADD_F32, false, tc::GRAD_DMAX>(A, B, p, batch, s);
+        launch_one<tc::MODE_ADD_F32, false, tc::GRAD_DMAX>(A, B, p, batch, s, pdl);
       break;
     case tc::MODE_STORE_SPLIT:
       if (wide)
-        launch_one<tc::MODE_STORE_SPLIT, true, tc::GRAD_DMAX>(A, B, p, batch, s);
+        launch_one<tc::MODE_STORE_SPLIT, true, tc::GRAD_DMAX>(A, B, p, batch, s, pdl);
       else
-        launch_one<tc::MODE_STORE_SPLIT, false, tc::GRAD_DMAX>(A, B, p, batch, s);
+        launch_one<tc::MODE_STORE_SPLIT, false, tc::GRAD_DMAX>(A, B, p, batch, s, pdl);
       break;
     case tc::MODE_GRAD:
       if (wide)
-        launch_one<tc::MODE_GRAD, true, 8>(A, B, p, batch, s);
+        launch_one<tc::MODE_GRAD, true, 8>(A, B, p, batch, s, pdl);
       else
-        launch_one<tc::MODE_GRAD, false, tc::GRAD_DMAX>(A, B, p, batch, s);
+        launch_one<tc::MODE_GRAD, false, tc::GRAD_DMAX>(A, B, p, batch, s, pdl);
       break;
     default:
       return cudaErrorInvalidValue;
@@ -733,10 +744,17 @@ cudaError_t tc_gemm_launch(int mode, const TcMat& A, const TcMat& B, const tc::T
 }
 
 cudaError_t tf32_split(const float* src, int64_t lds, int rows, int cols, float* hi, float* lo,
-                       int64_t ldo, cudaStream_t s) {
+                       int64_t ldo, cudaStream_t s, bool pdl) {
   const int64_t total = (int64_t)rows * cols;
   if (total <= 0) return cudaSuccess;
-  tc::tf32_split_kernel<<<(int)cdiv(total, 256), 256, 0, s>>>(src, lds, rows, cols, hi, lo, ldo);
+  PdlAttr attr(pdl);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)cdiv(total, 256));
+  cfg.blockDim = dim3(256);
+  cfg.stream = s;
+  cfg.attrs = attr.a;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, tc::tf32_split_kernel, src, lds, rows, cols, hi, lo, ldo);
   return launch_status();
 }
 

@@ -69,14 +69,16 @@ struct TcMap {
 };
 bool tc_make_map(TcMap* m, const float* hi, const float* lo, int64_t rows, int64_t cols,
                  int64_t ld);
+// pdl: launch as a programmatic dependent of the previous kernel in the stream
+// (only where that previous stream operation is a kernel launch).
 cudaError_t tc_gemm_run(int mode, const TcMap& A, const TcMap& B, const tc::TcParams& p,
-                        int batch, cudaStream_t s);
+                        int batch, cudaStream_t s, bool pdl = false);
 // Grid size (output tiles) tc_gemm_run launches for this mode and problem; the
 // MODE_GRAD epilogue writes one gpart row per tile.
 int tc_gemm_tiles(int mode, const tc::TcParams& p);
 
 // hi/lo TF32 split of a float32 matrix (rows x cols, ld) into hi/lo (ldo).
 cudaError_t tf32_split(const float* src, int64_t lds, int rows, int cols, float* hi, float* lo,
-                       int64_t ldo, cudaStream_t s);
+                       int64_t ldo, cudaStream_t s, bool pdl = false);
 
 }  // namespace gpk
