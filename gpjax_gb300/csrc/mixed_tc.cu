@@ -455,21 +455,36 @@ size_t leaf_smem_bytes() {
 }
 
 // y = op(Th + Tl) x over a triangle, float64 accumulation, one warp per row.
-__global__ void gemv_split_kernel(const float* __restrict__ Th, const float* __restrict__ Tl,
-                                  int64_t ld, int n, int lower, const double* __restrict__ x,
-                                  double* __restrict__ y, int accumulate) {
+// float32 products and per-lane sums (this applies the approximate inverse
+// inside the refinement loop, whose float64 residual sets the final accuracy);
+// float64 across lanes.  The 16-byte-aligned middle of each row is read as
+// float4 (four rows of loads in flight per lane), the ragged ends as scalars.
+__global__ void __launch_bounds__(256)
+    gemv_split_kernel(const float* __restrict__ Th, const float* __restrict__ Tl, int64_t ld,
+                      int n, int lower, const double* __restrict__ x, double* __restrict__ y,
+                      int accumulate) {
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (i >= n) return;
   const int c0 = lower ? 0 : i, c1 = lower ? i + 1 : n;
   const float* rh = Th + (int64_t)i * ld;
   const float* rl = Tl + (int64_t)i * ld;
-  // float32 products and per-lane sums (this applies the approximate inverse
-  // inside the refinement loop, whose float64 residual sets the final
-  // accuracy); float64 across lanes
-  float s = 0.f;
-  for (int c = c0 + lane; c < c1; c += 32) s = fmaf(rh[c] + rl[c], (float)x[c], s);
-  double sd = warp_sum((double)s);
+  const int a0 = (c0 + 3) & ~3, a1 = c1 & ~3;  // aligned middle [a0, a1) when a0 < a1
+  float s0 = 0.f, s1 = 0.f;
+  for (int c = c0 + lane; c < min(a0, c1); c += 32) s0 = fmaf(rh[c] + rl[c], (float)x[c], s0);
+#pragma unroll 4
+  for (int c = a0 + 4 * lane; c < a1; c += 128) {
+    const float4 h = *reinterpret_cast<const float4*>(rh + c);
+    const float4 l = *reinterpret_cast<const float4*>(rl + c);
+    const double2 xa = *reinterpret_cast<const double2*>(x + c);
+    const double2 xb = *reinterpret_cast<const double2*>(x + c + 2);
+    s0 = fmaf(h.x + l.x, (float)xa.x, s0);
+    s1 = fmaf(h.y + l.y, (float)xa.y, s1);
+    s0 = fmaf(h.z + l.z, (float)xb.x, s0);
+    s1 = fmaf(h.w + l.w, (float)xb.y, s1);
+  }
+  for (int c = max(a0, a1) + lane; c < c1; c += 32) s1 = fmaf(rh[c] + rl[c], (float)x[c], s1);
+  const double sd = warp_sum((double)s0 + (double)s1);
   if (lane == 0) y[i] = accumulate ? y[i] + sd : sd;
 }
 
@@ -591,6 +606,137 @@ __global__ void __launch_bounds__(AG_THREADS)
 }
 
 constexpr int kMaxDepth = 24;  // recursion depth bound (n_pad < 128 * 2^23)
+
+// Gram matrix of the factorisation, mirrored: the lower triangle gets
+// Sigma = K + (jitter + obs_stddev^2) I (gpjax/objectives.py:100-103) and the
+// strict upper triangle the same kernel values, written once per lower tile
+// and transposed through shared memory (both writes coalesced).  The
+// factorisation only ever touches the lower triangle, so the upper one still
+// holds Sigma for the residuals of the alpha refinement.
+constexpr int SG_T = 64;
+__global__ void __launch_bounds__(256)
+    gram_mirror_kernel(int kind, int n, int d, const float* __restrict__ xs,
+                       const double* __restrict__ theta, int n_ls, double jitter,
+                       float* __restrict__ A, int64_t lda) {
+  __shared__ float sx[SG_T][GPK_MAX_D + 1];
+  __shared__ float sy[SG_T][GPK_MAX_D + 1];
+  __shared__ float st[SG_T][SG_T + 1];
+  const int i0 = blockIdx.y * SG_T, j0 = blockIdx.x * SG_T;
+  if (j0 > i0) return;  // upper tiles are written as mirrors of lower ones
+  const float s2 = (float)theta[n_ls];
+  const double sd = theta[n_ls + 1];
+  for (int e = threadIdx.x; e < SG_T * d; e += blockDim.x) {
+    const int r = e / d, k = e % d;
+    sx[r][k] = (i0 + r < n) ? xs[(int64_t)(i0 + r) * d + k] : 0.f;
+    sy[r][k] = (j0 + r < n) ? xs[(int64_t)(j0 + r) * d + k] : 0.f;
+  }
+  __syncthreads();
+  const int c = threadIdx.x % SG_T, gj = j0 + c;
+  for (int r = threadIdx.x / SG_T; r < SG_T; r += 256 / SG_T) {
+    const int gi = i0 + r;
+    float kv = 0.f;
+    if (gi < n && gj < n && gj <= gi) {
+      float sq = 0.f;
+      for (int k = 0; k < d; ++k) {
+        const float df = sx[r][k] - sy[c][k];
+        sq = fmaf(df, df, sq);
+      }
+      kv = kval<float>(kind, sq, s2);
+      A[(int64_t)gi * lda + gj] = (gi == gj) ? (float)(((double)kv + jitter) + sd * sd) : kv;
+    }
+    st[r][c] = kv;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < SG_T * SG_T; e += blockDim.x) {
+    const int rr = e / SG_T, cc = e % SG_T;  // element (i0 + cc, j0 + rr) -> (j0 + rr, i0 + cc)
+    const int gi = i0 + cc, gjj = j0 + rr;
+    if (gi < n && gjj < gi) A[(int64_t)gjj * lda + gi] = st[cc][rr];
+  }
+}
+
+// Partial products of the stored strict upper triangle U of Sigma with alpha,
+// one 128 x 128 tile (I <= J) per CTA: row sums U alpha into rbuf[J][i],
+// column sums U^T alpha into cbuf[I][j]; float32 inside the tile, combined in
+// float64 by residual_upper_finish.
+constexpr int RU_T = 128;
+__global__ void __launch_bounds__(256)
+    residual_upper_kernel(int n, const float* __restrict__ A, int64_t lda,
+                          const double* __restrict__ alpha, double* __restrict__ rbuf,
+                          double* __restrict__ cbuf) {
+  __shared__ float sa_row[RU_T], sa_col[RU_T];
+  __shared__ float cpart[8][RU_T];
+  const int t = blockIdx.x;
+  int L = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+  while (L * (L + 1) / 2 > t) --L;
+  while ((L + 1) * (L + 2) / 2 <= t) ++L;
+  const int I = t - L * (L + 1) / 2, J = L;  // upper tile (I, J), I <= J
+  const int i0 = I * RU_T, j0 = J * RU_T;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int e = threadIdx.x; e < RU_T; e += blockDim.x) {
+    sa_row[e] = (i0 + e < n) ? (float)alpha[i0 + e] : 0.f;
+    sa_col[e] = (j0 + e < n) ? (float)alpha[j0 + e] : 0.f;
+  }
+  __syncthreads();
+  const int cb = 4 * lane;
+  float colacc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 4
+  for (int rr = 0; rr < RU_T / 8; ++rr) {
+    const int r = warp * (RU_T / 8) + rr, gi = i0 + r;
+    float u[4] = {0.f, 0.f, 0.f, 0.f};
+    if (gi < n) {
+      const int64_t base = (int64_t)gi * lda + j0 + cb;
+      if (j0 + cb + 3 < n) {
+        const float4 v = *reinterpret_cast<const float4*>(A + base);
+        u[0] = v.x;
+        u[1] = v.y;
+        u[2] = v.z;
+        u[3] = v.w;
+      } else {
+        for (int q = 0; q < 4; ++q)
+          if (j0 + cb + q < n) u[q] = A[base + q];
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (I == J && j0 + cb + q <= gi) u[q] = 0.f;  // strict upper only
+    }
+    float rp = 0.f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      rp = fmaf(u[q], sa_col[cb + q], rp);
+      colacc[q] = fmaf(u[q], sa_row[r], colacc[q]);
+    }
+    for (int off = 16; off > 0; off >>= 1) rp += __shfl_xor_sync(0xffffffffu, rp, off);
+    if (lane == 0 && gi < n) rbuf[(int64_t)J * n + gi] = (double)rp;
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) cpart[warp][cb + q] = colacc[q];
+  __syncthreads();
+  for (int c = threadIdx.x; c < RU_T; c += blockDim.x) {
+    if (j0 + c >= n) continue;
+    double tot = 0.0;
+    for (int w = 0; w < 8; ++w) tot += (double)cpart[w][c];
+    cbuf[(int64_t)I * n + j0 + c] = tot;
+  }
+}
+
+// r = diff - Sigma alpha: the diagonal (k(0) as the Gram kernel computes it,
+// plus jitter and noise) in float64, the off-diagonal partials summed in a
+// fixed order.
+__global__ void residual_upper_finish(int kind, int n, const double* __restrict__ theta, int n_ls,
+                                      double jitter, const double* __restrict__ diff,
+                                      const double* __restrict__ alpha,
+                                      const double* __restrict__ rbuf,
+                                      const double* __restrict__ cbuf, double* __restrict__ r) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int T = (n + RU_T - 1) / RU_T, ti = i / RU_T;
+  const double sd = theta[n_ls + 1];
+  const double kdiag = (double)kval<float>(kind, 0.f, (float)theta[n_ls]);
+  double s = (kdiag + (jitter + sd * sd)) * alpha[i];
+  for (int J = ti; J < T; ++J) s += rbuf[(int64_t)J * n + i];
+  for (int I = 0; I <= ti; ++I) s += cbuf[(int64_t)I * n + i];
+  r[i] = diff[i] - s;
+}
 
 struct TcChol {
   float* A;
@@ -739,7 +885,7 @@ struct TcBuffers {
   float *TTh[kMaxDepth], *TTl[kMaxDepth];
   int64_t ldtt[kMaxDepth];
   int ndepth;
-  double *diff, *z, *alpha, *r, *logdiag, *dtrack, *rpart, *gpart;
+  double *diff, *z, *alpha, *r, *logdiag, *dtrack, *rpart, *gpart, *rbuf, *cbuf;
   int* err;
 };
 
@@ -783,6 +929,8 @@ size_t tc_layout(int64_t n, int d, void* ws, TcBuffers& b) {
   b.logdiag = (double*)take((size_t)b.npad * 8);
   b.dtrack = (double*)take((size_t)b.npad * 8);
   b.rpart = (double*)take(residual_scratch_doubles((int)n) * 8);
+  b.rbuf = (double*)take((size_t)(b.npad / LEAF) * n * 8);  // residual partials, by tile
+  b.cbuf = (double*)take((size_t)(b.npad / LEAF) * n * 8);
   const size_t tm = (size_t)b.npad / LEAF;
   b.gpart = (double*)take(2 * (tm * (tm + 1) / 2) * (d + 2) * 8);  // adjoint tiles, alpha tiles
   b.err = (int*)take(64);
@@ -851,8 +999,11 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
   GPK_CUDA_TRY(scale_inputs<float>(x, ldx, n, d, theta, n_ls, b.xs, s));
   tc_diff_kernel<<<(int)cdiv(n, 256), 256, 0, s>>>(n, y, theta, n_ls, b.diff);
   GPK_LAUNCH_CHECK();
-  GPK_CUDA_TRY(cross_cov_scaled<float, float>(kind, n, n, d, b.xs, b.xs, theta, n_ls, 1, jitter,
-                                              b.A, b.ld, s));
+  {
+    const dim3 grid((unsigned)cdiv(n, SG_T), (unsigned)cdiv(n, SG_T));
+    gram_mirror_kernel<<<grid, 256, 0, s>>>(kind, n, d, b.xs, theta, n_ls, jitter, b.A, b.ld);
+    GPK_LAUNCH_CHECK();
+  }
   GPK_CUDA_TRY(sigma_diag_init(kind, n, theta, n_ls, jitter, b.dtrack, s));
   if (np > n) {
     pad_identity_kernel<<<(int)cdiv((int64_t)(np - n) * np, 256), 256, 0, s>>>(
@@ -942,8 +1093,16 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
   gemv_split_kernel<<<gb, 256, 0, sv>>>(b.Vh, b.Vl, b.ld, np, 0, b.z, b.alpha, 0);
   GPK_LAUNCH_CHECK();
   for (int it = 0; it < refine; ++it) {
-    GPK_CUDA_TRY(residual<float>(kind, n, d, b.xs, theta, n_ls, jitter, b.diff, b.alpha, b.r,
-                                 b.rpart, sv));
+    {  // r = diff - Sigma alpha from the mirrored upper triangle of the Gram matrix
+      const int tn = (int)cdiv(n, RU_T);
+      residual_upper_kernel<<<tn * (tn + 1) / 2, 256, 0, sv>>>(n, b.A, b.ld, b.alpha, b.rbuf,
+                                                               b.cbuf);
+      GPK_LAUNCH_CHECK();
+      residual_upper_finish<<<(int)cdiv(n, 256), 256, 0, sv>>>(kind, n, theta, n_ls, jitter,
+                                                               b.diff, b.alpha, b.rbuf, b.cbuf,
+                                                               b.r);
+      GPK_LAUNCH_CHECK();
+    }
     gemv_split_kernel<<<gb, 256, 0, sv>>>(b.Mh, b.Ml, b.ld, np, 1, b.r, b.z, 0);
     GPK_LAUNCH_CHECK();
     gemv_split_kernel<<<gb, 256, 0, sv>>>(b.Vh, b.Vl, b.ld, np, 0, b.z, b.alpha, 1);

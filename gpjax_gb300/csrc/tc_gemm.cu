@@ -440,7 +440,44 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       if (have) {
         const int64_t crow0 = p.c_row0 + (int64_t)z * p.c_zrow + i0;
         const int64_t ccol = p.c_col0 + (int64_t)z * p.c_zcol + j0;
-        if (p.c0) {
+        if (MODE == MODE_ADD_F32 && p.c0) {
+          // C += tile: each warp issues RB rows of C loads before it adds and
+          // stores, so the read-modify-write does not serialise on load latency
+          constexpr int RB = 8;
+          constexpr int NRC = BM * (BN / 128);  // (row, 128-column half) pairs
+          for (int rc0 = ew; rc0 < NRC; rc0 += EPI_WARPS * RB) {
+            float4 cv[RB];
+            bool f4[RB];
+#pragma unroll
+            for (int u = 0; u < RB; ++u) {
+              const int rc = rc0 + u * EPI_WARPS;
+              const int rr = rc % BM, c4 = (rc / BM) * 128 + lane * 4, grow = i0 + rr;
+              const int64_t base = (crow0 + rr) * p.ldc + ccol + c4;
+              f4[u] = rc < NRC && grow < p.M && (j0 + c4 + 3 < p.N) &&
+                      !(p.c_lower && j0 + c4 + 3 > grow) && ((base & 3) == 0);
+              if (f4[u]) cv[u] = *reinterpret_cast<const float4*>(p.c0 + base);
+            }
+#pragma unroll
+            for (int u = 0; u < RB; ++u) {
+              const int rc = rc0 + u * EPI_WARPS;
+              const int rr = rc % BM, c4 = (rc / BM) * 128 + lane * 4, grow = i0 + rr;
+              if (rc >= NRC || grow >= p.M) continue;
+              const float4 w4 = *reinterpret_cast<const float4*>(&otile[rr * TLD + c4]);
+              const int64_t base = (crow0 + rr) * p.ldc + ccol + c4;
+              if (f4[u]) {
+                *reinterpret_cast<float4*>(p.c0 + base) =
+                    make_float4(cv[u].x + w4.x, cv[u].y + w4.y, cv[u].z + w4.z, cv[u].w + w4.w);
+              } else {
+                const float wv[4] = {w4.x, w4.y, w4.z, w4.w};
+                for (int k = 0; k < 4; ++k) {
+                  const int gj = j0 + c4 + k;
+                  if (gj < p.N && !(p.c_lower && gj > grow)) p.c0[base + k] += wv[k];
+                }
+              }
+            }
+          }
+        }
+        if (MODE == MODE_STORE_SPLIT && p.c0) {
           for (int rc = ew; rc < BM * (BN / 128); rc += EPI_WARPS) {
             const int rr = rc % BM, c4 = (rc / BM) * 128 + lane * 4;
             const int grow = i0 + rr;
@@ -450,21 +487,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             const int64_t base = (crow0 + rr) * p.ldc + ccol + c4;
             const bool full4 = (j0 + c4 + 3 < p.N) && !(p.c_lower && j0 + c4 + 3 > grow) &&
                                ((base & 3) == 0);
-            if (MODE == MODE_ADD_F32) {
-              if (full4) {
-                float4 cv = *reinterpret_cast<float4*>(p.c0 + base);
-                cv.x += wv[0];
-                cv.y += wv[1];
-                cv.z += wv[2];
-                cv.w += wv[3];
-                *reinterpret_cast<float4*>(p.c0 + base) = cv;
-              } else {
-                for (int k = 0; k < 4; ++k) {
-                  const int gj = j0 + c4 + k;
-                  if (gj < p.N && !(p.c_lower && gj > grow)) p.c0[base + k] += wv[k];
-                }
-              }
-            } else {
+            {
               float hv[4], lv[4];
 #pragma unroll
               for (int k = 0; k < 4; ++k) split_tf32(wv[k], hv[k], lv[k]);
