@@ -324,12 +324,11 @@ def run_gpu(args):
     launches = lib.gpk_launch_count() - launches0
     t_dev = max_over_ranks(e0.elapsed_time(e1) / 1000.0)
     mll_mixed, g_mixed = float(out.item()), grad.cpu().numpy().copy()
-    # mixed form, caller's stream: Gram; recursive Cholesky that also forms
-    # L^-1 (with the T^T products overlapped on the library's side stream);
-    # the fork to the side stream (alpha solve + refinement + alpha terms of
-    # the gradient); the adjoint GEMM (-W terms); the wait for the side work
-    # still running after it; the float64 finalisation
-    phase_names = ["gram", "factor", "fork", "adjoint", "side_tail", "finalize"]
+    # mixed form: Gram; recursive Cholesky that also forms L^-1 (the T^T
+    # products overlapped on the library's low-priority stream); alpha solve +
+    # refinement; the adjoint GEMM; the join back to the caller's stream; the
+    # float64 finalisation
+    phase_names = ["gram", "factor", "solve_refine", "adjoint", "join", "finalize"]
     phases = {nm: float(np.mean([ph[s][k].elapsed_time(ph[s][k + 1]) for s in range(args.steps)]))
               for k, nm in enumerate(phase_names)}
 

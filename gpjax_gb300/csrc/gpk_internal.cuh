@@ -93,6 +93,8 @@ cudaError_t residual(int kind, int n, int d, const T* xs, const double* theta, i
                      double jitter, const double* diff, const double* alpha, double* r,
                      double* rpart, cudaStream_t s);
 size_t residual_scratch_doubles(int n);
+// Scratch (doubles) of the multi-block MLL finalisation.
+size_t mll_finalize_scratch_doubles(int d);
 
 // dtrack[i] = (k(x_i, x_i) + jitter) + obs_stddev^2 in float64.
 cudaError_t sigma_diag_init(int kind, int n, const double* theta, int n_ls, double jitter,

@@ -519,94 +519,6 @@ __global__ void tc_diff_kernel(int n, const double* __restrict__ y, const double
   if (i < n) diff[i] = y[i] - theta[n_ls + 2];
 }
 
-// alpha alpha^T contracted against dK/dtheta (unit variance) over the lower
-// triangle, one 128 x 128 tile per CTA and one row per thread: the alpha part
-// of the MLL gradient, which the finalisation adds to the adjoint GEMM's -W
-// part.  Per element in float32 as in the GEMM epilogue, 32-column partials,
-// float64 accumulation.  Sized (128 threads, DMAX-bounded registers) to fit
-// beside a resident GEMM CTA.
-constexpr int AG_THREADS = LEAF;
-template <int DMAX>
-__global__ void __launch_bounds__(AG_THREADS)
-    alpha_grad_kernel(int kind, int n, int d, const float* __restrict__ xs,
-                      const double* __restrict__ alpha, double* __restrict__ gpart) {
-  constexpr int T = LEAF, NW = AG_THREADS / 32;
-  __shared__ float gx[T * DMAX];
-  __shared__ float ga[T];
-  __shared__ double red[(DMAX + 2) * NW];
-  const int t = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  int I = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
-  while (I * (I + 1) / 2 > t) --I;
-  while ((I + 1) * (I + 2) / 2 <= t) ++I;
-  const int i0 = I * T, j0 = (t - I * (I + 1) / 2) * T;
-  for (int e = tid; e < T * DMAX; e += AG_THREADS) {
-    const int c = e / DMAX, k = e % DMAX, gj = j0 + c;
-    gx[e] = (gj < n && k < d) ? xs[(int64_t)gj * d + k] : 0.f;
-  }
-  for (int c = tid; c < T; c += AG_THREADS) ga[c] = (j0 + c < n) ? (float)alpha[j0 + c] : 0.f;
-  __syncthreads();
-  const int gi = i0 + tid;
-  double gl[DMAX];
-#pragma unroll
-  for (int k = 0; k < DMAX; ++k) gl[k] = 0.0;
-  double gvar = 0.0, gnoise = 0.0;
-  if (gi < n) {
-    float xi[DMAX];
-#pragma unroll
-    for (int k = 0; k < DMAX; ++k) xi[k] = k < d ? xs[(int64_t)gi * d + k] : 0.f;
-    const float ai = (float)alpha[gi];
-    for (int cb = 0; cb < T; cb += 32) {
-      float pl[DMAX];
-#pragma unroll
-      for (int k = 0; k < DMAX; ++k) pl[k] = 0.f;
-      float pvar = 0.f;
-      for (int q = 0; q < 32; ++q) {
-        const int c = cb + q, gj = j0 + c;
-        if (gj >= n || gj > gi) continue;
-        const float coef = ((gi == gj) ? 1.f : 2.f) * ai * ga[c];
-        float sq = 0.f;
-#pragma unroll
-        for (int k = 0; k < DMAX; ++k) {
-          const float df = xi[k] - gx[c * DMAX + k];
-          sq = fmaf(df, df, sq);
-        }
-        float k1, c1;
-        kval_dcoef<float>(kind, sq, 1.f, k1, c1);
-        pvar = fmaf(coef, k1, pvar);
-        const float cc = coef * c1;
-#pragma unroll
-        for (int k = 0; k < DMAX; ++k) {
-          const float df = xi[k] - gx[c * DMAX + k];
-          pl[k] = fmaf(cc, df * df, pl[k]);
-        }
-        if (gi == gj) gnoise += (double)ai * (double)ai;
-      }
-#pragma unroll
-      for (int k = 0; k < DMAX; ++k) gl[k] += (double)pl[k];
-      gvar += (double)pvar;
-    }
-  }
-  const int slots = d + 2;
-  for (int sidx = 0; sidx < slots; ++sidx) {
-    double val = (sidx == d) ? gvar : gnoise;
-    if (sidx < d) {
-#pragma unroll
-      for (int k = 0; k < DMAX; ++k)
-        if (k == sidx) val = gl[k];
-    }
-    val = warp_sum(val);
-    if (lane == 0) red[sidx * NW + warp] = val;
-  }
-  __syncthreads();
-  for (int sidx = tid; sidx < slots; sidx += AG_THREADS) {
-    double tot = 0.0;
-    for (int w = 0; w < NW; ++w) tot += red[sidx * NW + w];
-    gpart[(int64_t)t * slots + sidx] = tot;
-  }
-}
-
-constexpr int kMaxDepth = 24;  // recursion depth bound (n_pad < 128 * 2^23)
-
 // Gram matrix of the factorisation, mirrored: the lower triangle gets
 // Sigma = K + (jitter + obs_stddev^2) I (gpjax/objectives.py:100-103) and the
 // strict upper triangle the same kernel values, written once per lower tile
@@ -737,6 +649,8 @@ __global__ void residual_upper_finish(int kind, int n, const double* __restrict_
   for (int I = 0; I <= ti; ++I) s += cbuf[(int64_t)I * n + i];
   r[i] = diff[i] - s;
 }
+
+constexpr int kMaxDepth = 24;  // recursion depth bound (n_pad < 128 * 2^23)
 
 struct TcChol {
   float* A;
@@ -885,7 +799,7 @@ struct TcBuffers {
   float *TTh[kMaxDepth], *TTl[kMaxDepth];
   int64_t ldtt[kMaxDepth];
   int ndepth;
-  double *diff, *z, *alpha, *r, *logdiag, *dtrack, *rpart, *gpart, *rbuf, *cbuf;
+  double *diff, *z, *alpha, *r, *logdiag, *dtrack, *rpart, *gpart, *rbuf, *cbuf, *fin;
   int* err;
 };
 
@@ -931,8 +845,9 @@ size_t tc_layout(int64_t n, int d, void* ws, TcBuffers& b) {
   b.rpart = (double*)take(residual_scratch_doubles((int)n) * 8);
   b.rbuf = (double*)take((size_t)(b.npad / LEAF) * n * 8);  // residual partials, by tile
   b.cbuf = (double*)take((size_t)(b.npad / LEAF) * n * 8);
+  b.fin = (double*)take(mll_finalize_scratch_doubles(d) * 8);
   const size_t tm = (size_t)b.npad / LEAF;
-  b.gpart = (double*)take(2 * (tm * (tm + 1) / 2) * (d + 2) * 8);  // adjoint tiles, alpha tiles
+  b.gpart = (double*)take(tm * (tm + 1) / 2 * (d + 2) * 8);  // one row per adjoint tile
   b.err = (int*)take(64);
   return off + 1024;
 }
@@ -943,7 +858,8 @@ size_t tc_layout(int64_t n, int d, void* ws, TcBuffers& b) {
 cudaError_t mll_finalize_launch(int n, int d, const double* theta, int n_ls, const double* logdiag,
                                 const double* diff, const double* alpha, const double* gpart,
                                 int ntiles, int want_grad, double jitter, int* info,
-                                double* out_mll, double* out_grad, cudaStream_t s);
+                                double* out_mll, double* out_grad, cudaStream_t s,
+                                double* scratch);
 void prof_mark(int k, cudaStream_t s);
 
 namespace {
@@ -1040,8 +956,8 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
   }
   cudaFuncSetAttribute(leaf_chol_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)leaf_smem_bytes());
-  // The factor and the adjoint GEMM run on the library's high-priority stream
-  // (hs), the T^T products, the alpha solve and the alpha terms on its
+  // The factor, the alpha solve and the adjoint GEMM run on the library's
+  // high-priority stream (hs), the T^T products of the recursion on its
   // low-priority side stream; both fork from and join back into the caller's
   // stream s.  The streams and events are per device; the host-side enqueue
   // of one evaluation holds them.
@@ -1061,9 +977,31 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
   c.prev_kernel = true;
   GPK_CUDA_TRY(chol_inv_rec(c, 0, np, 0));
   prof_mark(2, hs);
-  const int tm = np / LEAF;
-  const int ntiles = tm * (tm + 1) / 2;  // alpha_grad_kernel tiles
-  tc::TcParams pg{};                      // the adjoint GEMM (launched below)
+  // alpha = Sigma^-1 (y - m), refined against float64 residuals from the
+  // mirrored upper triangle of the Gram matrix
+  const int gb = (int)cdiv((int64_t)np * 32, 256);
+  gemv_split_kernel<<<gb, 256, 0, hs>>>(b.Mh, b.Ml, b.ld, np, 1, b.diff, b.z, 0);
+  GPK_LAUNCH_CHECK();
+  gemv_split_kernel<<<gb, 256, 0, hs>>>(b.Vh, b.Vl, b.ld, np, 0, b.z, b.alpha, 0);
+  GPK_LAUNCH_CHECK();
+  for (int it = 0; it < refine; ++it) {
+    const int tn = (int)cdiv(n, RU_T);
+    residual_upper_kernel<<<tn * (tn + 1) / 2, 256, 0, hs>>>(n, b.A, b.ld, b.alpha, b.rbuf,
+                                                             b.cbuf);
+    GPK_LAUNCH_CHECK();
+    residual_upper_finish<<<(int)cdiv(n, 256), 256, 0, hs>>>(kind, n, theta, n_ls, jitter,
+                                                             b.diff, b.alpha, b.rbuf, b.cbuf,
+                                                             b.r);
+    GPK_LAUNCH_CHECK();
+    gemv_split_kernel<<<gb, 256, 0, hs>>>(b.Mh, b.Ml, b.ld, np, 1, b.r, b.z, 0);
+    GPK_LAUNCH_CHECK();
+    gemv_split_kernel<<<gb, 256, 0, hs>>>(b.Vh, b.Vl, b.ld, np, 0, b.z, b.alpha, 1);
+    GPK_LAUNCH_CHECK();
+  }
+  prof_mark(3, hs);
+  // the adjoint: W = V V^T tiles contracted with (alpha alpha^T - W) x dK/dtheta
+  // in the GEMM epilogue
+  tc::TcParams pg{};
   pg.M = np;
   pg.N = np;
   pg.K = np;
@@ -1074,62 +1012,20 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
   pg.d = d;
   pg.kind = kind;
   pg.xs = b.xs;
-  pg.avec = nullptr;  // the alpha terms come from alpha_grad_kernel
+  pg.avec = b.alpha;
   pg.gpart = b.gpart;
   pg.err = b.err;
   const int ntiles_adj = tc_gemm_tiles(tc::MODE_GRAD, pg);  // gpart rows of the adjoint
-  // alpha = Sigma^-1 (y - m), refined against float64 residuals.  With a
-  // gradient it runs on the side stream next to the adjoint GEMM (which then
-  // contracts only -W), followed there by the alpha alpha^T terms.
-  cudaStream_t sv = hs;
-  if (want_grad) {
-    GPK_CUDA_TRY(cudaEventRecord(c.efork, hs));
-    GPK_CUDA_TRY(cudaStreamWaitEvent(c.side, c.efork, 0));
-    sv = c.side;
-  }
-  const int gb = (int)cdiv((int64_t)np * 32, 256);
-  gemv_split_kernel<<<gb, 256, 0, sv>>>(b.Mh, b.Ml, b.ld, np, 1, b.diff, b.z, 0);
-  GPK_LAUNCH_CHECK();
-  gemv_split_kernel<<<gb, 256, 0, sv>>>(b.Vh, b.Vl, b.ld, np, 0, b.z, b.alpha, 0);
-  GPK_LAUNCH_CHECK();
-  for (int it = 0; it < refine; ++it) {
-    {  // r = diff - Sigma alpha from the mirrored upper triangle of the Gram matrix
-      const int tn = (int)cdiv(n, RU_T);
-      residual_upper_kernel<<<tn * (tn + 1) / 2, 256, 0, sv>>>(n, b.A, b.ld, b.alpha, b.rbuf,
-                                                               b.cbuf);
-      GPK_LAUNCH_CHECK();
-      residual_upper_finish<<<(int)cdiv(n, 256), 256, 0, sv>>>(kind, n, theta, n_ls, jitter,
-                                                               b.diff, b.alpha, b.rbuf, b.cbuf,
-                                                               b.r);
-      GPK_LAUNCH_CHECK();
-    }
-    gemv_split_kernel<<<gb, 256, 0, sv>>>(b.Mh, b.Ml, b.ld, np, 1, b.r, b.z, 0);
-    GPK_LAUNCH_CHECK();
-    gemv_split_kernel<<<gb, 256, 0, sv>>>(b.Vh, b.Vl, b.ld, np, 0, b.z, b.alpha, 1);
-    GPK_LAUNCH_CHECK();
-  }
-  if (want_grad) {
-    double* gp_alpha = b.gpart + (int64_t)ntiles_adj * (d + 2);
-    if (d <= 8)
-      alpha_grad_kernel<8><<<ntiles, AG_THREADS, 0, sv>>>(kind, n, d, b.xs, b.alpha, gp_alpha);
-    else
-      alpha_grad_kernel<tc::GRAD_DMAX><<<ntiles, AG_THREADS, 0, sv>>>(kind, n, d, b.xs, b.alpha,
-                                                                     gp_alpha);
-    GPK_LAUNCH_CHECK();
-    GPK_CUDA_TRY(cudaEventRecord(c.ejoin, sv));
-  }
-  prof_mark(3, hs);
   if (want_grad) GPK_CUDA_TRY(tc_gemm_run(tc::MODE_GRAD, c.mV, c.mV, pg, 1, hs));
   prof_mark(4, hs);
-  if (want_grad) GPK_CUDA_TRY(cudaStreamWaitEvent(hs, c.ejoin, 0));
   prof_mark(5, hs);
   GPK_CUDA_TRY(cudaEventRecord(sc->edone, hs));
   GPK_CUDA_TRY(cudaStreamWaitEvent(s, sc->edone, 0));
   tc_check_err<<<1, 1, 0, s>>>(b.err, info);
   GPK_LAUNCH_CHECK();
   GPK_CUDA_TRY(mll_finalize_launch(n, d, theta, n_ls, b.logdiag, b.diff, b.alpha, b.gpart,
-                                   want_grad ? ntiles_adj + ntiles : 0, want_grad, jitter, info,
-                                   out_mll, out_grad, s));
+                                   want_grad ? ntiles_adj : 0, want_grad, jitter, info,
+                                   out_mll, out_grad, s, b.fin));
   prof_mark(6, s);
   return GPK_OK;
 }

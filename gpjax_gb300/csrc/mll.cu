@@ -55,7 +55,7 @@ template <typename T>
 struct MllBuffers {
   int64_t ld;
   T *A, *M, *V, *scratch, *xs;
-  double *diff, *z, *alpha, *r, *logdiag, *rpart, *gpart, *dtrack;
+  double *diff, *z, *alpha, *r, *logdiag, *rpart, *gpart, *dtrack, *fin;
 };
 
 template <typename T>
@@ -76,6 +76,7 @@ static size_t mll_layout(int64_t n, int d, void* ws, MllBuffers<T>& b) {
   b.dtrack = a.take<double>(n);
   b.rpart = a.take<double>(residual_scratch_doubles((int)n));
   b.gpart = a.take<double>((size_t)lauum_grad_tiles<T>((int)n) * (d + 2));
+  b.fin = a.take<double>(mll_finalize_scratch_doubles(d));
   return a.off + 256;
 }
 
@@ -92,12 +93,13 @@ __global__ void axpy_kernel(int n, const double* __restrict__ x, double* __restr
   if (i < n) y[i] += x[i];
 }
 
-// Neumaier-compensated block sum of f(i) over i < n (one block).
+// Neumaier-compensated block sum of f(i) over lo <= i < hi (one block); the
+// result and its compensation term are valid on thread 0.
 template <typename F>
-__device__ double block_ksum(int n, F f) {
+__device__ void block_ksum_pair(int lo, int hi, F f, double& out_sum, double& out_c) {
   __shared__ double s_sum[32], s_c[32];
   double sum = 0.0, c = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+  for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
     const double v = f(i);
     const double t = sum + v;
     c += (fabs(sum) >= fabs(v)) ? (sum - t) + v : (v - t) + sum;
@@ -129,32 +131,22 @@ __device__ double block_ksum(int n, F f) {
     }
   }
   __syncthreads();
-  return tot + tc;  // valid on thread 0
+  out_sum = tot;
+  out_c = tc;
 }
 
-__global__ void __launch_bounds__(256)
-    mll_finalize_kernel(int n, int d, const double* __restrict__ theta, int n_ls,
-                        const double* __restrict__ logdiag, const double* __restrict__ diff,
-                        const double* __restrict__ alpha, const double* __restrict__ gpart,
-                        int ntiles, int want_grad, double jitter, int* __restrict__ info,
-                        double* __restrict__ out_mll, double* __restrict__ out_grad) {
-  const double logdet = 2.0 * block_ksum(n, [&](int i) { return logdiag[i]; });
-  const double quad = block_ksum(n, [&](int i) { return diff[i] * alpha[i]; });
-  const double asum = block_ksum(n, [&](int i) { return alpha[i]; });
-  const int slots = d + 2;
-  __shared__ double sg[GPK_MAX_D + 2];
-  if (want_grad) {
-    // one warp per slot, tiles summed in a fixed strided order
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    for (int s = w; s < slots; s += blockDim.x >> 5) {
-      double acc = 0.0;
-      for (int t = l; t < ntiles; t += 32) acc += gpart[(int64_t)t * slots + s];
-      acc = warp_sum(acc);
-      if (l == 0) sg[s] = acc;
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x != 0) return;
+template <typename F>
+__device__ double block_ksum(int n, F f) {
+  double s, c;
+  block_ksum_pair(0, n, f, s, c);
+  return s + c;  // valid on thread 0
+}
+
+// MLL and gradient from the reduced sums (thread 0).
+__device__ void finalize_outputs(int n, int d, const double* __restrict__ theta, int n_ls,
+                                 double jitter, double logdet, double quad, double asum,
+                                 const double* sg, int want_grad, int* __restrict__ info,
+                                 double* __restrict__ out_mll, double* __restrict__ out_grad) {
   int inf = *info;
   if (inf == INT_MAX) inf = 0;
   *info = inf;
@@ -183,12 +175,111 @@ __global__ void __launch_bounds__(256)
   out_grad[n_ls + 2] = inf ? nan : asum;
 }
 
+__global__ void __launch_bounds__(256)
+    mll_finalize_kernel(int n, int d, const double* __restrict__ theta, int n_ls,
+                        const double* __restrict__ logdiag, const double* __restrict__ diff,
+                        const double* __restrict__ alpha, const double* __restrict__ gpart,
+                        int ntiles, int want_grad, double jitter, int* __restrict__ info,
+                        double* __restrict__ out_mll, double* __restrict__ out_grad) {
+  const double logdet = 2.0 * block_ksum(n, [&](int i) { return logdiag[i]; });
+  const double quad = block_ksum(n, [&](int i) { return diff[i] * alpha[i]; });
+  const double asum = block_ksum(n, [&](int i) { return alpha[i]; });
+  const int slots = d + 2;
+  __shared__ double sg[GPK_MAX_D + 2];
+  if (want_grad) {
+    // one warp per slot, tiles summed in a fixed strided order
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    for (int s = w; s < slots; s += blockDim.x >> 5) {
+      double acc = 0.0;
+      for (int t = l; t < ntiles; t += 32) acc += gpart[(int64_t)t * slots + s];
+      acc = warp_sum(acc);
+      if (l == 0) sg[s] = acc;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  finalize_outputs(n, d, theta, n_ls, jitter, logdet, quad, asum, sg, want_grad, info, out_mll,
+                   out_grad);
+}
+
+// The fixed partition of the finalisation sums over FIN_BLOCKS blocks: per
+// block the compensated (sum, c) pairs of logdiag, diff * alpha and alpha over
+// its index range and the gradient slots over its tile range.
+constexpr int FIN_BLOCKS = 64;
+__global__ void __launch_bounds__(256)
+    mll_finalize_partial_kernel(int n, int d, const double* __restrict__ logdiag,
+                                const double* __restrict__ diff, const double* __restrict__ alpha,
+                                const double* __restrict__ gpart, int ntiles, int want_grad,
+                                double* __restrict__ part) {
+  const int b = blockIdx.x, stride = 6 + d + 2;
+  const int lo = (int)((int64_t)n * b / FIN_BLOCKS), hi = (int)((int64_t)n * (b + 1) / FIN_BLOCKS);
+  double v[6];
+  block_ksum_pair(lo, hi, [&](int i) { return logdiag[i]; }, v[0], v[1]);
+  block_ksum_pair(lo, hi, [&](int i) { return diff[i] * alpha[i]; }, v[2], v[3]);
+  block_ksum_pair(lo, hi, [&](int i) { return alpha[i]; }, v[4], v[5]);
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 6; ++k) part[(int64_t)b * stride + k] = v[k];
+  if (want_grad) {
+    const int tlo = (int)((int64_t)ntiles * b / FIN_BLOCKS);
+    const int thi = (int)((int64_t)ntiles * (b + 1) / FIN_BLOCKS);
+    const int slots = d + 2, w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    for (int sl = w; sl < slots; sl += blockDim.x >> 5) {
+      double acc = 0.0;
+      for (int t = tlo + l; t < thi; t += 32) acc += gpart[(int64_t)t * slots + sl];
+      acc = warp_sum(acc);
+      if (l == 0) part[(int64_t)b * stride + 6 + sl] = acc;
+    }
+  }
+}
+
+__global__ void mll_finalize_combine_kernel(int n, int d, const double* __restrict__ theta,
+                                            int n_ls, const double* __restrict__ part,
+                                            int want_grad, double jitter, int* __restrict__ info,
+                                            double* __restrict__ out_mll,
+                                            double* __restrict__ out_grad) {
+  if (threadIdx.x != 0) return;
+  const int stride = 6 + d + 2;
+  double tot[3], comp[3];
+  for (int q = 0; q < 3; ++q) {
+    tot[q] = 0.0;
+    comp[q] = 0.0;
+    for (int b = 0; b < FIN_BLOCKS; ++b) {
+      const double v = part[(int64_t)b * stride + 2 * q];
+      const double t = tot[q] + v;
+      comp[q] += part[(int64_t)b * stride + 2 * q + 1] +
+                 ((fabs(tot[q]) >= fabs(v)) ? (tot[q] - t) + v : (v - t) + tot[q]);
+      tot[q] = t;
+    }
+  }
+  double sg[GPK_MAX_D + 2];
+  for (int sl = 0; sl < d + 2; ++sl) {
+    double acc = 0.0;
+    if (want_grad)
+      for (int b = 0; b < FIN_BLOCKS; ++b) acc += part[(int64_t)b * stride + 6 + sl];
+    sg[sl] = acc;
+  }
+  finalize_outputs(n, d, theta, n_ls, jitter, 2.0 * (tot[0] + comp[0]), tot[1] + comp[1],
+                   tot[2] + comp[2], sg, want_grad, info, out_mll, out_grad);
+}
+
+size_t mll_finalize_scratch_doubles(int d) { return (size_t)FIN_BLOCKS * (6 + d + 2); }
+
 cudaError_t mll_finalize_launch(int n, int d, const double* theta, int n_ls, const double* logdiag,
                                 const double* diff, const double* alpha, const double* gpart,
                                 int ntiles, int want_grad, double jitter, int* info,
-                                double* out_mll, double* out_grad, cudaStream_t s) {
-  mll_finalize_kernel<<<1, 256, 0, s>>>(n, d, theta, n_ls, logdiag, diff, alpha, gpart, ntiles,
-                                        want_grad, jitter, info, out_mll, out_grad);
+                                double* out_mll, double* out_grad, cudaStream_t s,
+                                double* scratch) {
+  if (!scratch) {
+    mll_finalize_kernel<<<1, 256, 0, s>>>(n, d, theta, n_ls, logdiag, diff, alpha, gpart, ntiles,
+                                          want_grad, jitter, info, out_mll, out_grad);
+    return launch_status();
+  }
+  mll_finalize_partial_kernel<<<FIN_BLOCKS, 256, 0, s>>>(n, d, logdiag, diff, alpha, gpart, ntiles,
+                                                         want_grad, scratch);
+  cudaError_t e = launch_status();
+  if (e != cudaSuccess) return e;
+  mll_finalize_combine_kernel<<<1, 32, 0, s>>>(n, d, theta, n_ls, scratch, want_grad, jitter, info,
+                                               out_mll, out_grad);
   return launch_status();
 }
 
@@ -236,10 +327,9 @@ static gpk_status mll_run(int kind, int n, int d, const double* x, int64_t ldx, 
   if (want_grad)
     GPK_CUDA_TRY(lauum_grad<T>(kind, b.V, b.ld, n, d, b.xs, theta, n_ls, b.alpha, b.gpart, s));
   prof_mark(5, s);
-  mll_finalize_kernel<<<1, 256, 0, s>>>(n, d, theta, n_ls, b.logdiag, b.diff, b.alpha, b.gpart,
-                                        lauum_grad_tiles<T>(n), want_grad, jitter, info,
-                                        out_mll, out_grad);
-  GPK_LAUNCH_CHECK();
+  GPK_CUDA_TRY(mll_finalize_launch(n, d, theta, n_ls, b.logdiag, b.diff, b.alpha, b.gpart,
+                                   lauum_grad_tiles<T>(n), want_grad, jitter, info, out_mll,
+                                   out_grad, s, b.fin));
   prof_mark(6, s);
   return GPK_OK;
 }
