@@ -61,6 +61,14 @@ __device__ __forceinline__ void bar_arrive_n(int id, int n) {
   asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory");
 }
 
+__device__ __forceinline__ void fma2x4(float (&acc)[2][4], const float2 a, const float4 b) {
+  const float av[2] = {a.x, a.y}, bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+  for (int u = 0; u < 2; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(av[u], bv[v], acc[u][v]);
+}
+
 __device__ __forceinline__ void fma4x4(float (&acc)[4][4], const float4 a, const float4 b) {
   const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
 #pragma unroll
@@ -138,7 +146,8 @@ __device__ __forceinline__ void leaf_load_cols(const float* __restrict__ A, int6
 //    the k-major L (4 x 4 tiles, float4 operands);
 //  * the last warp inverts each 32 x 32 diagonal block as soon as it is
 //    factored (handed over through a named barrier) and writes it out;
-//  * two doubling merges M21 = -M22 (L21 M11) fill the rest of M.
+//  * two doubling merges M21 = -M22 (L21 M11), 2 x 4 register tiles, fill
+//    the rest of M.
 // Writes the lower blocks of M (hi/lo), the upper blocks of V = M^T (hi/lo)
 // and half the log of each pivot; the zero blocks of M and V come from
 // leaf_zero_kernel.
@@ -342,86 +351,73 @@ __global__ void __launch_bounds__(LEAF_NT)
     if (!(pv > 0.0)) atomicMin(info, o + i + 1);
   }
   // ---- off-diagonal blocks of M by doubling merges, M21 = -M22 (L21 M11),
-  //      4 x 4 tiles with float4 operands: both 32-wide pairs, then 64 ----
-  if (tid < 128) {  // T = L21 M11 for the pairs at 0 and 64 (lanes walk rows)
-    const int pr = tid >> 6, b = tid & 63, ob = pr * 64;
-    const int i0 = (b & 7) * 4, j0 = (b >> 3) * 4;
-    float acc[4][4] = {};
+  //      2 x 4 tiles with float2 / float4 operands: both 32-wide pairs, then 64 ----
+  if (tid < 256) {  // T = L21 M11 for the pairs at 0 and 64 (lanes walk row pairs)
+    const int pr = tid >> 7, b = tid & 127, ob = pr * 64;
+    const int i0 = (b & 15) * 2, j0 = (b >> 4) * 4;
+    float acc[2][4] = {};
 #pragma unroll 4
-    for (int c = j0; c < PB; ++c)  // M11[c][j] = 0 for c < j
-      fma4x4(acc, *reinterpret_cast<const float4*>(LT + (ob + c) * LDT + ob + PB + i0),
-             *reinterpret_cast<const float4*>(Ms + (ob + c) * LDT + ob + j0));
+    for (int c = j0; c < PB; ++c) {  // M11[c][j] = 0 for c < j
+      const float2 a2 = *reinterpret_cast<const float2*>(LT + (ob + c) * LDT + ob + PB + i0);
+      const float4 b4 = *reinterpret_cast<const float4*>(Ms + (ob + c) * LDT + ob + j0);
+      fma2x4(acc, a2, b4);
+    }
     float* T = Tt + pr * PB * TLD;
 #pragma unroll
-    for (int u = 0; u < 4; ++u)
+    for (int u = 0; u < 2; ++u)
       *reinterpret_cast<float4*>(T + (i0 + u) * TLD + j0) =
           make_float4(acc[u][0], acc[u][1], acc[u][2], acc[u][3]);
   }
   __syncthreads();
-  if (tid < 128) {  // M21 = -M22 T
-    const int pr = tid >> 6, b = tid & 63, ob = pr * 64;
-    const int i0 = (b >> 3) * 4, j0 = (b & 7) * 4;
+  if (tid < 256) {  // M21 = -M22 T
+    const int pr = tid >> 7, b = tid & 127, ob = pr * 64;
+    const int i0 = (b & 15) * 2, j0 = (b >> 4) * 4;
     const float* T = Tt + pr * PB * TLD;
-    float acc[4][4] = {};
+    float acc[2][4] = {};
 #pragma unroll 2
-    for (int c4 = 0; c4 <= i0 / 4; ++c4) {  // M22[i][c] = 0 for c > i
-      float4 mrow[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-        mrow[u] = *reinterpret_cast<const float4*>(Ms + (ob + PB + i0 + u) * LDT + ob + PB + 4 * c4);
-      fma4x4(acc, make_float4(mrow[0].x, mrow[1].x, mrow[2].x, mrow[3].x),
-             *reinterpret_cast<const float4*>(T + (4 * c4 + 0) * TLD + j0));
-      fma4x4(acc, make_float4(mrow[0].y, mrow[1].y, mrow[2].y, mrow[3].y),
-             *reinterpret_cast<const float4*>(T + (4 * c4 + 1) * TLD + j0));
-      fma4x4(acc, make_float4(mrow[0].z, mrow[1].z, mrow[2].z, mrow[3].z),
-             *reinterpret_cast<const float4*>(T + (4 * c4 + 2) * TLD + j0));
-      fma4x4(acc, make_float4(mrow[0].w, mrow[1].w, mrow[2].w, mrow[3].w),
-             *reinterpret_cast<const float4*>(T + (4 * c4 + 3) * TLD + j0));
+    for (int c4 = 0; c4 <= (i0 + 1) / 4; ++c4) {  // M22[i][c] = 0 for c > i
+      const float4 m0 = *reinterpret_cast<const float4*>(Ms + (ob + PB + i0) * LDT + ob + PB + 4 * c4);
+      const float4 m1 = *reinterpret_cast<const float4*>(Ms + (ob + PB + i0 + 1) * LDT + ob + PB + 4 * c4);
+      fma2x4(acc, make_float2(m0.x, m1.x), *reinterpret_cast<const float4*>(T + (4 * c4 + 0) * TLD + j0));
+      fma2x4(acc, make_float2(m0.y, m1.y), *reinterpret_cast<const float4*>(T + (4 * c4 + 1) * TLD + j0));
+      fma2x4(acc, make_float2(m0.z, m1.z), *reinterpret_cast<const float4*>(T + (4 * c4 + 2) * TLD + j0));
+      fma2x4(acc, make_float2(m0.w, m1.w), *reinterpret_cast<const float4*>(T + (4 * c4 + 3) * TLD + j0));
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u)
+    for (int u = 0; u < 2; ++u)
       *reinterpret_cast<float4*>(Ms + (ob + PB + i0 + u) * LDT + ob + j0) =
           make_float4(-acc[u][0], -acc[u][1], -acc[u][2], -acc[u][3]);
   }
   __syncthreads();
-  if (tid < 256) {  // T = L21 M11 for the 64-wide halves (lanes walk rows)
-    const int i0 = (tid & 15) * 4, j0 = (tid >> 4) * 4;
-    float acc[4][4] = {};
+  {  // T = L21 M11 for the 64-wide halves (lanes walk row pairs)
+    const int i0 = (tid & 31) * 2, j0 = (tid >> 5) * 4;
+    float acc[2][4] = {};
 #pragma unroll 4
-    for (int c = j0; c < 64; ++c)
-      fma4x4(acc, *reinterpret_cast<const float4*>(LT + c * LDT + 64 + i0),
-             *reinterpret_cast<const float4*>(Ms + c * LDT + j0));
-#pragma unroll
-    for (int u = 0; u < 4; ++u)
-      *reinterpret_cast<float4*>(Tt + (i0 + u) * TLD + j0) =
-          make_float4(acc[u][0], acc[u][1], acc[u][2], acc[u][3]);
-  } else if (tid < 384) {  // the 32-wide merge results are final: write them out
-    leaf_put_m(Ms, PB, PB, 0, PB, o, ldm, Mh, Ml, tid - 256, 128);
-    leaf_put_m(Ms, 3 * PB, PB, 2 * PB, PB, o, ldm, Mh, Ml, tid - 256, 128);
-    leaf_put_v(Ms, 0, PB, PB, PB, o, ldm, Vh, Vl, tid - 256, 128);
-    leaf_put_v(Ms, 2 * PB, PB, 3 * PB, PB, o, ldm, Vh, Vl, tid - 256, 128);
-  }
-  __syncthreads();
-  if (tid < 256) {  // M21 = -M22 T
-    const int i0 = (tid >> 4) * 4, j0 = (tid & 15) * 4;
-    float acc[4][4] = {};
-#pragma unroll 2
-    for (int c4 = 0; c4 <= i0 / 4; ++c4) {
-      float4 mrow[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-        mrow[u] = *reinterpret_cast<const float4*>(Ms + (64 + i0 + u) * LDT + 64 + 4 * c4);
-      fma4x4(acc, make_float4(mrow[0].x, mrow[1].x, mrow[2].x, mrow[3].x),
-             *reinterpret_cast<const float4*>(Tt + (4 * c4 + 0) * TLD + j0));
-      fma4x4(acc, make_float4(mrow[0].y, mrow[1].y, mrow[2].y, mrow[3].y),
-             *reinterpret_cast<const float4*>(Tt + (4 * c4 + 1) * TLD + j0));
-      fma4x4(acc, make_float4(mrow[0].z, mrow[1].z, mrow[2].z, mrow[3].z),
-             *reinterpret_cast<const float4*>(Tt + (4 * c4 + 2) * TLD + j0));
-      fma4x4(acc, make_float4(mrow[0].w, mrow[1].w, mrow[2].w, mrow[3].w),
-             *reinterpret_cast<const float4*>(Tt + (4 * c4 + 3) * TLD + j0));
+    for (int c = j0; c < 64; ++c) {
+      const float2 a2 = *reinterpret_cast<const float2*>(LT + c * LDT + 64 + i0);
+      const float4 b4 = *reinterpret_cast<const float4*>(Ms + c * LDT + j0);
+      fma2x4(acc, a2, b4);
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u)
+    for (int u = 0; u < 2; ++u)
+      *reinterpret_cast<float4*>(Tt + (i0 + u) * TLD + j0) =
+          make_float4(acc[u][0], acc[u][1], acc[u][2], acc[u][3]);
+  }
+  __syncthreads();
+  {  // M21 = -M22 T
+    const int i0 = (tid & 31) * 2, j0 = (tid >> 5) * 4;
+    float acc[2][4] = {};
+#pragma unroll 2
+    for (int c4 = 0; c4 <= (i0 + 1) / 4; ++c4) {
+      const float4 m0 = *reinterpret_cast<const float4*>(Ms + (64 + i0) * LDT + 64 + 4 * c4);
+      const float4 m1 = *reinterpret_cast<const float4*>(Ms + (64 + i0 + 1) * LDT + 64 + 4 * c4);
+      fma2x4(acc, make_float2(m0.x, m1.x), *reinterpret_cast<const float4*>(Tt + (4 * c4 + 0) * TLD + j0));
+      fma2x4(acc, make_float2(m0.y, m1.y), *reinterpret_cast<const float4*>(Tt + (4 * c4 + 1) * TLD + j0));
+      fma2x4(acc, make_float2(m0.z, m1.z), *reinterpret_cast<const float4*>(Tt + (4 * c4 + 2) * TLD + j0));
+      fma2x4(acc, make_float2(m0.w, m1.w), *reinterpret_cast<const float4*>(Tt + (4 * c4 + 3) * TLD + j0));
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
       *reinterpret_cast<float4*>(Ms + (64 + i0 + u) * LDT + j0) =
           make_float4(-acc[u][0], -acc[u][1], -acc[u][2], -acc[u][3]);
   }
@@ -429,6 +425,10 @@ __global__ void __launch_bounds__(LEAF_NT)
   // ---- the 64-wide merge result: M rows 64.., columns ..63 and its transpose ----
   leaf_put_m(Ms, 64, 64, 0, 64, o, ldm, Mh, Ml, tid, NT);
   leaf_put_v(Ms, 0, 64, 64, 64, o, ldm, Vh, Vl, tid, NT);
+  leaf_put_m(Ms, PB, PB, 0, PB, o, ldm, Mh, Ml, tid, NT);
+  leaf_put_m(Ms, 3 * PB, PB, 2 * PB, PB, o, ldm, Mh, Ml, tid, NT);
+  leaf_put_v(Ms, 0, PB, PB, PB, o, ldm, Vh, Vl, tid, NT);
+  leaf_put_v(Ms, 2 * PB, PB, 3 * PB, PB, o, ldm, Vh, Vl, tid, NT);
 }
 
 
