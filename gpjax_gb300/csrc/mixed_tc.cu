@@ -489,13 +489,18 @@ __global__ void __launch_bounds__(256)
 }
 
 // Identity padding of the factorisation input and the float64 diagonal.
-__global__ void pad_identity_kernel(float* A, int64_t lda, int n, int npad, double* dtrack,
-                                    double* vec0, double* vec1) {
+__global__ void pad_identity_kernel(float* A, float* Ah, float* Al, int64_t lda, int n, int npad,
+                                    double* dtrack, double* vec0, double* vec1) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int pad = npad - n;
   if (e >= (int64_t)pad * npad) return;
   const int i = n + (int)(e / npad), j = (int)(e % npad);
-  if (j <= i) A[(int64_t)i * lda + j] = (i == j) ? 1.f : 0.f;
+  if (j <= i) {
+    const float v = (i == j) ? 1.f : 0.f;
+    A[(int64_t)i * lda + j] = v;
+    Ah[(int64_t)i * lda + j] = v;
+    Al[(int64_t)i * lda + j] = 0.f;
+  }
   if (j == 0) {
     dtrack[i] = 1.0;
     vec0[i] = 0.0;
@@ -520,16 +525,18 @@ __global__ void tc_diff_kernel(int n, const double* __restrict__ y, const double
 }
 
 // Gram matrix of the factorisation, mirrored: the lower triangle gets
-// Sigma = K + (jitter + obs_stddev^2) I (gpjax/objectives.py:100-103) and the
-// strict upper triangle the same kernel values, written once per lower tile
-// and transposed through shared memory (both writes coalesced).  The
-// factorisation only ever touches the lower triangle, so the upper one still
-// holds Sigma for the residuals of the alpha refinement.
+// Sigma = K + (jitter + obs_stddev^2) I (gpjax/objectives.py:100-103), with
+// its TF32 hi/lo split in Ah/Al (the L21 products read their A operand from
+// there), and the strict upper triangle the same kernel values, written once
+// per lower tile and transposed through shared memory (both writes
+// coalesced).  The factorisation only ever touches the lower triangle, so the
+// upper one still holds Sigma for the residuals of the alpha refinement.
 constexpr int SG_T = 64;
 __global__ void __launch_bounds__(256)
     gram_mirror_kernel(int kind, int n, int d, const float* __restrict__ xs,
                        const double* __restrict__ theta, int n_ls, double jitter,
-                       float* __restrict__ A, int64_t lda) {
+                       float* __restrict__ A, float* __restrict__ Ah, float* __restrict__ Al,
+                       int64_t lda) {
   __shared__ float sx[SG_T][GPK_MAX_D + 1];
   __shared__ float sy[SG_T][GPK_MAX_D + 1];
   __shared__ float st[SG_T][SG_T + 1];
@@ -554,7 +561,11 @@ __global__ void __launch_bounds__(256)
         sq = fmaf(df, df, sq);
       }
       kv = kval<float>(kind, sq, s2);
-      A[(int64_t)gi * lda + gj] = (gi == gj) ? (float)(((double)kv + jitter) + sd * sd) : kv;
+      const float v = (gi == gj) ? (float)(((double)kv + jitter) + sd * sd) : kv;
+      const float vh = tf32_rna_f(v);
+      A[(int64_t)gi * lda + gj] = v;
+      Ah[(int64_t)gi * lda + gj] = vh;
+      Al[(int64_t)gi * lda + gj] = tf32_rna_f(v - vh);
     }
     st[r][c] = kv;
   }
@@ -655,9 +666,8 @@ constexpr int kMaxDepth = 24;  // recursion depth bound (n_pad < 128 * 2^23)
 struct TcChol {
   float* A;
   int64_t ld;
-  float *Lh, *Ll, *Mh, *Ml, *Vh, *Vl, *SAh, *SAl;
-  int64_t ldsa;
-  TcMap mL, mM, mV, mSA;
+  float *Lh, *Ll, *Mh, *Ml, *Vh, *Vl, *Ah, *Al;
+  TcMap mL, mM, mV, mA;  // mA: the TF32 split copy of the trailing matrix
   TcMap mTT[kMaxDepth];  // T^T scratch, one per depth: TT(node) lives until M21(node)
   float *TTh[kMaxDepth], *TTl[kMaxDepth];
   int64_t ldtt[kMaxDepth];
@@ -692,15 +702,13 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
   const int h2 = sz - h;
   cudaError_t e = chol_inv_rec(c, o, h, depth + 1);
   if (e != cudaSuccess) return e;
-  // A21 -> split scratch
-  e = tf32_split(c.A + (int64_t)(o + h) * c.ld + o, c.ld, h2, h, c.SAh, c.SAl, c.ldsa, c.s,
-                 c.prev_kernel);
-  if (e != cudaSuccess) return e;
   {  // L21 = A21 M11^T, float64 diagonal track of A22
     tc::TcParams p{};
     p.M = h2;
     p.N = h;
     p.K = h;
+    p.a_row0 = o + h;  // A21 in the split copy of the trailing matrix
+    p.a_col0 = o;
     p.b_row0 = o;
     p.b_col0 = o;
     p.b_tri = TRI_LOWER;
@@ -712,7 +720,8 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
     p.alpha = 1.f;
     p.dtrack = c.dtrack;
     p.err = c.err;
-    e = tc_gemm_run(tc::MODE_STORE_SPLIT, c.mSA, c.mM, p, 1, c.s, true);  // after the split
+    e = tc_gemm_run(tc::MODE_STORE_SPLIT, c.mA, c.mM, p, 1, c.s, c.prev_kernel);
+    c.prev_kernel = true;
     if (e != cudaSuccess) return e;
   }
   {  // T^T = (L21 M11)^T on the side stream; T[i, j] = sum_c L21[i, c] V11[j, c]
@@ -749,6 +758,8 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
     p.b_col0 = o;
     p.c_lower = 1;
     p.c0 = c.A;
+    p.s0 = c.Ah;  // TF32 split copy of the updated A22
+    p.s1 = c.Al;
     p.ldc = c.ld;
     p.c_row0 = o + h;
     p.c_col0 = o + h;
@@ -794,8 +805,8 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
 
 struct TcBuffers {
   int npad;
-  int64_t ld, ldsa;
-  float *A, *Lh, *Ll, *Mh, *Ml, *Vh, *Vl, *SAh, *SAl, *xs;
+  int64_t ld;
+  float *A, *Ah, *Al, *Lh, *Ll, *Mh, *Ml, *Vh, *Vl, *xs;
   float *TTh[kMaxDepth], *TTl[kMaxDepth];
   int64_t ldtt[kMaxDepth];
   int ndepth;
@@ -814,19 +825,16 @@ size_t tc_layout(int64_t n, int d, void* ws, TcBuffers& b) {
   };
   b.npad = (int)(((n + LEAF - 1) / LEAF) * LEAF);
   b.ld = b.npad;
-  const int hmax = ((b.npad / 2 + LEAF - 1) / LEAF) * LEAF;
-  b.ldsa = hmax > 0 ? hmax : LEAF;
   const size_t nn = (size_t)b.npad * b.ld * 4;
-  const size_t hh = (size_t)b.ldsa * b.ldsa * 4;
   b.A = (float*)take(nn);
+  b.Ah = (float*)take(nn);
+  b.Al = (float*)take(nn);
   b.Lh = (float*)take(nn);
   b.Ll = (float*)take(nn);
   b.Mh = (float*)take(nn);
   b.Ml = (float*)take(nn);
   b.Vh = (float*)take(nn);
   b.Vl = (float*)take(nn);
-  b.SAh = (float*)take(hh);
-  b.SAl = (float*)take(hh);
   // T^T at depth k is at most s_{k+1} x s_{k+1}, s_0 = n_pad, s_{k+1} = ceil128(s_k / 2)
   b.ndepth = 0;
   for (int64_t sk = b.npad; sk > LEAF && b.ndepth < kMaxDepth; ++b.ndepth) {
@@ -917,13 +925,14 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
   GPK_LAUNCH_CHECK();
   {
     const dim3 grid((unsigned)cdiv(n, SG_T), (unsigned)cdiv(n, SG_T));
-    gram_mirror_kernel<<<grid, 256, 0, s>>>(kind, n, d, b.xs, theta, n_ls, jitter, b.A, b.ld);
+    gram_mirror_kernel<<<grid, 256, 0, s>>>(kind, n, d, b.xs, theta, n_ls, jitter, b.A, b.Ah,
+                                            b.Al, b.ld);
     GPK_LAUNCH_CHECK();
   }
   GPK_CUDA_TRY(sigma_diag_init(kind, n, theta, n_ls, jitter, b.dtrack, s));
   if (np > n) {
     pad_identity_kernel<<<(int)cdiv((int64_t)(np - n) * np, 256), 256, 0, s>>>(
-        b.A, b.ld, n, np, b.dtrack, b.diff, b.r);
+        b.A, b.Ah, b.Al, b.ld, n, np, b.dtrack, b.diff, b.r);
     GPK_LAUNCH_CHECK();
   }
   prof_mark(1, s);
@@ -936,16 +945,15 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
   c.Ml = b.Ml;
   c.Vh = b.Vh;
   c.Vl = b.Vl;
-  c.SAh = b.SAh;
-  c.SAl = b.SAl;
-  c.ldsa = b.ldsa;
+  c.Ah = b.Ah;
+  c.Al = b.Al;
   c.dtrack = b.dtrack;
   c.logdiag = b.logdiag;
   c.info = info;
   c.err = b.err;
   if (!tc_make_map(&c.mL, b.Lh, b.Ll, np, np, b.ld) || !tc_make_map(&c.mM, b.Mh, b.Ml, np, np, b.ld) ||
       !tc_make_map(&c.mV, b.Vh, b.Vl, np, np, b.ld) ||
-      !tc_make_map(&c.mSA, b.SAh, b.SAl, b.ldsa, b.ldsa, b.ldsa))
+      !tc_make_map(&c.mA, b.Ah, b.Al, np, np, b.ld))
     return GPK_ERR_UNSUPPORTED;
   for (int k = 0; k < b.ndepth; ++k) {
     c.TTh[k] = b.TTh[k];

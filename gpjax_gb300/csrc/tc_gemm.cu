@@ -465,13 +465,26 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
               const float4 w4 = *reinterpret_cast<const float4*>(&otile[rr * TLD + c4]);
               const int64_t base = (crow0 + rr) * p.ldc + ccol + c4;
               if (f4[u]) {
-                *reinterpret_cast<float4*>(p.c0 + base) =
+                const float4 nv =
                     make_float4(cv[u].x + w4.x, cv[u].y + w4.y, cv[u].z + w4.z, cv[u].w + w4.w);
+                *reinterpret_cast<float4*>(p.c0 + base) = nv;
+                if (p.s0) {
+                  float hv[4], lv[4];
+                  const float nvv[4] = {nv.x, nv.y, nv.z, nv.w};
+#pragma unroll
+                  for (int k = 0; k < 4; ++k) split_tf32(nvv[k], hv[k], lv[k]);
+                  *reinterpret_cast<float4*>(p.s0 + base) = make_float4(hv[0], hv[1], hv[2], hv[3]);
+                  *reinterpret_cast<float4*>(p.s1 + base) = make_float4(lv[0], lv[1], lv[2], lv[3]);
+                }
               } else {
                 const float wv[4] = {w4.x, w4.y, w4.z, w4.w};
                 for (int k = 0; k < 4; ++k) {
                   const int gj = j0 + c4 + k;
-                  if (gj < p.N && !(p.c_lower && gj > grow)) p.c0[base + k] += wv[k];
+                  if (gj < p.N && !(p.c_lower && gj > grow)) {
+                    const float nv = p.c0[base + k] + wv[k];
+                    p.c0[base + k] = nv;
+                    if (p.s0) split_tf32(nv, p.s0[base + k], p.s1[base + k]);
+                  }
                 }
               }
             }

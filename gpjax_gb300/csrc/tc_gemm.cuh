@@ -34,6 +34,7 @@ struct TcParams {
   // outputs (MODE_ADD_F32: c0 += alpha*acc; MODE_STORE_SPLIT: hi/lo of alpha*acc
   // into c0/c1 at (i, j) and t0/t1 at (j, i))
   float *c0, *c1, *t0, *t1;
+  float *s0, *s1;  // MODE_ADD_F32, optional: TF32 hi/lo of the updated C, same layout as c0
   int64_t ldc, ldt;
   int64_t c_row0, c_col0, c_zrow, c_zcol;
   int64_t t_row0, t_col0, t_zrow, t_zcol;
