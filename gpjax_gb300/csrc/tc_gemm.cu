@@ -170,6 +170,9 @@ struct Tile {
   static constexpr int NBUF = 512 / BN;                        // TMEM accumulator buffers
   static constexpr int HC = BN / 2;  // accumulator columns owned by one epilogue thread
   static constexpr int TLD = BN + 4; // staged output tile row stride (floats)
+  // K slices summed by one TMEM accumulator before the epilogue drains it:
+  // 32 K elements either way (the accumulation length the accuracy needs)
+  static constexpr int SEG = WIDE ? 2 : 1;
 };
 
 template <int STAGES_>
@@ -183,10 +186,9 @@ struct SmemCtl {
 };
 
 // The tensor-core float32 accumulator rounds less carefully than an FMA, so
-// each accumulator only sums one K slice (BK elements, 3 MMAs per 8); the
-// epilogue warps drain finished segments into round-to-nearest float32
+// each accumulator only sums 32 K elements (Tile::SEG slices, 3 MMAs per 8);
+// the epilogue warps drain finished segments into round-to-nearest float32
 // registers while the MMA thread fills the next of NBUF TMEM buffers.
-constexpr int SEG_CHUNKS = 1;
 constexpr int EPI_WARPS = 8;   // epilogue warps: two per TMEM lane quarter
 constexpr int EPI_THREADS = EPI_WARPS * 32;
 
@@ -249,6 +251,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                    const __grid_constant__ CUtensorMap tb_hi, const __grid_constant__ CUtensorMap tb_lo,
                    const __grid_constant__ TcParams p) {
   using TL = Tile<WIDE>;
+  constexpr int SEG_CHUNKS = TL::SEG;
   constexpr int BN = TL::BN, BK = TL::BK, STAGES = TL::STAGES, NBUF = TL::NBUF, HC = TL::HC,
                 TLD = TL::TLD, STAGE_BYTES = TL::STAGE_BYTES, A_BYTES = TL::A_BYTES,
                 B_BYTES = TL::B_BYTES;
