@@ -125,6 +125,17 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
   for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
 }
 
+// 16 columns of one lane quarter (fewer live registers than x32)
+__device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+
 // two of these then one tcgen05.wait::ld keep two TMEM loads in flight
 __device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile(
@@ -406,12 +417,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         }
       } else {
 #pragma unroll
-        for (int cc = 0; cc < HC; cc += 32) {
-          uint32_t v0[32];
-          tmem_ld32_nowait(tb + cc, v0);
+        for (int cc = 0; cc < HC; cc += 16) {
+          uint32_t v0[16];
+          tmem_ld16_nowait(tb + cc, v0);
           asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-          for (int k = 0; k < 32; ++k) acc[cc + k] += __uint_as_float(v0[k]);
+          for (int k = 0; k < 16; ++k) acc[cc + k] += __uint_as_float(v0[k]);
         }
       }
       tc_fence_before();
@@ -544,7 +555,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       }
     }
     if (MODE == MODE_GRAD) {
-      asm volatile("bar.sync 1, %0;" ::"r"(EPI_THREADS) : "memory");  // gx / ga staged
+      // the finished W tile goes through the (now idle) operand ring, row
+      // stride BN + 1 so that lanes on consecutive rows hit distinct banks:
+      // the reduction below then holds no accumulator registers
+      constexpr int GLD = BN + 1;
+      asm volatile("bar.sync 1, %0;" ::"r"(EPI_THREADS) : "memory");  // gx / ga staged, ring free
+#pragma unroll
+      for (int c = 0; c < HC; ++c) otile[r * GLD + hcol + c] = have ? acc[c] : 0.f;
       // W tile -> reduction against dK/dtheta (unit variance); an aborted wait
       // contributes zeros but still joins the reduction barrier
       float xi[DM];
@@ -567,7 +584,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
           const int c = hcol + cb * 32 + k;
           const int gj = j0 + c;
           if (!have || gi >= p.n_true || gj >= p.n_true || gj > gi) continue;
-          const float w = acc[cb * 32 + k];
+          const float w = otile[r * GLD + c];
           const float f = (gi == gj) ? 1.f : 2.f;
           const float coef = f * (ai * ga[c] - w);
           float sq = 0.f;
