@@ -454,6 +454,13 @@ size_t leaf_smem_bytes() {
   return (size_t)(2 * LEAF * LEAF_LDT + 64 * LEAF_TLD + 5 * LEAF) * sizeof(float);
 }
 
+// x in float32 for the triangular GEMVs (a float64 -> float32 conversion per
+// matrix element would run at this part's float64 rate)
+__global__ void to_f32_kernel(int n, const double* __restrict__ x, float* __restrict__ xf) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) xf[i] = (float)x[i];
+}
+
 // y = op(Th + Tl) x over a triangle, float64 accumulation, one warp per row.
 // float32 products and per-lane sums (this applies the approximate inverse
 // inside the refinement loop, whose float64 residual sets the final accuracy);
@@ -461,7 +468,7 @@ size_t leaf_smem_bytes() {
 // float4 (four rows of loads in flight per lane), the ragged ends as scalars.
 __global__ void __launch_bounds__(256)
     gemv_split_kernel(const float* __restrict__ Th, const float* __restrict__ Tl, int64_t ld,
-                      int n, int lower, const double* __restrict__ x, double* __restrict__ y,
+                      int n, int lower, const float* __restrict__ x, double* __restrict__ y,
                       int accumulate) {
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
@@ -471,19 +478,18 @@ __global__ void __launch_bounds__(256)
   const float* rl = Tl + (int64_t)i * ld;
   const int a0 = (c0 + 3) & ~3, a1 = c1 & ~3;  // aligned middle [a0, a1) when a0 < a1
   float s0 = 0.f, s1 = 0.f;
-  for (int c = c0 + lane; c < min(a0, c1); c += 32) s0 = fmaf(rh[c] + rl[c], (float)x[c], s0);
+  for (int c = c0 + lane; c < min(a0, c1); c += 32) s0 = fmaf(rh[c] + rl[c], x[c], s0);
 #pragma unroll 4
   for (int c = a0 + 4 * lane; c < a1; c += 128) {
     const float4 h = *reinterpret_cast<const float4*>(rh + c);
     const float4 l = *reinterpret_cast<const float4*>(rl + c);
-    const double2 xa = *reinterpret_cast<const double2*>(x + c);
-    const double2 xb = *reinterpret_cast<const double2*>(x + c + 2);
-    s0 = fmaf(h.x + l.x, (float)xa.x, s0);
-    s1 = fmaf(h.y + l.y, (float)xa.y, s1);
-    s0 = fmaf(h.z + l.z, (float)xb.x, s0);
-    s1 = fmaf(h.w + l.w, (float)xb.y, s1);
+    const float4 xv = *reinterpret_cast<const float4*>(x + c);
+    s0 = fmaf(h.x + l.x, xv.x, s0);
+    s1 = fmaf(h.y + l.y, xv.y, s1);
+    s0 = fmaf(h.z + l.z, xv.z, s0);
+    s1 = fmaf(h.w + l.w, xv.w, s1);
   }
-  for (int c = max(a0, a1) + lane; c < c1; c += 32) s1 = fmaf(rh[c] + rl[c], (float)x[c], s1);
+  for (int c = max(a0, a1) + lane; c < c1; c += 32) s1 = fmaf(rh[c] + rl[c], x[c], s1);
   const double sd = warp_sum((double)s0 + (double)s1);
   if (lane == 0) y[i] = accumulate ? y[i] + sd : sd;
 }
@@ -806,7 +812,7 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
 struct TcBuffers {
   int npad;
   int64_t ld;
-  float *A, *Ah, *Al, *Lh, *Ll, *Mh, *Ml, *Vh, *Vl, *xs;
+  float *A, *Ah, *Al, *Lh, *Ll, *Mh, *Ml, *Vh, *Vl, *xs, *vf;
   float *TTh[kMaxDepth], *TTl[kMaxDepth];
   int64_t ldtt[kMaxDepth];
   int ndepth;
@@ -844,6 +850,7 @@ size_t tc_layout(int64_t n, int d, void* ws, TcBuffers& b) {
     b.TTl[b.ndepth] = (float*)take((size_t)sk * sk * 4);
   }
   b.xs = (float*)take((size_t)n * d * 4);
+  b.vf = (float*)take((size_t)b.npad * 4);
   b.diff = (double*)take((size_t)b.npad * 8);
   b.z = (double*)take((size_t)b.npad * 8);
   b.alpha = (double*)take((size_t)b.npad * 8);
@@ -987,11 +994,18 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
   prof_mark(2, hs);
   // alpha = Sigma^-1 (y - m), refined against float64 residuals from the
   // mirrored upper triangle of the Gram matrix
-  const int gb = (int)cdiv((int64_t)np * 32, 256);
-  gemv_split_kernel<<<gb, 256, 0, hs>>>(b.Mh, b.Ml, b.ld, np, 1, b.diff, b.z, 0);
-  GPK_LAUNCH_CHECK();
-  gemv_split_kernel<<<gb, 256, 0, hs>>>(b.Vh, b.Vl, b.ld, np, 0, b.z, b.alpha, 0);
-  GPK_LAUNCH_CHECK();
+  const int gb = (int)cdiv((int64_t)np * 32, 256), gv = (int)cdiv(np, 256);
+  auto gemv = [&](const float* Th, const float* Tl, int lower, const double* x, double* y,
+                  int accumulate) -> gpk_status {
+    to_f32_kernel<<<gv, 256, 0, hs>>>(np, x, b.vf);
+    GPK_LAUNCH_CHECK();
+    gemv_split_kernel<<<gb, 256, 0, hs>>>(Th, Tl, b.ld, np, lower, b.vf, y, accumulate);
+    GPK_LAUNCH_CHECK();
+    return GPK_OK;
+  };
+  gpk_status st = gemv(b.Mh, b.Ml, 1, b.diff, b.z, 0);
+  if (st == GPK_OK) st = gemv(b.Vh, b.Vl, 0, b.z, b.alpha, 0);
+  if (st != GPK_OK) return st;
   for (int it = 0; it < refine; ++it) {
     const int tn = (int)cdiv(n, RU_T);
     residual_upper_kernel<<<tn * (tn + 1) / 2, 256, 0, hs>>>(n, b.A, b.ld, b.alpha, b.rbuf,
@@ -1001,10 +1015,9 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
                                                              b.diff, b.alpha, b.rbuf, b.cbuf,
                                                              b.r);
     GPK_LAUNCH_CHECK();
-    gemv_split_kernel<<<gb, 256, 0, hs>>>(b.Mh, b.Ml, b.ld, np, 1, b.r, b.z, 0);
-    GPK_LAUNCH_CHECK();
-    gemv_split_kernel<<<gb, 256, 0, hs>>>(b.Vh, b.Vl, b.ld, np, 0, b.z, b.alpha, 1);
-    GPK_LAUNCH_CHECK();
+    st = gemv(b.Mh, b.Ml, 1, b.r, b.z, 0);
+    if (st == GPK_OK) st = gemv(b.Vh, b.Vl, 0, b.z, b.alpha, 1);
+    if (st != GPK_OK) return st;
   }
   prof_mark(3, hs);
   // the adjoint: W = V V^T tiles contracted with (alpha alpha^T - W) x dK/dtheta
