@@ -164,21 +164,25 @@ __device__ __forceinline__ void split_tf32(float x, float& hi, float& lo) {
 // ---------------------------------------------------------------------------
 // The kernel
 // ---------------------------------------------------------------------------
-// Two tile shapes.  Narrow: 128 x 128 outputs, 32-wide K slices in 128B
-// swizzle, 3 stages of 64 KB, 4 accumulator buffers of 128 TMEM columns.
-// Wide (large GEMMs): 128 x 256 outputs, 16-wide K slices in 64B swizzle, 4
-// stages of 48 KB, 2 buffers of 256 columns: a quarter fewer operand bytes,
-// both from L2 and from shared memory, per multiply-add.
-template <bool WIDE>
+// Three tile shapes (TS).  Narrow (0): 128 x 128 outputs, 32-wide K slices in
+// 128B swizzle, 3 stages of 64 KB, 4 accumulator buffers of 128 TMEM
+// columns.  Wide (1, large GEMMs): 128 x 256 outputs, 16-wide K slices in 64B
+// swizzle, 4 stages of 48 KB, 2 buffers of 256 columns: a quarter fewer
+// operand bytes, from L2 and from shared memory, per multiply-add.  Half (2,
+// small GEMMs): 128 x 64 outputs, 32-wide slices, 4 stages of 48 KB, 4 buffers
+// of 64 columns: twice the CTAs of the narrow tile where that leaves SMs idle.
+template <int TS>
 struct Tile {
-  static constexpr int BN = WIDE ? 256 : 128;
+  static constexpr bool WIDE = TS == 1;
+  static constexpr int BN = TS == 1 ? 256 : (TS == 2 ? 64 : 128);
   static constexpr int BK = WIDE ? 16 : 32;
-  static constexpr int STAGES = WIDE ? 4 : 3;
+  static constexpr int STAGES = TS == 0 ? 3 : 4;
   static constexpr int SWZ = BK * 4;  // bytes of one K slice row
   static constexpr int A_BYTES = BM * BK * 4;
   static constexpr int B_BYTES = BN * BK * 4;
   static constexpr int STAGE_BYTES = 2 * (A_BYTES + B_BYTES);  // A_hi, A_lo, B_hi, B_lo
-  static constexpr int NBUF = 512 / BN;                        // TMEM accumulator buffers
+  static constexpr int NBUF = BN >= 128 ? 512 / BN : 4;        // TMEM accumulator buffers
+  static constexpr int TMEM_COLS = NBUF * BN;                  // a power of two >= 32
   static constexpr int HC = BN / 2;  // accumulator columns owned by one epilogue thread
   static constexpr int TLD = BN + 4; // staged output tile row stride (floats)
   // K slices summed by one TMEM accumulator before the epilogue drains it:
@@ -206,10 +210,14 @@ constexpr int EPI_THREADS = EPI_WARPS * 32;
 // Launch index -> output tile (I, J), grouped so that the CTAs resident at
 // one time share operand panels in L2: groups of TILE_GROUP tile rows, walked
 // column by column (consecutive CTAs take consecutive rows of one column).
-// Column tiles are `ratio` row tiles wide; for c_lower only tiles holding
-// elements on or below the diagonal exist (J <= I / ratio).
+// Row tiles are BM high, column tiles bn wide; for c_lower only tiles holding
+// elements on or below the diagonal exist: row tile I reaches column tiles
+// J < ncols(I), and column tile J starts at row tile imin(J).
 constexpr int TILE_GROUP = 8;
-__host__ __device__ inline void tile_of(int t, int c_lower, int tiles_m, int tiles_n, int ratio,
+__host__ __device__ inline int lower_ncols(int I, int tiles_n, int bn) {
+  return min(tiles_n, (I * BM + BM - 1) / bn + 1);
+}
+__host__ __device__ inline void tile_of(int t, int c_lower, int tiles_m, int tiles_n, int bn,
                                         int& I, int& J) {
   constexpr int G = TILE_GROUP;
   if (!c_lower) {
@@ -223,20 +231,22 @@ __host__ __device__ inline void tile_of(int t, int c_lower, int tiles_m, int til
   for (;; ++g) {
     rows = min(G, tiles_m - g * G);
     int cnt = 0;
-    for (int r = 0; r < rows; ++r) cnt += (g * G + r) / ratio + 1;
+    for (int r = 0; r < rows; ++r) cnt += lower_ncols(g * G + r, tiles_n, bn);
     if (t < base + cnt) break;
     base += cnt;
   }
   int l = t - base;
-  const int full_cols = (g * G) / ratio;  // columns every row of the group reaches
+  const int full_cols = lower_ncols(g * G, tiles_n, bn);  // every row of the group reaches these
   if (l < full_cols * rows) {
     J = l / rows;
     I = g * G + l % rows;
     return;
   }
   l -= full_cols * rows;
-  for (J = full_cols;; ++J) {  // column J holds the group's rows I >= ratio * J
-    const int r0 = max(g * G, ratio * J);
+  for (J = full_cols;; ++J) {
+    const int num = J * bn - BM + 1;
+    const int imin = num > 0 ? (num + BM - 1) / BM : 0;
+    const int r0 = max(g * G, imin);
     const int cnt = g * G + rows - r0;
     if (l < cnt) {
       I = r0 + l;
@@ -247,21 +257,21 @@ __host__ __device__ inline void tile_of(int t, int c_lower, int tiles_m, int til
 }
 
 // Number of launch indices tile_of maps (the grid of one GEMM).
-__host__ __device__ inline int tile_count(int c_lower, int tiles_m, int tiles_n, int ratio) {
+__host__ __device__ inline int tile_count(int c_lower, int tiles_m, int tiles_n, int bn) {
   if (!c_lower) return tiles_m * tiles_n;
   int cnt = 0;
-  for (int I = 0; I < tiles_m; ++I) cnt += I / ratio + 1;
+  for (int I = 0; I < tiles_m; ++I) cnt += lower_ncols(I, tiles_n, bn);
   return cnt;
 }
 
-// MODE: epilogue.  WIDE: tile shape (Tile<WIDE>).  DM: bound on the input
+// MODE: epilogue.  TS: tile shape (Tile<TS>).  DM: bound on the input
 // dimension of the MODE_GRAD epilogue (registers scale with it).
-template <int MODE, bool WIDE, int DM>
+template <int MODE, int TS, int DM>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap ta_hi, const __grid_constant__ CUtensorMap ta_lo,
                    const __grid_constant__ CUtensorMap tb_hi, const __grid_constant__ CUtensorMap tb_lo,
                    const __grid_constant__ TcParams p) {
-  using TL = Tile<WIDE>;
+  using TL = Tile<TS>;
   constexpr int SEG_CHUNKS = TL::SEG;
   constexpr int BN = TL::BN, BK = TL::BK, STAGES = TL::STAGES, NBUF = TL::NBUF, HC = TL::HC,
                 TLD = TL::TLD, STAGE_BYTES = TL::STAGE_BYTES, A_BYTES = TL::A_BYTES,
@@ -278,7 +288,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int z = blockIdx.z;
   int I, J;
-  tile_of(blockIdx.x, p.c_lower, p.tiles_m, p.tiles_n, BN / BM, I, J);
+  tile_of(blockIdx.x, p.c_lower, p.tiles_m, p.tiles_n, BN, I, J);
   const int i0 = I * BM, j0 = J * BN;
   int klo = 0, khi = p.K;
   if (p.a_tri == TRI_LOWER) khi = min(khi, i0 + BM);
@@ -304,7 +314,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(&ctl->tmem)),
-                 "r"(NBUF * BN)
+                 "r"(TL::TMEM_COLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -405,7 +415,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       if (!have) break;
       tc_fence_after();
       const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN + hcol);
-      if (HC == 64) {
+      if (HC == 32) {
+        uint32_t v0[32];
+        tmem_ld32_nowait(tb, v0);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int k = 0; k < 32; ++k) acc[k] += __uint_as_float(v0[k]);
+      } else if (HC == 64) {
         uint32_t v0[32], v1[32];
         tmem_ld32_nowait(tb, v0);
         tmem_ld32_nowait(tb + 32, v1);
@@ -458,14 +474,15 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
           // C += tile: each warp issues RB rows of C loads before it adds and
           // stores, so the read-modify-write does not serialise on load latency
           constexpr int RB = 8;
-          constexpr int NRC = BM * (BN / 128);  // (row, 128-column half) pairs
+          constexpr int NRC = BM * BN / 128;  // warp passes of 32 float4 groups (rows of BN / 4)
           for (int rc0 = ew; rc0 < NRC; rc0 += EPI_WARPS * RB) {
             float4 cv[RB];
             bool f4[RB];
 #pragma unroll
             for (int u = 0; u < RB; ++u) {
               const int rc = rc0 + u * EPI_WARPS;
-              const int rr = rc % BM, c4 = (rc / BM) * 128 + lane * 4, grow = i0 + rr;
+              const int g = rc * 32 + lane, rr = g / (BN / 4), c4 = (g % (BN / 4)) * 4;
+              const int grow = i0 + rr;
               const int64_t base = (crow0 + rr) * p.ldc + ccol + c4;
               f4[u] = rc < NRC && grow < p.M && (j0 + c4 + 3 < p.N) &&
                       !(p.c_lower && j0 + c4 + 3 > grow) && ((base & 3) == 0);
@@ -474,7 +491,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 #pragma unroll
             for (int u = 0; u < RB; ++u) {
               const int rc = rc0 + u * EPI_WARPS;
-              const int rr = rc % BM, c4 = (rc / BM) * 128 + lane * 4, grow = i0 + rr;
+              const int g = rc * 32 + lane, rr = g / (BN / 4), c4 = (g % (BN / 4)) * 4;
+              const int grow = i0 + rr;
               if (rc >= NRC || grow >= p.M) continue;
               const float4 w4 = *reinterpret_cast<const float4*>(&otile[rr * TLD + c4]);
               const int64_t base = (crow0 + rr) * p.ldc + ccol + c4;
@@ -505,8 +523,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
           }
         }
         if (MODE == MODE_STORE_SPLIT && p.c0) {
-          for (int rc = ew; rc < BM * (BN / 128); rc += EPI_WARPS) {
-            const int rr = rc % BM, c4 = (rc / BM) * 128 + lane * 4;
+          for (int rc = ew; rc < BM * BN / 128; rc += EPI_WARPS) {
+            const int g = rc * 32 + lane, rr = g / (BN / 4), c4 = (g % (BN / 4)) * 4;
             const int grow = i0 + rr;
             if (grow >= p.M) continue;
             const float4 w4 = *reinterpret_cast<const float4*>(&otile[rr * TLD + c4]);
@@ -638,7 +656,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   __syncthreads();
   if (warp == 1) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(NBUF * BN)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TL::TMEM_COLS)
                  : "memory");
   }
 }
@@ -701,9 +719,9 @@ static bool make_map(CUtensorMap* m, const float* base, int64_t rows, int64_t co
   return r == CUDA_SUCCESS;
 }
 
-template <bool WIDE>
+template <int TS>
 static size_t tc_smem_bytes() {
-  using TL = tc::Tile<WIDE>;
+  using TL = tc::Tile<TS>;
   return 1024 + (size_t)TL::STAGES * TL::STAGE_BYTES + sizeof(tc::SmemCtl<TL::STAGES>) +
          (size_t)TL::BN * tc::GRAD_DMAX * 4 + TL::BN * 4 +
          (size_t)(tc::GRAD_DMAX + 2) * 8 * sizeof(double) + 64;
@@ -711,40 +729,46 @@ static size_t tc_smem_bytes() {
 
 bool tc_make_map(TcMap* m, const float* hi, const float* lo, int64_t rows, int64_t cols,
                  int64_t ld) {
-  using N = tc::Tile<false>;
-  using W = tc::Tile<true>;
+  using N = tc::Tile<0>;
+  using W = tc::Tile<1>;
+  using H = tc::Tile<2>;
   return make_map(&m->hi, hi, rows, cols, ld, N::BK, tc::BM) &&
          make_map(&m->lo, lo, rows, cols, ld, N::BK, tc::BM) &&
          make_map(&m->wa_hi, hi, rows, cols, ld, W::BK, tc::BM) &&
          make_map(&m->wa_lo, lo, rows, cols, ld, W::BK, tc::BM) &&
          make_map(&m->wb_hi, hi, rows, cols, ld, W::BK, W::BN) &&
-         make_map(&m->wb_lo, lo, rows, cols, ld, W::BK, W::BN);
+         make_map(&m->wb_lo, lo, rows, cols, ld, W::BK, W::BN) &&
+         make_map(&m->hb_hi, hi, rows, cols, ld, H::BK, H::BN) &&
+         make_map(&m->hb_lo, lo, rows, cols, ld, H::BK, H::BN);
 }
 
-// The wide tile pays off once a GEMM has several waves of tiles; the adjoint
-// epilogue keeps 128 accumulator columns per thread only with DM = 8.
-static bool use_wide(int mode, const tc::TcParams& p) {
-  if (p.M < 2048 || p.N < 2048) return false;
-  return mode != tc::MODE_GRAD || p.d <= 8;
+// Tile shape per problem: wide once a GEMM has several waves of tiles (the
+// adjoint epilogue keeps 128 accumulator columns per thread only with DM =
+// 8), half where narrow tiles would leave most SMs idle, narrow otherwise.
+static int tile_shape(int mode, const tc::TcParams& p) {
+  if (p.M >= 2048 && p.N >= 2048 && (mode != tc::MODE_GRAD || p.d <= 8)) return 1;
+  const int tm = (p.M + tc::BM - 1) / tc::BM, tn = (p.N + 127) / 128;
+  if (mode != tc::MODE_GRAD && tc::tile_count(p.c_lower, tm, tn, 128) <= 32) return 2;
+  return 0;
 }
 
 int tc_gemm_tiles(int mode, const tc::TcParams& p) {
-  const bool wide = use_wide(mode, p);
-  const int bn = wide ? tc::Tile<true>::BN : tc::Tile<false>::BN;
+  const int ts = tile_shape(mode, p);
+  const int bn = ts == 1 ? tc::Tile<1>::BN : (ts == 2 ? tc::Tile<2>::BN : tc::Tile<0>::BN);
   const int tm = (p.M + tc::BM - 1) / tc::BM, tn = (p.N + bn - 1) / bn;
-  return tc::tile_count(p.c_lower, tm, tn, bn / tc::BM);
+  return tc::tile_count(p.c_lower, tm, tn, bn);
 }
 
-template <int MODE, bool WIDE, int DM>
+template <int MODE, int TS, int DM>
 static void launch_one(const TcMap& A, const TcMap& B, const tc::TcParams& p0, int batch,
                        cudaStream_t s, bool pdl) {
-  using TL = tc::Tile<WIDE>;
+  using TL = tc::Tile<TS>;
   tc::TcParams p = p0;
   p.tiles_m = (p.M + tc::BM - 1) / tc::BM;
   p.tiles_n = (p.N + TL::BN - 1) / TL::BN;
-  dim3 grid(tc::tile_count(p.c_lower, p.tiles_m, p.tiles_n, TL::BN / tc::BM), 1, batch);
-  const size_t smem = tc_smem_bytes<WIDE>();
-  cudaFuncSetAttribute(tc::tc_gemm_kernel<MODE, WIDE, DM>,
+  dim3 grid(tc::tile_count(p.c_lower, p.tiles_m, p.tiles_n, TL::BN), 1, batch);
+  const size_t smem = tc_smem_bytes<TS>();
+  cudaFuncSetAttribute(tc::tc_gemm_kernel<MODE, TS, DM>,
                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   PdlAttr attr(pdl);
   cudaLaunchConfig_t cfg = {};
@@ -754,35 +778,41 @@ static void launch_one(const TcMap& A, const TcMap& B, const tc::TcParams& p0, i
   cfg.stream = s;
   cfg.attrs = attr.a;
   cfg.numAttrs = 1;
-  if (WIDE)
-    cudaLaunchKernelEx(&cfg, tc::tc_gemm_kernel<MODE, WIDE, DM>, A.wa_hi, A.wa_lo, B.wb_hi,
+  if (TS == 1)
+    cudaLaunchKernelEx(&cfg, tc::tc_gemm_kernel<MODE, TS, DM>, A.wa_hi, A.wa_lo, B.wb_hi,
                        B.wb_lo, p);
+  else if (TS == 2)
+    cudaLaunchKernelEx(&cfg, tc::tc_gemm_kernel<MODE, TS, DM>, A.hi, A.lo, B.hb_hi, B.hb_lo, p);
   else
-    cudaLaunchKernelEx(&cfg, tc::tc_gemm_kernel<MODE, WIDE, DM>, A.hi, A.lo, B.hi, B.lo, p);
+    cudaLaunchKernelEx(&cfg, tc::tc_gemm_kernel<MODE, TS, DM>, A.hi, A.lo, B.hi, B.lo, p);
 }
 
 cudaError_t tc_gemm_run(int mode, const TcMap& A, const TcMap& B, const tc::TcParams& p,
                         int batch, cudaStream_t s, bool pdl) {
   if (p.M <= 0 || p.N <= 0 || batch <= 0) return cudaSuccess;
-  const bool wide = use_wide(mode, p);
+  const int ts = tile_shape(mode, p);
   switch (mode) {
     case tc::MODE_ADD_F32:
-      if (wide)
-        launch_one<tc::MODE_ADD_F32, true, tc::GRAD_DMAX>(A, B, p, batch, s, pdl);
+      if (ts == 1)
+        launch_one<tc::MODE_ADD_F32, 1, tc::GRAD_DMAX>(A, B, p, batch, s, pdl);
+      else if (ts == 2)
+        launch_one<tc::MODE_ADD_F32, 2, tc::GRAD_DMAX>(A, B, p, batch, s, pdl);
       else
-        launch_one<tc::MODE_ADD_F32, false, tc::GRAD_DMAX>(A, B, p, batch, s, pdl);
+        launch_one<tc::MODE_ADD_F32, 0, tc::GRAD_DMAX>(A, B, p, batch, s, pdl);
       break;
     case tc::MODE_STORE_SPLIT:
-      if (wide)
-        launch_one<tc::MODE_STORE_SPLIT, true, tc::GRAD_DMAX>(A, B, p, batch, s, pdl);
+      if (ts == 1)
+        launch_one<tc::MODE_STORE_SPLIT, 1, tc::GRAD_DMAX>(A, B, p, batch, s, pdl);
+      else if (ts == 2)
+        launch_one<tc::MODE_STORE_SPLIT, 2, tc::GRAD_DMAX>(A, B, p, batch, s, pdl);
       else
-        launch_one<tc::MODE_STORE_SPLIT, false, tc::GRAD_DMAX>(A, B, p, batch, s, pdl);
+        launch_one<tc::MODE_STORE_SPLIT, 0, tc::GRAD_DMAX>(A, B, p, batch, s, pdl);
       break;
     case tc::MODE_GRAD:
-      if (wide)
-        launch_one<tc::MODE_GRAD, true, 8>(A, B, p, batch, s, pdl);
+      if (ts == 1)
+        launch_one<tc::MODE_GRAD, 1, 8>(A, B, p, batch, s, pdl);
       else
-        launch_one<tc::MODE_GRAD, false, tc::GRAD_DMAX>(A, B, p, batch, s, pdl);
+        launch_one<tc::MODE_GRAD, 0, tc::GRAD_DMAX>(A, B, p, batch, s, pdl);
       break;
     default:
       return cudaErrorInvalidValue;

@@ -9,8 +9,8 @@
 // tcgen05.mma into float32 accumulators in tensor memory, and eight epilogue
 // warps read them back with tcgen05.ld and apply a fused epilogue (trailing
 // update, split store with optional transpose, or the MLL adjoint reduction).
-// Two tile shapes (128 x 128, and 128 x 256 for large problems) share the
-// code.  Every mbarrier wait is bounded: on timeout the CTA sets an error
+// Three tile shapes (128 x 128; 128 x 256 for large problems; 128 x 64 where
+// few tiles would leave SMs idle) share the code.  Every mbarrier wait is bounded: on timeout the CTA sets an error
 // flag, drains its own copies and returns.
 #pragma once
 #include <cuda.h>
@@ -67,6 +67,7 @@ struct TcMap {
   CUtensorMap hi, lo;        // narrow tile: box 32 x 128
   CUtensorMap wa_hi, wa_lo;  // wide tile, A side: box 16 x 128
   CUtensorMap wb_hi, wb_lo;  // wide tile, B side: box 16 x 256
+  CUtensorMap hb_hi, hb_lo;  // half tile, B side: box 32 x 64
 };
 bool tc_make_map(TcMap* m, const float* hi, const float* lo, int64_t rows, int64_t cols,
                  int64_t ld);
