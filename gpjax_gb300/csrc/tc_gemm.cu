@@ -748,7 +748,7 @@ bool tc_make_map(TcMap* m, const float* hi, const float* lo, int64_t rows, int64
 static int tile_shape(int mode, const tc::TcParams& p) {
   if (p.M >= 2048 && p.N >= 2048 && (mode != tc::MODE_GRAD || p.d <= 8)) return 1;
   const int tm = (p.M + tc::BM - 1) / tc::BM, tn = (p.N + 127) / 128;
-  if (mode != tc::MODE_GRAD && tc::tile_count(p.c_lower, tm, tn, 128) <= 32) return 2;
+  if (mode != tc::MODE_GRAD && tc::tile_count(p.c_lower, tm, tn, 128) <= 76) return 2;
   return 0;
 }
 
