@@ -46,8 +46,11 @@ def parse_args():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    p.add_argument("--n", type=int, default=16384)
-    p.add_argument("--d", type=int, default=8)
+    p.add_argument("--workload", choices=["c2", "c3", "c5"], default="c2",
+                   help="c2: the headline MLL+grad line (default); c3: n=65536, d=16 RBF "
+                        "precision stress; c5: SGPR collapsed ELBO, n=1e6, m=1024")
+    p.add_argument("--n", type=int, default=None)
+    p.add_argument("--d", type=int, default=None)
     p.add_argument("--fp64-steps", type=int, default=2)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--seed", type=int, default=0)
@@ -422,11 +425,148 @@ def ctypes_void_array(k):
     return (ctypes.c_void_p * k)()
 
 
+def run_c3(args):
+    """Precision stress (SURVEY config C3): exact-GP MLL + gradient at n = 65536, d = 16,
+    RBF ARD, X ~ U[0,1]^16, lengthscales log-U[0.1, 1], variance 1, noise 1e-3,
+    jitter 1e-6; mixed form timed over a few evaluations, the float64 form once as the
+    accuracy reference.  y = sum_j sin(2 pi x_j) / 4 + N(0, 1e-3) (a smooth target in
+    place of a float64 prior sample, which would need a second n = 65536 float64
+    factorisation)."""
+    import torch
+
+    from gpjax_gb300 import _lib
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    lib = _lib.lib()
+    n, d = args.n or 65536, args.d or 16
+    rng = np.random.default_rng(args.seed)
+    x = rng.uniform(0.0, 1.0, (n, d))
+    ls = np.exp(rng.uniform(np.log(0.1), np.log(1.0), d))
+    y = np.sin(2 * np.pi * x).sum(axis=1) / 4 + np.sqrt(1e-3) * rng.standard_normal(n)
+    X = torch.as_tensor(x, device=dev)
+    Y = torch.as_tensor(y, device=dev)
+    theta = torch.tensor(list(ls) + [1.0, float(np.sqrt(1e-3)), 0.0], dtype=torch.float64,
+                         device=dev)
+    out = torch.zeros(1, dtype=torch.float64, device=dev)
+    grad = torch.zeros(d + 3, dtype=torch.float64, device=dev)
+    info = torch.zeros(1, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def run(prec, steps, warm):
+        ws = _lib.workspace(lib.gpk_conjugate_mll_workspace_bytes(n, d, prec), dev)
+        call = lambda: _lib.call("gpk_conjugate_mll", _lib.RBF, n, d, X.data_ptr(), d,
+                                 Y.data_ptr(), theta.data_ptr(), d, 1e-6, prec, 1,
+                                 out.data_ptr(), grad.data_ptr(), info.data_ptr(),
+                                 ws.data_ptr(), ws.numel(), stream.cuda_stream)
+        for _ in range(warm):
+            call()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            call()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        t = e0.elapsed_time(e1) / 1000.0 / steps
+        res = (float(out.item()), grad.cpu().numpy().copy(), int(info.item()), t)
+        del ws
+        torch.cuda.empty_cache()
+        return res
+
+    mm, gm, im, tm = run(_lib.PREC_MIXED, max(1, min(args.steps, 3)), 1)
+    line = {"workload": "c3 precision stress: exact GP MLL + gradient, RBF ARD, "
+                        f"n={n}, d={d}, X~U[0,1]^{d}, noise 1e-3",
+            "metric": f"MLL+grad evals/s at n={n}", "unit": "evals/s", "n": n, "d": d,
+            "mixed": {"evals_per_s": 1.0 / tm, "ms_per_step": 1000.0 * tm, "mll": mm,
+                      "info": im},
+            "data": "synthetic"}
+    if args.fp64_steps > 0:
+        m64, g64, i64, t64 = run(_lib.PREC_FP64, 1, 0)
+        line["fp64_form"] = {"evals_per_s": 1.0 / t64, "ms_per_step": 1000.0 * t64,
+                             "mll": m64, "info": i64}
+        line["speedup_vs_fp64"] = t64 / tm
+        line["rel_err_mll_vs_fp64"] = abs(mm - m64) / abs(m64)
+        line["rel_err_grad_vs_fp64"] = float(np.linalg.norm(gm - g64) / np.linalg.norm(g64))
+    print(json.dumps(line), flush=True)
+
+
+def run_c5(args):
+    """SGPR (SURVEY config C5): collapsed ELBO + gradient (theta and Z), n = 1e6,
+    m = 1024, d = 8; X a mixture of 16 Gaussians (means U[-5,5]^8, sd 0.5),
+    y = sum_j sin(x_j) + N(0, 0.1^2), Z a random subset of X, RBF ARD with
+    lengthscales log-U[0.5, 2]; mixed form against the float64 form."""
+    import torch
+
+    from gpjax_gb300 import _lib
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    lib = _lib.lib()
+    n, d, m = args.n or 1_000_000, args.d or 8, 1024
+    rng = np.random.default_rng(args.seed)
+    means = rng.uniform(-5.0, 5.0, (16, d))
+    x = means[rng.integers(0, 16, n)] + 0.5 * rng.standard_normal((n, d))
+    y = np.sin(x).sum(axis=1) + 0.1 * rng.standard_normal(n)
+    z = x[rng.choice(n, m, replace=False)]
+    ls = np.exp(rng.uniform(np.log(0.5), np.log(2.0), d))
+    X, Y, Z = (torch.as_tensor(a, device=dev) for a in (x, y, z))
+    theta = torch.tensor(list(ls) + [1.0, 0.1, 0.0], dtype=torch.float64, device=dev)
+    out = torch.zeros(1, dtype=torch.float64, device=dev)
+    grad = torch.zeros(d + 3, dtype=torch.float64, device=dev)
+    gz = torch.zeros((m, d), dtype=torch.float64, device=dev)
+    info = torch.zeros(1, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def run(prec, steps, warm):
+        ws = _lib.workspace(lib.gpk_collapsed_elbo_workspace_bytes(n, m, d, prec), dev)
+        call = lambda: _lib.call("gpk_collapsed_elbo", _lib.RBF, n, m, d, X.data_ptr(), d,
+                                 Y.data_ptr(), Z.data_ptr(), d, theta.data_ptr(), d, 1e-6,
+                                 prec, 1, out.data_ptr(), grad.data_ptr(), gz.data_ptr(),
+                                 info.data_ptr(), ws.data_ptr(), ws.numel(),
+                                 stream.cuda_stream)
+        for _ in range(warm):
+            call()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            call()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        t = e0.elapsed_time(e1) / 1000.0 / steps
+        res = (float(out.item()), grad.cpu().numpy().copy(), gz.cpu().numpy().copy(),
+               int(info.item()), t)
+        del ws
+        torch.cuda.empty_cache()
+        return res
+
+    em, gm, zm, im, tm = run(_lib.PREC_MIXED, max(1, min(args.steps, 5)), 1)
+    e64, g64, z64, i64, t64 = run(_lib.PREC_FP64, max(1, min(args.fp64_steps, 2)), 1)
+    print(json.dumps({
+        "workload": f"c5 SGPR collapsed ELBO + gradient (theta, Z), RBF ARD, n={n}, m={m}, "
+                    f"d={d}, X a 16-component Gaussian mixture",
+        "metric": f"ELBO+grad evals/s at n={n}, m={m}", "unit": "evals/s",
+        "n": n, "m": m, "d": d,
+        "mixed": {"evals_per_s": 1.0 / tm, "ms_per_step": 1000.0 * tm, "elbo": em, "info": im},
+        "fp64_form": {"evals_per_s": 1.0 / t64, "ms_per_step": 1000.0 * t64, "elbo": e64,
+                      "info": i64},
+        "speedup_vs_fp64": t64 / tm,
+        "rel_err_elbo_vs_fp64": abs(em - e64) / abs(e64),
+        "rel_err_grad_vs_fp64": float(np.linalg.norm(gm - g64) / np.linalg.norm(g64)),
+        "rel_err_grad_z_vs_fp64": float(np.linalg.norm(zm - z64) / np.linalg.norm(z64)),
+        "data": "synthetic"}), flush=True)
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
+        args.n, args.d = args.n or 16384, args.d or 8
         run_reference(args)
+    elif args.workload == "c3":
+        run_c3(args)
+    elif args.workload == "c5":
+        run_c5(args)
     else:
+        args.n, args.d = args.n or 16384, args.d or 8
         run_gpu(args)
 
 
