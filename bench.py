@@ -46,9 +46,10 @@ def parse_args():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    p.add_argument("--workload", choices=["c2", "c3", "c5"], default="c2",
+    p.add_argument("--workload", choices=["c2", "c3", "c4", "c5"], default="c2",
                    help="c2: the headline MLL+grad line (default); c3: n=65536, d=16 RBF "
-                        "precision stress; c5: SGPR collapsed ELBO, n=1e6, m=1024")
+                        "precision stress; c4: 512 batched GPs; c5: SGPR collapsed ELBO, "
+                        "n=1e6, m=1024")
     p.add_argument("--n", type=int, default=None)
     p.add_argument("--d", type=int, default=None)
     p.add_argument("--fp64-steps", type=int, default=2)
@@ -556,6 +557,96 @@ def run_c5(args):
         "data": "synthetic"}), flush=True)
 
 
+def c4_instances(count, seed):
+    """SURVEY config C4: n_i ~ U{64..2048}, d_i ~ U{2..10}, X ~ U[-1,1]^d, RBF or
+    Matern-3/2 with probability 1/2, ARD lengthscales log-U[0.1, 2], variance
+    log-U[0.5, 2], noise log-U[1e-4, 1e-1]; y = a random-Fourier-feature prior
+    sample (100 frequencies, cos and sin features) + N(0, 0.05^2)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        n, d = int(rng.integers(64, 2049)), int(rng.integers(2, 11))
+        kind = 0 if rng.random() < 0.5 else 1  # RBF, Matern-3/2
+        x = rng.uniform(-1.0, 1.0, (n, d))
+        ls = np.exp(rng.uniform(np.log(0.1), np.log(2.0), d))
+        var = float(np.exp(rng.uniform(np.log(0.5), np.log(2.0))))
+        noise = float(np.exp(rng.uniform(np.log(1e-4), np.log(1e-1))))
+        z = rng.standard_normal((100, d))
+        if kind == 1:  # Matern-3/2 spectral density: multivariate t with 3 degrees of freedom
+            z = z / np.sqrt(rng.chisquare(3.0, (100, 1)) / 3.0)
+        proj = (x / ls) @ z.T
+        feats = np.concatenate([np.cos(proj), np.sin(proj)], axis=1) * np.sqrt(var / 100)
+        y = feats @ rng.standard_normal(200) + 0.05 * rng.standard_normal(n)
+        out.append((kind, x, y, np.concatenate([ls, [var, np.sqrt(noise), 0.0]])))
+    return out
+
+
+def run_c4(args):
+    """512 independent GPs per step: MLL + gradient of every instance in one batched
+    library call (float32 compute), captured once into a CUDA graph and replayed."""
+    import ctypes
+
+    import torch
+
+    from gpjax_gb300 import _lib
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    lib = _lib.lib()
+    count = 512
+    insts = c4_instances(count, args.seed)
+    xs = [torch.as_tensor(i[1], device=dev) for i in insts]
+    ys = [torch.as_tensor(i[2], device=dev) for i in insts]
+    ths = [torch.as_tensor(i[3], device=dev) for i in insts]
+    mll = torch.zeros(count, dtype=torch.float64, device=dev)
+    grads = [torch.zeros(x.shape[1] + 3, dtype=torch.float64, device=dev) for x in xs]
+    info = torch.zeros(count, dtype=torch.int32, device=dev)
+    i32, i64, ptr = ctypes.c_int * count, ctypes.c_int64 * count, ctypes.c_void_p * count
+    n = i64(*[x.shape[0] for x in xs])
+    d = i32(*[x.shape[1] for x in xs])
+    host = dict(kind=i32(*[i[0] for i in insts]), x=ptr(*[x.data_ptr() for x in xs]),
+                ldx=i64(*[x.shape[1] for x in xs]), y=ptr(*[y.data_ptr() for y in ys]),
+                th=ptr(*[t.data_ptr() for t in ths]), nls=i32(*[x.shape[1] for x in xs]),
+                out=ptr(*[mll.data_ptr() + 8 * k for k in range(count)]),
+                g=ptr(*[g.data_ptr() for g in grads]))
+    ws = _lib.workspace(lib.gpk_conjugate_mll_batched_workspace_bytes(count, n, d), dev)
+
+    def step():
+        _lib.call("gpk_conjugate_mll_batched", count, host["kind"], n, d, host["x"], host["ldx"],
+                  host["y"], host["th"], host["nls"], 1e-6, 1, host["out"], host["g"],
+                  info.data_ptr(), ws.data_ptr(), ws.numel(),
+                  torch.cuda.current_stream(dev).cuda_stream)
+
+    for _ in range(max(args.warmup, 1)):
+        step()
+    torch.cuda.synchronize(dev)
+    graph, mode = None, "eager"
+    try:
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            step()
+        graph.replay()
+        torch.cuda.synchronize(dev)
+        mode = "cuda graph"
+    except Exception:  # capture unsupported here: time the eager calls
+        graph = None
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        graph.replay() if graph is not None else step()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    t = e0.elapsed_time(e1) / 1000.0 / args.steps
+    sum_n3 = float(sum(float(x.shape[0]) ** 3 for x in xs))
+    print(json.dumps({
+        "workload": "c4 batched: 512 exact GPs, n_i~U{64..2048}, d_i~U{2..10}, RBF / Matern-3/2, "
+                    "MLL + gradient of all instances per step",
+        "metric": "MLL+grad steps/s (512 GPs per step)", "unit": "steps/s", "value": 1.0 / t,
+        "ms_per_step": 1000.0 * t, "launch": mode, "sum_n3": sum_n3,
+        "tflops_n3_convention": sum_n3 / t / 1e12, "dtype": "f32 + f64 refinement",
+        "failed_instances": int((info.cpu() != 0).sum()), "data": "synthetic"}), flush=True)
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
@@ -565,6 +656,8 @@ def main():
         run_c3(args)
     elif args.workload == "c5":
         run_c5(args)
+    elif args.workload == "c4":
+        run_c4(args)
     else:
         args.n, args.d = args.n or 16384, args.d or 8
         run_gpu(args)

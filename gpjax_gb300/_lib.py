@@ -49,6 +49,10 @@ SIGNATURES = {
     "gpk_conjugate_mll": (_c_int, [_c_int, _c_i64, _c_int, _c_ptr, _c_i64, _c_ptr, _c_ptr, _c_int,
                                    _c_dbl, _c_int, _c_int, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_size,
                                    _c_ptr]),
+    "gpk_conjugate_mll_batched_workspace_bytes": (_c_size, [_c_int, _c_ptr, _c_ptr]),
+    "gpk_conjugate_mll_batched": (_c_int, [_c_int, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr,
+                                           _c_ptr, _c_ptr, _c_dbl, _c_int, _c_ptr, _c_ptr,
+                                           _c_ptr, _c_ptr, _c_size, _c_ptr]),
     "gpk_conjugate_mll_noalloc_max_n": (_c_size, []),
     "gpk_conjugate_mll_noalloc": (_c_int, [_c_int, _c_i64, _c_int, _c_ptr, _c_i64, _c_ptr, _c_ptr,
                                            _c_int, _c_dbl, _c_int, _c_ptr, _c_ptr, _c_ptr,

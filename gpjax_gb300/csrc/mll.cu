@@ -10,10 +10,12 @@
 // and alpha = Sigma^-1 diff = V (M diff) with M = L^-1, V = M^T, refined
 // against residuals accumulated in float64.  The gradient is the fused
 // inverse-product/kernel-derivative reduction of adjoint.cu.
+#include <algorithm>
 #include <atomic>
 #include <climits>
 #include <cmath>
 #include <mutex>
+#include <vector>
 #include "gpk_internal.cuh"
 
 namespace gpk {
@@ -408,6 +410,106 @@ extern "C" gpk_status gpk_conjugate_mll(int kind, int64_t n, int d, const double
                       out_grad, info, workspace, stream);
   return mll_run<float>(kind, (int)n, d, x, ldx, y, theta, n_ls, jitter, 2, want_grad, out_mll,
                         out_grad, info, workspace, stream);
+}
+
+// ---------------------------------------------------------------------------
+// Batched MLL + gradient: independent GPs of different sizes in one call, each
+// in the float32 form (SIMT), spread over a few internal streams that fork
+// from and join back into the caller's stream.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr int kBatchStreams = 8;
+struct BatchCtx {
+  cudaStream_t s[kBatchStreams] = {};
+  cudaEvent_t fork = nullptr;
+  cudaEvent_t join[kBatchStreams] = {};
+};
+std::mutex g_batch_mu;
+BatchCtx g_batch[64];
+
+cudaError_t batch_ctx(BatchCtx** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  BatchCtx& c = g_batch[dev];
+  if (!c.fork) {
+    e = cudaEventCreateWithFlags(&c.fork, cudaEventDisableTiming);
+    for (int k = 0; k < kBatchStreams && e == cudaSuccess; ++k) {
+      e = cudaStreamCreateWithFlags(&c.s[k], cudaStreamNonBlocking);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c.join[k], cudaEventDisableTiming);
+    }
+    if (e != cudaSuccess) return e;
+  }
+  *out = &c;
+  return cudaSuccess;
+}
+
+// Per-instance workspace offsets (256-byte aligned); returns the total.
+size_t batch_offsets(int count, const int64_t* n, const int* d, size_t* off) {
+  size_t tot = 0;
+  for (int i = 0; i < count; ++i) {
+    MllBuffers<float> b;
+    const size_t w = (mll_layout<float>(n[i], d[i], nullptr, b) + 255) & ~size_t(255);
+    if (off) off[i] = tot;
+    tot += w;
+  }
+  return tot + 256;
+}
+}  // namespace
+
+extern "C" size_t gpk_conjugate_mll_batched_workspace_bytes(int count, const int64_t* n,
+                                                            const int* d) {
+  if (count <= 0 || !n || !d) return 256;
+  for (int i = 0; i < count; ++i)
+    if (n[i] <= 0 || d[i] <= 0) return 256;
+  return batch_offsets(count, n, d, nullptr);
+}
+
+extern "C" gpk_status gpk_conjugate_mll_batched(
+    int count, const int* kind, const int64_t* n, const int* d, const double* const* x,
+    const int64_t* ldx, const double* const* y, const double* const* theta, const int* n_ls,
+    double jitter, int want_grad, double* const* out_mll, double* const* out_grad, int* info,
+    void* workspace, size_t workspace_bytes, cudaStream_t stream) {
+  if (count < 0) return GPK_ERR_BAD_ARG;
+  if (count == 0) return GPK_OK;
+  if (!kind || !n || !d || !x || !ldx || !y || !theta || !n_ls || !out_mll || !info ||
+      (want_grad && !out_grad) || !workspace)
+    return GPK_ERR_BAD_ARG;
+  for (int i = 0; i < count; ++i) {
+    if (n[i] <= 0 || !mll_args_ok(kind[i], n[i], d[i], ldx[i], n_ls[i], GPK_PREC_MIXED))
+      return GPK_ERR_BAD_ARG;
+    if (!x[i] || !y[i] || !theta[i] || !out_mll[i] || (want_grad && !out_grad[i]))
+      return GPK_ERR_BAD_ARG;
+  }
+  std::vector<size_t> off(count);
+  if (workspace_bytes < batch_offsets(count, n, d, off.data())) return GPK_ERR_WORKSPACE;
+  // largest first, each onto the least loaded stream (cost ~ n^3)
+  std::vector<int> order(count);
+  for (int i = 0; i < count; ++i) order[i] = i;
+  std::sort(order.begin(), order.end(), [&](int a, int b) { return n[a] > n[b]; });
+  std::lock_guard<std::mutex> lock(g_batch_mu);
+  BatchCtx* bc = nullptr;
+  GPK_CUDA_TRY(batch_ctx(&bc));
+  GPK_CUDA_TRY(cudaEventRecord(bc->fork, stream));
+  for (int k = 0; k < kBatchStreams; ++k) GPK_CUDA_TRY(cudaStreamWaitEvent(bc->s[k], bc->fork, 0));
+  double load[kBatchStreams] = {};
+  for (int i : order) {
+    int k = 0;
+    for (int q = 1; q < kBatchStreams; ++q)
+      if (load[q] < load[k]) k = q;
+    load[k] += (double)n[i] * (double)n[i] * (double)n[i];
+    const gpk_status st =
+        mll_run<float>(kind[i], (int)n[i], d[i], x[i], ldx[i], y[i], theta[i], n_ls[i], jitter, 2,
+                       want_grad, out_mll[i], want_grad ? out_grad[i] : nullptr, info + i,
+                       static_cast<char*>(workspace) + off[i], bc->s[k]);
+    if (st != GPK_OK) return st;
+  }
+  for (int k = 0; k < kBatchStreams; ++k) {
+    GPK_CUDA_TRY(cudaEventRecord(bc->join[k], bc->s[k]));
+    GPK_CUDA_TRY(cudaStreamWaitEvent(stream, bc->join[k], 0));
+  }
+  return GPK_OK;
 }
 
 extern "C" gpk_status gpk_lower_cholesky(int64_t n, int dtype, void* A, int64_t lda,

@@ -150,3 +150,41 @@ def cross_covariance_vjp(kind, n_ls, theta, x, y, G, need_x=False, need_y=False)
               theta.data_ptr(), n_ls, Gc.data_ptr(), m, gth.data_ptr(), _lib.ptr(gx),
               _lib.ptr(gy), ws.data_ptr(), ws.numel(), _lib.stream_ptr(dev))
     return gth, gx, gy
+
+
+def conjugate_mll_batched(kinds, xs, ys, thetas, n_ls, jitter: float = 1e-6,
+                          want_grad: bool = True):
+    """conjugate_mll (gpjax/objectives.py:36-107) and its gradient for a batch of
+    independent GPs of different sizes in one library call (float32 compute,
+    instances spread over internal streams).
+
+    kinds: kernel codes (``_lib.RBF`` / ``MATERN32`` / ``MATERN52``); xs: [n_i, d_i]
+    float64 CUDA tensors; ys: [n_i]; thetas: the gpk theta layout
+    ``[lengthscale (n_ls[i]), variance, obs_stddev, constant]``.  Returns
+    (mll [B] float64, list of gradients in the theta layout, info [B] int32).
+    The call is stream-ordered and capturable into a CUDA graph when the
+    workspace is reused (pass the tensors of a previous call's inputs).
+    """
+    import ctypes
+
+    B = len(xs)
+    dev = _lib.require_cuda(*xs)
+    xs = [x.detach().contiguous() for x in xs]
+    ys = [y.detach().reshape(-1).contiguous() for y in ys]
+    thetas = [t.detach().contiguous() for t in thetas]
+    mll = torch.empty(B, dtype=torch.float64, device=dev)
+    grads = [torch.zeros(int(nl) + 3, dtype=torch.float64, device=dev) for nl in n_ls]
+    info = torch.zeros(B, dtype=torch.int32, device=dev)
+    i32, i64, ptr = ctypes.c_int * B, ctypes.c_int64 * B, ctypes.c_void_p * B
+    n = i64(*[x.shape[0] for x in xs])
+    d = i32(*[x.shape[1] for x in xs])
+    lib = _lib.lib()
+    ws = _lib.workspace(lib.gpk_conjugate_mll_batched_workspace_bytes(B, n, d), dev)
+    _lib.call("gpk_conjugate_mll_batched", B, i32(*[int(k) for k in kinds]), n, d,
+              ptr(*[x.data_ptr() for x in xs]), i64(*[x.shape[1] for x in xs]),
+              ptr(*[y.data_ptr() for y in ys]), ptr(*[t.data_ptr() for t in thetas]),
+              i32(*[int(v) for v in n_ls]), float(jitter), int(want_grad),
+              ptr(*[mll.data_ptr() + 8 * i for i in range(B)]),
+              ptr(*[g.data_ptr() for g in grads]), info.data_ptr(), ws.data_ptr(), ws.numel(),
+              _lib.stream_ptr(dev))
+    return mll, grads, info

@@ -187,6 +187,27 @@ gpk_status gpk_collapsed_elbo(int kind, int64_t n, int64_t m, int d,
                               cudaStream_t stream);
 
 /* ---------------------------------------------------------------------------
+ * Batched MLL + gradient over independent GPs of different sizes (no single
+ * reference counterpart: the reference evaluates conjugate_mll
+ * (gpjax/objectives.py:36-107) per model, e.g. under jax.vmap for equal
+ * shapes).  Instance i has kind[i], n[i], d[i] and device pointers x[i]
+ * ([n, d], ldx[i]), y[i], theta[i] (layout as gpk_conjugate_mll, n_ls[i]
+ * lengthscales); out_mll[i] (1 double), out_grad[i] (n_ls[i] + 3 doubles)
+ * and info[i] (device int array [count]) receive the results.  The host
+ * arrays are read during the call only.  Float32 compute (SIMT), instances
+ * spread over internal streams joined back into `stream`; workspace from
+ * gpk_conjugate_mll_batched_workspace_bytes.
+ * ------------------------------------------------------------------------- */
+size_t gpk_conjugate_mll_batched_workspace_bytes(int count, const int64_t* n, const int* d);
+gpk_status gpk_conjugate_mll_batched(int count, const int* kind, const int64_t* n, const int* d,
+                                     const double* const* x, const int64_t* ldx,
+                                     const double* const* y, const double* const* theta,
+                                     const int* n_ls, double jitter, int want_grad,
+                                     double* const* out_mll, double* const* out_grad, int* info,
+                                     void* workspace, size_t workspace_bytes,
+                                     cudaStream_t stream);
+
+/* ---------------------------------------------------------------------------
  * Prediction: ConjugatePosterior.predict (gpjax/gps.py:443-526).
  * mean [t] and var [t] float64 (var = diag of the predictive covariance,
  * GaussianDistribution.variance, distributions.py:79-81); cov [t, t] float64

@@ -104,3 +104,19 @@ def test_product_has_no_cpu_fallback():
     for f in os.listdir(pkg):
         if f.endswith(".py"):
             assert "oracle" not in open(os.path.join(pkg, f)).read().replace("oracle is", ""), f
+
+
+def test_batched_mll_rejects_bad_arguments(built_lib):
+    from gpjax_gb300 import _lib
+    lib = _lib.lib()
+    n = (ctypes.c_int64 * 1)(100)
+    d = (ctypes.c_int * 1)(2)
+    assert lib.gpk_conjugate_mll_batched_workspace_bytes(1, n, d) > 256
+    nul = [None] * 5
+    # (count, kind, n, d, x, ldx, y, theta, n_ls, jitter, want_grad, out_mll, out_grad,
+    #  info, workspace, workspace_bytes, stream)
+    assert lib.gpk_conjugate_mll_batched(-1, None, n, d, *nul, 1e-6, 1, None, None, None, None,
+                                         0, None) == 1
+    # null per-instance arrays are refused before any device work
+    assert lib.gpk_conjugate_mll_batched(1, None, n, d, *nul, 1e-6, 1, None, None, None, None,
+                                         0, None) == 1
