@@ -418,7 +418,7 @@ extern "C" gpk_status gpk_conjugate_mll(int kind, int64_t n, int d, const double
 // from and join back into the caller's stream.
 // ---------------------------------------------------------------------------
 namespace {
-constexpr int kBatchStreams = 8;
+constexpr int kBatchStreams = 64;
 struct BatchCtx {
   cudaStream_t s[kBatchStreams] = {};
   cudaEvent_t fork = nullptr;
