@@ -72,6 +72,14 @@ __device__ __forceinline__ void kval_dcoef(int kind, T sq, T s2, T& k, T& c) {
   c = T(5.0 / 3.0) * (T(1) + r5 * t) * e;
 }
 
+// float32 -> TF32 (10 explicit mantissa bits), round to nearest, ties away
+// from zero; the result is a float32 bit pattern with the low 13 bits clear.
+__device__ __forceinline__ float tf32_round(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
 // warp / block reductions
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {

@@ -14,12 +14,18 @@
 // from the scaled inputs; the reference differentiates the same sequence
 // with JAX reverse mode.
 //
-// The m x n work (Phi, P, c, the fused H Phi adjoint) runs in T (float64 for
-// the plain form, float32 for the mixed form); the m x m algebra always runs
-// in float64.  Reductions go through per-block partials summed in a fixed
-// order.
+// The m x n work has two forms.  Plain (float64): Phi, P, c and the fused
+// H Phi adjoint on CUDA cores.  Mixed: Phi is generated once in float32 and
+// stored as TF32 hi/lo pairs in both layouts (m x n for P, n x m for the
+// adjoint); P = Phi Phi^T per n-chunk and G = H Phi run on the tensor cores
+// (split-TF32 tcgen05 GEMM), with G reduced against dPhi/dtheta, dPhi/dZ in
+// the GEMM epilogue; c = Phi d and Phi 1 are summed in float-float during
+// generation.  The m x m algebra always runs in float64.  Reductions go
+// through per-block partials summed in a fixed order.
 #include <climits>
+#include <type_traits>
 #include "gpk_internal.cuh"
+#include "tc_gemm.cuh"
 
 namespace gpk {
 namespace {
@@ -44,27 +50,61 @@ constexpr int DMAXS = 16;       // input dimension limit of the SGPR path
 
 inline int64_t pad64(int64_t n) { return ((n + 63) / 64) * 64; }
 
+constexpr int PG_I = 64;    // Phi generation: inducing rows per block
+constexpr int PG_X = 128;   // data columns per sub-tile
+constexpr int PG_SUB = 4;   // sub-tiles per block
+constexpr int CS_PARTS = 64;  // first-level partials of the column sums
+
+// Tile parameters of the mixed-form adjoint GEMM (G = H Phi, M = m, N = n, K = m).
+inline tc::TcParams sg_adj_params(int64_t n, int64_t m, int d) {
+  tc::TcParams q{};
+  q.M = (int)m;
+  q.N = (int)n;
+  q.K = (int)m;
+  q.d = d;
+  return q;
+}
+
 template <typename T>
 struct SgprBuf {
+  static constexpr bool kMixed = std::is_same<T, float>::value;
   int64_t ldn, ldm;
-  int nchunks;
-  T *zs, *xs, *Phi, *Pparts, *Ht;
+  int nchunks, nb, nxb, gtiles, gcols;
+  T *zs, *xs, *Phi, *Pparts, *Ht;                 // Phi, Ht: plain form only
+  float *Phh, *Phl, *PTh, *PTl, *Hh, *Hl;         // mixed form only
   double *zs64, *Kf, *Lz, *Mz, *Vz, *Kinv, *Su, *Mu, *Vu, *Suinv, *P64, *T1, *KPK, *GK, *scr;
-  double *dv, *cv, *phi1, *gam, *pgam, *ldK, *ldU, *red, *thK, *dzK, *thP, *dzP;
+  double *dv, *cv, *phi1, *gam, *gams, *pgam, *ldK, *ldU, *red, *thK, *dzK, *thP, *dzP;
+  double *ddpart, *cpart, *colpart, *sth, *gzs, *ddds;
+  int* err;
 };
 
 template <typename T>
 size_t sgpr_layout(int64_t n, int64_t m, int d, void* ws, SgprBuf<T>& b) {
+  constexpr bool mixed = SgprBuf<T>::kMixed;
   Arena a(ws);
   b.ldn = pad64(n);
   b.ldm = pad64(m);
   b.nchunks = (int)((n + KCHUNK - 1) / KCHUNK);
+  b.nb = (int)((n + 255) / 256);
+  b.nxb = (int)((n + PG_X * PG_SUB - 1) / (PG_X * PG_SUB));
+  const tc::TcParams q = sg_adj_params(n, m, d);
+  b.gtiles = mixed ? tc_gemm_tiles(tc::MODE_SGPR, q) : 0;
+  b.gcols = mixed ? tc_gemm_col_tiles(tc::MODE_SGPR, q) : 0;
   const size_t mm = (size_t)m * b.ldm;
   b.zs = a.take<T>((size_t)m * d);
   b.xs = a.take<T>((size_t)n * d);
-  b.Phi = a.take<T>((size_t)m * b.ldn);
+  b.Phi = mixed ? nullptr : a.take<T>((size_t)m * b.ldn);
   b.Pparts = a.take<T>((size_t)b.nchunks * m * m);
-  b.Ht = a.take<T>(mm);
+  b.Ht = mixed ? nullptr : a.take<T>(mm);
+  b.Phh = b.Phl = b.PTh = b.PTl = b.Hh = b.Hl = nullptr;
+  if (mixed) {
+    b.Phh = a.take<float>((size_t)m * b.ldn);
+    b.Phl = a.take<float>((size_t)m * b.ldn);
+    b.PTh = a.take<float>((size_t)n * b.ldm);
+    b.PTl = a.take<float>((size_t)n * b.ldm);
+    b.Hh = a.take<float>(mm);
+    b.Hl = a.take<float>(mm);
+  }
   b.zs64 = a.take<double>((size_t)m * d);
   b.Kf = a.take<double>(mm);
   b.Lz = a.take<double>(mm);
@@ -81,9 +121,10 @@ size_t sgpr_layout(int64_t n, int64_t m, int d, void* ws, SgprBuf<T>& b) {
   b.GK = a.take<double>(mm);
   b.scr = a.take<double>((size_t)m * m / 2 + 64);
   b.dv = a.take<double>(n);
-  b.cv = a.take<double>(m);
-  b.phi1 = a.take<double>(m);
+  b.cv = a.take<double>(2 * m);  // c, then Phi 1
+  b.phi1 = b.cv ? b.cv + m : nullptr;
   b.gam = a.take<double>(m);
+  b.gams = a.take<double>(m);
   b.pgam = a.take<double>(m);
   b.ldK = a.take<double>(m);
   b.ldU = a.take<double>(m);
@@ -91,16 +132,211 @@ size_t sgpr_layout(int64_t n, int64_t m, int d, void* ws, SgprBuf<T>& b) {
   b.thK = a.take<double>((size_t)m * (d + 1));
   b.dzK = a.take<double>((size_t)m * d);
   const int mt = (int)((m + AB - 1) / AB);
-  b.thP = a.take<double>((size_t)ASPLIT * mt * (d + 1));
-  b.dzP = a.take<double>((size_t)ASPLIT * m * d);
+  if (mixed) {
+    b.thP = a.take<double>((size_t)b.gtiles * (d + 1));
+    b.dzP = a.take<double>((size_t)b.gcols * m * d);
+    b.cpart = a.take<double>((size_t)b.nxb * 2 * m);
+  } else {
+    b.thP = a.take<double>((size_t)ASPLIT * mt * (d + 1));
+    b.dzP = a.take<double>((size_t)ASPLIT * m * d);
+    b.cpart = nullptr;
+  }
+  b.ddpart = a.take<double>((size_t)b.nb * 2);
+  int64_t maxcols = 2 * m > (int64_t)m * d ? 2 * m : (int64_t)m * d;
+  if (maxcols < 32) maxcols = 32;
+  b.colpart = a.take<double>((size_t)CS_PARTS * maxcols);
+  b.sth = a.take<double>(GPK_MAX_D + 2);
+  b.gzs = a.take<double>((size_t)m * d);
+  b.ddds = a.take<double>(2);
+  b.err = a.take<int>(1);
   return a.off + 256;
 }
 
-__global__ void sg_init(int* info, const double* __restrict__ y, const double* __restrict__ theta,
-                        int n_ls, int n, double* __restrict__ dv) {
+// Column sums of a row-major double array a[rows][cols] in a fixed order:
+// block (bx, by) sums rows [by * rchunk, (by + 1) * rchunk) of columns
+// [32 bx, 32 bx + 32), eight warps striding over the rows.
+__global__ void __launch_bounds__(256)
+    colsum_part(const double* __restrict__ a, int64_t rows, int64_t cols, int64_t rchunk,
+                double* __restrict__ part) {
+  __shared__ double sh[8][33];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t c = (int64_t)blockIdx.x * 32 + lane;
+  const int64_t r0 = (int64_t)blockIdx.y * rchunk;
+  const int64_t r1 = r0 + rchunk < rows ? r0 + rchunk : rows;
+  double s = 0.0;
+  if (c < cols)
+    for (int64_t r = r0 + w; r < r1; r += 8) s += a[r * cols + c];
+  sh[w][lane] = s;
+  __syncthreads();
+  if (w == 0 && c < cols) {
+    double t = 0.0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) t += sh[q][lane];
+    part[(int64_t)blockIdx.y * cols + c] = t;
+  }
+}
+
+__global__ void colsum_final(const double* __restrict__ part, int nparts, int64_t cols,
+                             double* __restrict__ out, int accumulate) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= cols) return;
+  double t = 0.0;
+  for (int q = 0; q < nparts; ++q) t += part[(int64_t)q * cols + c];
+  out[c] = accumulate ? out[c] + t : t;
+}
+
+// out[c] (+)= sum_r a[r][c]; part holds CS_PARTS * cols doubles
+cudaError_t colsum(const double* a, int64_t rows, int64_t cols, double* out, bool accumulate,
+                   double* part, cudaStream_t s) {
+  if (cols <= 0) return cudaSuccess;
+  int nparts = 0;
+  if (rows > 0) {
+    const int64_t rchunk = (rows + CS_PARTS - 1) / CS_PARTS;
+    nparts = (int)((rows + rchunk - 1) / rchunk);
+    colsum_part<<<dim3((unsigned)cdiv(cols, 32), (unsigned)nparts), 256, 0, s>>>(a, rows, cols,
+                                                                                rchunk, part);
+    cudaError_t e = launch_status();
+    if (e != cudaSuccess) return e;
+  }
+  colsum_final<<<(unsigned)cdiv(cols, 256), 256, 0, s>>>(part, nparts, cols, out,
+                                                         accumulate ? 1 : 0);
+  return launch_status();
+}
+
+// d = y - mean; block partials of d^T d and 1^T d (256 threads per block)
+__global__ void __launch_bounds__(256)
+    sg_init(int* info, int* err, const double* __restrict__ y, const double* __restrict__ theta,
+            int n_ls, int n, double* __restrict__ dv, double* __restrict__ ddpart) {
+  __shared__ double sh[2][8];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i == 0) *info = INT_MAX;
-  if (i < n) dv[i] = y[i] - theta[n_ls + 2];
+  if (i == 0) {
+    *info = INT_MAX;
+    *err = 0;
+  }
+  double v = 0.0;
+  if (i < n) {
+    v = y[i] - theta[n_ls + 2];
+    dv[i] = v;
+  }
+  const double a = warp_sum(v * v), b = warp_sum(v);
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    sh[0][w] = a;
+    sh[1][w] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x < 2) {
+    double t = 0.0;
+    for (int q = 0; q < 8; ++q) t += sh[threadIdx.x][q];
+    ddpart[(int64_t)blockIdx.x * 2 + threadIdx.x] = t;
+  }
+}
+
+// float-float accumulation: (hi, lo) += a, with the rounding error of the
+// addition kept in lo (Knuth's two-sum); explicit _rn operations keep the
+// compiler from contracting the error terms
+__device__ __forceinline__ void ff_acc(float& hi, float& lo, float a) {
+  const float s = __fadd_rn(hi, a);
+  const float bb = __fsub_rn(s, hi);
+  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(a, bb));
+  hi = s;
+  lo = __fadd_rn(lo, err);
+}
+
+// Mixed form: Phi = K(Z, X) (float32) for PG_I inducing rows and PG_SUB
+// sub-tiles of PG_X data columns, stored as TF32 hi/lo pairs row-major
+// (Phh/Phl, m x n, the P operand) and transposed (PTh/PTl, n x m, the adjoint
+// operand); c = Phi d and Phi 1 of the block's columns summed in float-float
+// (d split into float hi + lo) into cpart[block column][c (m) | Phi 1 (m)].
+template <int D>
+__global__ void __launch_bounds__(256)
+    sg_phi_gen(int kind, int m, int n, int d, const float* __restrict__ zs,
+               const float* __restrict__ xs, const double* __restrict__ theta, int n_ls,
+               const double* __restrict__ dv, float* __restrict__ Phh, float* __restrict__ Phl,
+               int64_t ldn, float* __restrict__ PTh, float* __restrict__ PTl, int64_t ldt,
+               double* __restrict__ cpart) {
+  __shared__ __align__(16) float tile[PG_I][PG_X + 1];
+  __shared__ float sz[PG_I][D + 1];
+  __shared__ float sxp[PG_X][D + 1];
+  __shared__ float sdh[PG_X], sdl[PG_X];
+  const int i0 = blockIdx.y * PG_I;
+  const int64_t xb0 = (int64_t)blockIdx.x * PG_X * PG_SUB;
+  const float s2 = (float)theta[n_ls];
+  const int t = threadIdx.x;
+  for (int e = t; e < PG_I * D; e += 256) {
+    const int r = e / D, k = e % D;
+    sz[r][k] = (i0 + r < m && k < d) ? zs[(int64_t)(i0 + r) * d + k] : 0.f;
+  }
+  const int bi = t & (PG_I - 1), bg = t >> 6;  // transposed pass: row bi, columns bg + 4 q
+  float ch = 0.f, cl = 0.f, ph = 0.f, pl = 0.f;
+  for (int sub = 0; sub < PG_SUB; ++sub) {
+    const int64_t x0 = xb0 + (int64_t)sub * PG_X;
+    if (x0 >= n) break;
+    __syncthreads();  // the previous sub-tile is consumed
+    for (int e = t; e < PG_X * D; e += 256) {
+      const int c = e / D, k = e % D;
+      sxp[c][k] = (x0 + c < n && k < d) ? xs[(x0 + c) * d + k] : 0.f;
+    }
+    for (int c = t; c < PG_X; c += 256) {
+      const double v = x0 + c < n ? dv[x0 + c] : 0.0;
+      const float h = (float)v;
+      sdh[c] = h;
+      sdl[c] = (float)(v - (double)h);
+    }
+    __syncthreads();
+    {  // row-major pass: column a, rows (t >> 7) + 2 r
+      const int a = t & (PG_X - 1);
+      const int64_t gx = x0 + a;
+      float xr[D];
+#pragma unroll
+      for (int k = 0; k < D; ++k) xr[k] = sxp[a][k];
+      for (int r = t >> 7; r < PG_I; r += 2) {
+        float sq = 0.f;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+          const float df = sz[r][k] - xr[k];
+          sq = fmaf(df, df, sq);
+        }
+        const float v = kval<float>(kind, sq, s2);
+        tile[r][a] = v;
+        if (gx < n && i0 + r < m) {
+          const float h = tf32_round(v);
+          Phh[(int64_t)(i0 + r) * ldn + gx] = h;
+          Phl[(int64_t)(i0 + r) * ldn + gx] = tf32_round(v - h);
+        }
+      }
+    }
+    __syncthreads();
+    if (i0 + bi < m) {  // transposed pass and the c / Phi 1 sums
+      for (int c = bg; c < PG_X; c += 4) {
+        const int64_t gx = x0 + c;
+        if (gx >= n) break;
+        const float v = tile[bi][c];
+        const float h = tf32_round(v);
+        PTh[gx * ldt + i0 + bi] = h;
+        PTl[gx * ldt + i0 + bi] = tf32_round(v - h);
+        const float p = __fmul_rn(v, sdh[c]);
+        const float e = fmaf(v, sdh[c], -p);  // exact product error
+        ff_acc(ch, cl, p);
+        cl = __fadd_rn(cl, fmaf(v, sdl[c], e));
+        ff_acc(ph, pl, v);
+      }
+    }
+  }
+  __syncthreads();
+  double* red = reinterpret_cast<double*>(&tile[0][0]);  // [4][PG_I][2]
+  red[(bg * PG_I + bi) * 2 + 0] = (double)ch + (double)cl;
+  red[(bg * PG_I + bi) * 2 + 1] = (double)ph + (double)pl;
+  __syncthreads();
+  if (t < PG_I && i0 + t < m) {
+    double c = 0.0, p = 0.0;
+    for (int g = 0; g < 4; ++g) {
+      c += red[(g * PG_I + t) * 2 + 0];
+      p += red[(g * PG_I + t) * 2 + 1];
+    }
+    cpart[(int64_t)blockIdx.x * 2 * m + i0 + t] = c;
+    cpart[(int64_t)blockIdx.x * 2 * m + m + i0 + t] = p;
+  }
 }
 
 // c = Phi d and phi1 = Phi 1 (float64 accumulation), one warp per row of Phi
@@ -144,21 +380,34 @@ __global__ void sg_reduce_P(const T* __restrict__ parts, int nchunks, int m, int
   Su[(int64_t)i * ldm + j] = Kf[(int64_t)i * ldm + j] + (i == j ? jitter : 0.0) + s / (sd * sd);
 }
 
-// H (in T), GK (float64) and the traces tr(K^-1 P), tr(Su^-1 P) (block partials)
+// H (in T for the plain form; TF32 hi/lo Hh, Hl for the mixed form), GK
+// (float64), gams = gamma / s^2 and the traces tr(K^-1 P), tr(Su^-1 P)
+// (block partials)
 template <typename T>
 __global__ void sg_combine(int m, int64_t ldm, const double* __restrict__ Kinv,
                            const double* __restrict__ Suinv, const double* __restrict__ KPK,
                            const double* __restrict__ P64, const double* __restrict__ gam,
                            const double* __restrict__ theta, int n_ls, T* __restrict__ Ht,
-                           double* __restrict__ GK, double* __restrict__ red) {
+                           float* __restrict__ Hh, float* __restrict__ Hl,
+                           double* __restrict__ gams, double* __restrict__ GK,
+                           double* __restrict__ red) {
   const double sd = theta[n_ls + 1], s = sd * sd;
   double tK = 0.0, tU = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
+    gams[i] = gam[i] / (s * s);
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < (int64_t)m * m;
        e += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(e / m), j = (int)(e % m);
     const int64_t o = (int64_t)i * ldm + j;
     const double ki = Kinv[o], ui = Suinv[o], gg = gam[i] * gam[j], p = P64[o];
-    Ht[o] = (T)((ki - ui) / s - gg / (s * s * s));
+    const double h = (ki - ui) / s - gg / (s * s * s);
+    if (Hh) {
+      const float hv = tf32_round((float)h);
+      Hh[o] = hv;
+      Hl[o] = tf32_round((float)(h - (double)hv));
+    } else {
+      Ht[o] = (T)h;
+    }
     GK[o] = 0.5 * (ki - ui - gg / (s * s) - KPK[o] / s);
     tK += ki * p;
     tU += ui * p;
@@ -377,23 +626,24 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// value, theta gradient and the Z gradient from all partials
+// value, theta gradient and the Z gradient from the reduced sums:
+// sth[0..d] theta sums (Kzz and Phi parts), gzs[m][d] the Phi part of the Z
+// sums, ddds = (d^T d, 1^T d)
 __global__ void __launch_bounds__(256)
     sg_finalize(int n, int m, int d, const double* __restrict__ theta, int n_ls,
                 const double* __restrict__ ldK, const double* __restrict__ ldU,
-                const double* __restrict__ dv, const double* __restrict__ cv,
-                const double* __restrict__ gam, const double* __restrict__ pgam,
-                const double* __restrict__ phi1, const double* __restrict__ red,
-                const double* __restrict__ thK, const double* __restrict__ dzK,
-                const double* __restrict__ thP, const double* __restrict__ dzP, int mt,
-                int want_grad, int* __restrict__ info, double* __restrict__ out_elbo,
+                const double* __restrict__ cv, const double* __restrict__ gam,
+                const double* __restrict__ pgam, const double* __restrict__ phi1,
+                const double* __restrict__ red, const double* __restrict__ sth,
+                const double* __restrict__ ddds, const double* __restrict__ dzK,
+                const double* __restrict__ gzs, const int* __restrict__ err, int want_grad,
+                int* __restrict__ info, double* __restrict__ out_elbo,
                 double* __restrict__ out_grad, double* __restrict__ out_gz) {
   __shared__ double sh[8];
-  __shared__ double sth[GPK_MAX_D + 2];
-  __shared__ double part[7][256];
+  __shared__ double part[5][256];
   const int tid = threadIdx.x;
   {
-    double a = 0.0, b = 0.0, cg = 0.0, gpg = 0.0, pg1 = 0.0, dd = 0.0, ds = 0.0;
+    double a = 0.0, b = 0.0, cg = 0.0, gpg = 0.0, pg1 = 0.0;
     for (int i = tid; i < m; i += blockDim.x) {
       a += ldK[i];
       b += ldU[i];
@@ -401,51 +651,35 @@ __global__ void __launch_bounds__(256)
       gpg += gam[i] * pgam[i];
       pg1 += phi1[i] * gam[i];
     }
-    for (int j = tid; j < n; j += blockDim.x) {
-      dd += dv[j] * dv[j];
-      ds += dv[j];
-    }
     part[0][tid] = a;
     part[1][tid] = b;
     part[2][tid] = cg;
     part[3][tid] = gpg;
     part[4][tid] = pg1;
-    part[5][tid] = dd;
-    part[6][tid] = ds;
   }
   __syncthreads();
-  if (tid < 7) {
+  if (tid < 5) {
     double t = 0.0;
     for (int q = 0; q < (int)blockDim.x; ++q) t += part[tid][q];
     sh[tid] = (tid < 2) ? 2.0 * t : t;  // log|K|, log|Su| from log-diagonals
   }
   __syncthreads();
-  if (want_grad) {
-    for (int k = tid; k <= d; k += blockDim.x) {
-      double t = 0.0;
-      for (int i = 0; i < m; ++i) t += thK[(int64_t)i * (d + 1) + k];
-      for (int q = 0; q < ASPLIT * mt; ++q) t += thP[(int64_t)q * (d + 1) + k];
-      sth[k] = t;
-    }
-  }
-  __syncthreads();
   int inf = *info;
   if (inf == INT_MAX) inf = 0;
+  if (inf == 0 && *err) inf = -1;  // a tensor-core wait timed out
   const double nan = __longlong_as_double(0x7ff8000000000000ULL);
   const double s2 = theta[n_ls], sd = theta[n_ls + 1], s = sd * sd;
   if (want_grad) {
     for (int e = tid; e < m * d; e += blockDim.x) {
-      const int i = e / d, k = e % d;
-      double t = dzK[e];
-      for (int q = 0; q < ASPLIT; ++q) t += dzP[((int64_t)q * m + i) * d + k];
+      const int k = e % d;
       const double l = theta[n_ls == 1 ? 0 : k];
-      out_gz[e] = inf ? nan : -s2 * t / l;
+      out_gz[e] = inf ? nan : -s2 * (dzK[e] + gzs[e]) / l;
     }
   }
   if (tid != 0) return;
   *info = inf;
-  const double ldK_ = sh[0], ldU_ = sh[1], cg = sh[2], gpg = sh[3], pg1 = sh[4], dd = sh[5],
-               ds = sh[6];
+  const double ldK_ = sh[0], ldU_ = sh[1], cg = sh[2], gpg = sh[3], pg1 = sh[4], dd = ddds[0],
+               ds = ddds[1];
   const double trKP = red[0], trUP = red[1];
   const double two_log_prob =
       -(double)n * log(2.0 * 3.141592653589793 * s) - (ldU_ - ldK_) - (dd / s - cg / (s * s));
@@ -476,24 +710,55 @@ gpk_status sgpr_run(int kind, int n, int m, int d, const double* x, int64_t ldx,
                     const double* z, int64_t ldz, const double* theta, int n_ls, double jitter,
                     int want_grad, double* out_elbo, double* out_grad, double* out_gz, int* info,
                     void* ws, cudaStream_t s) {
+  constexpr bool mixed = SgprBuf<T>::kMixed;
   SgprBuf<T> b;
   sgpr_layout<T>(n, m, d, ws, b);
   const int64_t ldm = b.ldm;
-  sg_init<<<(int)cdiv(n, 256), 256, 0, s>>>(info, y, theta, n_ls, n, b.dv);
+  sg_init<<<b.nb, 256, 0, s>>>(info, b.err, y, theta, n_ls, n, b.dv, b.ddpart);
   GPK_LAUNCH_CHECK();
   sg_zero<<<1, 64, 0, s>>>(b.red, 64);
   GPK_LAUNCH_CHECK();
   GPK_CUDA_TRY(scale_inputs<T>(x, ldx, n, d, theta, n_ls, b.xs, s));
   GPK_CUDA_TRY(scale_inputs<T>(z, ldz, m, d, theta, n_ls, b.zs, s));
   GPK_CUDA_TRY(scale_inputs<double>(z, ldz, m, d, theta, n_ls, b.zs64, s));
-  // Phi = K(z, x) (m x n, T), c = Phi d, phi1 = Phi 1
-  GPK_CUDA_TRY(cross_cov_scaled<T, T>(kind, m, n, d, b.zs, b.xs, theta, n_ls, 0, 0.0, b.Phi, b.ldn,
-                                      s));
-  sg_phi_gemv<T><<<(int)cdiv((int64_t)m * 32, 256), 256, 0, s>>>(b.Phi, b.ldn, m, n, b.dv, b.cv,
-                                                                   b.phi1);
-  GPK_LAUNCH_CHECK();
-  // P: lower triangles of Phi_k Phi_k^T per n-chunk, summed in float64
-  {
+  TcMap mphi, mh, mpt;
+  if constexpr (mixed) {
+    // Phi (both layouts, TF32 hi/lo), c = Phi d and Phi 1
+    const dim3 grid((unsigned)b.nxb, (unsigned)cdiv(m, PG_I));
+    if (d <= 8)
+      sg_phi_gen<8><<<grid, 256, 0, s>>>(kind, m, n, d, b.zs, b.xs, theta, n_ls, b.dv, b.Phh,
+                                         b.Phl, b.ldn, b.PTh, b.PTl, ldm, b.cpart);
+    else
+      sg_phi_gen<DMAXS><<<grid, 256, 0, s>>>(kind, m, n, d, b.zs, b.xs, theta, n_ls, b.dv, b.Phh,
+                                             b.Phl, b.ldn, b.PTh, b.PTl, ldm, b.cpart);
+    GPK_LAUNCH_CHECK();
+    GPK_CUDA_TRY(colsum(b.cpart, b.nxb, 2 * (int64_t)m, b.cv, false, b.colpart, s));
+    // P: lower triangles of Phi_k Phi_k^T per n-chunk (tensor cores, one
+    // batched launch; columns past n read as zeros), summed in float64
+    if (!tc_make_map(&mphi, b.Phh, b.Phl, m, n, b.ldn) ||
+        !tc_make_map(&mh, b.Hh, b.Hl, m, m, ldm) || !tc_make_map(&mpt, b.PTh, b.PTl, n, m, ldm))
+      return GPK_ERR_CUDA;
+    GPK_CUDA_TRY(cudaMemsetAsync(b.Pparts, 0, sizeof(float) * (size_t)b.nchunks * m * m, s));
+    tc::TcParams p{};
+    p.M = p.N = m;
+    p.K = KCHUNK;
+    p.a_zcol = p.b_zcol = KCHUNK;
+    p.c_lower = 1;
+    p.force_shape = m >= 256 ? 2 : 0;  // wide tiles: the batch supplies the parallelism
+    p.c0 = b.Pparts;
+    p.ldc = m;
+    p.c_zrow = m;
+    p.alpha = 1.f;
+    p.err = b.err;
+    GPK_CUDA_TRY(tc_gemm_run(tc::MODE_ADD_F32, mphi, mphi, p, b.nchunks, s));
+  } else {
+    // Phi = K(z, x) (m x n), c = Phi d, phi1 = Phi 1
+    GPK_CUDA_TRY(cross_cov_scaled<T, T>(kind, m, n, d, b.zs, b.xs, theta, n_ls, 0, 0.0, b.Phi,
+                                        b.ldn, s));
+    sg_phi_gemv<T><<<(int)cdiv((int64_t)m * 32, 256), 256, 0, s>>>(b.Phi, b.ldn, m, n, b.dv,
+                                                                     b.cv, b.phi1);
+    GPK_LAUNCH_CHECK();
+    // P: lower triangles of Phi_k Phi_k^T per n-chunk, summed in float64
     const int full = n / KCHUNK;
     GemmProb<T> p{};
     p.A = b.Phi;
@@ -565,23 +830,45 @@ gpk_status sgpr_run(int kind, int n, int m, int d, const double* x, int64_t ldx,
   GPK_CUDA_TRY(gemv_dense<double>(b.Suinv, ldm, m, m, b.cv, b.gam, s));
   GPK_CUDA_TRY(gemv_dense<double>(b.P64, ldm, m, m, b.gam, b.pgam, s));
   sg_combine<T><<<256, 256, 0, s>>>(m, ldm, b.Kinv, b.Suinv, b.KPK, b.P64, b.gam, theta, n_ls,
-                                    b.Ht, b.GK, b.red);
+                                    b.Ht, b.Hh, b.Hl, b.gams, b.GK, b.red);
   GPK_LAUNCH_CHECK();
-  const int mt = (m + AB - 1) / AB;
   if (want_grad) {
     sg_grad_kzz<<<m, 256, 0, s>>>(kind, m, d, ldm, b.zs64, b.GK, b.thK, b.dzK);
     GPK_LAUNCH_CHECK();
-    dim3 grid(mt, ASPLIT);
-    const size_t smem = (size_t)(2 * 16 + AB) * (AB + 1) * sizeof(T) +
-                        (size_t)2 * AB * (DMAXS + 1) * sizeof(T) + 16 +
-                        (size_t)(AB + 8) * (DMAXS + 1) * sizeof(double);
-    cudaFuncSetAttribute(sg_phi_adjoint<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    sg_phi_adjoint<T><<<grid, 256, smem, s>>>(kind, m, n, d, b.Ht, ldm, b.Phi, b.ldn, b.zs, b.xs,
-                                           b.gam, b.dv, theta, n_ls, b.thP, b.dzP);
-    GPK_LAUNCH_CHECK();
+    if constexpr (mixed) {
+      // G = H Phi + gamma d^T / s^2 on the tensor cores, reduced in the epilogue
+      tc::TcParams p = sg_adj_params(n, m, d);
+      p.n_true = n;
+      p.kind = kind;
+      p.xs = b.xs;
+      p.zs = b.zs;
+      p.avec = b.gams;
+      p.bvec = b.dv;
+      p.gpart = b.thP;
+      p.zpart = b.dzP;
+      p.err = b.err;
+      GPK_CUDA_TRY(tc_gemm_run(tc::MODE_SGPR, mh, mpt, p, 1, s));
+      GPK_CUDA_TRY(colsum(b.thP, b.gtiles, d + 1, b.sth, false, b.colpart, s));
+      GPK_CUDA_TRY(colsum(b.dzP, b.gcols, (int64_t)m * d, b.gzs, false, b.colpart, s));
+    } else {
+      const int mt = (m + AB - 1) / AB;
+      dim3 grid(mt, ASPLIT);
+      const size_t smem = (size_t)(2 * 16 + AB) * (AB + 1) * sizeof(T) +
+                          (size_t)2 * AB * (DMAXS + 1) * sizeof(T) + 16 +
+                          (size_t)(AB + 8) * (DMAXS + 1) * sizeof(double);
+      cudaFuncSetAttribute(sg_phi_adjoint<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem);
+      sg_phi_adjoint<T><<<grid, 256, smem, s>>>(kind, m, n, d, b.Ht, ldm, b.Phi, b.ldn, b.zs,
+                                                b.xs, b.gam, b.dv, theta, n_ls, b.thP, b.dzP);
+      GPK_LAUNCH_CHECK();
+      GPK_CUDA_TRY(colsum(b.thP, (int64_t)ASPLIT * mt, d + 1, b.sth, false, b.colpart, s));
+      GPK_CUDA_TRY(colsum(b.dzP, ASPLIT, (int64_t)m * d, b.gzs, false, b.colpart, s));
+    }
+    GPK_CUDA_TRY(colsum(b.thK, m, d + 1, b.sth, true, b.colpart, s));
   }
-  sg_finalize<<<1, 256, 0, s>>>(n, m, d, theta, n_ls, b.ldK, b.ldU, b.dv, b.cv, b.gam, b.pgam,
-                                b.phi1, b.red, b.thK, b.dzK, b.thP, b.dzP, mt, want_grad, info,
+  GPK_CUDA_TRY(colsum(b.ddpart, b.nb, 2, b.ddds, false, b.colpart, s));
+  sg_finalize<<<1, 256, 0, s>>>(n, m, d, theta, n_ls, b.ldK, b.ldU, b.cv, b.gam, b.pgam, b.phi1,
+                                b.red, b.sth, b.ddds, b.dzK, b.gzs, b.err, want_grad, info,
                                 out_elbo, out_grad, out_gz);
   GPK_LAUNCH_CHECK();
   return GPK_OK;

@@ -393,7 +393,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     const int r = q * 32 + lane;
     const int gi = i0 + r;  // row within the problem
     const int et = threadIdx.x - 64;
-    if (MODE == MODE_GRAD) {
+    if (MODE == MODE_GRAD || MODE == MODE_SGPR) {
+      // column points and column coefficients of this tile
+      const double* cvec = MODE == MODE_GRAD ? p.avec : p.bvec;
       for (int e = et; e < BN * DM; e += EPI_THREADS) {
         const int c = e / DM, k = e % DM;
         const int gj = j0 + c;
@@ -401,7 +403,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       }
       for (int c = et; c < BN; c += EPI_THREADS) {
         const int gj = j0 + c;
-        ga[c] = (p.avec && gj < p.n_true) ? (float)p.avec[gj] : 0.f;
+        ga[c] = (cvec && gj < p.n_true) ? (float)cvec[gj] : 0.f;
       }
     }
     // drain the accumulator segments into float32 registers (round to nearest)
@@ -651,6 +653,94 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         p.gpart[(int64_t)tile_id * slots + sidx] = tot;
       }
     }
+    if (MODE == MODE_SGPR) {
+      // G = acc + avec_i bvec_j (rows: inducing points z_i, columns: data
+      // points x_j), contracted against the unit-variance kernel and its
+      // derivatives: per tile  sum_ij G k1, sum_ij G c1 (z_ik - x_jk)^2  and
+      // per row  sum_j G c1 (z_ik - x_jk)
+      constexpr int GLD = BN + 1;
+      static_assert(BM * GLD * 4 + BM * DM * 8 <= STAGES * STAGE_BYTES, "staging exceeds the ring");
+      double* zrow = reinterpret_cast<double*>(otile + BM * GLD);  // [BM][DM], second half-row
+      asm volatile("bar.sync 1, %0;" ::"r"(EPI_THREADS) : "memory");  // gx / ga staged, ring free
+#pragma unroll
+      for (int c = 0; c < HC; ++c) otile[r * GLD + hcol + c] = have ? acc[c] : 0.f;
+      const bool row_ok = have && gi < p.M;
+      float zi[DM];
+#pragma unroll
+      for (int k = 0; k < DM; ++k) zi[k] = (row_ok && k < p.d) ? p.zs[(int64_t)gi * p.d + k] : 0.f;
+      const float ai = row_ok ? (float)p.avec[gi] : 0.f;
+      double gl[DM], gz[DM];
+#pragma unroll
+      for (int k = 0; k < DM; ++k) gl[k] = gz[k] = 0.0;
+      double gvar = 0.0;
+#pragma unroll 1
+      for (int cb = 0; cb < HC / 32; ++cb) {
+        float pl[DM], pz[DM];
+#pragma unroll
+        for (int k = 0; k < DM; ++k) pl[k] = pz[k] = 0.f;
+        float pvar = 0.f;
+#pragma unroll 4
+        for (int k = 0; k < 32; ++k) {
+          const int c = hcol + cb * 32 + k;
+          if (!row_ok || j0 + c >= p.n_true) continue;
+          const float g = fmaf(ai, ga[c], otile[r * GLD + c]);
+          float sq = 0.f;
+#pragma unroll
+          for (int kk = 0; kk < DM; ++kk) {
+            const float df = zi[kk] - gx[c * DM + kk];
+            sq = fmaf(df, df, sq);
+          }
+          float k1, c1;
+          kval_dcoef<float>(p.kind, sq, 1.f, k1, c1);
+          pvar = fmaf(g, k1, pvar);
+          const float gc = g * c1;
+#pragma unroll
+          for (int kk = 0; kk < DM; ++kk) {
+            const float df = zi[kk] - gx[c * DM + kk];
+            const float t = gc * df;
+            pz[kk] += t;
+            pl[kk] = fmaf(t, df, pl[kk]);
+          }
+        }
+#pragma unroll
+        for (int kk = 0; kk < DM; ++kk) {
+          gl[kk] += (double)pl[kk];
+          gz[kk] += (double)pz[kk];
+        }
+        gvar += (double)pvar;
+      }
+      // per-row z partials: the two threads of a row combine in a fixed order
+      if (hcol != 0) {
+#pragma unroll
+        for (int kk = 0; kk < DM; ++kk) zrow[r * DM + kk] = gz[kk];
+      }
+      // theta partials: reduce over the epilogue warps into gpart[tile]
+      const int slots = p.d + 1;
+      for (int sidx = 0; sidx < slots; ++sidx) {
+        double val = gvar;
+        if (sidx < p.d) {
+          val = 0.0;
+#pragma unroll
+          for (int kk = 0; kk < DM; ++kk)
+            if (kk == sidx) val = gl[kk];
+        }
+        val = warp_sum(val);
+        if (lane == 0) gred[sidx * EPI_WARPS + ew] = val;
+      }
+      asm volatile("bar.sync 1, %0;" ::"r"(EPI_THREADS) : "memory");
+      if (hcol == 0 && gi < p.M) {
+        double* zp = p.zpart + ((int64_t)z * p.tiles_n + J) * (int64_t)p.M * p.d + (int64_t)gi * p.d;
+#pragma unroll
+        for (int kk = 0; kk < DM; ++kk)
+          if (kk < p.d) zp[kk] = row_ok ? gz[kk] + zrow[r * DM + kk] : 0.0;
+      }
+      const int tile_id = blockIdx.x + (int)gridDim.x * z;
+      for (int sidx = et; sidx < slots; sidx += EPI_THREADS) {
+        double tot = 0.0;
+        for (int w8 = 0; w8 < EPI_WARPS; ++w8) tot += gred[sidx * EPI_WARPS + w8];
+        p.gpart[(int64_t)tile_id * slots + sidx] = tot;
+      }
+    }
   }
   tc_fence_before();
   __syncthreads();
@@ -746,10 +836,18 @@ bool tc_make_map(TcMap* m, const float* hi, const float* lo, int64_t rows, int64
 // adjoint epilogue keeps 128 accumulator columns per thread only with DM =
 // 8), half where narrow tiles would leave most SMs idle, narrow otherwise.
 static int tile_shape(int mode, const tc::TcParams& p) {
+  if (p.force_shape > 0) return p.force_shape - 1;
+  if (mode == tc::MODE_SGPR) return (p.N >= 2048 && p.d <= 8) ? 1 : 0;
   if (p.M >= 2048 && p.N >= 2048 && (mode != tc::MODE_GRAD || p.d <= 8)) return 1;
   const int tm = (p.M + tc::BM - 1) / tc::BM, tn = (p.N + 127) / 128;
   if (mode != tc::MODE_GRAD && tc::tile_count(p.c_lower, tm, tn, 128) <= 76) return 2;
   return 0;
+}
+
+int tc_gemm_col_tiles(int mode, const tc::TcParams& p) {
+  const int ts = tile_shape(mode, p);
+  const int bn = ts == 1 ? tc::Tile<1>::BN : (ts == 2 ? tc::Tile<2>::BN : tc::Tile<0>::BN);
+  return (p.N + bn - 1) / bn;
 }
 
 int tc_gemm_tiles(int mode, const tc::TcParams& p) {
@@ -813,6 +911,14 @@ cudaError_t tc_gemm_run(int mode, const TcMap& A, const TcMap& B, const tc::TcPa
         launch_one<tc::MODE_GRAD, 1, 8>(A, B, p, batch, s, pdl);
       else
         launch_one<tc::MODE_GRAD, 0, tc::GRAD_DMAX>(A, B, p, batch, s, pdl);
+      break;
+    case tc::MODE_SGPR:
+      if (ts == 1)
+        launch_one<tc::MODE_SGPR, 1, 8>(A, B, p, batch, s, pdl);
+      else if (p.d <= 8)
+        launch_one<tc::MODE_SGPR, 0, 8>(A, B, p, batch, s, pdl);
+      else
+        launch_one<tc::MODE_SGPR, 0, tc::GRAD_DMAX>(A, B, p, batch, s, pdl);
       break;
     default:
       return cudaErrorInvalidValue;

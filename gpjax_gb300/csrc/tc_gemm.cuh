@@ -23,7 +23,7 @@ constexpr int BM = 128;                        // output tile rows (TMEM lanes)
 constexpr int NUM_THREADS = 320;               // w0 TMA, w1 MMA + TMEM, w2..w9 epilogue
 constexpr int GRAD_DMAX = 16;                  // largest input dimension of the adjoint epilogue
 
-enum Mode { MODE_ADD_F32 = 0, MODE_STORE_SPLIT = 1, MODE_GRAD = 2 };
+enum Mode { MODE_ADD_F32 = 0, MODE_STORE_SPLIT = 1, MODE_GRAD = 2, MODE_SGPR = 3 };
 
 struct TcParams {
   int M, N, K;
@@ -31,6 +31,7 @@ struct TcParams {
   int a_zrow, a_zcol, b_zrow, b_zcol;   // per-batch (blockIdx.z) origin increments
   int a_tri, b_tri, c_lower;
   int tiles_m, tiles_n;
+  int force_shape;  // 0: chosen per problem; 1 + Tile shape index to force one
   // outputs (MODE_ADD_F32: c0 += alpha*acc; MODE_STORE_SPLIT: hi/lo of alpha*acc
   // into c0/c1 at (i, j) and t0/t1 at (j, i))
   float *c0, *c1, *t0, *t1;
@@ -40,11 +41,17 @@ struct TcParams {
   int64_t t_row0, t_col0, t_zrow, t_zcol;
   float alpha;
   double* dtrack;  // optional: dtrack[c_row0 + i] -= sum_j (alpha*acc)^2
-  // adjoint epilogue
+  // adjoint epilogues.  MODE_GRAD (exact GP, square symmetric): rows and
+  // columns both index xs, avec = alpha.  MODE_SGPR (rows = inducing points
+  // zs, columns = data points xs): G = acc + avec_i * bvec_j, reduced against
+  // dK/dtheta into gpart[tile] and against dK/dz into zpart[column tile][row].
   int n_true, d, kind;
   const float* xs;
+  const float* zs;
   const double* avec;
+  const double* bvec;
   double* gpart;
+  double* zpart;
   int* err;
 };
 
@@ -78,6 +85,8 @@ cudaError_t tc_gemm_run(int mode, const TcMap& A, const TcMap& B, const tc::TcPa
 // Grid size (output tiles) tc_gemm_run launches for this mode and problem; the
 // MODE_GRAD epilogue writes one gpart row per tile.
 int tc_gemm_tiles(int mode, const tc::TcParams& p);
+// Column tiles of that grid (MODE_SGPR writes zpart[column tile][row]).
+int tc_gemm_col_tiles(int mode, const tc::TcParams& p);
 
 // hi/lo TF32 split of a float32 matrix (rows x cols, ld) into hi/lo (ldo).
 cudaError_t tf32_split(const float* src, int64_t lds, int rows, int cols, float* hi, float* lo,

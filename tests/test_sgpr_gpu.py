@@ -101,6 +101,38 @@ def test_collapsed_elbo_mixed(cuda_lib):
     assert np.linalg.norm(gm - g64) <= 1e-2 * np.linalg.norm(g64)
 
 
+@pytest.mark.parametrize("kind,n,m,d,vtol,ztol", [
+    (0, 20000, 128, 8, 1e-5, 2e-3),   # wide adjoint tiles (n >= 2048, d <= 8)
+    (2, 1500, 70, 3, 1e-5, 2e-3),     # narrow adjoint tiles, ragged m
+    (1, 5000, 300, 12, 1e-5, 2e-3),   # narrow tiles with the 16-wide input bound
+    # wide tiles for P (two n-chunks, the last ragged); 1024 inducing points in
+    # 8 tight clusters: the Z gradient is a difference of its Phi and Kzz parts
+    # (norms ~5e3 and ~4.5e3 against ~1.8e3) and moves by ~1e-2 for a random
+    # 1e-7 relative error in P, which float32 accumulation of P already makes
+    # (CPU emulation with float32 chunks of P: 9.5e-3)
+    (0, 9000, 1024, 8, 2e-5, 5e-2),
+])
+def test_collapsed_elbo_mixed_tensor_core(cuda_lib, kind, n, m, d, vtol, ztol):
+    """Mixed form (Phi in TF32 hi/lo, P and the Phi adjoint on the tensor cores,
+    float64 m x m algebra) against the float64 form on the same inputs."""
+    rng = np.random.default_rng(n + m + d)
+    means = rng.uniform(-3, 3, size=(8, d))
+    x = means[rng.integers(0, 8, n)] + 0.5 * rng.standard_normal((n, d))
+    y = np.sin(x).sum(1, keepdims=True) + 0.1 * rng.standard_normal((n, 1))
+    Z = x[rng.choice(n, m, replace=False)]
+    ls = np.exp(rng.uniform(np.log(0.7), np.log(2.0), d))
+    v64, g64, z64 = _run(kind, x, y, Z, ls, 1.1, 0.2, 0.05, "fp64")
+    vm, gm, zm = _run(kind, x, y, Z, ls, 1.1, 0.2, 0.05, "mixed")
+    ev = abs(vm - v64) / abs(v64)
+    eg = np.linalg.norm(gm - g64) / np.linalg.norm(g64)
+    ez = np.linalg.norm(zm - z64) / np.linalg.norm(z64)
+    print(f"SGPR mixed kind={kind} n={n} m={m} d={d}: value {ev:.2e}, theta grad {eg:.2e}, "
+          f"Z grad {ez:.2e}")
+    assert ev <= vtol
+    assert eg <= 1e-3
+    assert ez <= ztol
+
+
 @pytest.mark.parametrize("kind", [0, 1, 2])
 @pytest.mark.parametrize("ard", [True, False])
 def test_cross_covariance_vjp(cuda_lib, kind, ard):
