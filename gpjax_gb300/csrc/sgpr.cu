@@ -86,7 +86,10 @@ size_t sgpr_layout(int64_t n, int64_t m, int d, void* ws, SgprBuf<T>& b) {
   b.ldm = pad64(m);
   b.nchunks = (int)((n + KCHUNK - 1) / KCHUNK);
   b.nb = (int)((n + 255) / 256);
-  b.nxb = (int)((n + PG_X * PG_SUB - 1) / (PG_X * PG_SUB));
+  // Phi generation blocks: the chunk-blocked P operand is written (zeros past
+  // n) up to nchunks * KCHUNK columns
+  b.nxb = mixed ? b.nchunks * (KCHUNK / (PG_X * PG_SUB))
+                : (int)((n + PG_X * PG_SUB - 1) / (PG_X * PG_SUB));
   const tc::TcParams q = sg_adj_params(n, m, d);
   b.gtiles = mixed ? tc_gemm_tiles(tc::MODE_SGPR, q) : 0;
   b.gcols = mixed ? tc_gemm_col_tiles(tc::MODE_SGPR, q) : 0;
@@ -98,8 +101,10 @@ size_t sgpr_layout(int64_t n, int64_t m, int d, void* ws, SgprBuf<T>& b) {
   b.Ht = mixed ? nullptr : a.take<T>(mm);
   b.Phh = b.Phl = b.PTh = b.PTl = b.Hh = b.Hl = nullptr;
   if (mixed) {
-    b.Phh = a.take<float>((size_t)m * b.ldn);
-    b.Phl = a.take<float>((size_t)m * b.ldn);
+    // chunk-blocked: Phh[c][i][k] = hi(Phi[i][c * KCHUNK + k]), so that one
+    // chunk of the P product reads one contiguous m x KCHUNK block
+    b.Phh = a.take<float>((size_t)b.nchunks * m * KCHUNK);
+    b.Phl = a.take<float>((size_t)b.nchunks * m * KCHUNK);
     b.PTh = a.take<float>((size_t)n * b.ldm);
     b.PTl = a.take<float>((size_t)n * b.ldm);
     b.Hh = a.take<float>(mm);
@@ -244,17 +249,20 @@ __device__ __forceinline__ void ff_acc(float& hi, float& lo, float a) {
 }
 
 // Mixed form: Phi = K(Z, X) (float32) for PG_I inducing rows and PG_SUB
-// sub-tiles of PG_X data columns, stored as TF32 hi/lo pairs row-major
-// (Phh/Phl, m x n, the P operand) and transposed (PTh/PTl, n x m, the adjoint
-// operand); c = Phi d and Phi 1 of the block's columns summed in float-float
-// (d split into float hi + lo) into cpart[block column][c (m) | Phi 1 (m)].
+// sub-tiles of PG_X data columns, stored as TF32 hi/lo pairs chunk-blocked
+// (Phh/Phl [c][i][k] for column c * KCHUNK + k, zeros past n: the P operand)
+// and transposed (PTh/PTl, n x m, the adjoint operand); c = Phi d and Phi 1 of
+// the block's columns summed in float-float (d split into float hi + lo) into
+// cpart[block column][c (m) | Phi 1 (m)].  The grid covers npad columns (a
+// multiple of KCHUNK; PG_X * PG_SUB divides KCHUNK).
 template <int D>
 __global__ void __launch_bounds__(256)
-    sg_phi_gen(int kind, int m, int n, int d, const float* __restrict__ zs,
+    sg_phi_gen(int kind, int m, int n, int64_t npad, int d, const float* __restrict__ zs,
                const float* __restrict__ xs, const double* __restrict__ theta, int n_ls,
                const double* __restrict__ dv, float* __restrict__ Phh, float* __restrict__ Phl,
-               int64_t ldn, float* __restrict__ PTh, float* __restrict__ PTl, int64_t ldt,
+               float* __restrict__ PTh, float* __restrict__ PTl, int64_t ldt,
                double* __restrict__ cpart) {
+  static_assert(KCHUNK % (PG_X * PG_SUB) == 0, "generation blocks must not straddle chunks");
   __shared__ __align__(16) float tile[PG_I][PG_X + 1];
   __shared__ float sz[PG_I][D + 1];
   __shared__ float sxp[PG_X][D + 1];
@@ -271,7 +279,7 @@ __global__ void __launch_bounds__(256)
   float ch = 0.f, cl = 0.f, ph = 0.f, pl = 0.f;
   for (int sub = 0; sub < PG_SUB; ++sub) {
     const int64_t x0 = xb0 + (int64_t)sub * PG_X;
-    if (x0 >= n) break;
+    if (x0 >= npad) break;
     __syncthreads();  // the previous sub-tile is consumed
     for (int e = t; e < PG_X * D; e += 256) {
       const int c = e / D, k = e % D;
@@ -284,9 +292,10 @@ __global__ void __launch_bounds__(256)
       sdl[c] = (float)(v - (double)h);
     }
     __syncthreads();
-    {  // row-major pass: column a, rows (t >> 7) + 2 r
+    {  // chunk-blocked pass: column a, rows (t >> 7) + 2 r
       const int a = t & (PG_X - 1);
       const int64_t gx = x0 + a;
+      const int64_t cbase = (gx / KCHUNK) * (int64_t)m * KCHUNK + gx % KCHUNK;
       float xr[D];
 #pragma unroll
       for (int k = 0; k < D; ++k) xr[k] = sxp[a][k];
@@ -297,12 +306,12 @@ __global__ void __launch_bounds__(256)
           const float df = sz[r][k] - xr[k];
           sq = fmaf(df, df, sq);
         }
-        const float v = kval<float>(kind, sq, s2);
+        const float v = gx < n ? kval<float>(kind, sq, s2) : 0.f;
         tile[r][a] = v;
-        if (gx < n && i0 + r < m) {
+        if (i0 + r < m) {
           const float h = tf32_round(v);
-          Phh[(int64_t)(i0 + r) * ldn + gx] = h;
-          Phl[(int64_t)(i0 + r) * ldn + gx] = tf32_round(v - h);
+          Phh[cbase + (int64_t)(i0 + r) * KCHUNK] = h;
+          Phl[cbase + (int64_t)(i0 + r) * KCHUNK] = tf32_round(v - h);
         }
       }
     }
@@ -724,25 +733,28 @@ gpk_status sgpr_run(int kind, int n, int m, int d, const double* x, int64_t ldx,
   TcMap mphi, mh, mpt;
   if constexpr (mixed) {
     // Phi (both layouts, TF32 hi/lo), c = Phi d and Phi 1
+    const int64_t npad = (int64_t)b.nchunks * KCHUNK;
     const dim3 grid((unsigned)b.nxb, (unsigned)cdiv(m, PG_I));
     if (d <= 8)
-      sg_phi_gen<8><<<grid, 256, 0, s>>>(kind, m, n, d, b.zs, b.xs, theta, n_ls, b.dv, b.Phh,
-                                         b.Phl, b.ldn, b.PTh, b.PTl, ldm, b.cpart);
+      sg_phi_gen<8><<<grid, 256, 0, s>>>(kind, m, n, npad, d, b.zs, b.xs, theta, n_ls, b.dv,
+                                         b.Phh, b.Phl, b.PTh, b.PTl, ldm, b.cpart);
     else
-      sg_phi_gen<DMAXS><<<grid, 256, 0, s>>>(kind, m, n, d, b.zs, b.xs, theta, n_ls, b.dv, b.Phh,
-                                             b.Phl, b.ldn, b.PTh, b.PTl, ldm, b.cpart);
+      sg_phi_gen<DMAXS><<<grid, 256, 0, s>>>(kind, m, n, npad, d, b.zs, b.xs, theta, n_ls, b.dv,
+                                             b.Phh, b.Phl, b.PTh, b.PTl, ldm, b.cpart);
     GPK_LAUNCH_CHECK();
     GPK_CUDA_TRY(colsum(b.cpart, b.nxb, 2 * (int64_t)m, b.cv, false, b.colpart, s));
     // P: lower triangles of Phi_k Phi_k^T per n-chunk (tensor cores, one
-    // batched launch; columns past n read as zeros), summed in float64
-    if (!tc_make_map(&mphi, b.Phh, b.Phl, m, n, b.ldn) ||
+    // batched launch over the chunk-blocked operand, rows c * m + i), summed
+    // in float64.  A tile's rows past m (read from the next chunk) only reach
+    // outputs past m, which the epilogue drops.
+    if (!tc_make_map(&mphi, b.Phh, b.Phl, (int64_t)b.nchunks * m, KCHUNK, KCHUNK) ||
         !tc_make_map(&mh, b.Hh, b.Hl, m, m, ldm) || !tc_make_map(&mpt, b.PTh, b.PTl, n, m, ldm))
       return GPK_ERR_CUDA;
     GPK_CUDA_TRY(cudaMemsetAsync(b.Pparts, 0, sizeof(float) * (size_t)b.nchunks * m * m, s));
     tc::TcParams p{};
     p.M = p.N = m;
     p.K = KCHUNK;
-    p.a_zcol = p.b_zcol = KCHUNK;
+    p.a_zrow = p.b_zrow = m;
     p.c_lower = 1;
     p.force_shape = m >= 256 ? 2 : 0;  // wide tiles: the batch supplies the parallelism
     p.c0 = b.Pparts;
