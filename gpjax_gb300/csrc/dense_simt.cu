@@ -15,11 +15,11 @@ namespace gpk {
 // ---------------------------------------------------------------------------
 // Batched NT GEMM, register-tiled.
 // ---------------------------------------------------------------------------
-template <typename T>
-__global__ void __launch_bounds__((GemmCfg<T>::BM / GemmCfg<T>::TM) * (GemmCfg<T>::BN / GemmCfg<T>::TN))
+template <typename T, typename Cfg>
+__global__ void __launch_bounds__((Cfg::BM / Cfg::TM) * (Cfg::BN / Cfg::TN))
     gemm_nt_kernel(GemmProb<T> p) {
-  constexpr int BM = GemmCfg<T>::BM, BN = GemmCfg<T>::BN, BK = GemmCfg<T>::BK;
-  constexpr int TM = GemmCfg<T>::TM, TN = GemmCfg<T>::TN;
+  constexpr int BM = Cfg::BM, BN = Cfg::BN, BK = Cfg::BK;
+  constexpr int TM = Cfg::TM, TN = Cfg::TN;
   constexpr int NTX = BN / TN, NTY = BM / TM;
   const int z = blockIdx.z;
   const T* A = p.A + (int64_t)z * p.sA;
@@ -42,13 +42,14 @@ __global__ void __launch_bounds__((GemmCfg<T>::BM / GemmCfg<T>::TM) * (GemmCfg<T
   int klo, khi;
   tile_krange<BM, BN, BK>(p.K, p.a_tri, p.b_tri, i0, j0, klo, khi);
 
-  __shared__ SimtSmem<T> sm;
+  __shared__ SimtSmem<T, Cfg> sm;
   T acc[TM][TN];
 #pragma unroll
   for (int a = 0; a < TM; ++a)
 #pragma unroll
     for (int b = 0; b < TN; ++b) acc[a][b] = T(0);
-  simt_tile_mma<T>(A, p.lda, p.M, p.a_tri, B, p.ldb, p.N, p.b_tri, i0, j0, klo, khi, sm, acc);
+  simt_tile_mma<T, Cfg>(A, p.lda, p.M, p.a_tri, B, p.ldb, p.N, p.b_tri, i0, j0, klo, khi, sm,
+                        acc);
 
   const int tx = threadIdx.x % NTX, ty = threadIdx.x / NTX;
 #pragma unroll
@@ -70,21 +71,38 @@ __global__ void __launch_bounds__((GemmCfg<T>::BM / GemmCfg<T>::TM) * (GemmCfg<T
   }
 }
 
+template <typename T, typename Cfg>
+static int gemm_tiles(const GemmProb<T>& p) {
+  const int tilesM = (p.M + Cfg::BM - 1) / Cfg::BM, tilesN = (p.N + Cfg::BN - 1) / Cfg::BN;
+  return p.c_lower ? tilesM * (tilesM + 1) / 2 : tilesM * tilesN;
+}
+
+template <typename T, typename Cfg>
+static cudaError_t gemm_nt_cfg(const GemmProb<T>& p, int batch, cudaStream_t s) {
+  constexpr int NT = (Cfg::BM / Cfg::TM) * (Cfg::BN / Cfg::TN);
+  dim3 grid(gemm_tiles<T, Cfg>(p), 1, batch);
+  gemm_nt_kernel<T, Cfg><<<grid, NT, 0, s>>>(p);
+  return launch_status();
+}
+
+constexpr int SIMT_SMALL_BELOW = 152;  // CTAs of the full-size grid (one wave)
+
 template <typename T>
 cudaError_t gemm_nt(const GemmProb<T>& p, int batch, cudaStream_t s) {
-  constexpr int BM = GemmCfg<T>::BM, BN = GemmCfg<T>::BN;
-  constexpr int NT = (GemmCfg<T>::BM / GemmCfg<T>::TM) * (GemmCfg<T>::BN / GemmCfg<T>::TN);
   if (p.M <= 0 || p.N <= 0 || batch <= 0) return cudaSuccess;
-  const int tilesM = (p.M + BM - 1) / BM, tilesN = (p.N + BN - 1) / BN;
-  const int tiles = p.c_lower ? tilesM * (tilesM + 1) / 2 : tilesM * tilesN;
-  dim3 grid(tiles, 1, batch);
-  gemm_nt_kernel<T><<<grid, NT, 0, s>>>(p);
-  return launch_status();
+  // float64 only: the float32 form runs many independent GPs side by side
+  // (batched MLL), where total work rather than one launch's latency counts
+  if (sizeof(T) == 8 && (int64_t)gemm_tiles<T, GemmCfg<T>>(p) * batch < SIMT_SMALL_BELOW)
+    return gemm_nt_cfg<T, GemmCfgSmall<T>>(p, batch, s);
+  return gemm_nt_cfg<T, GemmCfg<T>>(p, batch, s);
 }
 
 // ---------------------------------------------------------------------------
 // Diagonal-block Cholesky: one CTA factors the nb x nb block at (k0, k0) in
-// shared memory (unblocked right-looking, two barriers per column).
+// shared memory (unblocked right-looking, two barriers per column).  Each
+// pivot's square root and reciprocal are taken once, by the thread that
+// finishes that diagonal entry (float64 square roots and divisions are slow
+// on this part: one per thread per column dominated the block).
 // ---------------------------------------------------------------------------
 template <typename T, int NB>
 __global__ void __launch_bounds__(512) potrf_diag_kernel(T* A, int64_t lda, int n, int k0,
@@ -96,29 +114,34 @@ __global__ void __launch_bounds__(512) potrf_diag_kernel(T* A, int64_t lda, int 
   double* Pv = Dd + NB;                              // float64 pivots
   T* S = reinterpret_cast<T*>(Pv + NB);
   T* col = S + NB * LD;
-  T* dl = col + NB;
+  T* dl = col + NB;   // L[j, j]
+  T* rl = dl + NB;    // 1 / L[j, j]
   const int nb = min(NB, n - k0);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
     int i = e / nb, j = e % nb;
     if (j <= i) S[i * LD + j] = A[(int64_t)(k0 + i) * lda + k0 + j];
   }
+  // NaN when the pivot is negative, as in the reference; float64 square
+  // root only when the factor itself is float64
+  auto pivot = [&](int j) {
+    const double pivd = Dd[j];
+    const T ljj = sizeof(T) == 8 ? (T)sqrt(pivd) : (T)sqrtf((float)pivd);
+    Pv[j] = pivd;
+    dl[j] = ljj;
+    rl[j] = T(1) / ljj;
+  };
   for (int i = threadIdx.x; i < nb; i += blockDim.x)
     Dd[i] = dtrack ? dtrack[k0 + i] : (double)A[(int64_t)(k0 + i) * lda + k0 + i];
   __syncthreads();
+  if (threadIdx.x == 0 && nb > 0) pivot(0);
+  __syncthreads();
   for (int j = 0; j < nb; ++j) {
-    const double pivd = Dd[j];
-    // NaN when the pivot is negative, as in the reference; float64 square
-    // root only when the factor itself is float64
-    const T ljj = sizeof(T) == 8 ? (T)sqrt(pivd) : (T)sqrtf((float)pivd);
+    const T rj = rl[j];
     for (int i = j + 1 + threadIdx.x; i < nb; i += blockDim.x) {
-      T v = S[i * LD + j] / ljj;
+      T v = S[i * LD + j] * rj;
       S[i * LD + j] = v;
       col[i] = v;
-    }
-    if (threadIdx.x == 0) {
-      dl[j] = ljj;
-      Pv[j] = pivd;
     }
     __syncthreads();
     for (int i = j + 1 + warp; i < nb; i += nwarps) {
@@ -128,6 +151,7 @@ __global__ void __launch_bounds__(512) potrf_diag_kernel(T* A, int64_t lda, int 
     for (int i = j + 1 + threadIdx.x; i < nb; i += blockDim.x) {
       const double c = (double)col[i];
       Dd[i] -= c * c;
+      if (i == j + 1) pivot(i);  // Dd[j + 1] is final after this column
     }
     __syncthreads();
   }
@@ -168,10 +192,11 @@ __global__ void zero_upper_kernel(T* A, int64_t lda, int n, int nb) {
   if (j > i && (j / nb) != (i / nb)) A[(int64_t)i * lda + j] = T(0);
 }
 
-// Panel solve: rows r >= k0+nb of the block column, X L_kk^T = A_panel,
-// one thread per row, L_kk and the rows staged in shared memory.
+// Panel solve, float32 form: one thread per row, 128 rows per CTA, L_kk and
+// the rows staged in shared memory (the float32 form serves the batched MLL,
+// where many solves run side by side).
 template <typename T, int NB>
-__global__ void __launch_bounds__(128) trsm_rows_kernel(T* A, int64_t lda, int n, int k0) {
+__global__ void __launch_bounds__(128) trsm_rows_thread_kernel(T* A, int64_t lda, int n, int k0) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int LD = NB + 1;
   T* Ls = reinterpret_cast<T*>(smem_raw);
@@ -215,16 +240,65 @@ __global__ void __launch_bounds__(128) trsm_rows_kernel(T* A, int64_t lda, int n
   }
 }
 
+// Panel solve, float64 form: TRSM_ROWS rows per CTA (so that a short panel
+// still spreads over many SMs: float64 throughput per SM is low), eliminated
+// column by column by all threads: after column j is final, every later
+// column c of every row takes x[c] -= (x[j] / L[j, j]) L[c, j].  The columns
+// stay unscaled until the end (one barrier per column).
+constexpr int TRSM_ROWS = 32;
+template <typename T, int NB>
+__global__ void __launch_bounds__(256) trsm_rows_kernel(T* A, int64_t lda, int n, int k0) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int LD = NB + 1;
+  T* Ls = reinterpret_cast<T*>(smem_raw);
+  T* Xs = Ls + NB * LD;
+  T* rinv = Xs + TRSM_ROWS * LD;
+  const int nb = min(NB, n - k0);
+  const int r0 = k0 + nb + blockIdx.x * TRSM_ROWS;
+  const int rows = min(TRSM_ROWS, n - r0);
+  if (rows <= 0) return;
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+    int i = e / nb, j = e % nb;
+    Ls[i * LD + j] = (j <= i) ? A[(int64_t)(k0 + i) * lda + k0 + j] : T(0);
+  }
+  for (int e = threadIdx.x; e < rows * nb; e += blockDim.x) {
+    int r = e / nb, c = e % nb;
+    Xs[r * LD + c] = A[(int64_t)(r0 + r) * lda + k0 + c];
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < nb; j += blockDim.x) rinv[j] = T(1) / Ls[j * LD + j];
+  __syncthreads();
+  for (int j = 0; j + 1 < nb; ++j) {
+    const int w = nb - 1 - j;  // columns j+1 .. nb-1
+    const T rj = rinv[j];
+    for (int e = threadIdx.x; e < rows * w; e += blockDim.x) {
+      const int r = e / w, c = j + 1 + e % w;
+      Xs[r * LD + c] -= (Xs[r * LD + j] * rj) * Ls[c * LD + j];
+    }
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < rows * nb; e += blockDim.x) {
+    int r = e / nb, c = e % nb;
+    A[(int64_t)(r0 + r) * lda + k0 + c] = Xs[r * LD + c] * rinv[c];
+  }
+}
+
 template <typename T>
 cudaError_t potrf_lower(T* A, int64_t lda, int n, double* logdiag, int* info, double* dtrack,
                         bool zero_upper, cudaStream_t s) {
   constexpr int NB = Blk<T>::NB;
-  const size_t smem_diag = (size_t)(NB * (NB + 1) + 2 * NB) * sizeof(T) + 2 * NB * sizeof(double);
-  const size_t smem_trsm = (size_t)(NB * (NB + 1) + 128 * (NB + 1) + NB) * sizeof(T);
+  const size_t smem_diag = (size_t)(NB * (NB + 1) + 3 * NB) * sizeof(T) + 2 * NB * sizeof(double);
+  constexpr bool f64 = sizeof(T) == 8;
+  const size_t smem_trsm =
+      (size_t)(NB * (NB + 1) + (f64 ? TRSM_ROWS : 128) * (NB + 1) + NB) * sizeof(T);
   cudaFuncSetAttribute(potrf_diag_kernel<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)smem_diag);
-  cudaFuncSetAttribute(trsm_rows_kernel<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)smem_trsm);
+  if (f64)
+    cudaFuncSetAttribute(trsm_rows_kernel<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem_trsm);
+  else
+    cudaFuncSetAttribute(trsm_rows_thread_kernel<T, NB>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_trsm);
   if (zero_upper && n > NB) {
     zero_upper_kernel<T><<<(int)cdiv((int64_t)n * n, 256), 256, 0, s>>>(A, lda, n, NB);
     cudaError_t e0 = launch_status();
@@ -237,7 +311,11 @@ cudaError_t potrf_lower(T* A, int64_t lda, int n, double* logdiag, int* info, do
     if (e != cudaSuccess) return e;
     const int rest = n - k0 - nb;
     if (rest <= 0) break;
-    trsm_rows_kernel<T, NB><<<(rest + 127) / 128, 128, smem_trsm, s>>>(A, lda, n, k0);
+    if (f64)
+      trsm_rows_kernel<T, NB><<<(rest + TRSM_ROWS - 1) / TRSM_ROWS, 256, smem_trsm, s>>>(A, lda, n,
+                                                                                       k0);
+    else
+      trsm_rows_thread_kernel<T, NB><<<(rest + 127) / 128, 128, smem_trsm, s>>>(A, lda, n, k0);
     e = launch_status();
     if (e != cudaSuccess) return e;
     if (dtrack) {
@@ -277,6 +355,7 @@ __global__ void __launch_bounds__(NB) trtri_diag_kernel(const T* L, int64_t ldl,
   constexpr int LD = NB + 1;
   T* Ls = reinterpret_cast<T*>(smem_raw);
   T* Ms = Ls + NB * LD;
+  T* ri = Ms + NB * LD;  // 1 / L[i, i], one division per row
   const int k0 = blockIdx.x * NB;
   const int nb = min(NB, n - k0);
   for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
@@ -284,10 +363,12 @@ __global__ void __launch_bounds__(NB) trtri_diag_kernel(const T* L, int64_t ldl,
     Ls[i * LD + j] = (j <= i) ? L[(int64_t)(k0 + i) * ldl + k0 + j] : T(0);
   }
   __syncthreads();
+  if (threadIdx.x < nb) ri[threadIdx.x] = T(1) / Ls[threadIdx.x * LD + threadIdx.x];
+  __syncthreads();
   const int c = threadIdx.x;
   if (c < nb) {
     for (int i = 0; i < c; ++i) Ms[i * LD + c] = T(0);
-    Ms[c * LD + c] = T(1) / Ls[c * LD + c];
+    Ms[c * LD + c] = ri[c];
     for (int i = c + 1; i < nb; ++i) {
       T s0 = T(0), s1 = T(0);
       const T* li = Ls + i * LD;
@@ -297,7 +378,7 @@ __global__ void __launch_bounds__(NB) trtri_diag_kernel(const T* L, int64_t ldl,
         s1 += li[k + 1] * Ms[(k + 1) * LD + c];
       }
       if (k < i) s0 += li[k] * Ms[k * LD + c];
-      Ms[i * LD + c] = -(s0 + s1) / li[i];
+      Ms[i * LD + c] = -(s0 + s1) * ri[i];
     }
   }
   __syncthreads();
@@ -360,7 +441,7 @@ template <typename T>
 cudaError_t trtri_lower(const T* L, int64_t ldl, int n, T* M, int64_t ldm, T* V, int64_t ldv,
                         T* scratch, cudaStream_t s) {
   constexpr int NB = Blk<T>::NB;
-  const size_t smem = (size_t)2 * NB * (NB + 1) * sizeof(T);
+  const size_t smem = (size_t)(2 * NB * (NB + 1) + NB) * sizeof(T);
   cudaFuncSetAttribute(trtri_diag_kernel<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)smem);
   const int nblk = (n + NB - 1) / NB;

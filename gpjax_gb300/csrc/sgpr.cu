@@ -23,6 +23,7 @@
 // generation.  The m x m algebra always runs in float64.  Reductions go
 // through per-block partials summed in a fixed order.
 #include <climits>
+#include <mutex>
 #include <type_traits>
 #include "gpk_internal.cuh"
 #include "tc_gemm.cuh"
@@ -709,9 +710,51 @@ __global__ void __launch_bounds__(256)
   out_grad[n_ls + 2] = inf ? nan : ds / s - pg1 / (s * s);
 }
 
+// Copies the lower triangle of up to three symmetric m x m matrices into
+// their upper triangles.
+__global__ void sg_mirror3(int m, int64_t ld, double* __restrict__ a, double* __restrict__ b,
+                           double* __restrict__ c) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (int64_t)m * m) return;
+  const int i = (int)(e / m), j = (int)(e % m);
+  if (j <= i) return;
+  const int64_t up = (int64_t)i * ld + j, lo = (int64_t)j * ld + i;
+  a[up] = a[lo];
+  b[up] = b[lo];
+  if (c) c[up] = c[lo];
+}
+
 __global__ void sg_zero(double* p, int count) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < count) p[i] = 0.0;
+}
+
+// Side stream for the Kzz chain (its Cholesky factor, inverse and K^-1 do not
+// depend on Phi or P, so they run beside the Phi generation and the P
+// product), forked from and joined back into the caller's stream.  The mutex
+// is held for a whole call's enqueue so that concurrent calls cannot
+// interleave their uses of the shared fork/join events.
+struct SgSide {
+  cudaStream_t s = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+};
+std::mutex g_sg_mu;
+SgSide g_sg_side[64];
+
+cudaError_t sg_side(SgSide** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  SgSide& c = g_sg_side[dev];
+  if (!c.s) {
+    e = cudaEventCreateWithFlags(&c.fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c.join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c.s, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return e;
+  }
+  *out = &c;
+  return cudaSuccess;
 }
 
 template <typename T>
@@ -730,6 +773,38 @@ gpk_status sgpr_run(int kind, int n, int m, int d, const double* x, int64_t ldx,
   GPK_CUDA_TRY(scale_inputs<T>(x, ldx, n, d, theta, n_ls, b.xs, s));
   GPK_CUDA_TRY(scale_inputs<T>(z, ldz, m, d, theta, n_ls, b.zs, s));
   GPK_CUDA_TRY(scale_inputs<double>(z, ldz, m, d, theta, n_ls, b.zs64, s));
+  // Kzz chain on the side stream: K (float64, full), Lz = chol(K + jitter I),
+  // Mz = Lz^-1, Vz = Mz^T, K^-1 = Vz Vz^T
+  std::lock_guard<std::mutex> lock(g_sg_mu);
+  SgSide* side = nullptr;
+  GPK_CUDA_TRY(sg_side(&side));
+  const cudaStream_t ss = side->s;
+  const unsigned mgrid = (unsigned)cdiv((int64_t)m * m, 256);
+  GPK_CUDA_TRY(cudaEventRecord(side->fork, s));
+  GPK_CUDA_TRY(cudaStreamWaitEvent(ss, side->fork, 0));
+  GPK_CUDA_TRY(cross_cov_scaled<double, double>(kind, m, m, d, b.zs64, b.zs64, theta, n_ls, 0, 0.0,
+                                                b.Kf, ldm, ss));
+  GPK_CUDA_TRY(cross_cov_scaled<double, double>(kind, m, m, d, b.zs64, b.zs64, theta, n_ls, 2,
+                                                jitter, b.Lz, ldm, ss));
+  GPK_CUDA_TRY(potrf_lower<double>(b.Lz, ldm, m, b.ldK, info, nullptr, false, ss));
+  GPK_CUDA_TRY(trtri_lower<double>(b.Lz, ldm, m, b.Mz, ldm, b.Vz, ldm, b.scr, ss));
+  {
+    GemmProb<double> p{};
+    p.A = b.Vz;
+    p.B = b.Vz;
+    p.lda = p.ldb = ldm;
+    p.a_tri = p.b_tri = TRI_UPPER;
+    p.C = b.Kinv;
+    p.ldc = ldm;
+    p.M = p.N = p.K = m;
+    p.c_lower = 1;
+    p.alpha = 1.0;
+    p.beta = 0.0;
+    GPK_CUDA_TRY(gemm_nt<double>(p, 1, ss));
+    sg_mirror3<<<mgrid, 256, 0, ss>>>(m, ldm, b.Kinv, b.Kinv, nullptr);
+    GPK_LAUNCH_CHECK();
+  }
+  GPK_CUDA_TRY(cudaEventRecord(side->join, ss));
   TcMap mphi, mh, mpt;
   if constexpr (mixed) {
     // Phi (both layouts, TF32 hi/lo), c = Phi d and Phi 1
@@ -795,35 +870,29 @@ gpk_status sgpr_run(int kind, int n, int m, int d, const double* x, int64_t ldx,
       GPK_CUDA_TRY(gemm_nt<T>(p, 1, s));
     }
   }
-  // K (float64, full) and Lz
-  GPK_CUDA_TRY(cross_cov_scaled<double, double>(kind, m, m, d, b.zs64, b.zs64, theta, n_ls, 0, 0.0,
-                                                b.Kf, ldm, s));
-  GPK_CUDA_TRY(cross_cov_scaled<double, double>(kind, m, m, d, b.zs64, b.zs64, theta, n_ls, 2,
-                                                jitter, b.Lz, ldm, s));
+  GPK_CUDA_TRY(cudaStreamWaitEvent(s, side->join, 0));
   sg_reduce_P<T><<<(int)cdiv((int64_t)m * m, 256), 256, 0, s>>>(b.Pparts, b.nchunks, m, ldm, b.Kf,
                                                                   theta, n_ls, jitter, b.P64, b.Su);
   GPK_LAUNCH_CHECK();
-  GPK_CUDA_TRY(potrf_lower<double>(b.Lz, ldm, m, b.ldK, info, nullptr, false, s));
-  GPK_CUDA_TRY(trtri_lower<double>(b.Lz, ldm, m, b.Mz, ldm, b.Vz, ldm, b.scr, s));
   GPK_CUDA_TRY(potrf_lower<double>(b.Su, ldm, m, b.ldU, info, nullptr, true, s));
   GPK_CUDA_TRY(trtri_lower<double>(b.Su, ldm, m, b.Mu, ldm, b.Vu, ldm, b.scr, s));
-  {  // K^-1 = Vz Vz^T, Su^-1 = Vu Vu^T (full squares)
+  {  // Su^-1 = Vu Vu^T (lower triangle, then mirrored)
     GemmProb<double> p{};
-    p.A = b.Vz;
-    p.B = b.Vz;
+    p.A = b.Vu;
+    p.B = b.Vu;
     p.lda = p.ldb = ldm;
     p.a_tri = p.b_tri = TRI_UPPER;
-    p.C = b.Kinv;
+    p.C = b.Suinv;
     p.ldc = ldm;
     p.M = p.N = p.K = m;
+    p.c_lower = 1;
     p.alpha = 1.0;
     p.beta = 0.0;
     GPK_CUDA_TRY(gemm_nt<double>(p, 1, s));
-    p.A = b.Vu;
-    p.B = b.Vu;
-    p.C = b.Suinv;
-    GPK_CUDA_TRY(gemm_nt<double>(p, 1, s));
-    // T1 = K^-1 P ; KPK = T1 K^-1   (symmetric operands: NT form)
+    sg_mirror3<<<mgrid, 256, 0, s>>>(m, ldm, b.Suinv, b.Suinv, nullptr);
+    GPK_LAUNCH_CHECK();
+    // T1 = K^-1 P ; KPK = T1 K^-1 (symmetric operands: NT form; KPK is
+    // symmetric, so its lower triangle is formed and mirrored)
     GemmProb<double> q{};
     q.A = b.Kinv;
     q.B = b.P64;
@@ -837,7 +906,10 @@ gpk_status sgpr_run(int kind, int n, int m, int d, const double* x, int64_t ldx,
     q.A = b.T1;
     q.B = b.Kinv;
     q.C = b.KPK;
+    q.c_lower = 1;
     GPK_CUDA_TRY(gemm_nt<double>(q, 1, s));
+    sg_mirror3<<<mgrid, 256, 0, s>>>(m, ldm, b.KPK, b.KPK, nullptr);
+    GPK_LAUNCH_CHECK();
   }
   GPK_CUDA_TRY(gemv_dense<double>(b.Suinv, ldm, m, m, b.cv, b.gam, s));
   GPK_CUDA_TRY(gemv_dense<double>(b.P64, ldm, m, m, b.gam, b.pgam, s));

@@ -12,6 +12,16 @@ template <> struct GemmCfg<double> {
 template <> struct GemmCfg<float> {
   static constexpr int BM = 128, BN = 128, BK = 16, TM = 8, TN = 8;
 };
+// Quarter-size tiles for products whose full-size grid would leave most SMs
+// idle (float64 throughput per SM is low on this part, so a lone 64 x 64
+// tile is slow): four times the CTAs, same 256 threads.
+template <typename T> struct GemmCfgSmall;
+template <> struct GemmCfgSmall<double> {
+  static constexpr int BM = 32, BN = 32, BK = 16, TM = 2, TN = 2;
+};
+template <> struct GemmCfgSmall<float> {
+  static constexpr int BM = 64, BN = 64, BK = 16, TM = 4, TN = 4;
+};
 
 // Linear lower-triangle tile index t -> (I, J), I >= J.
 __device__ __forceinline__ void tri_index(int t, int& I, int& J) {
@@ -44,19 +54,19 @@ __device__ __forceinline__ void tile_krange(int K, int a_tri, int b_tri, int i0,
   klo = (klo / BK) * BK;
 }
 
-template <typename T>
+template <typename T, typename Cfg = GemmCfg<T>>
 struct SimtSmem {
-  T As[GemmCfg<T>::BK][GemmCfg<T>::BM + 4];
-  T Bs[GemmCfg<T>::BK][GemmCfg<T>::BN + 4];
+  T As[Cfg::BK][Cfg::BM + 4];
+  T Bs[Cfg::BK][Cfg::BN + 4];
 };
 
-template <typename T>
+template <typename T, typename Cfg = GemmCfg<T>>
 __device__ __forceinline__ void simt_tile_mma(const T* A, int64_t lda, int M, int a_tri, const T* B,
                                               int64_t ldb, int N, int b_tri, int i0, int j0,
-                                              int klo, int khi, SimtSmem<T>& sm,
-                                              T (&acc)[GemmCfg<T>::TM][GemmCfg<T>::TN]) {
-  constexpr int BM = GemmCfg<T>::BM, BN = GemmCfg<T>::BN, BK = GemmCfg<T>::BK;
-  constexpr int TM = GemmCfg<T>::TM, TN = GemmCfg<T>::TN;
+                                              int klo, int khi, SimtSmem<T, Cfg>& sm,
+                                              T (&acc)[Cfg::TM][Cfg::TN]) {
+  constexpr int BM = Cfg::BM, BN = Cfg::BN, BK = Cfg::BK;
+  constexpr int TM = Cfg::TM, TN = Cfg::TN;
   constexpr int NTX = BN / TN, NTY = BM / TM, NT = NTX * NTY;
   const int tx = threadIdx.x % NTX, ty = threadIdx.x / NTX;
   for (int k0 = klo; k0 < khi; k0 += BK) {
