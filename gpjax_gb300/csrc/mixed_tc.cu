@@ -19,8 +19,10 @@
 // 128 with an identity block, which leaves the factor, the inverse, the
 // log-determinant and alpha of the original system unchanged.
 #include <climits>
+#include <cuda_fp16.h>
 #include <mutex>
 #include "tc_gemm.cuh"
+#include "simt_tile.cuh"
 
 namespace gpk {
 namespace {
@@ -538,32 +540,39 @@ __global__ void tc_diff_kernel(int n, const double* __restrict__ y, const double
 // coalesced).  The factorisation only ever touches the lower triangle, so the
 // upper one still holds Sigma for the residuals of the alpha refinement.
 constexpr int SG_T = 64;
+// One CTA per lower 64 x 64 tile (linear lower-tile index); D bounds the input
+// dimension so that the distance loop unrolls and each thread keeps its
+// column point in registers.
+template <int D>
 __global__ void __launch_bounds__(256)
     gram_mirror_kernel(int kind, int n, int d, const float* __restrict__ xs,
                        const double* __restrict__ theta, int n_ls, double jitter,
                        float* __restrict__ A, float* __restrict__ Ah, float* __restrict__ Al,
                        int64_t lda) {
-  __shared__ float sx[SG_T][GPK_MAX_D + 1];
-  __shared__ float sy[SG_T][GPK_MAX_D + 1];
+  __shared__ float sx[SG_T][D + 1];
   __shared__ float st[SG_T][SG_T + 1];
-  const int i0 = blockIdx.y * SG_T, j0 = blockIdx.x * SG_T;
-  if (j0 > i0) return;  // upper tiles are written as mirrors of lower ones
+  int I, J;
+  tri_index(blockIdx.x, I, J);
+  const int i0 = I * SG_T, j0 = J * SG_T;
   const float s2 = (float)theta[n_ls];
   const double sd = theta[n_ls + 1];
-  for (int e = threadIdx.x; e < SG_T * d; e += blockDim.x) {
-    const int r = e / d, k = e % d;
-    sx[r][k] = (i0 + r < n) ? xs[(int64_t)(i0 + r) * d + k] : 0.f;
-    sy[r][k] = (j0 + r < n) ? xs[(int64_t)(j0 + r) * d + k] : 0.f;
+  for (int e = threadIdx.x; e < SG_T * D; e += blockDim.x) {
+    const int r = e / D, k = e % D;
+    sx[r][k] = (i0 + r < n && k < d) ? xs[(int64_t)(i0 + r) * d + k] : 0.f;
   }
-  __syncthreads();
   const int c = threadIdx.x % SG_T, gj = j0 + c;
+  float yv[D];
+#pragma unroll
+  for (int k = 0; k < D; ++k) yv[k] = (gj < n && k < d) ? xs[(int64_t)gj * d + k] : 0.f;
+  __syncthreads();
   for (int r = threadIdx.x / SG_T; r < SG_T; r += 256 / SG_T) {
     const int gi = i0 + r;
     float kv = 0.f;
     if (gi < n && gj < n && gj <= gi) {
       float sq = 0.f;
-      for (int k = 0; k < d; ++k) {
-        const float df = sx[r][k] - sy[c][k];
+#pragma unroll
+      for (int k = 0; k < D; ++k) {
+        const float df = sx[r][k] - yv[k];
         sq = fmaf(df, df, sq);
       }
       kv = kval<float>(kind, sq, s2);
@@ -576,10 +585,18 @@ __global__ void __launch_bounds__(256)
     st[r][c] = kv;
   }
   __syncthreads();
-  for (int e = threadIdx.x; e < SG_T * SG_T; e += blockDim.x) {
-    const int rr = e / SG_T, cc = e % SG_T;  // element (i0 + cc, j0 + rr) -> (j0 + rr, i0 + cc)
-    const int gi = i0 + cc, gjj = j0 + rr;
-    if (gi < n && gjj < gi) A[(int64_t)gjj * lda + gi] = st[cc][rr];
+  if (I == J) {
+    for (int e = threadIdx.x; e < SG_T * SG_T; e += blockDim.x) {
+      const int rr = e / SG_T, cc = e % SG_T;  // element (i0 + cc, j0 + rr) -> (j0 + rr, i0 + cc)
+      const int gi = i0 + cc, gjj = j0 + rr;
+      if (gi < n && gjj < gi) A[(int64_t)gjj * lda + gi] = st[cc][rr];
+    }
+  } else {
+    for (int e = threadIdx.x; e < SG_T * SG_T; e += blockDim.x) {
+      const int rr = e / SG_T, cc = e % SG_T;
+      const int gi = i0 + cc, gjj = j0 + rr;
+      if (gi < n && gjj < n) A[(int64_t)gjj * lda + gi] = st[cc][rr];
+    }
   }
 }
 
@@ -809,10 +826,62 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
   return cudaSuccess;
 }
 
+// V (TF32 hi + lo, upper triangular) -> float16 hi/lo with a power-of-two
+// scale per row that brings the row's largest magnitude into [2^13, 2^14):
+// float16 then keeps an 11-bit significand for every entry down to ~2^-17 of
+// the row maximum (smaller ones lose relative precision but not absolute), and
+// the split pair carries ~22 bits like the TF32 split.  One warp per row; row r
+// is converted from column 128 * (r / 128) on, the part the adjoint reads for
+// outputs it keeps.  vscale[r] = 1 / scale (the epilogue's exact undo).
+constexpr int V16_TARGET_EXP = 14;
+__global__ void __launch_bounds__(256)
+    v16_convert_kernel(int np, const float* __restrict__ Vh, const float* __restrict__ Vl,
+                       int64_t ld, __half* __restrict__ Hh, __half* __restrict__ Hl,
+                       float* __restrict__ vscale) {
+  const int r = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (r >= np) return;
+  const int c0 = (r / LEAF) * LEAF;
+  const int64_t o = (int64_t)r * ld;
+  float mx = 0.f;
+  for (int c = c0 + lane * 4; c < np; c += 128) {
+    const float4 h = *reinterpret_cast<const float4*>(Vh + o + c);
+    const float4 l = *reinterpret_cast<const float4*>(Vl + o + c);
+    mx = fmaxf(mx, fmaxf(fmaxf(fabsf(h.x + l.x), fabsf(h.y + l.y)),
+                         fmaxf(fabsf(h.z + l.z), fabsf(h.w + l.w))));
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  int e = 0;
+  if (mx > 0.f && isfinite(mx)) frexpf(mx, &e);  // mx = f * 2^e, f in [0.5, 1)
+  e = max(e, -100);  // keeps both scales finite
+  const float sc = ldexpf(1.f, V16_TARGET_EXP - e), inv = ldexpf(1.f, e - V16_TARGET_EXP);
+  for (int c = c0 + lane * 4; c < np; c += 128) {
+    const float4 h = *reinterpret_cast<const float4*>(Vh + o + c);
+    const float4 l = *reinterpret_cast<const float4*>(Vl + o + c);
+    const float v[4] = {(h.x + l.x) * sc, (h.y + l.y) * sc, (h.z + l.z) * sc, (h.w + l.w) * sc};
+    __half hv[4], lv[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      hv[k] = __float2half_rn(v[k]);
+      lv[k] = __float2half_rn(v[k] - __half2float(hv[k]));
+    }
+    *reinterpret_cast<uint2*>(Hh + o + c) = make_uint2(
+        (uint32_t)__half_as_ushort(hv[0]) | ((uint32_t)__half_as_ushort(hv[1]) << 16),
+        (uint32_t)__half_as_ushort(hv[2]) | ((uint32_t)__half_as_ushort(hv[3]) << 16));
+    *reinterpret_cast<uint2*>(Hl + o + c) = make_uint2(
+        (uint32_t)__half_as_ushort(lv[0]) | ((uint32_t)__half_as_ushort(lv[1]) << 16),
+        (uint32_t)__half_as_ushort(lv[2]) | ((uint32_t)__half_as_ushort(lv[3]) << 16));
+  }
+  if (lane == 0) vscale[r] = inv;
+}
+
 struct TcBuffers {
   int npad;
   int64_t ld;
   float *A, *Ah, *Al, *Lh, *Ll, *Mh, *Ml, *Vh, *Vl, *xs, *vf;
+  __half *V16h, *V16l;  // row-scaled float16 hi/lo of V (the adjoint's operand)
+  float* vscale;        // inverse power-of-two row scales of V16
   float *TTh[kMaxDepth], *TTl[kMaxDepth];
   int64_t ldtt[kMaxDepth];
   int ndepth;
@@ -841,6 +910,9 @@ size_t tc_layout(int64_t n, int d, void* ws, TcBuffers& b) {
   b.Ml = (float*)take(nn);
   b.Vh = (float*)take(nn);
   b.Vl = (float*)take(nn);
+  b.V16h = (__half*)take(nn / 2);
+  b.V16l = (__half*)take(nn / 2);
+  b.vscale = (float*)take((size_t)b.npad * 4);
   // T^T at depth k is at most s_{k+1} x s_{k+1}, s_0 = n_pad, s_{k+1} = ceil128(s_k / 2)
   b.ndepth = 0;
   for (int64_t sk = b.npad; sk > LEAF && b.ndepth < kMaxDepth; ++b.ndepth) {
@@ -931,9 +1003,17 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
   tc_diff_kernel<<<(int)cdiv(n, 256), 256, 0, s>>>(n, y, theta, n_ls, b.diff);
   GPK_LAUNCH_CHECK();
   {
-    const dim3 grid((unsigned)cdiv(n, SG_T), (unsigned)cdiv(n, SG_T));
-    gram_mirror_kernel<<<grid, 256, 0, s>>>(kind, n, d, b.xs, theta, n_ls, jitter, b.A, b.Ah,
-                                            b.Al, b.ld);
+    const int64_t tt = cdiv(n, SG_T);
+    const unsigned grid = (unsigned)(tt * (tt + 1) / 2);  // lower tiles
+    if (d <= 8)
+      gram_mirror_kernel<8><<<grid, 256, 0, s>>>(kind, n, d, b.xs, theta, n_ls, jitter, b.A, b.Ah,
+                                                 b.Al, b.ld);
+    else if (d <= 16)
+      gram_mirror_kernel<16><<<grid, 256, 0, s>>>(kind, n, d, b.xs, theta, n_ls, jitter, b.A,
+                                                  b.Ah, b.Al, b.ld);
+    else
+      gram_mirror_kernel<GPK_MAX_D><<<grid, 256, 0, s>>>(kind, n, d, b.xs, theta, n_ls, jitter,
+                                                         b.A, b.Ah, b.Al, b.ld);
     GPK_LAUNCH_CHECK();
   }
   GPK_CUDA_TRY(sigma_diag_init(kind, n, theta, n_ls, jitter, b.dtrack, s));
@@ -1036,8 +1116,25 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
   pg.avec = b.alpha;
   pg.gpart = b.gpart;
   pg.err = b.err;
+  // large problems with d <= 8 (the wide tile): float16 split of V, rows
+  // scaled by powers of two (twice the MMA rate and half the operand bytes of
+  // the TF32 split at the same 11-bit significand)
+  const bool f16adj = np >= 2048 && d <= 8;
+  TcMap mV16;
+  if (f16adj) {
+    pg.force_shape = 4;  // Tile shape 3
+    pg.rscale = b.vscale;
+  }
   const int ntiles_adj = tc_gemm_tiles(tc::MODE_GRAD, pg);  // gpart rows of the adjoint
-  if (want_grad) GPK_CUDA_TRY(tc_gemm_run(tc::MODE_GRAD, c.mV, c.mV, pg, 1, hs));
+  if (want_grad && f16adj) {
+    if (!tc_make_map_f16(&mV16, b.V16h, b.V16l, np, np, b.ld)) return GPK_ERR_CUDA;
+    v16_convert_kernel<<<(unsigned)cdiv((int64_t)np * 32, 256), 256, 0, hs>>>(
+        np, b.Vh, b.Vl, b.ld, b.V16h, b.V16l, b.vscale);
+    GPK_LAUNCH_CHECK();
+    GPK_CUDA_TRY(tc_gemm_run(tc::MODE_GRAD, mV16, mV16, pg, 1, hs, true));
+  } else if (want_grad) {
+    GPK_CUDA_TRY(tc_gemm_run(tc::MODE_GRAD, c.mV, c.mV, pg, 1, hs));
+  }
   prof_mark(4, hs);
   prof_mark(5, hs);
   GPK_CUDA_TRY(cudaEventRecord(sc->edone, hs));

@@ -23,9 +23,11 @@ template <> struct GemmCfgSmall<float> {
   static constexpr int BM = 64, BN = 64, BK = 16, TM = 4, TN = 4;
 };
 
-// Linear lower-triangle tile index t -> (I, J), I >= J.
+// Linear lower-triangle tile index t -> (I, J), I >= J.  A float32 estimate
+// corrected by the integer loops (every thread of a CTA calls this; float64
+// square roots are slow on this part).
 __device__ __forceinline__ void tri_index(int t, int& I, int& J) {
-  int i = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+  int i = (int)((sqrtf(8.f * (float)t + 1.f) - 1.f) * 0.5f);
   while (i * (i + 1) / 2 > t) --i;
   while ((i + 1) * (i + 2) / 2 <= t) ++i;
   I = i;

@@ -101,6 +101,21 @@ __device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t a, uint64_t b
       : "memory");
 }
 
+// kind::f16 with float16 A and B (both the same type), float32 accumulate
+__host__ __device__ constexpr uint32_t idesc_f16(int m, int n) {
+  return (1u << 4) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc,
+                                        uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile(
       "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -171,15 +186,20 @@ __device__ __forceinline__ void split_tf32(float x, float& hi, float& lo) {
 // operand bytes, from L2 and from shared memory, per multiply-add.  Half (2,
 // small GEMMs): 128 x 64 outputs, 32-wide slices, 4 stages of 48 KB, 4 buffers
 // of 64 columns: twice the CTAs of the narrow tile where that leaves SMs idle.
+// Wide float16 (3): the wide tile's byte geometry (64-byte K slice rows, 64B
+// swizzle, 4 stages of 48 KB) holding 32 float16 K elements per slice, two
+// kind::f16 MMAs of K = 16 per slice.
 template <int TS>
 struct Tile {
-  static constexpr bool WIDE = TS == 1;
-  static constexpr int BN = TS == 1 ? 256 : (TS == 2 ? 64 : 128);
-  static constexpr int BK = WIDE ? 16 : 32;
+  static constexpr bool F16 = TS == 3;
+  static constexpr bool WIDE = TS == 1 || TS == 3;
+  static constexpr int ELEM = F16 ? 2 : 4;  // operand bytes
+  static constexpr int BN = WIDE ? 256 : (TS == 2 ? 64 : 128);
+  static constexpr int BK = TS == 1 ? 16 : 32;
   static constexpr int STAGES = TS == 0 ? 3 : 4;
-  static constexpr int SWZ = BK * 4;  // bytes of one K slice row
-  static constexpr int A_BYTES = BM * BK * 4;
-  static constexpr int B_BYTES = BN * BK * 4;
+  static constexpr int SWZ = BK * ELEM;  // bytes of one K slice row
+  static constexpr int A_BYTES = BM * BK * ELEM;
+  static constexpr int B_BYTES = BN * BK * ELEM;
   static constexpr int STAGE_BYTES = 2 * (A_BYTES + B_BYTES);  // A_hi, A_lo, B_hi, B_lo
   static constexpr int NBUF = BN >= 128 ? 512 / BN : 4;        // TMEM accumulator buffers
   static constexpr int TMEM_COLS = NBUF * BN;                  // a power of two >= 32
@@ -187,7 +207,8 @@ struct Tile {
   static constexpr int TLD = BN + 4; // staged output tile row stride (floats)
   // K slices summed by one TMEM accumulator before the epilogue drains it:
   // 32 K elements either way (the accumulation length the accuracy needs)
-  static constexpr int SEG = WIDE ? 2 : 1;
+  static constexpr int SEG = TS == 1 ? 2 : 1;
+  static constexpr int KSTEP = F16 ? 16 : 8;  // K elements per MMA (32 bytes either way)
 };
 
 template <int STAGES_>
@@ -282,7 +303,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   SmemCtl<STAGES>* ctl = reinterpret_cast<SmemCtl<STAGES>*>(tiles + STAGES * STAGE_BYTES);
   float* gx = reinterpret_cast<float*>(ctl + 1);  // MODE_GRAD: column points and alphas
   float* ga = gx + BN * DM;
-  double* gred = reinterpret_cast<double*>(ga + BN);
+  float* gsc = ga + BN;  // MODE_GRAD: column scales of a scaled operand
+  double* gred = reinterpret_cast<double*>(gsc + BN);
   float* otile = reinterpret_cast<float*>(tiles);  // output tile, reuses the operand ring
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -353,7 +375,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      constexpr uint32_t idesc = idesc_tf32(BM, BN);
+      constexpr uint32_t idesc = TL::F16 ? idesc_f16(BM, BN) : idesc_tf32(BM, BN);
       bool ok = true;
       for (int kc = 0; kc < nk && ok; ++kc) {
         const int seg = kc / SEG_CHUNKS, b = seg % NBUF;
@@ -373,11 +395,17 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         const uint64_t blo = sdesc<TL::SWZ>(sb + 2 * A_BYTES + B_BYTES);
         const bool first = (kc % SEG_CHUNKS) == 0;
 #pragma unroll
-        for (int k4 = 0; k4 < BK / 8; ++k4) {
-          const uint64_t off = (uint64_t)((k4 * 32) >> 4);  // 32 bytes per K = 8 step
-          mma_tf32(tacc, alo + off, bhi + off, idesc, (first && k4 == 0) ? 0u : 1u);
-          mma_tf32(tacc, ahi + off, blo + off, idesc, 1u);
-          mma_tf32(tacc, ahi + off, bhi + off, idesc, 1u);
+        for (int k4 = 0; k4 < BK / TL::KSTEP; ++k4) {
+          const uint64_t off = (uint64_t)((k4 * 32) >> 4);  // 32 bytes per MMA K step
+          if (TL::F16) {
+            mma_f16(tacc, alo + off, bhi + off, idesc, (first && k4 == 0) ? 0u : 1u);
+            mma_f16(tacc, ahi + off, blo + off, idesc, 1u);
+            mma_f16(tacc, ahi + off, bhi + off, idesc, 1u);
+          } else {
+            mma_tf32(tacc, alo + off, bhi + off, idesc, (first && k4 == 0) ? 0u : 1u);
+            mma_tf32(tacc, ahi + off, blo + off, idesc, 1u);
+            mma_tf32(tacc, ahi + off, bhi + off, idesc, 1u);
+          }
         }
         mma_commit(&ctl->empty[s]);
         if (kc % SEG_CHUNKS == SEG_CHUNKS - 1 || kc == nk - 1) mma_commit(&ctl->tfull[b]);
@@ -404,6 +432,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       for (int c = et; c < BN; c += EPI_THREADS) {
         const int gj = j0 + c;
         ga[c] = (cvec && gj < p.n_true) ? (float)cvec[gj] : 0.f;
+        gsc[c] = (MODE == MODE_GRAD && p.rscale && gj < p.N) ? p.rscale[gj] : 1.f;
       }
     }
     // drain the accumulator segments into float32 registers (round to nearest)
@@ -580,8 +609,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       // the reduction below then holds no accumulator registers
       constexpr int GLD = BN + 1;
       asm volatile("bar.sync 1, %0;" ::"r"(EPI_THREADS) : "memory");  // gx / ga staged, ring free
+      // undo the operand's power-of-two row scales (exact)
+      const float rsi = (p.rscale && gi < p.M) ? p.rscale[gi] : 1.f;
 #pragma unroll
-      for (int c = 0; c < HC; ++c) otile[r * GLD + hcol + c] = have ? acc[c] : 0.f;
+      for (int c = 0; c < HC; ++c)
+        otile[r * GLD + hcol + c] = have ? acc[c] * (rsi * gsc[hcol + c]) : 0.f;
       // W tile -> reduction against dK/dtheta (unit variance); an aborted wait
       // contributes zeros but still joins the reduction barrier
       float xi[DM];
@@ -793,18 +825,20 @@ static EncodeTiledFn encode_fn() {
 
 // float32 row-major [rows, cols] with leading dimension ld; box bk x box_rows
 // (bk = 32: 128B swizzle, bk = 16: 64B swizzle; one K slice row per box row)
-static bool make_map(CUtensorMap* m, const float* base, int64_t rows, int64_t cols, int64_t ld,
-                     int bk, int box_rows) {
+static bool make_map(CUtensorMap* m, const void* base, int64_t rows, int64_t cols, int64_t ld,
+                     int bk, int box_rows, int elem = 4) {
   EncodeTiledFn fn = encode_fn();
   if (!fn) return false;
-  if ((reinterpret_cast<uintptr_t>(base) & 15u) != 0 || ((ld * 4) & 15) != 0) return false;
+  if ((reinterpret_cast<uintptr_t>(base) & 15u) != 0 || ((ld * elem) & 15) != 0) return false;
   cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)(ld * 4)};
+  cuuint64_t strides[1] = {(cuuint64_t)(ld * elem)};
   cuuint32_t box[2] = {(cuuint32_t)bk, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
-  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides,
-                  box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                  bk == 32 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+  const int row_bytes = bk * elem;  // 128 -> 128B swizzle, 64 -> 64B swizzle
+  CUresult r = fn(m, elem == 2 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                  2, const_cast<void*>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  row_bytes == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
 }
@@ -813,7 +847,7 @@ template <int TS>
 static size_t tc_smem_bytes() {
   using TL = tc::Tile<TS>;
   return 1024 + (size_t)TL::STAGES * TL::STAGE_BYTES + sizeof(tc::SmemCtl<TL::STAGES>) +
-         (size_t)TL::BN * tc::GRAD_DMAX * 4 + TL::BN * 4 +
+         (size_t)TL::BN * tc::GRAD_DMAX * 4 + 2 * TL::BN * 4 +
          (size_t)(tc::GRAD_DMAX + 2) * 8 * sizeof(double) + 64;
 }
 
@@ -832,6 +866,15 @@ bool tc_make_map(TcMap* m, const float* hi, const float* lo, int64_t rows, int64
          make_map(&m->hb_lo, lo, rows, cols, ld, H::BK, H::BN);
 }
 
+bool tc_make_map_f16(TcMap* m, const void* hi, const void* lo, int64_t rows, int64_t cols,
+                     int64_t ld) {
+  using F = tc::Tile<3>;
+  return make_map(&m->fa_hi, hi, rows, cols, ld, F::BK, tc::BM, 2) &&
+         make_map(&m->fa_lo, lo, rows, cols, ld, F::BK, tc::BM, 2) &&
+         make_map(&m->fb_hi, hi, rows, cols, ld, F::BK, F::BN, 2) &&
+         make_map(&m->fb_lo, lo, rows, cols, ld, F::BK, F::BN, 2);
+}
+
 // Tile shape per problem: wide once a GEMM has several waves of tiles (the
 // adjoint epilogue keeps 128 accumulator columns per thread only with DM =
 // 8), half where narrow tiles would leave most SMs idle, narrow otherwise.
@@ -844,15 +887,17 @@ static int tile_shape(int mode, const tc::TcParams& p) {
   return 0;
 }
 
+static int tile_bn(int ts) {
+  return ts == 1 || ts == 3 ? tc::Tile<1>::BN : (ts == 2 ? tc::Tile<2>::BN : tc::Tile<0>::BN);
+}
+
 int tc_gemm_col_tiles(int mode, const tc::TcParams& p) {
-  const int ts = tile_shape(mode, p);
-  const int bn = ts == 1 ? tc::Tile<1>::BN : (ts == 2 ? tc::Tile<2>::BN : tc::Tile<0>::BN);
+  const int bn = tile_bn(tile_shape(mode, p));
   return (p.N + bn - 1) / bn;
 }
 
 int tc_gemm_tiles(int mode, const tc::TcParams& p) {
-  const int ts = tile_shape(mode, p);
-  const int bn = ts == 1 ? tc::Tile<1>::BN : (ts == 2 ? tc::Tile<2>::BN : tc::Tile<0>::BN);
+  const int bn = tile_bn(tile_shape(mode, p));
   const int tm = (p.M + tc::BM - 1) / tc::BM, tn = (p.N + bn - 1) / bn;
   return tc::tile_count(p.c_lower, tm, tn, bn);
 }
@@ -876,7 +921,10 @@ static void launch_one(const TcMap& A, const TcMap& B, const tc::TcParams& p0, i
   cfg.stream = s;
   cfg.attrs = attr.a;
   cfg.numAttrs = 1;
-  if (TS == 1)
+  if (TS == 3)
+    cudaLaunchKernelEx(&cfg, tc::tc_gemm_kernel<MODE, TS, DM>, A.fa_hi, A.fa_lo, B.fb_hi,
+                       B.fb_lo, p);
+  else if (TS == 1)
     cudaLaunchKernelEx(&cfg, tc::tc_gemm_kernel<MODE, TS, DM>, A.wa_hi, A.wa_lo, B.wb_hi,
                        B.wb_lo, p);
   else if (TS == 2)
@@ -907,7 +955,9 @@ cudaError_t tc_gemm_run(int mode, const TcMap& A, const TcMap& B, const tc::TcPa
         launch_one<tc::MODE_STORE_SPLIT, 0, tc::GRAD_DMAX>(A, B, p, batch, s, pdl);
       break;
     case tc::MODE_GRAD:
-      if (ts == 1)
+      if (ts == 3)
+        launch_one<tc::MODE_GRAD, 3, 8>(A, B, p, batch, s, pdl);
+      else if (ts == 1)
         launch_one<tc::MODE_GRAD, 1, 8>(A, B, p, batch, s, pdl);
       else
         launch_one<tc::MODE_GRAD, 0, tc::GRAD_DMAX>(A, B, p, batch, s, pdl);

@@ -4,7 +4,10 @@
 //   computed as A_lo B_hi + A_hi B_lo + A_hi B_hi
 // where *_hi is the operand rounded to TF32 and *_lo the TF32 rounding of the
 // remainder (both stored as float32 bit patterns with zero low 13 bits), which
-// recovers float32-class products on the TF32 pipe.  Operands are staged by
+// recovers float32-class products on the TF32 pipe.  One tile shape takes the
+// same split in float16 instead (same 11-bit significand, twice the MMA rate,
+// half the operand bytes), on operands whose rows were scaled by powers of two
+// into float16's range; the epilogue undoes the scales exactly.  Operands are staged by
 // TMA (swizzled) into a shared-memory ring, one elected thread issues
 // tcgen05.mma into float32 accumulators in tensor memory, and eight epilogue
 // warps read them back with tcgen05.ld and apply a fused epilogue (trailing
@@ -46,6 +49,8 @@ struct TcParams {
   // zs, columns = data points xs): G = acc + avec_i * bvec_j, reduced against
   // dK/dtheta into gpart[tile] and against dK/dz into zpart[column tile][row].
   int n_true, d, kind;
+  const float* rscale;  // MODE_GRAD, optional: acc[i, j] *= rscale[i] * rscale[j] (power-of-2
+                        // row scales of a scaled float16 operand)
   const float* xs;
   const float* zs;
   const double* avec;
@@ -75,9 +80,15 @@ struct TcMap {
   CUtensorMap wa_hi, wa_lo;  // wide tile, A side: box 16 x 128
   CUtensorMap wb_hi, wb_lo;  // wide tile, B side: box 16 x 256
   CUtensorMap hb_hi, hb_lo;  // half tile, B side: box 32 x 64
+  CUtensorMap fa_hi, fa_lo;  // float16 wide tile, A side: box 32 x 128
+  CUtensorMap fb_hi, fb_lo;  // float16 wide tile, B side: box 32 x 256
 };
 bool tc_make_map(TcMap* m, const float* hi, const float* lo, int64_t rows, int64_t cols,
                  int64_t ld);
+// float16 hi/lo operand pair (2-byte elements, ld in elements): fills the fa/fb
+// maps, used by the float16 wide tile shape (index 3) of MODE_GRAD.
+bool tc_make_map_f16(TcMap* m, const void* hi, const void* lo, int64_t rows, int64_t cols,
+                     int64_t ld);
 // pdl: launch as a programmatic dependent of the previous kernel in the stream
 // (only where that previous stream operation is a kernel launch).
 cudaError_t tc_gemm_run(int mode, const TcMap& A, const TcMap& B, const tc::TcParams& p,

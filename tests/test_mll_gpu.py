@@ -68,7 +68,7 @@ def test_mll_mixed_parity_c2(cuda_lib, n):
     _mixed_check(val, g, ref, gref, abs(ref))
 
 
-@pytest.mark.parametrize("kind,n,d", [(0, 1024, 4), (1, 1500, 6), (0, 555, 16)])
+@pytest.mark.parametrize("kind,n,d", [(0, 1024, 4), (1, 1500, 6), (0, 555, 16), (1, 2600, 5)])
 def test_mll_mixed_parity_other_kernels(cuda_lib, kind, n, d):
     """Other kernels: MLL error relative to the size of its terms
     (|log det| + |quad| + n log 2pi) / 2, which stays meaningful when the MLL
