@@ -206,8 +206,11 @@ struct Tile {
   static constexpr int HC = BN / 2;  // accumulator columns owned by one epilogue thread
   static constexpr int TLD = BN + 4; // staged output tile row stride (floats)
   // K slices summed by one TMEM accumulator before the epilogue drains it:
-  // 32 K elements either way (the accumulation length the accuracy needs)
-  static constexpr int SEG = TS == 1 ? 2 : 1;
+  // twelve MMAs (3 products x 4 K steps: 32 K elements for TF32, 64 for
+  // float16, whose MMAs take K = 16) -- the accumulation length the accuracy
+  // needs -- and, for the wide float16 tile, drains no more often than the
+  // epilogue's 16-column TMEM loads keep up with
+  static constexpr int SEG = TS == 1 || TS == 3 ? 2 : 1;
   static constexpr int KSTEP = F16 ? 16 : 8;  // K elements per MMA (32 bytes either way)
 };
 
