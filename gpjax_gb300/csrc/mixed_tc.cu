@@ -706,6 +706,10 @@ struct TcChol {
 // L21 = A21 M11^T, A22 -= L21 L21^T, [L22, M22] = chol_inv(A22) (right), and
 // M21 = -M22 T with T = L21 M11.  T^T only needs L21 and the left child, so it
 // runs on the side stream while the right subtree is factored; M21 waits for it.
+// Nodes whose halves are at most this wide run T^T inline (measured at n =
+// 16384: 0 -> 20.9 ms factor, 128 -> 20.7, 512 -> 20.1, 1024 -> 20.3,
+// 4096 -> 21.0).
+constexpr int TT_INLINE_MAX = 512;
 cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
   if (sz == LEAF) {
     PdlAttr attr(c.prev_kernel);
@@ -747,11 +751,18 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
     c.prev_kernel = true;
     if (e != cudaSuccess) return e;
   }
-  {  // T^T = (L21 M11)^T on the side stream; T[i, j] = sum_c L21[i, c] V11[j, c]
+  // T^T = (L21 M11)^T; T[i, j] = sum_c L21[i, c] V11[j, c].  Large nodes run it
+  // on the side stream beside the trailing update and the right recursion;
+  // small ones inline, where the fork and join events would cost the next
+  // launches on the critical path their programmatic-dependent overlap.
+  const bool tt_inline = h <= TT_INLINE_MAX;
+  if (!tt_inline) {
     e = cudaEventRecord(c.efork, c.s);
     c.prev_kernel = false;
     if (e == cudaSuccess) e = cudaStreamWaitEvent(c.side, c.efork, 0);
     if (e != cudaSuccess) return e;
+  }
+  {
     tc::TcParams p{};
     p.M = h2;
     p.N = h;
@@ -766,8 +777,13 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
     p.ldt = c.ldtt[depth];
     p.alpha = 1.f;
     p.err = c.err;
-    e = tc_gemm_run(tc::MODE_STORE_SPLIT, c.mL, c.mV, p, 1, c.side);
-    if (e == cudaSuccess) e = cudaEventRecord(c.ejoin, c.side);
+    if (tt_inline) {
+      e = tc_gemm_run(tc::MODE_STORE_SPLIT, c.mL, c.mV, p, 1, c.s, c.prev_kernel);
+      c.prev_kernel = true;
+    } else {
+      e = tc_gemm_run(tc::MODE_STORE_SPLIT, c.mL, c.mV, p, 1, c.side);
+      if (e == cudaSuccess) e = cudaEventRecord(c.ejoin, c.side);
+    }
     if (e != cudaSuccess) return e;
   }
   {  // A22 -= L21 L21^T (lower tiles)
@@ -794,11 +810,13 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
   }
   e = chol_inv_rec(c, o + h, h2, depth + 1);
   if (e != cudaSuccess) return e;
-  // the latest T^T on the side stream is this node's or a later one: either
-  // way this node's is complete when it is
-  e = cudaStreamWaitEvent(c.s, c.ejoin, 0);
-  c.prev_kernel = false;
-  if (e != cudaSuccess) return e;
+  if (!tt_inline) {
+    // the latest T^T on the side stream is this node's or a later one:
+    // either way this node's is complete when it is
+    e = cudaStreamWaitEvent(c.s, c.ejoin, 0);
+    c.prev_kernel = false;
+    if (e != cudaSuccess) return e;
+  }
   {  // M21 = -M22 T ; M21[i, j] = sum_c M22[i, c] TT[j, c]; V12 = M21^T
     tc::TcParams p{};
     p.M = h2;
