@@ -37,7 +37,7 @@ PEAK_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustaine
 # profiles/tc_gemm_grad_dram_n16384.txt.  The algorithmic operand volume is
 # 1.07 GB (the upper triangle of V in TF32 hi/lo): tiles of one L2-resident
 # group share panels, the groups re-read them.
-ADJOINT_TRAFFIC_BYTES_N16384 = 8.98e9 + 4.54e6
+ADJOINT_TRAFFIC_BYTES_N16384 = 3.68e9 + 41.1e6
 
 
 def parse_args():
@@ -392,13 +392,15 @@ def run_gpu(args):
         "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 Gram + f32/tf32x3 factor + f64 refinement/accumulation",
+        "dtype": "f32 Gram + tf32x3 factor + f16x3 adjoint + f64 refinement/accumulation",
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "n": n, "d": d, "kernel": "Matern52",
                    "precision": "mixed", "parallelism": "replicas" if world > 1 else "single",
                    "l2": "working set (3 x n^2 float32 = 3.2 GB) larger than L2; no flush"},
         "roofline": {"bound": "tensor",
-                     "kernel": "tc_gemm_kernel<MODE_GRAD> (W = L^-T L^-1 tiles contracted with dK/dtheta)",
+                     "kernel": "tc_gemm_kernel<MODE_GRAD, float16 wide> (W = L^-T L^-1 tiles "
+                               "contracted with dK/dtheta); timed with its float16 conversion of "
+                               "L^-T (the adjoint phase)",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "peak_kind": f"{peak_kind} bf16 dense",
                      "traffic": ADJOINT_TRAFFIC_BYTES_N16384,
