@@ -452,6 +452,25 @@ __global__ void leaf_zero_kernel(float* Mh, float* Ml, float* Vh, float* Vl, int
   }
 }
 
+// Zeros of the first off-diagonal 128 x 128 blocks outside the triangles of M
+// (lower: blocks (b, b + 1)) and V (upper: blocks (b + 1, b)).  A 256-wide
+// GEMM tile over a triangular B operand (L21 reads M11, T^T reads V11) masks K
+// per tile, so its rows in one 128-block read the neighbouring block on the
+// wrong side of the diagonal; nothing else writes there, so without this the
+// products would read whatever the workspace held.
+__global__ void band_zero_kernel(float* Mh, float* Ml, float* Vh, float* Vl, int64_t ldm) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;  // (row, float4) of one block
+  if (e >= LEAF * (LEAF / 4)) return;
+  const int b = blockIdx.y, i = e / (LEAF / 4), c = 4 * (e % (LEAF / 4));
+  const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+  const int64_t om = (int64_t)(b * LEAF + i) * ldm + (b + 1) * LEAF + c;   // M[b][b + 1]
+  const int64_t ov = (int64_t)((b + 1) * LEAF + i) * ldm + b * LEAF + c;   // V[b + 1][b]
+  *reinterpret_cast<float4*>(Mh + om) = z;
+  *reinterpret_cast<float4*>(Ml + om) = z;
+  *reinterpret_cast<float4*>(Vh + ov) = z;
+  *reinterpret_cast<float4*>(Vl + ov) = z;
+}
+
 size_t leaf_smem_bytes() {
   return (size_t)(2 * LEAF * LEAF_LDT + 64 * LEAF_TLD + 5 * LEAF) * sizeof(float);
 }
@@ -1086,6 +1105,11 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
   GPK_CUDA_TRY(cudaStreamWaitEvent(hs, sc->estart, 0));
   leaf_zero_kernel<<<dim3(cdiv(LEAF * 24, 256), np / LEAF), 256, 0, hs>>>(b.Mh, b.Ml, b.Vh, b.Vl,
                                                                            b.ld);
+  GPK_LAUNCH_CHECK();
+  if (np > LEAF) {
+    band_zero_kernel<<<dim3(LEAF * (LEAF / 4) / 256, np / LEAF - 1), 256, 0, hs>>>(b.Mh, b.Ml, b.Vh,
+                                                                                 b.Vl, b.ld);
+  }
   GPK_LAUNCH_CHECK();
   c.prev_kernel = true;
   GPK_CUDA_TRY(chol_inv_rec(c, 0, np, 0));

@@ -113,3 +113,36 @@ def test_mll_deterministic(cuda_lib):
     a, ga = run(2, x, y, ls, 1.0, 0.1, 0.0, "mixed")
     b, gb = run(2, x, y, ls, 1.0, 0.1, 0.0, "mixed")
     assert a == b and np.array_equal(ga, gb)
+
+
+@pytest.mark.parametrize("n", [4500])
+def test_mll_mixed_dirty_workspace(cuda_lib, n):
+    """The mixed form must not depend on the workspace's prior contents: run it
+    through the C ABI on a workspace filled with a finite non-zero byte pattern
+    (float32 785.07), at a size whose recursion has 2304-wide nodes (256-wide
+    GEMM tiles over triangular operands), and compare with a clean workspace
+    and the oracle."""
+    from gpjax_gb300 import _lib
+    x, y, ls = c2_like(n, 8, seed=n + 1, kind=2)
+    dev = torch.device("cuda", 0)
+    theta = torch.tensor(list(ls) + [1.0, 0.1, 0.0], dtype=torch.float64, device=dev)
+    X = torch.as_tensor(x, device=dev)
+    Y = torch.as_tensor(y[:, 0], device=dev).contiguous()
+    nbytes = _lib.lib().gpk_conjugate_mll_workspace_bytes(n, 8, _lib.PREC_MIXED)
+    results = []
+    for fill in (0x00, 0x44):
+        ws = torch.full((nbytes,), fill, dtype=torch.uint8, device=dev)
+        out = torch.zeros(1, dtype=torch.float64, device=dev)
+        grad = torch.zeros(11, dtype=torch.float64, device=dev)
+        info = torch.zeros(1, dtype=torch.int32, device=dev)
+        _lib.call("gpk_conjugate_mll", _lib.MATERN52, n, 8, X.data_ptr(), 8, Y.data_ptr(),
+                  theta.data_ptr(), 8, 1e-6, _lib.PREC_MIXED, 1, out.data_ptr(),
+                  grad.data_ptr(), info.data_ptr(), ws.data_ptr(), ws.numel(),
+                  _lib.stream_ptr(dev))
+        torch.cuda.synchronize(dev)
+        assert int(info.item()) == 0
+        results.append((float(out.item()), grad.cpu().numpy().copy()))
+    ref = O.conjugate_mll(2, x, y, ls, 1.0, 0.1, 0.0)
+    (v0, g0), (v1, g1) = results
+    assert abs(v1 - ref) <= 1e-6 * abs(ref), (v1, ref)
+    assert v1 == v0 and np.array_equal(g1, g0)
