@@ -703,7 +703,86 @@ __global__ void residual_upper_finish(int kind, int n, const double* __restrict_
   r[i] = diff[i] - s;
 }
 
+// float16 row scaling: each row's largest magnitude lands in [2^13, 2^14)
+constexpr int V16_TARGET_EXP = 14;
+
+// Rows [0, rows) of the rows x cols block at (row0, col0) of a TF32 pair
+// (hi + lo, leading dimension ld) to compact float16 hi/lo [rows][cols] with
+// the power-of-two row scales of v16_convert_kernel (rinv[r] = 1 / scale).
+// tri = TRI_LOWER / TRI_UPPER keeps the block's lower / upper triangle and
+// writes zeros elsewhere (so nothing outside the operand reaches a scale or
+// a product), TRI_NONE the whole row.  One warp per row; cols % 4 == 0,
+// col0 % 4 == 0.
+__global__ void __launch_bounds__(256)
+    split16_block_kernel(const float* __restrict__ hi, const float* __restrict__ lo, int64_t ld,
+                         int row0, int col0, int rows, int cols, int tri, __half* __restrict__ dh,
+                         __half* __restrict__ dl, float* __restrict__ rinv) {
+  const int r = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (r >= rows) return;
+  const int cb = tri == TRI_UPPER ? r : 0;
+  const int ce = tri == TRI_LOWER ? min(cols, r + 1) : cols;  // exclusive
+  const int64_t o = (int64_t)(row0 + r) * ld + col0;
+  float mx = 0.f;
+  for (int c = (cb & ~3) + lane * 4; c < ce; c += 128) {
+    const float4 h = *reinterpret_cast<const float4*>(hi + o + c);
+    const float4 l = *reinterpret_cast<const float4*>(lo + o + c);
+    const float v[4] = {h.x + l.x, h.y + l.y, h.z + l.z, h.w + l.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (c + k >= cb && c + k < ce) mx = fmaxf(mx, fabsf(v[k]));
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  int e = 0;
+  if (mx > 0.f && isfinite(mx)) frexpf(mx, &e);
+  e = max(e, -100);
+  const float sc = ldexpf(1.f, V16_TARGET_EXP - e);
+  const int64_t d0 = (int64_t)r * cols;
+  for (int c = lane * 4; c < cols; c += 128) {
+    float v[4] = {0.f, 0.f, 0.f, 0.f};
+    if (c + 3 >= cb && c < ce) {
+      const float4 h = *reinterpret_cast<const float4*>(hi + o + c);
+      const float4 l = *reinterpret_cast<const float4*>(lo + o + c);
+      const float w[4] = {h.x + l.x, h.y + l.y, h.z + l.z, h.w + l.w};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) v[k] = (c + k >= cb && c + k < ce) ? w[k] * sc : 0.f;
+    }
+    __half hv[4], lv[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      hv[k] = __float2half_rn(v[k]);
+      lv[k] = __float2half_rn(v[k] - __half2float(hv[k]));
+    }
+    *reinterpret_cast<uint2*>(dh + d0 + c) = make_uint2(
+        (uint32_t)__half_as_ushort(hv[0]) | ((uint32_t)__half_as_ushort(hv[1]) << 16),
+        (uint32_t)__half_as_ushort(hv[2]) | ((uint32_t)__half_as_ushort(hv[3]) << 16));
+    *reinterpret_cast<uint2*>(dl + d0 + c) = make_uint2(
+        (uint32_t)__half_as_ushort(lv[0]) | ((uint32_t)__half_as_ushort(lv[1]) << 16),
+        (uint32_t)__half_as_ushort(lv[2]) | ((uint32_t)__half_as_ushort(lv[3]) << 16));
+  }
+  if (lane == 0) rinv[r] = ldexpf(1.f, e - V16_TARGET_EXP);
+}
+
 constexpr int kMaxDepth = 24;  // recursion depth bound (n_pad < 128 * 2^23)
+// Nodes whose halves are both at least this wide run their four products as
+// split-float16 GEMMs on float16 copies of the operands (the wide-tile range).
+constexpr int F16_MIN = 2048;
+
+// float16 operand copies of one depth's nodes (compact, row-scaled):
+//   a: A21, later M22     m: M11, later T^T     l: L21     v: V11
+// with their inverse row scales; each array holds up to cap elements.
+struct F16Set {
+  __half *ah, *al, *mh, *ml, *lh, *ll, *vh, *vl;
+  float *ra, *rm, *rl, *rv;
+};
+
+cudaError_t to16(const float* hi, const float* lo, int64_t ld, int row0, int col0, int rows,
+                 int cols, int tri, __half* dh, __half* dl, float* rinv, cudaStream_t s) {
+  split16_block_kernel<<<(unsigned)cdiv((int64_t)rows * 32, 256), 256, 0, s>>>(
+      hi, lo, ld, row0, col0, rows, cols, tri, dh, dl, rinv);
+  return launch_status();
+}
 
 struct TcChol {
   float* A;
@@ -719,6 +798,8 @@ struct TcChol {
   cudaStream_t side;  // T^T = (L21 M11)^T products, overlapped with the right subtree
   cudaEvent_t efork, ejoin;
   bool prev_kernel;   // the last operation enqueued on s was a kernel launch (PDL allowed)
+  F16Set f16[kMaxDepth];
+  int nf16;           // depths [0, nf16) have float16 buffers
 };
 
 // A node of size sz at depth `depth`: [L11, M11] = chol_inv(A11) (left, size h),
@@ -748,6 +829,10 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
   const int h2 = sz - h;
   cudaError_t e = chol_inv_rec(c, o, h, depth + 1);
   if (e != cudaSuccess) return e;
+  // wide nodes: split-float16 products on row-scaled float16 copies
+  const bool f16 = h2 >= F16_MIN && depth < c.nf16;
+  F16Set* f = f16 ? &c.f16[depth] : nullptr;
+  TcMap fa, fm, fl, fv;  // float16 maps of this node's operand copies
   {  // L21 = A21 M11^T, float64 diagonal track of A22
     tc::TcParams p{};
     p.M = h2;
@@ -766,7 +851,26 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
     p.alpha = 1.f;
     p.dtrack = c.dtrack;
     p.err = c.err;
-    e = tc_gemm_run(tc::MODE_STORE_SPLIT, c.mA, c.mM, p, 1, c.s, c.prev_kernel);
+    if (f16) {
+      e = to16(c.Ah, c.Al, c.ld, o + h, o, h2, h, TRI_NONE, f->ah, f->al, f->ra, c.s);
+      if (e == cudaSuccess)
+        e = to16(c.Mh, c.Ml, c.ld, o, o, h, h, TRI_LOWER, f->mh, f->ml, f->rm, c.s);
+      if (e != cudaSuccess) return e;
+      if (!tc_make_map_f16(&fa, f->ah, f->al, h2, h, h) ||
+          !tc_make_map_f16(&fm, f->mh, f->ml, h, h, h))
+        return cudaErrorInvalidValue;
+      p.a_row0 = p.a_col0 = p.b_row0 = p.b_col0 = 0;
+      p.force_shape = 4;
+      p.ra = f->ra;
+      p.rb = f->rm;
+      e = tc_gemm_run(tc::MODE_STORE_SPLIT, fa, fm, p, 1, c.s, true);
+      if (e == cudaSuccess)
+        e = to16(c.Lh, c.Ll, c.ld, o + h, o, h2, h, TRI_NONE, f->lh, f->ll, f->rl, c.s);
+      if (e == cudaSuccess && !tc_make_map_f16(&fl, f->lh, f->ll, h2, h, h))
+        e = cudaErrorInvalidValue;
+    } else {
+      e = tc_gemm_run(tc::MODE_STORE_SPLIT, c.mA, c.mM, p, 1, c.s, c.prev_kernel);
+    }
     c.prev_kernel = true;
     if (e != cudaSuccess) return e;
   }
@@ -796,7 +900,21 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
     p.ldt = c.ldtt[depth];
     p.alpha = 1.f;
     p.err = c.err;
-    if (tt_inline) {
+    if (f16) {  // (never inline: h > TT_INLINE_MAX) V11 and T^T to float16 on the side
+      e = to16(c.Vh, c.Vl, c.ld, o, o, h, h, TRI_UPPER, f->vh, f->vl, f->rv, c.side);
+      if (e == cudaSuccess && !tc_make_map_f16(&fv, f->vh, f->vl, h, h, h))
+        e = cudaErrorInvalidValue;
+      if (e != cudaSuccess) return e;
+      p.a_row0 = p.a_col0 = p.b_row0 = p.b_col0 = 0;
+      p.force_shape = 4;
+      p.ra = f->rl;
+      p.rb = f->rv;
+      e = tc_gemm_run(tc::MODE_STORE_SPLIT, fl, fv, p, 1, c.side);
+      if (e == cudaSuccess)  // T^T (h x h2) into the M11 copy's storage, now free
+        e = to16(c.TTh[depth], c.TTl[depth], c.ldtt[depth], 0, 0, h, h2, TRI_NONE, f->mh,
+                 f->ml, f->rm, c.side);
+      if (e == cudaSuccess) e = cudaEventRecord(c.ejoin, c.side);
+    } else if (tt_inline) {
       e = tc_gemm_run(tc::MODE_STORE_SPLIT, c.mL, c.mV, p, 1, c.s, c.prev_kernel);
       c.prev_kernel = true;
     } else {
@@ -823,12 +941,27 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
     p.c_col0 = o + h;
     p.alpha = -1.f;
     p.err = c.err;
-    e = tc_gemm_run(tc::MODE_ADD_F32, c.mL, c.mL, p, 1, c.s, c.prev_kernel);
+    if (f16) {
+      p.a_row0 = p.a_col0 = p.b_row0 = p.b_col0 = 0;
+      p.force_shape = 4;
+      p.ra = p.rb = f->rl;
+      e = tc_gemm_run(tc::MODE_ADD_F32, fl, fl, p, 1, c.s, c.prev_kernel);
+    } else {
+      e = tc_gemm_run(tc::MODE_ADD_F32, c.mL, c.mL, p, 1, c.s, c.prev_kernel);
+    }
     c.prev_kernel = true;
     if (e != cudaSuccess) return e;
   }
   e = chol_inv_rec(c, o + h, h2, depth + 1);
   if (e != cudaSuccess) return e;
+  if (f16) {  // M22 into the A21 copy's storage (free since L21)
+    e = to16(c.Mh, c.Ml, c.ld, o + h, o + h, h2, h2, TRI_LOWER, f->ah, f->al, f->ra, c.s);
+    if (e == cudaSuccess && (!tc_make_map_f16(&fa, f->ah, f->al, h2, h2, h2) ||
+                             !tc_make_map_f16(&fm, f->mh, f->ml, h, h2, h2)))
+      e = cudaErrorInvalidValue;
+    if (e != cudaSuccess) return e;
+    c.prev_kernel = true;
+  }
   if (!tt_inline) {
     // the latest T^T on the side stream is this node's or a later one:
     // either way this node's is complete when it is
@@ -856,7 +989,15 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
     p.t_col0 = o + h;
     p.alpha = -1.f;
     p.err = c.err;
-    e = tc_gemm_run(tc::MODE_STORE_SPLIT, c.mM, c.mTT[depth], p, 1, c.s, c.prev_kernel);
+    if (f16) {
+      p.a_row0 = p.a_col0 = p.b_row0 = p.b_col0 = 0;
+      p.force_shape = 4;
+      p.ra = f->ra;
+      p.rb = f->rm;
+      e = tc_gemm_run(tc::MODE_STORE_SPLIT, fa, fm, p, 1, c.s, c.prev_kernel);
+    } else {
+      e = tc_gemm_run(tc::MODE_STORE_SPLIT, c.mM, c.mTT[depth], p, 1, c.s, c.prev_kernel);
+    }
     c.prev_kernel = true;
     if (e != cudaSuccess) return e;
   }
@@ -870,7 +1011,6 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
 // the split pair carries ~22 bits like the TF32 split.  One warp per row; row r
 // is converted from column 128 * (r / 128) on, the part the adjoint reads for
 // outputs it keeps.  vscale[r] = 1 / scale (the epilogue's exact undo).
-constexpr int V16_TARGET_EXP = 14;
 __global__ void __launch_bounds__(256)
     v16_convert_kernel(int np, const float* __restrict__ Vh, const float* __restrict__ Vl,
                        int64_t ld, __half* __restrict__ Hh, __half* __restrict__ Hl,
@@ -922,6 +1062,8 @@ struct TcBuffers {
   float *TTh[kMaxDepth], *TTl[kMaxDepth];
   int64_t ldtt[kMaxDepth];
   int ndepth;
+  F16Set f16[kMaxDepth];  // float16 operand copies of the wide nodes, per depth
+  int nf16;
   double *diff, *z, *alpha, *r, *logdiag, *dtrack, *rpart, *gpart, *rbuf, *cbuf, *fin;
   int* err;
 };
@@ -957,6 +1099,28 @@ size_t tc_layout(int64_t n, int d, void* ws, TcBuffers& b) {
     b.ldtt[b.ndepth] = sk;
     b.TTh[b.ndepth] = (float*)take((size_t)sk * sk * 4);
     b.TTl[b.ndepth] = (float*)take((size_t)sk * sk * 4);
+  }
+  // float16 copies for the depths whose nodes can have both halves >= F16_MIN:
+  // a node of size s at depth k has halves at most h_k = ceil128(s_k / 2)
+  b.nf16 = 0;
+  for (int64_t sk = b.npad; b.nf16 < kMaxDepth; ++b.nf16) {
+    const int64_t hk = ((sk / 2 + LEAF - 1) / LEAF) * LEAF;
+    if (sk - hk < F16_MIN) break;
+    const size_t cap = (size_t)hk * hk;
+    F16Set& f = b.f16[b.nf16];
+    f.ah = (__half*)take(cap * 2);
+    f.al = (__half*)take(cap * 2);
+    f.mh = (__half*)take(cap * 2);
+    f.ml = (__half*)take(cap * 2);
+    f.lh = (__half*)take(cap * 2);
+    f.ll = (__half*)take(cap * 2);
+    f.vh = (__half*)take(cap * 2);
+    f.vl = (__half*)take(cap * 2);
+    f.ra = (float*)take((size_t)hk * 4);
+    f.rm = (float*)take((size_t)hk * 4);
+    f.rl = (float*)take((size_t)hk * 4);
+    f.rv = (float*)take((size_t)hk * 4);
+    sk = hk;
   }
   b.xs = (float*)take((size_t)n * d * 4);
   b.vf = (float*)take((size_t)b.npad * 4);
@@ -1079,6 +1243,8 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
       !tc_make_map(&c.mV, b.Vh, b.Vl, np, np, b.ld) ||
       !tc_make_map(&c.mA, b.Ah, b.Al, np, np, b.ld))
     return GPK_ERR_UNSUPPORTED;
+  c.nf16 = b.nf16;
+  for (int k = 0; k < b.nf16; ++k) c.f16[k] = b.f16[k];
   for (int k = 0; k < b.ndepth; ++k) {
     c.TTh[k] = b.TTh[k];
     c.TTl[k] = b.TTl[k];
@@ -1165,7 +1331,7 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
   TcMap mV16;
   if (f16adj) {
     pg.force_shape = 4;  // Tile shape 3
-    pg.rscale = b.vscale;
+    pg.ra = pg.rb = b.vscale;
   }
   const int ntiles_adj = tc_gemm_tiles(tc::MODE_GRAD, pg);  // gpart rows of the adjoint
   if (want_grad && f16adj) {

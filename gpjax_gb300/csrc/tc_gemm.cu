@@ -435,9 +435,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       for (int c = et; c < BN; c += EPI_THREADS) {
         const int gj = j0 + c;
         ga[c] = (cvec && gj < p.n_true) ? (float)cvec[gj] : 0.f;
-        gsc[c] = (MODE == MODE_GRAD && p.rscale && gj < p.N) ? p.rscale[gj] : 1.f;
       }
     }
+    if (p.ra)  // column scales of a float16 B operand (1 where rb is absent)
+      for (int c = et; c < BN; c += EPI_THREADS)
+        gsc[c] = (p.rb && j0 + c < p.N) ? p.rb[j0 + c] : 1.f;
     // drain the accumulator segments into float32 registers (round to nearest)
     float acc[HC];
 #pragma unroll
@@ -480,6 +482,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(
                                       smem_u32(&ctl->tempty[b]))
                                   : "memory");
+    }
+    if (p.ra) {
+      // undo the float16 operands' power-of-two row scales (exact)
+      asm volatile("bar.sync 1, %0;" ::"r"(EPI_THREADS) : "memory");  // gsc staged
+      const float rsi = gi < p.M ? p.ra[gi] : 1.f;
+#pragma unroll
+      for (int c = 0; c < HC; ++c) acc[c] *= rsi * gsc[hcol + c];
     }
     if (MODE == MODE_ADD_F32 || MODE == MODE_STORE_SPLIT) {
       // dtrack: sum of squares of this row's outputs (float64)
@@ -612,11 +621,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       // the reduction below then holds no accumulator registers
       constexpr int GLD = BN + 1;
       asm volatile("bar.sync 1, %0;" ::"r"(EPI_THREADS) : "memory");  // gx / ga staged, ring free
-      // undo the operand's power-of-two row scales (exact)
-      const float rsi = (p.rscale && gi < p.M) ? p.rscale[gi] : 1.f;
 #pragma unroll
-      for (int c = 0; c < HC; ++c)
-        otile[r * GLD + hcol + c] = have ? acc[c] * (rsi * gsc[hcol + c]) : 0.f;
+      for (int c = 0; c < HC; ++c) otile[r * GLD + hcol + c] = have ? acc[c] : 0.f;
       // W tile -> reduction against dK/dtheta (unit variance); an aborted wait
       // contributes zeros but still joins the reduction barrier
       float xi[DM];
@@ -942,7 +948,9 @@ cudaError_t tc_gemm_run(int mode, const TcMap& A, const TcMap& B, const tc::TcPa
   const int ts = tile_shape(mode, p);
   switch (mode) {
     case tc::MODE_ADD_F32:
-      if (ts == 1)
+      if (ts == 3)
+        launch_one<tc::MODE_ADD_F32, 3, tc::GRAD_DMAX>(A, B, p, batch, s, pdl);
+      else if (ts == 1)
         launch_one<tc::MODE_ADD_F32, 1, tc::GRAD_DMAX>(A, B, p, batch, s, pdl);
       else if (ts == 2)
         launch_one<tc::MODE_ADD_F32, 2, tc::GRAD_DMAX>(A, B, p, batch, s, pdl);
@@ -950,7 +958,9 @@ cudaError_t tc_gemm_run(int mode, const TcMap& A, const TcMap& B, const tc::TcPa
         launch_one<tc::MODE_ADD_F32, 0, tc::GRAD_DMAX>(A, B, p, batch, s, pdl);
       break;
     case tc::MODE_STORE_SPLIT:
-      if (ts == 1)
+      if (ts == 3)
+        launch_one<tc::MODE_STORE_SPLIT, 3, tc::GRAD_DMAX>(A, B, p, batch, s, pdl);
+      else if (ts == 1)
         launch_one<tc::MODE_STORE_SPLIT, 1, tc::GRAD_DMAX>(A, B, p, batch, s, pdl);
       else if (ts == 2)
         launch_one<tc::MODE_STORE_SPLIT, 2, tc::GRAD_DMAX>(A, B, p, batch, s, pdl);

@@ -48,9 +48,12 @@ struct TcParams {
   // columns both index xs, avec = alpha.  MODE_SGPR (rows = inducing points
   // zs, columns = data points xs): G = acc + avec_i * bvec_j, reduced against
   // dK/dtheta into gpart[tile] and against dK/dz into zpart[column tile][row].
+  // optional, every mode: acc[i, j] *= ra[i] * rb[j] before the epilogue uses
+  // it (the inverse power-of-two row scales of float16 operands A and B;
+  // indices are rows of the product, 0 <= i < M, 0 <= j < N)
+  const float* ra;
+  const float* rb;
   int n_true, d, kind;
-  const float* rscale;  // MODE_GRAD, optional: acc[i, j] *= rscale[i] * rscale[j] (power-of-2
-                        // row scales of a scaled float16 operand)
   const float* xs;
   const float* zs;
   const double* avec;
@@ -86,7 +89,7 @@ struct TcMap {
 bool tc_make_map(TcMap* m, const float* hi, const float* lo, int64_t rows, int64_t cols,
                  int64_t ld);
 // float16 hi/lo operand pair (2-byte elements, ld in elements): fills the fa/fb
-// maps, used by the float16 wide tile shape (index 3) of MODE_GRAD.
+// maps, used by the float16 wide tile shape (index 3; force_shape = 4).
 bool tc_make_map_f16(TcMap* m, const void* hi, const void* lo, int64_t rows, int64_t cols,
                      int64_t ld);
 // pdl: launch as a programmatic dependent of the previous kernel in the stream
