@@ -806,9 +806,10 @@ struct TcChol {
 // L21 = A21 M11^T, A22 -= L21 L21^T, [L22, M22] = chol_inv(A22) (right), and
 // M21 = -M22 T with T = L21 M11.  T^T only needs L21 and the left child, so it
 // runs on the side stream while the right subtree is factored; M21 waits for it.
-// Nodes whose halves are at most this wide run T^T inline (measured at n =
-// 16384: 0 -> 20.9 ms factor, 128 -> 20.7, 512 -> 20.1, 1024 -> 20.3,
-// 4096 -> 21.0).
+// Nodes whose halves are at most this wide run T^T inline (factor at n =
+// 16384 with the fork after the trailing update: 0 -> 18.8 ms, 128 -> 18.5,
+// 512 -> 18.0; with the fork before it: 0 -> 20.9, 128 -> 20.7, 512 -> 20.1,
+// 1024 -> 20.3, 4096 -> 21.0, measured before the float16 wide nodes).
 constexpr int TT_INLINE_MAX = 512;
 cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
   if (sz == LEAF) {
@@ -879,13 +880,15 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
   // small ones inline, where the fork and join events would cost the next
   // launches on the critical path their programmatic-dependent overlap.
   const bool tt_inline = h <= TT_INLINE_MAX;
-  if (!tt_inline) {
-    e = cudaEventRecord(c.efork, c.s);
-    c.prev_kernel = false;
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(c.side, c.efork, 0);
-    if (e != cudaSuccess) return e;
-  }
-  {
+  // T^T: inline before the trailing update, or on the side stream forked after
+  // it (so that the update keeps its programmatic-dependent launch)
+  auto tt = [&]() -> cudaError_t {
+    if (!tt_inline) {
+      cudaError_t ee = cudaEventRecord(c.efork, c.s);
+      c.prev_kernel = false;
+      if (ee == cudaSuccess) ee = cudaStreamWaitEvent(c.side, c.efork, 0);
+      if (ee != cudaSuccess) return ee;
+    }
     tc::TcParams p{};
     p.M = h2;
     p.N = h;
@@ -921,6 +924,10 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
       e = tc_gemm_run(tc::MODE_STORE_SPLIT, c.mL, c.mV, p, 1, c.side);
       if (e == cudaSuccess) e = cudaEventRecord(c.ejoin, c.side);
     }
+    return e;
+  };
+  if (tt_inline) {
+    e = tt();
     if (e != cudaSuccess) return e;
   }
   {  // A22 -= L21 L21^T (lower tiles)
@@ -950,6 +957,10 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
       e = tc_gemm_run(tc::MODE_ADD_F32, c.mL, c.mL, p, 1, c.s, c.prev_kernel);
     }
     c.prev_kernel = true;
+    if (e != cudaSuccess) return e;
+  }
+  if (!tt_inline) {
+    e = tt();
     if (e != cudaSuccess) return e;
   }
   e = chol_inv_rec(c, o + h, h2, depth + 1);
