@@ -491,9 +491,10 @@ __global__ void __launch_bounds__(256)
     gemv_split_kernel(const float* __restrict__ Th, const float* __restrict__ Tl, int64_t ld,
                       int n, int lower, const float* __restrict__ x, double* __restrict__ y,
                       int accumulate) {
-  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (i >= n) return;
+  if (w >= n) return;
+  const int i = lower ? n - 1 - w : w;  // longest rows first: no long tail in the last wave
   const int c0 = lower ? 0 : i, c1 = lower ? i + 1 : n;
   const float* rh = Th + (int64_t)i * ld;
   const float* rl = Tl + (int64_t)i * ld;
@@ -595,16 +596,26 @@ __global__ void __launch_bounds__(256)
         sq = fmaf(df, df, sq);
       }
       kv = kval<float>(kind, sq, s2);
-      const float v = (gi == gj) ? (float)(((double)kv + jitter) + sd * sd) : kv;
-      const float vh = tf32_rna_f(v);
-      A[(int64_t)gi * lda + gj] = v;
+      const float vh = tf32_rna_f(kv);
+      A[(int64_t)gi * lda + gj] = kv;
       Ah[(int64_t)gi * lda + gj] = vh;
-      Al[(int64_t)gi * lda + gj] = tf32_rna_f(v - vh);
+      Al[(int64_t)gi * lda + gj] = tf32_rna_f(kv - vh);
     }
     st[r][c] = kv;
   }
   __syncthreads();
   if (I == J) {
+    // the diagonal gets (K + jitter) + obs_stddev^2, summed in float64 once
+    // per element (inside the loop above the float64 arithmetic of a select
+    // ran for every element and made this kernel float64-pipe bound)
+    if (threadIdx.x < SG_T && i0 + threadIdx.x < n) {
+      const int gi = i0 + threadIdx.x;
+      const float v = (float)(((double)st[threadIdx.x][threadIdx.x] + jitter) + sd * sd);
+      const float vh = tf32_rna_f(v);
+      A[(int64_t)gi * lda + gi] = v;
+      Ah[(int64_t)gi * lda + gi] = vh;
+      Al[(int64_t)gi * lda + gi] = tf32_rna_f(v - vh);
+    }
     for (int e = threadIdx.x; e < SG_T * SG_T; e += blockDim.x) {
       const int rr = e / SG_T, cc = e % SG_T;  // element (i0 + cc, j0 + rr) -> (j0 + rr, i0 + cc)
       const int gi = i0 + cc, gjj = j0 + rr;
@@ -630,11 +641,8 @@ __global__ void __launch_bounds__(256)
                           double* __restrict__ cbuf) {
   __shared__ float sa_row[RU_T], sa_col[RU_T];
   __shared__ float cpart[8][RU_T];
-  const int t = blockIdx.x;
-  int L = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
-  while (L * (L + 1) / 2 > t) --L;
-  while ((L + 1) * (L + 2) / 2 <= t) ++L;
-  const int I = t - L * (L + 1) / 2, J = L;  // upper tile (I, J), I <= J
+  int J, I;
+  tri_index(blockIdx.x, J, I);  // upper tile (I, J), I <= J
   const int i0 = I * RU_T, j0 = J * RU_T;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int e = threadIdx.x; e < RU_T; e += blockDim.x) {

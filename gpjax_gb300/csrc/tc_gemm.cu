@@ -492,14 +492,22 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     }
     if (MODE == MODE_ADD_F32 || MODE == MODE_STORE_SPLIT) {
       // dtrack: sum of squares of this row's outputs (float64)
+      // in float-float (exact squares by FMA, Knuth's two-sum), not float64:
+      // per-element float64 arithmetic here ran at this part's float64 rate
       if (MODE == MODE_STORE_SPLIT && p.dtrack && have && gi < p.M) {
-        double dsum = 0.0;
+        float sh = 0.f, sl = 0.f;
 #pragma unroll
         for (int c = 0; c < HC; ++c) {
-          const float w = p.alpha * acc[c];
-          if (j0 + hcol + c < p.N) dsum += (double)w * (double)w;
+          const float w = (j0 + hcol + c < p.N) ? p.alpha * acc[c] : 0.f;
+          const float q = __fmul_rn(w, w);
+          const float qe = fmaf(w, w, -q);  // q + qe = w^2 exactly
+          const float t = __fadd_rn(sh, q);
+          const float bb = __fsub_rn(t, sh);
+          const float te = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bb)), __fsub_rn(q, bb));
+          sh = t;
+          sl = __fadd_rn(sl, __fadd_rn(te, qe));
         }
-        atomicAdd(&p.dtrack[p.c_row0 + (int64_t)z * p.c_zrow + gi], -dsum);
+        atomicAdd(&p.dtrack[p.c_row0 + (int64_t)z * p.c_zrow + gi], -((double)sh + (double)sl));
       }
       // stage the tile, then write whole rows (coalesced, 4 floats per lane)
       asm volatile("bar.sync 1, %0;" ::"r"(EPI_THREADS) : "memory");  // ring is free
@@ -663,11 +671,19 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             const float df = xi[kk] - gx[c * DM + kk];
             pl[kk] = fmaf(cc, df * df, pl[kk]);
           }
-          if (gi == gj) gnoise += (double)ai * (double)ai - (double)w;
         }
 #pragma unroll
         for (int kk = 0; kk < DM; ++kk) gl[kk] += (double)pl[kk];
         gvar += (double)pvar;
+      }
+      // the diagonal's noise term, outside the column loop (float64 there
+      // would run for every element of an if-converted branch)
+      {
+        const int cd = gi - j0;  // this row's diagonal column within the tile
+        if (have && gi < p.n_true && cd >= hcol && cd < hcol + HC) {
+          const float w = otile[r * GLD + cd];
+          gnoise = (double)ai * (double)ai - (double)w;
+        }
       }
       // reduce over the 4 epilogue warps into gpart[tile]
       const int slots = p.d + 2;
