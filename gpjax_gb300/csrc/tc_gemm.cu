@@ -165,6 +165,15 @@ __device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, uint32_t (&r)[3
       : "r"(taddr));
 }
 
+// float-float accumulation (hi, lo) += a with the rounding error of the
+// addition kept (Knuth's two-sum); the _rn forms keep it from being contracted
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float a) {
+  const float s = __fadd_rn(hi, a);
+  const float bb = __fsub_rn(s, hi);
+  lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(a, bb)));
+  hi = s;
+}
+
 __device__ __forceinline__ float tf32_rna(float x) {
   uint32_t r;
   asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
@@ -638,10 +647,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       for (int k = 0; k < DM; ++k)
         xi[k] = (gi < p.n_true && k < p.d) ? p.xs[(int64_t)gi * p.d + k] : 0.f;
       const float ai = (p.avec && gi < p.n_true) ? (float)p.avec[gi] : 0.f;  // null: -W terms only
-      double gl[DM];
+      // per-thread sums in float-float (float64 here ran at this part's float64 rate)
+      float glh[DM], gll[DM];
 #pragma unroll
-      for (int k = 0; k < DM; ++k) gl[k] = 0.0;
-      double gnoise = 0.0, gvar = 0.0;
+      for (int k = 0; k < DM; ++k) glh[k] = gll[k] = 0.f;
+      double gnoise = 0.0;
+      float gvh = 0.f, gvl = 0.f;
 #pragma unroll
       for (int cb = 0; cb < HC / 32; ++cb) {
         float pl[DM];
@@ -673,8 +684,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
           }
         }
 #pragma unroll
-        for (int kk = 0; kk < DM; ++kk) gl[kk] += (double)pl[kk];
-        gvar += (double)pvar;
+        for (int kk = 0; kk < DM; ++kk) ff_add(glh[kk], gll[kk], pl[kk]);
+        ff_add(gvh, gvl, pvar);
       }
       // the diagonal's noise term, outside the column loop (float64 there
       // would run for every element of an if-converted branch)
@@ -693,9 +704,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
           val = 0.0;
 #pragma unroll
           for (int kk = 0; kk < DM; ++kk)
-            if (kk == sidx) val = gl[kk];
+            if (kk == sidx) val = (double)glh[kk] + (double)gll[kk];
         } else if (sidx == p.d) {
-          val = gvar;
+          val = (double)gvh + (double)gvl;
         } else {
           val = gnoise;
         }
@@ -726,10 +737,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 #pragma unroll
       for (int k = 0; k < DM; ++k) zi[k] = (row_ok && k < p.d) ? p.zs[(int64_t)gi * p.d + k] : 0.f;
       const float ai = row_ok ? (float)p.avec[gi] : 0.f;
-      double gl[DM], gz[DM];
+      float glh[DM], gll[DM], gzh[DM], gzl[DM];  // float-float sums
 #pragma unroll
-      for (int k = 0; k < DM; ++k) gl[k] = gz[k] = 0.0;
-      double gvar = 0.0;
+      for (int k = 0; k < DM; ++k) glh[k] = gll[k] = gzh[k] = gzl[k] = 0.f;
+      float gvh = 0.f, gvl = 0.f;
 #pragma unroll 1
       for (int cb = 0; cb < HC / 32; ++cb) {
         float pl[DM], pz[DM];
@@ -761,25 +772,25 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         }
 #pragma unroll
         for (int kk = 0; kk < DM; ++kk) {
-          gl[kk] += (double)pl[kk];
-          gz[kk] += (double)pz[kk];
+          ff_add(glh[kk], gll[kk], pl[kk]);
+          ff_add(gzh[kk], gzl[kk], pz[kk]);
         }
-        gvar += (double)pvar;
+        ff_add(gvh, gvl, pvar);
       }
       // per-row z partials: the two threads of a row combine in a fixed order
       if (hcol != 0) {
 #pragma unroll
-        for (int kk = 0; kk < DM; ++kk) zrow[r * DM + kk] = gz[kk];
+        for (int kk = 0; kk < DM; ++kk) zrow[r * DM + kk] = (double)gzh[kk] + (double)gzl[kk];
       }
       // theta partials: reduce over the epilogue warps into gpart[tile]
       const int slots = p.d + 1;
       for (int sidx = 0; sidx < slots; ++sidx) {
-        double val = gvar;
+        double val = (double)gvh + (double)gvl;
         if (sidx < p.d) {
           val = 0.0;
 #pragma unroll
           for (int kk = 0; kk < DM; ++kk)
-            if (kk == sidx) val = gl[kk];
+            if (kk == sidx) val = (double)glh[kk] + (double)gll[kk];
         }
         val = warp_sum(val);
         if (lane == 0) gred[sidx * EPI_WARPS + ew] = val;
@@ -789,7 +800,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         double* zp = p.zpart + ((int64_t)z * p.tiles_n + J) * (int64_t)p.M * p.d + (int64_t)gi * p.d;
 #pragma unroll
         for (int kk = 0; kk < DM; ++kk)
-          if (kk < p.d) zp[kk] = row_ok ? gz[kk] + zrow[r * DM + kk] : 0.0;
+          if (kk < p.d) zp[kk] = row_ok ? ((double)gzh[kk] + (double)gzl[kk]) + zrow[r * DM + kk] : 0.0;
       }
       const int tile_id = blockIdx.x + (int)gridDim.x * z;
       for (int sidx = et; sidx < slots; sidx += EPI_THREADS) {
