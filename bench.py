@@ -228,20 +228,59 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------------------
+# Replicas: the multi-GPU path (one process per GPU, no data-path collective)
+# ---------------------------------------------------------------------------
+class Replicas:
+    """Host side of an N-GPU run of independent replicas: reads RANK /
+    WORLD_SIZE / LOCAL_RANK, joins the process group for N > 1, and provides the
+    barrier and the max-over-ranks time; the whole-job value is N x steps over
+    that time.  The backend is NCCL on GPUs (gloo in the CPU tests)."""
+
+    def __init__(self, backend: str):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group(backend)
+
+    def barrier(self, device=None):
+        import torch
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        if device is not None and device.type == "cuda":
+            torch.cuda.synchronize(device)
+
+    def max(self, v: float, device) -> float:
+        if self.world == 1:
+            return v
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([v], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def value(self, steps: int, seconds: float) -> float:
+        return self.world * steps / seconds
+
+    def close(self):
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
 # GPU leg
 # ---------------------------------------------------------------------------
 def run_gpu(args):
     import torch
-    import torch.distributed as dist
 
     import gpjax_gb300 as gpx
     from gpjax_gb300 import _lib
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        dist.init_process_group("nccl")
+    reps = Replicas("nccl")
+    world, rank, local = reps.world, reps.rank, reps.local
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     lib = _lib.lib()
@@ -270,16 +309,10 @@ def run_gpu(args):
                   info.data_ptr(), ws.data_ptr(), ws.numel(), stream.cuda_stream)
 
     def barrier():
-        if world > 1:
-            dist.barrier()
-        torch.cuda.synchronize(dev)
+        reps.barrier(dev)
 
     def max_over_ranks(v):
-        if world == 1:
-            return v
-        t = torch.tensor([v], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return reps.max(v, dev)
 
     # ---- plain FP64 form (reference precision) ----
     fp64 = None
@@ -369,8 +402,7 @@ def run_gpu(args):
     d2h = r.numel() * 8
 
     if rank != 0:
-        if world > 1:
-            dist.destroy_process_group()
+        reps.close()
         return
 
     peaks, peak_kind = measured_peaks()
@@ -387,7 +419,7 @@ def run_gpu(args):
                   "rel_err": [float(abs(a - b) / max(abs(b), 1e-300))
                               for a, b in zip(g_mixed, g64)]}
                  if g64 is not None else None)
-    value = world * args.steps / t_dev
+    value = reps.value(args.steps, t_dev)
     line = {
         "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev / args.steps,
@@ -411,7 +443,7 @@ def run_gpu(args):
         "rel_err_mll_vs_fp64": rel_mll, "rel_err_grad_vs_fp64": rel_grad,
         "grad_components": grad_comp,
         "mll": mll_mixed,
-        "e2e": {"value": world * args.steps / t_e2e, "unit": "evals/s",
+        "e2e": {"value": reps.value(args.steps, t_e2e), "unit": "evals/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "path": "gpjax_gb300.objectives.conjugate_mll(...).backward() from pinned host X, y"},
         "gpu_launches": int(launches),
@@ -419,8 +451,7 @@ def run_gpu(args):
         "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)
-    if world > 1:
-        dist.destroy_process_group()
+    reps.close()
 
 
 def ctypes_void_array(k):
