@@ -710,18 +710,13 @@ __global__ void __launch_bounds__(256)
   out_grad[n_ls + 2] = inf ? nan : ds / s - pg1 / (s * s);
 }
 
-// Copies the lower triangle of up to three symmetric m x m matrices into
-// their upper triangles.
-__global__ void sg_mirror3(int m, int64_t ld, double* __restrict__ a, double* __restrict__ b,
-                           double* __restrict__ c) {
+// Copies the lower triangle of a symmetric m x m matrix into its upper one.
+__global__ void sg_mirror(int m, int64_t ld, double* __restrict__ a) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= (int64_t)m * m) return;
   const int i = (int)(e / m), j = (int)(e % m);
   if (j <= i) return;
-  const int64_t up = (int64_t)i * ld + j, lo = (int64_t)j * ld + i;
-  a[up] = a[lo];
-  b[up] = b[lo];
-  if (c) c[up] = c[lo];
+  a[(int64_t)i * ld + j] = a[(int64_t)j * ld + i];
 }
 
 __global__ void sg_zero(double* p, int count) {
@@ -801,7 +796,7 @@ gpk_status sgpr_run(int kind, int n, int m, int d, const double* x, int64_t ldx,
     p.alpha = 1.0;
     p.beta = 0.0;
     GPK_CUDA_TRY(gemm_nt<double>(p, 1, ss));
-    sg_mirror3<<<mgrid, 256, 0, ss>>>(m, ldm, b.Kinv, b.Kinv, nullptr);
+    sg_mirror<<<mgrid, 256, 0, ss>>>(m, ldm, b.Kinv);
     GPK_LAUNCH_CHECK();
   }
   GPK_CUDA_TRY(cudaEventRecord(side->join, ss));
@@ -889,7 +884,7 @@ gpk_status sgpr_run(int kind, int n, int m, int d, const double* x, int64_t ldx,
     p.alpha = 1.0;
     p.beta = 0.0;
     GPK_CUDA_TRY(gemm_nt<double>(p, 1, s));
-    sg_mirror3<<<mgrid, 256, 0, s>>>(m, ldm, b.Suinv, b.Suinv, nullptr);
+    sg_mirror<<<mgrid, 256, 0, s>>>(m, ldm, b.Suinv);
     GPK_LAUNCH_CHECK();
     // T1 = K^-1 P ; KPK = T1 K^-1 (symmetric operands: NT form; KPK is
     // symmetric, so its lower triangle is formed and mirrored)
@@ -908,7 +903,7 @@ gpk_status sgpr_run(int kind, int n, int m, int d, const double* x, int64_t ldx,
     q.C = b.KPK;
     q.c_lower = 1;
     GPK_CUDA_TRY(gemm_nt<double>(q, 1, s));
-    sg_mirror3<<<mgrid, 256, 0, s>>>(m, ldm, b.KPK, b.KPK, nullptr);
+    sg_mirror<<<mgrid, 256, 0, s>>>(m, ldm, b.KPK);
     GPK_LAUNCH_CHECK();
   }
   GPK_CUDA_TRY(gemv_dense<double>(b.Suinv, ldm, m, m, b.cv, b.gam, s));
