@@ -188,7 +188,7 @@ __device__ __forceinline__ void split_tf32(float x, float& hi, float& lo) {
 // ---------------------------------------------------------------------------
 // The kernel
 // ---------------------------------------------------------------------------
-// Three tile shapes (TS).  Narrow (0): 128 x 128 outputs, 32-wide K slices in
+// Four tile shapes (TS).  Narrow (0): 128 x 128 outputs, 32-wide K slices in
 // 128B swizzle, 3 stages of 64 KB, 4 accumulator buffers of 128 TMEM
 // columns.  Wide (1, large GEMMs): 128 x 256 outputs, 16-wide K slices in 64B
 // swizzle, 4 stages of 48 KB, 2 buffers of 256 columns: a quarter fewer

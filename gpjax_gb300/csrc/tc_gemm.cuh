@@ -6,15 +6,17 @@
 // remainder (both stored as float32 bit patterns with zero low 13 bits), which
 // recovers float32-class products on the TF32 pipe.  One tile shape takes the
 // same split in float16 instead (same 11-bit significand, twice the MMA rate,
-// half the operand bytes), on operands whose rows were scaled by powers of two
-// into float16's range; the epilogue undoes the scales exactly.  Operands are staged by
-// TMA (swizzled) into a shared-memory ring, one elected thread issues
-// tcgen05.mma into float32 accumulators in tensor memory, and eight epilogue
-// warps read them back with tcgen05.ld and apply a fused epilogue (trailing
-// update, split store with optional transpose, or the MLL adjoint reduction).
-// Three tile shapes (128 x 128; 128 x 256 for large problems; 128 x 64 where
-// few tiles would leave SMs idle) share the code.  Every mbarrier wait is bounded: on timeout the CTA sets an error
-// flag, drains its own copies and returns.
+// half the operand bytes), on operands whose rows were scaled by powers of
+// two into float16's range; the epilogue undoes the scales exactly.  Operands
+// are staged by TMA (swizzled) into a shared-memory ring, one elected thread
+// issues tcgen05.mma into float32 accumulators in tensor memory, and eight
+// epilogue warps read them back with tcgen05.ld and apply a fused epilogue
+// (trailing update, split store with optional transpose, the MLL adjoint
+// reduction or the SGPR adjoint reduction).  Four tile shapes (128 x 128;
+// 128 x 256 for large problems; 128 x 64 where few tiles would leave SMs idle;
+// 128 x 256 on float16 operands) share the code.  Every mbarrier wait is
+// bounded: on timeout the CTA sets an error flag, drains its own copies and
+// returns.
 #pragma once
 #include <cuda.h>
 #include "gpk_internal.cuh"
