@@ -32,11 +32,11 @@ WORKLOAD = ("exact GP conjugate_mll + gradient, Matern-5/2 ARD, n=16384, d=8, X~
             "lengthscales log-U[0.3,3], variance 1, noise 1e-2, y = prior sample + noise")
 PEAK_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
 # dram__bytes_read.sum + dram__bytes_write.sum of one adjoint GEMM launch
-# (tc_gemm_kernel<MODE_GRAD>) on this workload at full size, n = 16384: 8.98 GB
-# read + 4.54 MB written, from a one-pass ncu capture summarised in
-# profiles/tc_gemm_grad_dram_n16384.txt.  The algorithmic operand volume is
-# 1.07 GB (the upper triangle of V in TF32 hi/lo): tiles of one L2-resident
-# group share panels, the groups re-read them.
+# (tc_gemm_kernel<MODE_GRAD, float16 wide>) on this workload at full size,
+# n = 16384: 3.68 GB read + 41.1 MB written, from a one-pass ncu capture
+# summarised in profiles/tc_gemm_grad_dram_n16384.txt.  The algorithmic operand
+# volume is 0.54 GB (the upper triangle of V in float16 hi/lo): tiles of one
+# L2-resident group share panels, the groups re-read them.
 ADJOINT_TRAFFIC_BYTES_N16384 = 3.68e9 + 41.1e6
 
 

@@ -12,7 +12,10 @@
 //
 // Every product is one split-TF32 NT GEMM (tc_gemm.cu) reading K-contiguous
 // operands: L (rows), M = L^-1 and V = M^T are each kept row-major as TF32
-// hi/lo pairs.  Recursion leaves are 128 x 128 diagonal blocks factored and
+// hi/lo pairs.  The products of the wide nodes (both halves >= 2048) and the
+// adjoint run as split-float16 GEMMs instead, on float16 hi/lo copies of their
+// operands scaled row by row by powers of two (the epilogues undo the scales
+// exactly): the same 11-bit significand at twice the MMA rate.  Recursion leaves are 128 x 128 diagonal blocks factored and
 // inverted by one CTA in float32, with pivots from a float64 diagonal track
 // (decremented by every L21 product; carried as float-float pairs inside the
 // leaf).  n is padded to a multiple of
