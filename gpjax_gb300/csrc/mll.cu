@@ -515,6 +515,7 @@ extern "C" gpk_status gpk_conjugate_mll_batched(
 extern "C" gpk_status gpk_lower_cholesky(int64_t n, int dtype, void* A, int64_t lda,
                                          double* logdiag, int* info, cudaStream_t stream) {
   if (n < 0 || n > (1 << 20) || lda < n || !info) return GPK_ERR_BAD_ARG;
+  if (dtype != GPK_F64 && dtype != GPK_F32) return GPK_ERR_BAD_ARG;  // before any device work
   if (n == 0) {
     zero_outputs_kernel<<<1, 1, 0, stream>>>(nullptr, nullptr, 0, info);
     GPK_LAUNCH_CHECK();

@@ -122,3 +122,110 @@ def test_batched_mll_rejects_bad_arguments(built_lib):
     # null per-instance arrays are refused before any device work
     assert lib.gpk_conjugate_mll_batched(1, None, n, d, *nul, 1e-6, 1, None, None, None, None,
                                          0, None) == 1
+
+
+# ---------------------------------------------------------------------------
+# Argument checks of the remaining entry points: every case below is refused
+# on the host before any device work (fake pointers are never dereferenced)
+# ---------------------------------------------------------------------------
+_P = ctypes.c_void_p(0x1000)
+
+
+def test_kernel_entry_points_reject_bad_arguments(built_lib):
+    from gpjax_gb300 import _lib
+    lib = _lib.lib()
+    # gram / diagonal: unknown kernel, ldx < d, n_ls neither 1 nor d, null output
+    assert lib.gpk_gram(9, 4, 2, _P, 2, _P, 1, 0, _P, 4, None) == 1
+    assert lib.gpk_gram(0, 4, 2, _P, 1, _P, 1, 0, _P, 4, None) == 1
+    assert lib.gpk_gram(0, 4, 3, _P, 3, _P, 2, 0, _P, 4, None) == 1
+    assert lib.gpk_gram(0, 4, 2, _P, 2, _P, 1, 0, None, 4, None) == 1
+    assert lib.gpk_gram(0, 0, 2, None, 2, None, 1, 0, None, 0, None) == 0  # empty: no work
+    assert lib.gpk_diagonal(0, 4, 2, _P, 1, _P, 1, _P, None) == 1
+    assert lib.gpk_diagonal(0, 4, 2, None, 2, _P, 1, _P, None) == 1
+    # cross-covariance cotangent: m < 0, ldy < d, missing outputs, small workspace
+    ws = lib.gpk_cross_covariance_vjp_workspace_bytes(5, 6, 2)
+    assert ws > 0
+    assert lib.gpk_cross_covariance_vjp(0, 5, -1, 2, _P, 2, _P, 2, _P, 1, _P, 6, _P, None, None,
+                                        _P, ws, None) == 1
+    assert lib.gpk_cross_covariance_vjp(0, 5, 6, 2, _P, 2, _P, 1, _P, 1, _P, 6, _P, None, None,
+                                        _P, ws, None) == 1
+    assert lib.gpk_cross_covariance_vjp(0, 5, 6, 2, _P, 2, _P, 2, _P, 1, _P, 6, None, None,
+                                        None, _P, ws, None) == 1
+    assert lib.gpk_cross_covariance_vjp(0, 5, 6, 2, _P, 2, _P, 2, _P, 1, _P, 6, _P, None, None,
+                                        _P, 8, None) == 3
+
+
+def test_linalg_entry_points_reject_bad_arguments(built_lib):
+    from gpjax_gb300 import _lib
+    lib = _lib.lib()
+    info = _P
+    assert lib.gpk_lower_cholesky(-1, _lib.F64, _P, 4, None, info, None) == 1
+    assert lib.gpk_lower_cholesky(8, _lib.F64, _P, 4, None, info, None) == 1   # lda < n
+    assert lib.gpk_lower_cholesky(8, _lib.F64, _P, 8, None, None, None) == 1   # info missing
+    assert lib.gpk_lower_cholesky(8, 7, _P, 8, None, info, None) == 1          # unknown dtype
+    ws = lib.gpk_solve_triangular_workspace_bytes(8, 3, _lib.F64)
+    assert lib.gpk_solve_triangular(8, 3, _lib.F64, _P, 8, _P, 2, _P, ws, None) == 1  # ldb < nrhs
+    assert lib.gpk_solve_triangular(8, 3, _lib.F64, _P, 8, _P, 3, _P, 8, None) == 3
+    assert lib.gpk_solve_triangular(8, 3, 7, _P, 8, _P, 3, _P, ws, None) == 1
+    assert lib.gpk_solve_triangular(0, 3, _lib.F64, None, 0, None, 3, None, 0, None) == 0
+    assert lib.gpk_logdet_triangular(8, _lib.F64, None, 8, _P, None) == 1
+    assert lib.gpk_logdet_triangular(8, _lib.F64, _P, 4, _P, None) == 1
+    assert lib.gpk_logdet_triangular(8, 7, _P, 8, _P, None) == 1
+
+
+def test_objective_entry_points_reject_bad_arguments(built_lib):
+    from gpjax_gb300 import _lib
+    lib = _lib.lib()
+    # collapsed ELBO: (kind, n, m, d, x, ldx, y, z, ldz, theta, n_ls, jitter, precision,
+    # want_grad, out_elbo, out_grad, out_grad_z, info, workspace, workspace_bytes, stream)
+    ws = lib.gpk_collapsed_elbo_workspace_bytes(100, 10, 2, _lib.PREC_MIXED)
+    ok = [0, 100, 10, 2, _P, 2, _P, _P, 2, _P, 1, 1e-6, _lib.PREC_MIXED, 1, _P, _P, _P, _P, _P,
+          ws, None]
+
+    def elbo(**kw):
+        a = list(ok)
+        for k, v in kw.items():
+            a[int(k[1:])] = v
+        return lib.gpk_collapsed_elbo(*a)
+
+    assert elbo(a0=7) == 1                # unknown kernel
+    assert elbo(a2=20000) == 1            # m above the inducing-point bound
+    assert elbo(a3=17) == 1               # d above the SGPR input bound
+    assert elbo(a10=3) == 1               # n_ls neither 1 nor d
+    assert elbo(a12=5) == 1               # unknown precision
+    assert elbo(a15=None) == 1            # gradient wanted, no output
+    assert elbo(a19=16) == 3              # workspace too small
+    # predict: (kind, n, t, d, x, ldx, y, xt, ldxt, theta, n_ls, jitter, prior_jitter,
+    # precision, mean, var, cov, ldcov, info, workspace, workspace_bytes, stream)
+    pws = lib.gpk_predict_workspace_bytes(50, 5, 2, _lib.PREC_FP64)
+    assert lib.gpk_predict(0, 0, 5, 2, _P, 2, _P, _P, 2, _P, 1, 1e-6, 1e-6, 0, _P, _P, None, 0,
+                           _P, _P, pws, None) == 1                       # n = 0
+    assert lib.gpk_predict(0, 50, 5, 2, _P, 2, _P, _P, 1, _P, 1, 1e-6, 1e-6, 0, _P, _P, None, 0,
+                           _P, _P, pws, None) == 1                       # ldxt < d
+    assert lib.gpk_predict(0, 50, 5, 2, _P, 2, _P, _P, 2, _P, 1, 1e-6, 1e-6, 0, _P, _P, _P, 3,
+                           _P, _P, pws, None) == 1                       # ldcov < t
+    assert lib.gpk_predict(0, 50, 0, 2, None, 2, None, None, 2, None, 1, 1e-6, 1e-6, 0, None,
+                           None, None, 0, None, None, 0, None) == 0      # t = 0: no work
+    # the allocation-free MLL: sizes past its static scratch are unsupported
+    big = lib.gpk_conjugate_mll_noalloc_max_n() + 1
+    assert lib.gpk_conjugate_mll_noalloc(0, big, 2, _P, 2, _P, _P, 1, 1e-6, 1, _P, _P, _P,
+                                         None) == 6
+    assert lib.gpk_conjugate_mll_noalloc(0, 10, 2, _P, 2, _P, None, 1, 1e-6, 1, _P, _P, _P,
+                                         None) == 1
+
+
+def test_gemm_entry_point_rejects_bad_arguments(built_lib):
+    from gpjax_gb300 import _lib
+    lib = _lib.lib()
+    ws = lib.gpk_gemm_tf32x3_workspace_bytes(64, 64, 32)
+    # (M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lower_only, err_flag, workspace, bytes, stream)
+    assert lib.gpk_gemm_tf32x3(-1, 64, 32, 1.0, _P, 32, _P, 32, 0.0, _P, 64, 0, None, _P, ws,
+                               None) == 1
+    assert lib.gpk_gemm_tf32x3(64, 64, 32, 1.0, _P, 16, _P, 32, 0.0, _P, 64, 0, None, _P, ws,
+                               None) == 1                                  # lda < K
+    assert lib.gpk_gemm_tf32x3(64, 48, 32, 1.0, _P, 32, _P, 32, 0.0, _P, 64, 1, None, _P, ws,
+                               None) == 1                                  # lower_only, M != N
+    assert lib.gpk_gemm_tf32x3(64, 64, 32, 1.0, _P, 32, _P, 32, 0.0, _P, 64, 0, None, _P, 8,
+                               None) == 3
+    assert lib.gpk_gemm_tf32x3(0, 64, 32, 1.0, None, 32, None, 32, 0.0, None, 64, 0, None, None,
+                               0, None) == 0                               # empty product
