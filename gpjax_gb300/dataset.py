@@ -8,7 +8,14 @@ import torch
 
 
 class Dataset:
-    """Inputs X [n, d] and outputs y [n, q] as float64 CUDA tensors."""
+    """Inputs X [n, d] and outputs y [n, q] as float64 CUDA tensors.
+
+    As the reference's Dataset (gpjax/dataset.py:26-126): row counts must
+    agree, non-float64 inputs are converted with a warning, ``+`` stacks two
+    datasets (a side missing from either is None in the sum), and
+    ``is_supervised`` / ``is_unsupervised`` tell X-and-y from y-only data.
+    One extension: a 1-D X or y is taken as a single column.
+    """
 
     def __init__(self, X=None, y=None, device=None):
         dev = device if device is not None else (
@@ -27,19 +34,31 @@ class Dataset:
             if arr is not None and getattr(arr, "dtype", None) not in (np.float64, torch.float64):
                 warnings.warn(f"{name} is not of type float64; converted to float64", UserWarning)
 
+    def is_supervised(self) -> bool:
+        return self.X is not None and self.y is not None
+
+    def is_unsupervised(self) -> bool:
+        return self.X is None and self.y is not None
+
     @property
     def n(self) -> int:
-        return 0 if self.X is None else int(self.X.shape[0])
+        if self.X is not None:
+            return int(self.X.shape[0])
+        return 0 if self.y is None else int(self.y.shape[0])
 
     @property
     def in_dim(self) -> int:
         return int(self.X.shape[1])
 
     def __add__(self, other: "Dataset") -> "Dataset":
-        return Dataset(torch.cat([self.X, other.X]), torch.cat([self.y, other.y]))
+        X = torch.cat([self.X, other.X]) if self.X is not None and other.X is not None else None
+        y = torch.cat([self.y, other.y]) if self.y is not None and other.y is not None else None
+        dev = (X if X is not None else y).device if (X is not None or y is not None) else None
+        return Dataset(X=X, y=y, device=dev)
 
     def __repr__(self) -> str:
-        return f"Dataset(n={self.n}, X={tuple(self.X.shape)}, y={tuple(self.y.shape)})"
+        dim = self.in_dim if self.X is not None else 0
+        return f"Dataset(Number of observations: {self.n} - Input dimension: {dim})"
 
 
 def _to(a, dev) -> torch.Tensor:

@@ -1,0 +1,76 @@
+"""Host-side pieces of the Python layer, on CPU: the Dataset container and the
+parameter types behave as the reference's (gpjax/dataset.py:26-126,
+gpjax/parameters.py:69-146; behaviours restated from tests/test_dataset.py and
+tests/test_parameters.py of the reference), and the precision setting."""
+import numpy as np
+import pytest
+import torch
+
+import gpjax_gb300 as gpx
+from gpjax_gb300 import config, parameters
+
+
+@pytest.mark.parametrize("n", [1, 2, 10])
+@pytest.mark.parametrize("in_dim", [1, 2, 10])
+def test_dataset_shapes_and_kinds(n, in_dim):
+    x, y = np.ones((n, in_dim)), np.ones((n, 1))
+    D = gpx.Dataset(X=x, y=y, device="cpu")
+    assert D.n == n and D.in_dim == in_dim
+    assert repr(D) == f"Dataset(Number of observations: {n} - Input dimension: {in_dim})"
+    assert D.is_supervised() and not D.is_unsupervised()
+    U = gpx.Dataset(y=y, device="cpu")
+    assert U.is_unsupervised() and not U.is_supervised() and U.X is None
+    assert gpx.Dataset(X=x, device="cpu").y is None
+
+
+@pytest.mark.parametrize("n1,n2", [(1, 2), (10, 1)])
+def test_dataset_add_stacks_rows(n1, n2):
+    a = gpx.Dataset(X=np.ones((n1, 3)), y=np.ones((n1, 1)), device="cpu")
+    b = gpx.Dataset(X=2 * np.ones((n2, 3)), y=2 * np.ones((n2, 1)), device="cpu")
+    c = a + b
+    assert c.n == n1 + n2 and c.in_dim == 3
+    assert torch.equal(c.X[n1:], b.X) and torch.equal(c.y[:n1], a.y)
+    u = gpx.Dataset(y=np.ones((n1, 1)), device="cpu") + gpx.Dataset(y=np.ones((n2, 1)), device="cpu")
+    assert u.is_unsupervised() and u.n == n1 + n2
+
+
+def test_dataset_rejects_mismatched_rows():
+    with pytest.raises(ValueError, match="same number of rows"):
+        gpx.Dataset(X=np.ones((3, 2)), y=np.ones((4, 1)), device="cpu")
+
+
+@pytest.mark.parametrize("dx,dy,warns", [(np.float32, np.float64, 1), (np.float64, np.float32, 1),
+                                         (np.float32, np.float32, 2)])
+def test_dataset_warns_on_low_precision(dx, dy, warns):
+    with pytest.warns(UserWarning, match="not of type float64") as rec:
+        D = gpx.Dataset(X=np.ones((4, 2), dtype=dx), y=np.ones((4, 1), dtype=dy), device="cpu")
+    assert len(rec) == warns
+    assert D.X.dtype == torch.float64 and D.y.dtype == torch.float64
+
+
+def test_parameter_constraints():
+    assert parameters.PositiveReal(0.5).value.item() == 0.5
+    with pytest.raises(ValueError):
+        parameters.PositiveReal(0.0)
+    with pytest.raises(ValueError):
+        parameters.PositiveReal(np.array([1.0, -2.0]))
+    assert parameters.NonNegativeReal(0.0).value.item() == 0.0
+    with pytest.raises(ValueError):
+        parameters.NonNegativeReal(-1e-9)
+    assert parameters.Real(-3.0).value.item() == -3.0
+    p = parameters.PositiveReal(np.array([0.3, 2.0])).requires_grad_(True)
+    assert p.value.requires_grad and p.value.dtype == torch.float64 and p.tag == "positive"
+
+
+def test_softplus_inverse_round_trip():
+    x = torch.tensor([1e-3, 0.5, 3.0, 20.0], dtype=torch.float64)
+    y = parameters.softplus_inverse(x)
+    assert torch.allclose(torch.nn.functional.softplus(y), x, rtol=1e-12, atol=0)
+
+
+def test_precision_codes():
+    from gpjax_gb300 import _lib
+    assert config.precision_code("fp64") == _lib.PREC_FP64
+    assert config.precision_code("mixed") == _lib.PREC_MIXED
+    with pytest.raises(ValueError):
+        config.precision_code("bf16")
