@@ -229,3 +229,32 @@ def test_gemm_entry_point_rejects_bad_arguments(built_lib):
                                None) == 3
     assert lib.gpk_gemm_tf32x3(0, 64, 32, 1.0, None, 32, None, 32, 0.0, None, 64, 0, None, None,
                                0, None) == 0                               # empty product
+
+
+def test_header_is_plain_c_and_links(built_lib, tmp_path):
+    """include/gpk.h compiles as C (no C++ or torch types across the boundary),
+    and a C program links libgpk.so and calls its host-only entry points."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    cuda_inc = "/usr/local/cuda/include"
+    if gcc is None or not os.path.isdir(cuda_inc):
+        pytest.skip("gcc or the CUDA headers are not available")
+    src = tmp_path / "probe.c"
+    src.write_text(
+        '#include <stdio.h>\n#include <string.h>\n#include "gpk.h"\n'
+        "int main(void) {\n"
+        "  if (gpk_version() <= 0) return 1;\n"
+        "  if (strlen(gpk_status_string(GPK_ERR_BAD_ARG)) == 0) return 2;\n"
+        "  if (gpk_conjugate_mll(7, 10, 2, NULL, 2, NULL, NULL, 1, 1e-6, GPK_PREC_FP64, 1,\n"
+        "                        NULL, NULL, NULL, NULL, 0, NULL) != GPK_ERR_BAD_ARG) return 3;\n"
+        '  printf("ok %d\\n", gpk_version());\n'
+        "  return 0;\n}\n")
+    exe = tmp_path / "probe"
+    libdir = os.path.dirname(str(built_lib))
+    r = subprocess.run([gcc, "-std=c99", "-Wall", "-Werror", "-x", "c", str(src), "-o", str(exe),
+                        f"-I{os.path.join(ROOT, 'include')}", f"-I{cuda_inc}", f"-L{libdir}",
+                        "-lgpk", f"-Wl,-rpath,{libdir}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    run = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert run.returncode == 0 and run.stdout.startswith("ok"), (run.returncode, run.stderr)
