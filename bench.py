@@ -174,12 +174,12 @@ def cpu_mll_grad_time(n, d, seed, threads):
 
 
 def pick_cpu_sample(n_full, d, seed, threads, budget_s):
-    t_small = cpu_mll_grad_time(1024, d, seed, threads)
-    n_s = 1024
+    n_s = min(1024, n_full)  # never a sample larger than the workload
+    t_small = cpu_mll_grad_time(n_s, d, seed, threads)
     for cand in (2048, 3072, 4096, 6144, 8192, 12288, 16384):
         if cand > n_full:
             break
-        if t_small * (cand / 1024.0) ** 3 <= budget_s:
+        if t_small * (cand / float(min(1024, n_full))) ** 3 <= budget_s:
             n_s = cand
     return n_s
 
