@@ -2,8 +2,9 @@
 
 ``default_precision`` selects the arithmetic of the objectives and predict:
 "fp64" computes every step in float64 (the reference's precision under
-jax_enable_x64); "mixed" uses the float32 Gram with split-TF32 tensor-core
-factorisation and float64 refinement.
+jax_enable_x64); "mixed" uses the float32 Gram with a tensor-core
+factorisation and adjoint (split-TF32, and split-float16 on row-scaled
+operands for the large products) and float64 refinement.
 """
 from __future__ import annotations
 
