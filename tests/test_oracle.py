@@ -112,3 +112,21 @@ def test_golden_fixtures_reproduce():
         val = O.conjugate_mll(kind, p("x"), p("y"), p("ls"), float(p("var")), float(p("sd")),
                               float(p("c")))
         assert np.isclose(val, float(p("mll")), rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("kind,nu", [(O.RBF, None), (O.MATERN32, 1.5), (O.MATERN52, 2.5)])
+@pytest.mark.parametrize("ard", [True, False])
+def test_kernel_values_match_an_independent_implementation(kind, nu, ard):
+    """The oracle's stationary kernels (kernels/stationary/rbf.py:40-44,
+    matern32.py:41-54, matern52.py:42-53 of the reference) against
+    scikit-learn's RBF / Matern on the same scaled Euclidean distance."""
+    gpk = pytest.importorskip("sklearn.gaussian_process.kernels")
+    rng = np.random.default_rng(7)
+    x, y = rng.standard_normal((40, 3)), rng.standard_normal((30, 3))
+    ls = np.array([0.4, 1.1, 2.5]) if ard else 0.8
+    var = 1.7
+    base = gpk.RBF(length_scale=ls) if nu is None else gpk.Matern(length_scale=ls, nu=nu)
+    ref = (gpk.ConstantKernel(var) * base)(x, y)
+    assert np.allclose(O.cross_covariance(kind, x, y, ls, var), ref, rtol=1e-12, atol=1e-14)
+    K = O.gram(kind, x, ls, var)
+    assert np.allclose(K, (gpk.ConstantKernel(var) * base)(x), rtol=1e-12, atol=1e-14)
