@@ -130,3 +130,29 @@ def test_kernel_values_match_an_independent_implementation(kind, nu, ard):
     assert np.allclose(O.cross_covariance(kind, x, y, ls, var), ref, rtol=1e-12, atol=1e-14)
     K = O.gram(kind, x, ls, var)
     assert np.allclose(K, (gpk.ConstantKernel(var) * base)(x), rtol=1e-12, atol=1e-14)
+
+
+@pytest.mark.parametrize("kind,nu", [(O.RBF, None), (O.MATERN32, 1.5), (O.MATERN52, 2.5)])
+def test_mll_matches_an_independent_implementation(kind, nu):
+    """The oracle's conjugate_mll and its gradient against scikit-learn's
+    Gaussian-process log marginal likelihood (zero mean, Sigma = var K +
+    (obs_stddev^2 + jitter) I); scikit-learn differentiates in log
+    hyperparameters, so d/dlog(l) = l d/dl and d/dlog(var) = var d/dvar."""
+    gpk = pytest.importorskip("sklearn.gaussian_process.kernels")
+    gpr_mod = pytest.importorskip("sklearn.gaussian_process")
+    rng = np.random.default_rng(11)
+    n, d = 60, 3
+    x = rng.uniform(-2, 2, size=(n, d))
+    y = (np.sin(x).sum(1) + 0.1 * rng.standard_normal(n))[:, None]
+    ls, var, sd, jitter = np.array([0.6, 1.3, 2.2]), 1.4, 0.3, 1e-6
+    base = gpk.RBF(length_scale=ls) if nu is None else gpk.Matern(length_scale=ls, nu=nu)
+    kern = gpk.ConstantKernel(var) * base
+    gpr = gpr_mod.GaussianProcessRegressor(kernel=kern, alpha=sd * sd + jitter, optimizer=None,
+                                           normalize_y=False).fit(x, y[:, 0])
+    lml, dlml = gpr.log_marginal_likelihood(gpr.kernel_.theta, eval_gradient=True)
+    val = O.conjugate_mll(kind, x, y, ls, var, sd, 0.0, jitter=jitter)
+    assert abs(val - lml) <= 1e-10 * abs(lml)
+    _, g = O.conjugate_mll_torch(kind, x, y, ls, var, sd, 0.0, lu=False)
+    # scikit-learn's theta: [log var, log l_1 .. log l_d]
+    assert np.isclose(dlml[0], var * g["variance"], rtol=1e-8)
+    assert np.allclose(dlml[1:], ls * np.asarray(g["lengthscale"]), rtol=1e-8)
