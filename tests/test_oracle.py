@@ -156,3 +156,25 @@ def test_mll_matches_an_independent_implementation(kind, nu):
     # scikit-learn's theta: [log var, log l_1 .. log l_d]
     assert np.isclose(dlml[0], var * g["variance"], rtol=1e-8)
     assert np.allclose(dlml[1:], ls * np.asarray(g["lengthscale"]), rtol=1e-8)
+
+
+@pytest.mark.parametrize("kind,nu", [(O.RBF, None), (O.MATERN52, 2.5)])
+def test_predict_matches_an_independent_implementation(kind, nu):
+    """The oracle's ConjugatePosterior.predict against scikit-learn's posterior
+    mean and covariance (alpha = obs_stddev^2 + posterior jitter; the oracle
+    adds the prior's jitter to the predictive covariance, gps.py:523)."""
+    gpk = pytest.importorskip("sklearn.gaussian_process.kernels")
+    gpr_mod = pytest.importorskip("sklearn.gaussian_process")
+    rng = np.random.default_rng(13)
+    x = rng.uniform(-2, 2, size=(80, 2))
+    y = (np.sin(2 * x).sum(1) + 0.1 * rng.standard_normal(80))[:, None]
+    t = rng.uniform(-2.5, 2.5, size=(25, 2))
+    ls, var, sd, jit, pjit = np.array([0.7, 1.2]), 1.1, 0.2, 1e-6, 1e-5
+    base = gpk.RBF(length_scale=ls) if nu is None else gpk.Matern(length_scale=ls, nu=nu)
+    gpr = gpr_mod.GaussianProcessRegressor(kernel=gpk.ConstantKernel(var) * base,
+                                           alpha=sd * sd + jit, optimizer=None,
+                                           normalize_y=False).fit(x, y[:, 0])
+    m_ref, c_ref = gpr.predict(t, return_cov=True)
+    mean, cov = O.predict(kind, x, y, t, ls, var, sd, 0.0, jitter=jit, prior_jitter=pjit)
+    assert np.allclose(mean, m_ref, rtol=1e-9, atol=1e-10)
+    assert np.allclose(cov - pjit * np.eye(len(t)), c_ref, rtol=1e-8, atol=1e-10)
