@@ -178,3 +178,26 @@ def test_predict_matches_an_independent_implementation(kind, nu):
     mean, cov = O.predict(kind, x, y, t, ls, var, sd, 0.0, jitter=jit, prior_jitter=pjit)
     assert np.allclose(mean, m_ref, rtol=1e-9, atol=1e-10)
     assert np.allclose(cov - pjit * np.eye(len(t)), c_ref, rtol=1e-8, atol=1e-10)
+
+
+@pytest.mark.parametrize("kind", [O.RBF, O.MATERN32, O.MATERN52])
+@pytest.mark.parametrize("m", [5, 25])
+def test_collapsed_elbo_matches_the_textbook_form(kind, m):
+    """The oracle follows the reference's op sequence (objectives.py:341-416:
+    A = Lz^-1 Kzx / sqrt(s), B = I + A A^T); here the same bound from its
+    closed form log N(y; mean, Q + s I) - tr(Kxx - Q) / (2 s), Q = Kxz Kzz^-1 Kzx,
+    evaluated densely -- an independent formula for the same quantity."""
+    rng = np.random.default_rng(m + kind)
+    n, d = 70, 2
+    x = rng.uniform(-2, 2, size=(n, d))
+    y = (np.sin(x).sum(1) + 0.1 * rng.standard_normal(n))[:, None]
+    z = x[rng.choice(n, m, replace=False)] + 0.05 * rng.standard_normal((m, d))
+    ls, var, sd, c, jit = np.array([0.8, 1.3]), 1.2, 0.3, 0.1, 1e-6
+    s = sd * sd
+    Kzz = O.gram(kind, z, ls, var) + jit * np.eye(m)
+    Kxz = O.cross_covariance(kind, x, z, ls, var)
+    Q = Kxz @ np.linalg.solve(Kzz, Kxz.T)
+    ref = scipy.stats.multivariate_normal(np.full(n, c), Q + s * np.eye(n)).logpdf(y[:, 0])
+    ref -= (np.sum(O.diagonal(kind, x, ls, var)) - np.trace(Q)) / (2 * s)
+    got = O.collapsed_elbo(kind, x, y, z, ls, var, sd, c, jitter=jit)
+    assert abs(got - ref) <= 1e-9 * abs(ref), (got, ref)
