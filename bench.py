@@ -460,7 +460,7 @@ def ctypes_void_array(k):
 
 
 def run_c3(args):
-    """Precision stress (SURVEY config C3): exact-GP MLL + gradient at n = 65536, d = 16,
+    """Precision stress (workload c3): exact-GP MLL + gradient at n = 65536, d = 16,
     RBF ARD, X ~ U[0,1]^16, lengthscales log-U[0.1, 1], variance 1, noise 1e-3,
     jitter 1e-6; mixed form timed over a few evaluations, the float64 form once as the
     accuracy reference.  y = sum_j sin(2 pi x_j) / 4 + N(0, 1e-3) (a smooth target in
@@ -525,7 +525,7 @@ def run_c3(args):
 
 
 def run_c5(args):
-    """SGPR (SURVEY config C5): collapsed ELBO + gradient (theta and Z), n = 1e6,
+    """SGPR (workload c5): collapsed ELBO + gradient (theta and Z), n = 1e6,
     m = 1024, d = 8; X a mixture of 16 Gaussians (means U[-5,5]^8, sd 0.5),
     y = sum_j sin(x_j) + N(0, 0.1^2), Z a random subset of X, RBF ARD with
     lengthscales log-U[0.5, 2]; mixed form against the float64 form."""
@@ -591,7 +591,7 @@ def run_c5(args):
 
 
 def c4_instances(count, seed):
-    """SURVEY config C4: n_i ~ U{64..2048}, d_i ~ U{2..10}, X ~ U[-1,1]^d, RBF or
+    """Batched GPs (workload c4): n_i ~ U{64..2048}, d_i ~ U{2..10}, X ~ U[-1,1]^d, RBF or
     Matern-3/2 with probability 1/2, ARD lengthscales log-U[0.1, 2], variance
     log-U[0.5, 2], noise log-U[1e-4, 1e-1]; y = a random-Fourier-feature prior
     sample (100 frequencies, cos and sin features) + N(0, 0.05^2)."""
