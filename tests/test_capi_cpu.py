@@ -258,3 +258,23 @@ def test_header_is_plain_c_and_links(built_lib, tmp_path):
     assert r.returncode == 0, r.stderr
     run = subprocess.run([str(exe)], capture_output=True, text=True)
     assert run.returncode == 0 and run.stdout.startswith("ok"), (run.returncode, run.stderr)
+
+
+def test_workspace_queries_grow_with_the_problem(built_lib):
+    """Layout sanity: every workspace query is monotone in the problem size
+    (the mixed MLL gains per-depth float16 operand copies from n = 4096 on)."""
+    from gpjax_gb300 import _lib
+    lib = _lib.lib()
+    for prec in (_lib.PREC_FP64, _lib.PREC_MIXED):
+        sizes = [lib.gpk_conjugate_mll_workspace_bytes(n, 8, prec)
+                 for n in (100, 128, 129, 1000, 2048, 4095, 4096, 4097, 8192, 16384)]
+        assert all(b >= a for a, b in zip(sizes, sizes[1:])), (prec, sizes)
+        el = [lib.gpk_collapsed_elbo_workspace_bytes(n, m, 4, prec)
+              for n, m in ((1000, 10), (1000, 100), (5000, 100), (9000, 100), (9000, 1024))]
+        assert all(b >= a for a, b in zip(el, el[1:])), (prec, el)
+        pr = [lib.gpk_predict_workspace_bytes(n, t, 4, prec)
+              for n, t in ((100, 10), (100, 100), (1000, 100), (4000, 512))]
+        assert all(b >= a for a, b in zip(pr, pr[1:])), (prec, pr)
+    # the float16 copies of the wide nodes: present from n_pad = 4096 (halves of 2048)
+    mixed = {n: lib.gpk_conjugate_mll_workspace_bytes(n, 8, _lib.PREC_MIXED) for n in (3968, 4096)}
+    assert mixed[4096] - mixed[3968] > 16 * 2048 * 2048
