@@ -74,3 +74,45 @@ def test_precision_codes():
     assert config.precision_code("mixed") == _lib.PREC_MIXED
     with pytest.raises(ValueError):
         config.precision_code("bf16")
+
+
+# structured operators: the reference's dispatch (linalg/operations.py:22-222)
+# answers these without a factorisation; restated from its tests/test_linalg.py
+from gpjax_gb300 import linalg as la  # noqa: E402
+
+
+def _t(v):
+    return torch.tensor(v, dtype=torch.float64)
+
+
+def test_structured_cholesky():
+    L = la.lower_cholesky(la.Diagonal(_t([1.0, 4.0, 9.0])))
+    assert isinstance(L, la.Diagonal) and torch.allclose(L.diagonal, _t([1.0, 2.0, 3.0]))
+    eye = la.Identity(4, device="cpu")
+    assert la.lower_cholesky(eye) is eye and eye.shape == (4, 4)
+
+
+def test_structured_solve():
+    b = _t([1.0, 2.0, 3.0])
+    assert torch.allclose(la.solve(la.Identity(3, device="cpu"), b), b)
+    x = la.solve(la.Diagonal(_t([2.0, 4.0, 5.0])), _t([2.0, 8.0, 10.0]))
+    assert torch.allclose(x, _t([1.0, 2.0, 2.0]))
+    X = la.solve(la.Diagonal(_t([2.0, 4.0])), _t([[2.0, 4.0], [8.0, 12.0]]))
+    assert X.shape == (2, 2) and torch.allclose(X, _t([[1.0, 2.0], [2.0, 3.0]]))
+
+
+def test_structured_logdet_and_diag():
+    assert float(la.logdet(la.Identity(3, device="cpu"))) == 0.0
+    d = _t([2.0, 3.0, 4.0])
+    assert torch.isclose(la.logdet(la.Diagonal(d)), torch.log(d).sum())
+    assert torch.allclose(la.diag(la.Identity(4, device="cpu")), torch.ones(4, dtype=torch.float64))
+    assert torch.equal(la.diag(la.Diagonal(d)), d)
+
+
+def test_add_jitter():
+    K = _t([[1.0, 0.5], [0.5, 2.0]])
+    J = la.add_jitter(K, 1e-3)
+    assert torch.allclose(J, K + 1e-3 * torch.eye(2, dtype=torch.float64))
+    assert torch.equal(K, _t([[1.0, 0.5], [0.5, 2.0]]))  # the input is not modified
+    with pytest.raises(ValueError):
+        la.add_jitter(_t([[1.0, 2.0, 3.0]]))
