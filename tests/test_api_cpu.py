@@ -116,3 +116,27 @@ def test_add_jitter():
     assert torch.equal(K, _t([[1.0, 0.5], [0.5, 2.0]]))  # the input is not modified
     with pytest.raises(ValueError):
         la.add_jitter(_t([[1.0, 2.0, 3.0]]))
+
+
+def test_theta_layout_and_model_parameters():
+    """The theta vector that crosses the C ABI is [lengthscale..., variance,
+    obs_stddev, mean constant] (include/gpk.h), and the posterior exposes its
+    trainable parameters by name as the reference's model state does."""
+    from gpjax_gb300.objectives import named_parameters
+    ls = np.array([0.5, 1.5, 2.5])
+    kern = gpx.kernels.Matern52(lengthscale=ls, variance=1.3)
+    assert kern.n_ls == 3 and kern.kind == 2
+    th = kern.theta_vector("cpu", torch.tensor(0.2, dtype=torch.float64),
+                           torch.tensor(0.7, dtype=torch.float64))
+    assert torch.allclose(th, _t([0.5, 1.5, 2.5, 1.3, 0.2, 0.7]))
+    iso = gpx.kernels.RBF(lengthscale=0.9, variance=1.0)
+    assert iso.n_ls == 1
+    assert torch.allclose(iso.theta_vector("cpu"), _t([0.9, 1.0, 0.0, 0.0]))
+    prior = gpx.gps.Prior(kernel=kern, mean_function=gpx.mean_functions.Constant(
+        gpx.parameters.Real(0.7)))
+    post = prior * gpx.likelihoods.Gaussian(num_datapoints=10, obs_stddev=0.2)
+    names = named_parameters(post)
+    assert any(k.endswith("lengthscale") for k in names)
+    assert any(k.endswith("variance") for k in names)
+    assert any(k.endswith("obs_stddev") for k in names)
+    assert any(k.endswith("constant") for k in names)
