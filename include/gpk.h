@@ -61,8 +61,10 @@ const char* gpk_status_string(int status);
  * gpk_launch_count: kernel launches issued by the library since it was loaded.
  * gpk_set_profile_events: when given >= 7 cudaEvent_t handles, each
  * gpk_conjugate_mll call records them on its stream at its phase boundaries
- * (0 start, 1 Gram built, 2 Cholesky done, 3 triangular inverse done,
- * 4 alpha solved and refined, 5 adjoint done, 6 end); NULL disables.
+ * (float64 form: 0 start, 1 Gram built, 2 Cholesky done, 3 triangular inverse
+ * done, 4 alpha solved and refined, 5 adjoint done, 6 end; mixed form: 0 start,
+ * 1 Gram built, 2 factor and inverse done, 3 alpha solved and refined,
+ * 4 adjoint done, 5 internal streams joined, 6 end); NULL disables.
  * Process-global and not thread-safe: meant for benchmarks. */
 long long gpk_launch_count(void);
 void gpk_set_profile_events(void* const* events, int count);
