@@ -46,8 +46,10 @@ typedef enum { GPK_RBF = 0, GPK_MATERN32 = 1, GPK_MATERN52 = 2 } gpk_kernel_kind
 typedef enum { GPK_F64 = 0, GPK_F32 = 1 } gpk_dtype;
 
 /* GPK_PREC_FP64: every step in float64.
- * GPK_PREC_MIXED: float32 Gram, split-TF32 tensor-core factorisation and
- * inversion with float32 accumulation, float64 residual refinement of
+ * GPK_PREC_MIXED: float32 Gram, tensor-core factorisation, inversion and
+ * adjoint with float32 accumulation -- split-TF32 products, and split-float16
+ * products on power-of-two row-scaled operand copies for the large ones (the
+ * same 11-bit significand split) -- float64 residual refinement of
  * alpha = Sigma^-1 (y - m), float64 log-det and gradient accumulation. */
 typedef enum { GPK_PREC_FP64 = 0, GPK_PREC_MIXED = 1 } gpk_precision;
 
