@@ -160,67 +160,76 @@ def measured_peaks():
 # ---------------------------------------------------------------------------
 # CPU leg: the float64 oracle (the reference's op sequence) on the host cores
 # ---------------------------------------------------------------------------
-def cpu_mll_grad_time(n, d, seed, threads):
-    """Seconds for one MLL + gradient of the oracle at size n (LU value and
-    torch float64 autograd gradient, the reference's slogdet/solve path)."""
-    import torch
-    from oracle import gp_oracle as O
-    torch.set_num_threads(threads)
+def c2_config(n, d, world=1):
+    """The workload description both arms print (identical dicts)."""
+    return {"workload": WORKLOAD if (n, d) == (16384, 8) else
+            WORKLOAD.replace("n=16384, d=8", f"n={n}, d={d}"),
+            "n": n, "d": d, "kernel": "Matern52",
+            "parallelism": "replicas" if world > 1 else "single",
+            "l2": "working set (3 x n^2 float32 = 3.2 GB) larger than L2; no flush"}
+
+
+def cpu_eval_setup(n, d, seed):
     x, ls, eps = c2_inputs(n, d, seed)
-    y = c2_y_host(x, ls, eps)
+    return x, ls, c2_y_host(x, ls, eps)
+
+
+def cpu_eval(x, y, ls):
+    """Seconds of one float64 MLL + gradient of the oracle port on the host: the
+    reference's op sequence (slogdet / solve through an LU factorisation, the
+    gradient as reverse-mode differentiation forms it), row-blocked, torch
+    threads."""
+    from oracle import gp_oracle as O
     t0 = time.perf_counter()
-    O.conjugate_mll_torch(O.MATERN52, x, y[:, None], ls, 1.0, 0.1, 0.0, lu=True)
+    O.conjugate_mll_grad_lu(O.MATERN52, x, y, ls, 1.0, 0.1, 0.0)
     return time.perf_counter() - t0
 
 
-def pick_cpu_sample(n_full, d, seed, threads, budget_s):
-    n_s = min(1024, n_full)  # never a sample larger than the workload
-    t_small = cpu_mll_grad_time(n_s, d, seed, threads)
-    for cand in (2048, 3072, 4096, 6144, 8192, 12288, 16384):
-        if cand > n_full:
-            break
-        if t_small * (cand / float(min(1024, n_full))) ** 3 <= budget_s:
-            n_s = cand
-    return n_s
-
-
-def cpu_baseline(n_full, d, seed, budget_s=20.0):
+def cpu_baseline(n_full, d, seed):
+    """One full-size evaluation (n = 16384: ~10-30 s of host work)."""
+    import torch
     threads = os.cpu_count() or 1
-    n_s = pick_cpu_sample(n_full, d, seed, threads, budget_s)
-    t = cpu_mll_grad_time(n_s, d, seed, threads)
-    scale = (n_s / n_full) ** 3
-    return {"value": scale / t, "unit": "evals/s", "cores": threads, "kind": "port",
-            "sample": (f"one float64 MLL+grad of the oracle port (LU slogdet/solve value, torch "
-                       f"float64 autograd gradient) at n={n_s} on the same generator, "
-                       f"{t:.2f} s, scaled by (n/{n_full})^3 to n={n_full}")}
+    torch.set_num_threads(threads)
+    x, ls, y = cpu_eval_setup(n_full, d, seed)
+    t = cpu_eval(x, y, ls)
+    return {"value": 1.0 / t, "unit": "evals/s", "cores": threads, "kind": "port",
+            "sample": (f"one float64 MLL+grad of the oracle port at the full workload (n={n_full}, "
+                       f"d={d}): Sigma assembly, one LU shared by slogdet and solve, Sigma^-1 "
+                       f"from the LU factors, gradient contraction; {t:.2f} s on {threads} "
+                       "host threads")}
 
 
 def run_reference(args):
+    """--impl reference: the reference's algorithm for this path (the float64
+    oracle port; JAX cannot be installed here) on the host cores, each timed
+    step one full-size MLL + gradient evaluation of the same workload.
+    Warm-up steps run the same evaluation at n = min(n, 2048) (thread pools
+    and allocator)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    import torch
     threads = os.cpu_count() or 1
-    budget = max(2.0, 150.0 / max(1, args.steps + args.warmup))
-    n_s = pick_cpu_sample(args.n, args.d, args.seed, threads, budget)
-    times = []
-    for i in range(args.warmup + args.steps):
-        t = cpu_mll_grad_time(n_s, args.d, args.seed, threads)
-        if i >= args.warmup:
-            times.append(t)
-    tot = sum(times)
-    scale = (n_s / args.n) ** 3
-    value = scale * args.steps / tot
+    torch.set_num_threads(threads)
+    nw = min(args.n, 2048)
+    xw, lw, yw = cpu_eval_setup(nw, args.d, args.seed)
+    for _ in range(args.warmup):
+        cpu_eval(xw, yw, lw)
+    x, ls, y = cpu_eval_setup(args.n, args.d, args.seed)
+    tot = 0.0
+    for _ in range(args.steps):
+        tot += cpu_eval(x, y, ls)
+    value = args.steps / tot
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "evals/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1000.0 * tot / args.steps / scale, "higher_is_better": True,
+        "ms_per_step": 1000.0 * tot / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n": args.n, "d": args.d, "kernel": "Matern52",
-                   "parallelism": "replicas"},
+        "config": c2_config(args.n, args.d),
         "cpu_baseline": {"value": value, "unit": "evals/s", "cores": threads, "kind": "port",
-                         "sample": (f"each step: one float64 MLL+grad of the oracle port at "
-                                    f"n={n_s} (LU slogdet/solve value, torch float64 autograd "
-                                    f"gradient), scaled by (n/{args.n})^3")},
+                         "sample": (f"each timed step: one float64 MLL+grad of the oracle port "
+                                    f"at the full workload (n={args.n}, d={args.d}); warm-up "
+                                    f"steps at n={nw}")},
         "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -406,10 +415,13 @@ def run_gpu(args):
         return
 
     peaks, peak_kind = measured_peaks()
-    flops_adjoint = n ** 3 / 3.0  # W = V V^T over the lower triangle
-    t_adj = phases["adjoint"] / 1000.0
-    achieved = flops_adjoint / t_adj / 1e12
     peak = float(peaks.get("bf16_tflops", PEAK_FALLBACK["bf16_tflops"]))
+    # the factor phase (the largest share of the step): Cholesky n^3/3 + inverse n^3/3
+    flops_factor = 2.0 * n ** 3 / 3.0
+    ach_factor = flops_factor / (phases["factor"] / 1000.0) / 1e12
+    # the adjoint: W = V V^T over the lower triangle, n^3/3
+    flops_adjoint = n ** 3 / 3.0
+    ach_adj = flops_adjoint / (phases["adjoint"] / 1000.0) / 1e12
     rel_mll = abs(mll_mixed - mll64) / abs(mll64) if mll64 is not None else None
     rel_grad = (float(np.linalg.norm(g_mixed - g64) / np.linalg.norm(g64))
                 if g64 is not None else None)
@@ -426,17 +438,24 @@ def run_gpu(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 Gram + tf32x3 factor + f16x3 adjoint + f64 refinement/accumulation",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n": n, "d": d, "kernel": "Matern52",
-                   "precision": "mixed", "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "working set (3 x n^2 float32 = 3.2 GB) larger than L2; no flush"},
+        "config": c2_config(n, d, world),
         "roofline": {"bound": "tensor",
-                     "kernel": "tc_gemm_kernel<MODE_GRAD, float16 wide> (W = L^-T L^-1 tiles "
-                               "contracted with dK/dtheta); timed with its float16 conversion of "
-                               "L^-T (the adjoint phase)",
-                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "peak_kind": f"{peak_kind} bf16 dense",
-                     "traffic": ADJOINT_TRAFFIC_BYTES_N16384,
-                     "algorithmic_flops_per_launch": flops_adjoint},
+                     "kernel": "factor phase: recursive Cholesky + inverse L^-1 (tc_gemm_kernel "
+                               "STORE_SPLIT / ADD_F32 products, leaf_chol_inv_kernel leaves, "
+                               "float16 operand conversions), timed with CUDA events on the "
+                               "library's stream at the phase boundaries",
+                     "achieved": ach_factor, "peak": peak, "unit": "TFLOP/s",
+                     "frac": ach_factor / peak, "peak_kind": f"{peak_kind} bf16 dense",
+                     "traffic": None, "algorithmic_flops_per_launch": flops_factor,
+                     "share_of_step": phases["factor"] / (1000.0 * t_dev / args.steps)},
+        "roofline_adjoint": {"bound": "tensor",
+                             "kernel": "tc_gemm_kernel<MODE_GRAD, float16 wide> (W = L^-T L^-1 "
+                                       "tiles contracted with dK/dtheta), timed with its float16 "
+                                       "conversion of L^-T (the adjoint phase)",
+                             "achieved": ach_adj, "peak": peak, "unit": "TFLOP/s",
+                             "frac": ach_adj / peak, "peak_kind": f"{peak_kind} bf16 dense",
+                             "traffic": ADJOINT_TRAFFIC_BYTES_N16384 if n == 16384 else None,
+                             "algorithmic_flops_per_launch": flops_adjoint},
         "phases_ms": phases,
         "fp64_form": fp64,
         "speedup_vs_fp64": (value / fp64["evals_per_s"]) if fp64 else None,

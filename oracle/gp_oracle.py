@@ -296,6 +296,86 @@ def conjugate_mll_torch(kind, X, y, ls, variance, obs_stddev, mean_const=0.0,
     return float(mll.detach()), grads
 
 
+def conjugate_mll_grad_lu(kind, X, y, ls, variance, obs_stddev, mean_const=0.0,
+                          jitter=DEFAULT_JITTER, block=1024):
+    """MLL and gradient by the reference's op sequence, lean enough for n = 16384.
+
+    Same quantities as ``conjugate_mll_torch(lu=True)`` without its n x n x d
+    autograd graph: Sigma is assembled row block by row block
+    (``dense.py:32-36``, ``objectives.py:100-103``); ``slogdet`` and ``solve``
+    (``operations.py:111,164``) read one LU factorisation -- the reference
+    issues the same LU twice, which XLA's common-subexpression pass merges under
+    ``jit`` -- and the gradient is what reverse-mode differentiation of that
+    sequence forms: the cotangent of Sigma, 1/2 (alpha alpha^T - Sigma^-1),
+    with Sigma^-1 from the LU factors (``solve`` against the identity, as the
+    transpose of ``slogdet``'s tangent), contracted block by block with
+    dK/dlengthscale and dK/dvariance, plus 2 obs_stddev tr(cotangent) and
+    sum(alpha) for the constant mean.  torch float64 on the host's threads.
+    Returns (value, dict of float64 numpy gradients) like conjugate_mll_torch.
+    """
+    torch = _torch()
+    Xt = torch.as_tensor(np.asarray(X, np.float64))
+    yt = torch.as_tensor(np.asarray(y, np.float64).reshape(-1))
+    n, d = Xt.shape
+    ls_v = np.broadcast_to(np.asarray(ls, np.float64), (d,)).copy()
+    xs = Xt / torch.as_tensor(ls_v)
+    s2, sd = float(variance), float(obs_stddev)
+    r3, r5 = math.sqrt(3.0), math.sqrt(5.0)
+
+    def sqdist(r0, r1):
+        sq = torch.zeros((r1 - r0, n), dtype=torch.float64)
+        for k in range(d):  # utils.py:53, one input dimension at a time
+            sq += (xs[r0:r1, k, None] - xs[None, :, k]) ** 2
+        return sq
+
+    def kval(sq):  # unit variance: rbf.py:43, matern32.py:48-53, matern52.py:46-52
+        if kind == RBF:
+            return torch.exp(-0.5 * sq)
+        tau = torch.sqrt(torch.clamp(sq, min=_FLOOR))
+        if kind == MATERN32:
+            return (1.0 + r3 * tau) * torch.exp(-r3 * tau)
+        return (1.0 + r5 * tau + 5.0 / 3.0 * tau * tau) * torch.exp(-r5 * tau)
+
+    def dcoef(sq):  # dk/dl_k = s2 * dcoef * (x_k - y_k)^2 / l_k^3 (zero below the floor)
+        if kind == RBF:
+            return torch.exp(-0.5 * sq)
+        tau = torch.sqrt(torch.clamp(sq, min=_FLOOR))
+        if kind == MATERN32:
+            c = 3.0 * torch.exp(-r3 * tau)
+        else:
+            c = 5.0 / 3.0 * (1.0 + r5 * tau) * torch.exp(-r5 * tau)
+        return torch.where(sq > _FLOOR, c, torch.zeros_like(c))
+
+    Sigma = torch.empty((n, n), dtype=torch.float64)
+    for r0 in range(0, n, block):
+        r1 = min(n, r0 + block)
+        Sigma[r0:r1] = s2 * kval(sqdist(r0, r1))
+    Sigma.diagonal().add_(jitter).add_(sd * sd)
+    diff = yt - float(mean_const)
+    LU, piv = torch.linalg.lu_factor(Sigma)
+    logdet = torch.log(torch.abs(torch.diagonal(LU))).sum()
+    alpha = torch.linalg.lu_solve(LU, piv, diff[:, None])[:, 0]
+    mll = -0.5 * (n * math.log(2.0 * math.pi) + float(logdet) + float(diff @ alpha))
+    del Sigma
+    W = torch.linalg.lu_solve(LU, piv, torch.eye(n, dtype=torch.float64))  # Sigma^-1
+    del LU
+    g_ls = np.zeros(d)
+    g_var = 0.0
+    for r0 in range(0, n, block):
+        r1 = min(n, r0 + block)
+        sq = sqdist(r0, r1)
+        G = 0.5 * (alpha[r0:r1, None] * alpha[None, :] - W[r0:r1])  # cotangent of Sigma
+        g_var += float((G * kval(sq)).sum())
+        Gc = G * dcoef(sq)
+        for k in range(d):
+            g_ls[k] += s2 * float((Gc * (xs[r0:r1, k, None] - xs[None, :, k]) ** 2).sum()) / ls_v[k]
+    g_noise = 0.5 * float((alpha * alpha).sum() - torch.diagonal(W).sum())
+    ls_grad = np.array(g_ls.sum()) if np.ndim(ls) == 0 else g_ls
+    grads = {"lengthscale": ls_grad, "variance": g_var, "obs_stddev": 2.0 * sd * g_noise,
+             "constant": float(alpha.sum())}
+    return mll, grads
+
+
 def collapsed_elbo_torch(kind, X, y, Z, ls, variance, obs_stddev, mean_const=0.0,
                          jitter=DEFAULT_JITTER):
     """collapsed_elbo and gradients w.r.t. (lengthscale, variance, obs_stddev,
