@@ -14,7 +14,7 @@ import torch
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libgpk.so")
 
 # enums (include/gpk.h)
-RBF, MATERN32, MATERN52 = 0, 1, 2
+RBF, MATERN32, MATERN52, MATERN12, RATIONAL_QUADRATIC = 0, 1, 2, 3, 4
 F64, F32 = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
 
@@ -53,6 +53,10 @@ SIGNATURES = {
     "gpk_conjugate_mll_batched": (_c_int, [_c_int, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr,
                                            _c_ptr, _c_ptr, _c_dbl, _c_int, _c_ptr, _c_ptr,
                                            _c_ptr, _c_ptr, _c_size, _c_ptr]),
+    "gpk_conjugate_loocv_workspace_bytes": (_c_size, [_c_i64, _c_int]),
+    "gpk_conjugate_loocv": (_c_int, [_c_int, _c_i64, _c_int, _c_ptr, _c_i64, _c_ptr, _c_ptr,
+                                     _c_int, _c_dbl, _c_int, _c_ptr, _c_ptr, _c_ptr, _c_ptr,
+                                     _c_size, _c_ptr]),
     "gpk_conjugate_mll_noalloc_max_n": (_c_size, []),
     "gpk_conjugate_mll_noalloc": (_c_int, [_c_int, _c_i64, _c_int, _c_ptr, _c_i64, _c_ptr, _c_ptr,
                                            _c_int, _c_dbl, _c_int, _c_ptr, _c_ptr, _c_ptr,

@@ -24,7 +24,7 @@ template <typename T, int DMAX>
 __global__ void __launch_bounds__((GemmCfg<T>::BM / GemmCfg<T>::TM) * (GemmCfg<T>::BN / GemmCfg<T>::TN))
     lauum_grad_kernel(int kind, const T* __restrict__ V, int64_t ldv, int n, int d,
                       const T* __restrict__ xs, const double* __restrict__ alpha,
-                      double* __restrict__ gpart) {
+                      double* __restrict__ gpart, const double* __restrict__ kaptr) {
   constexpr int BM = GemmCfg<T>::BM, BN = GemmCfg<T>::BN, BK = GemmCfg<T>::BK;
   constexpr int TM = GemmCfg<T>::TM, TN = GemmCfg<T>::TN;
   constexpr int NTX = BN / TN, NTY = BM / TM, NT = NTX * NTY;
@@ -72,6 +72,7 @@ __global__ void __launch_bounds__((GemmCfg<T>::BM / GemmCfg<T>::TM) * (GemmCfg<T
   for (int e = threadIdx.x; e < BN; e += NT) saj[e] = (j0 + e < n) ? (T)alpha[j0 + e] : T(0);
   __syncthreads();
 
+  const T ka = kaptr ? (T)*kaptr : T(1);  // kernel shape parameter (rational quadratic)
   // float64 accumulators: the terms cancel heavily (the variance and noise
   // sums are differences of O(n) quantities), so per-thread sums stay exact
   // to float64 while each term is formed in T
@@ -98,7 +99,7 @@ __global__ void __launch_bounds__((GemmCfg<T>::BM / GemmCfg<T>::TM) * (GemmCfg<T
       sq += dsq[k];
     }
     T k1, c1;
-    kval_dcoef<T>(kind, sq, T(1), k1, c1);
+    kval_dcoef<T>(kind, sq, T(1), k1, c1, ka);
     gvar += (double)(coef * k1);
     const T cc = coef * c1;
 #pragma unroll
@@ -132,7 +133,8 @@ __global__ void __launch_bounds__((GemmCfg<T>::BM / GemmCfg<T>::TM) * (GemmCfg<T
 
 template <typename T, int DMAX>
 static cudaError_t launch_lauum_grad(int kind, const T* V, int64_t ldv, int n, int d, const T* xs,
-                                     const double* alpha, double* gpart, cudaStream_t s) {
+                                     const double* alpha, double* gpart, const double* kaptr,
+                                     cudaStream_t s) {
   constexpr int BM = GemmCfg<T>::BM, BN = GemmCfg<T>::BN;
   constexpr int NT = (GemmCfg<T>::BM / GemmCfg<T>::TM) * (GemmCfg<T>::BN / GemmCfg<T>::TN);
   const int tiles_m = (n + BM - 1) / BM;
@@ -144,7 +146,8 @@ static cudaError_t launch_lauum_grad(int kind, const T* V, int64_t ldv, int n, i
                       (size_t)(GPK_MAX_D + 2) * (NT / 32) * sizeof(double);
   cudaFuncSetAttribute(lauum_grad_kernel<T, DMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)smem);
-  lauum_grad_kernel<T, DMAX><<<tiles, NT, smem, s>>>(kind, V, ldv, n, d, xs, alpha, gpart);
+  lauum_grad_kernel<T, DMAX><<<tiles, NT, smem, s>>>(kind, V, ldv, n, d, xs, alpha, gpart,
+                                                     kaptr);
   return launch_status();
 }
 
@@ -160,12 +163,11 @@ template <typename T>
 cudaError_t lauum_grad(int kind, const T* V, int64_t ldv, int n, int d, const T* xs,
                        const double* theta, int n_ls, const double* alpha, double* gpart,
                        cudaStream_t s) {
-  (void)theta;
-  (void)n_ls;
   if (n <= 0) return cudaSuccess;
-  if (d <= 8) return launch_lauum_grad<T, 8>(kind, V, ldv, n, d, xs, alpha, gpart, s);
-  if (d <= 16) return launch_lauum_grad<T, 16>(kind, V, ldv, n, d, xs, alpha, gpart, s);
-  if (d <= 32) return launch_lauum_grad<T, 32>(kind, V, ldv, n, d, xs, alpha, gpart, s);
+  const double* ka = kind == GPK_RATIONAL_QUADRATIC ? theta + n_ls + 3 : nullptr;
+  if (d <= 8) return launch_lauum_grad<T, 8>(kind, V, ldv, n, d, xs, alpha, gpart, ka, s);
+  if (d <= 16) return launch_lauum_grad<T, 16>(kind, V, ldv, n, d, xs, alpha, gpart, ka, s);
+  if (d <= 32) return launch_lauum_grad<T, 32>(kind, V, ldv, n, d, xs, alpha, gpart, ka, s);
   return cudaErrorInvalidValue;
 }
 
@@ -214,7 +216,7 @@ __global__ void __launch_bounds__(RES_ROWS)
           sq = fma(df, df, sq);
         }
       }
-      part = fma(kval<T>(kind, sq, s2), sa[c], part);
+      part = fma(kval<T>(kind, sq, s2, kshape<T>(kind, theta, n_ls)), sa[c], part);
     }
     accd += (double)part;
   }

@@ -16,6 +16,8 @@ namespace gpk {
 // RBF       k = s2 exp(-sq/2)                          (kernels/stationary/rbf.py:40-44)
 // Matern32  k = s2 (1 + sqrt3 t) exp(-sqrt3 t)         (matern32.py:41-54)
 // Matern52  k = s2 (1 + sqrt5 t + 5/3 t^2) exp(-sqrt5 t) (matern52.py:42-53)
+// Matern12  k = s2 exp(-t)                             (matern12.py:44-48)
+// RationalQuadratic  k = s2 (1 + sq / (2 alpha))^-alpha (rational_quadratic.py:76-83)
 // with t = sqrt(max(sq, 1e-36)) (stationary/utils.py:56-67).
 //
 // dcoef(sq) returns c with dk/dl_d = c * (x_d - y_d)^2 / l_d^3 and
@@ -38,10 +40,22 @@ __device__ __forceinline__ float d_sqrt(float x) { return sqrtf(x); }
 __device__ __forceinline__ double d_log(double x) { return log(x); }
 __device__ __forceinline__ float d_log(float x) { return logf(x); }
 
+__device__ __forceinline__ double d_log1p(double x) { return log1p(x); }
+__device__ __forceinline__ float d_log1p(float x) { return log1pf(x); }
+
+// Shape parameter of the kernel: alpha of the rational quadratic, read from
+// theta[n_ls + 3] (after the mean constant); 1 (unused) for the others.
 template <typename T>
-__device__ __forceinline__ T kval(int kind, T sq, T s2) {
+__device__ __forceinline__ T kshape(int kind, const double* theta, int n_ls) {
+  return kind == GPK_RATIONAL_QUADRATIC ? (T)theta[n_ls + 3] : T(1);
+}
+
+template <typename T>
+__device__ __forceinline__ T kval(int kind, T sq, T s2, T ka = T(1)) {
   if (kind == GPK_RBF) return s2 * d_exp(T(-0.5) * sq);
+  if (kind == GPK_RATIONAL_QUADRATIC) return s2 * d_exp(-ka * d_log1p(sq / (T(2) * ka)));
   T t = d_sqrt(sq > Consts<T>::floor_() ? sq : Consts<T>::floor_());
+  if (kind == GPK_MATERN12) return s2 * d_exp(-t);
   if (kind == GPK_MATERN32) {
     const T r3 = T(1.7320508075688772);
     return s2 * (T(1) + r3 * t) * d_exp(-r3 * t);
@@ -52,13 +66,25 @@ __device__ __forceinline__ T kval(int kind, T sq, T s2) {
 
 // value and derivative coefficient together (one exp)
 template <typename T>
-__device__ __forceinline__ void kval_dcoef(int kind, T sq, T s2, T& k, T& c) {
+__device__ __forceinline__ void kval_dcoef(int kind, T sq, T s2, T& k, T& c, T ka = T(1)) {
   if (kind == GPK_RBF) {
     k = s2 * d_exp(T(-0.5) * sq);
     c = k;
     return;
   }
-  T t = d_sqrt(sq > Consts<T>::floor_() ? sq : Consts<T>::floor_());
+  if (kind == GPK_RATIONAL_QUADRATIC) {
+    const T base = T(1) + sq / (T(2) * ka);
+    k = s2 * d_exp(-ka * d_log1p(sq / (T(2) * ka)));
+    c = k / base;  // -2 dk/dsq = s2 (1 + sq / (2 alpha))^-(alpha + 1)
+    return;
+  }
+  const bool above = sq > Consts<T>::floor_();
+  T t = d_sqrt(above ? sq : Consts<T>::floor_());
+  if (kind == GPK_MATERN12) {
+    k = s2 * d_exp(-t);
+    c = above ? k / t : T(0);  // -2 dk/dsq = s2 exp(-t) / t; zero below the floor
+    return;
+  }
   if (kind == GPK_MATERN32) {
     const T r3 = T(1.7320508075688772);
     T e = s2 * d_exp(-r3 * t);

@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(256)
           sq = fma(df, df, sq);
         }
       }
-      T kv = kval<T>(kind, sq, s2);
+      T kv = kval<T>(kind, sq, s2, kshape<T>(kind, theta, n_ls));
       if (mode == 1 && gi == gj) {
         // (K + I*jitter) + I*obs_stddev^2 (objectives.py:100-103)
         double dv = ((double)kv + jitter) + sd * sd;
@@ -112,7 +112,7 @@ __global__ void sigma_diag_kernel(int kind, int n, const double* __restrict__ th
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double sd = theta[n_ls + 1];
-  dtrack[i] = (kval<double>(kind, 0.0, theta[n_ls]) + jitter) + sd * sd;
+  dtrack[i] = (kval<double>(kind, 0.0, theta[n_ls], kshape<double>(kind, theta, n_ls)) + jitter) + sd * sd;
 }
 
 cudaError_t sigma_diag_init(int kind, int n, const double* theta, int n_ls, double jitter,
@@ -159,7 +159,7 @@ __global__ void cross_cov_raw_kernel(int kind, int n, int m, int d, const double
     T df = (T)(x[(int64_t)i * ldx + k] / l) - (T)(y[(int64_t)j * ldy + k] / l);
     sq = fma(df, df, sq);
   }
-  T v = kval<T>(kind, sq, (T)theta[n_ls]);
+  T v = kval<T>(kind, sq, (T)theta[n_ls], kshape<T>(kind, theta, n_ls));
   if (diag_only)
     out[i] = v;
   else
@@ -167,7 +167,7 @@ __global__ void cross_cov_raw_kernel(int kind, int n, int m, int d, const double
 }
 
 static bool valid_common(int kind, int64_t n, int d, int n_ls) {
-  if (kind < GPK_RBF || kind > GPK_MATERN52) return false;
+  if (kind < GPK_RBF || kind > GPK_RATIONAL_QUADRATIC) return false;
   if (n < 0 || d <= 0 || d > GPK_MAX_D) return false;
   if (!(n_ls == 1 || n_ls == d)) return false;
   if (n > (int64_t)1 << 30) return false;
@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(256)
       sq += df[k] * df[k];
     }
     double k1, c1;
-    kval_dcoef<double>(kind, sq, 1.0, k1, c1);
+    kval_dcoef<double>(kind, sq, 1.0, k1, c1, kshape<double>(kind, theta, n_ls));
     av += g * k1;
     for (int k = 0; k < d; ++k) {
       al[k] += g * c1 * df[k] * df[k];

@@ -598,7 +598,7 @@ __global__ void __launch_bounds__(256)
         const float df = sx[r][k] - yv[k];
         sq = fmaf(df, df, sq);
       }
-      kv = kval<float>(kind, sq, s2);
+      kv = kval<float>(kind, sq, s2, kshape<float>(kind, theta, n_ls));
       const float vh = tf32_rna_f(kv);
       A[(int64_t)gi * lda + gj] = kv;
       Ah[(int64_t)gi * lda + gj] = vh;
@@ -707,7 +707,7 @@ __global__ void residual_upper_finish(int kind, int n, const double* __restrict_
   if (i >= n) return;
   const int T = (n + RU_T - 1) / RU_T, ti = i / RU_T;
   const double sd = theta[n_ls + 1];
-  const double kdiag = (double)kval<float>(kind, 0.f, (float)theta[n_ls]);
+  const double kdiag = (double)kval<float>(kind, 0.f, (float)theta[n_ls], kshape<float>(kind, theta, n_ls));
   double s = (kdiag + (jitter + sd * sd)) * alpha[i];
   for (int J = ti; J < T; ++J) s += rbuf[(int64_t)J * n + i];
   for (int I = 0; I <= ti; ++I) s += cbuf[(int64_t)I * n + i];
@@ -1342,6 +1342,7 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
   pg.n_true = n;
   pg.d = d;
   pg.kind = kind;
+  pg.kaptr = kind == GPK_RATIONAL_QUADRATIC ? theta + n_ls + 3 : nullptr;
   pg.xs = b.xs;
   pg.avec = b.alpha;
   pg.gpart = b.gpart;

@@ -366,7 +366,7 @@ extern "C" const char* gpk_status_string(int status) {
 }
 
 static bool mll_args_ok(int kind, int64_t n, int d, int64_t ldx, int n_ls, int precision) {
-  if (kind < GPK_RBF || kind > GPK_MATERN52) return false;
+  if (kind < GPK_RBF || kind > GPK_RATIONAL_QUADRATIC) return false;
   if (n < 0 || n > (1 << 20)) return false;
   if (d <= 0 || d > GPK_MAX_D || ldx < d) return false;
   if (!(n_ls == 1 || n_ls == d)) return false;
@@ -651,22 +651,23 @@ extern "C" gpk_status gpk_logdet_triangular(int64_t n, int dtype, const void* L,
 // hand a custom call no workspace; embedded or real-time hosts that forbid
 // allocation after start-up) use this entry point instead of
 // gpk_conjugate_mll: its scratch is a file-scope device array, so the call
-// allocates nothing.  The array holds GPK_NOALLOC_SCRATCH_BYTES, enough for
-// n <= GPK_NOALLOC_MAX_N and d <= GPK_NOALLOC_MAX_D; every GPU that loads the
+// allocates nothing.  The array holds kNoallocBytes (8 MiB), enough for
+// n <= kNoallocMaxN (512, reported by gpk_conjugate_mll_noalloc_max_n()) at
+// every d the library accepts (d <= GPK_MAX_D); every GPU that loads the
 // library keeps it until the process exits.
 // ---------------------------------------------------------------------------
 namespace {
 
 constexpr size_t kNoallocBytes = (size_t)8 << 20;  // 8 MiB
 constexpr int kNoallocMaxN = 512;
-constexpr int kNoallocMaxD = 32;
 constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
 
 // Device address of g_noalloc_scratch per device.  In host code the array's
 // name is only a host-side stand-in, so the address comes from
-// cudaGetSymbolAddress, taken once per device with that device current.
+// cudaGetSymbolAddress, taken once per device with that device current.  The
+// cache is keyed by device ordinal, i.e. the runtime's primary context.
 static void* g_noalloc_ptr[kMaxDevices];
 static std::mutex g_noalloc_mutex;
 
@@ -694,8 +695,9 @@ extern "C" gpk_status gpk_conjugate_mll_noalloc(int kind, int64_t n, int d, cons
                                                 double* out_grad, int* info,
                                                 cudaStream_t stream) {
   if (!mll_args_ok(kind, n, d, ldx, n_ls, GPK_PREC_FP64)) return GPK_ERR_BAD_ARG;
-  // sizes beyond the static scratch are refused, never truncated
-  if (n > kNoallocMaxN || d > kNoallocMaxD) return GPK_ERR_UNSUPPORTED;
+  // sizes beyond the static scratch are refused, never truncated (d is bounded
+  // by GPK_MAX_D above, like every entry point of the library)
+  if (n > kNoallocMaxN) return GPK_ERR_UNSUPPORTED;
   if (!out_mll || !info || !theta || (want_grad && !out_grad)) return GPK_ERR_BAD_ARG;
   if (n == 0) {
     zero_outputs_kernel<<<1, 1, 0, stream>>>(out_mll, want_grad ? out_grad : nullptr, n_ls + 3,

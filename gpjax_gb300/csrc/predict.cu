@@ -93,7 +93,7 @@ __global__ void pred_mean_var_kernel(int n, int t, const T* __restrict__ Ktx,
   if (lane == 0) {
     const double nan = __longlong_as_double(0x7ff8000000000000ULL);
     const bool bad = *info != 0 && *info != INT_MAX;
-    const double kaa = kval<double>(kind, 0.0, theta[n_ls]);
+    const double kaa = kval<double>(kind, 0.0, theta[n_ls], kshape<double>(kind, theta, n_ls));
     mean[a] = bad ? nan : theta[n_ls + 2] + sm;
     var[a] = bad ? nan : (kaa - sq) + prior_jitter;
   }
@@ -115,7 +115,7 @@ __global__ void pred_cov_kernel(int t, int d, int kind, const double* __restrict
     const double df = tsd[(int64_t)a * d + k] - tsd[(int64_t)b * d + k];
     sq = fma(df, df, sq);
   }
-  const double kab = kval<double>(kind, sq, theta[n_ls]);
+  const double kab = kval<double>(kind, sq, theta[n_ls], kshape<double>(kind, theta, n_ls));
   double v = kab - (double)QQ[(int64_t)hi * ldq + lo];
   if (a == b) v += prior_jitter;
   const bool bad = *info != 0 && *info != INT_MAX;
@@ -218,7 +218,7 @@ extern "C" gpk_status gpk_predict(int kind, int64_t n, int64_t t, int d, const d
                                   double prior_jitter, int precision, double* mean, double* var,
                                   double* cov, int64_t ldcov, int* info, void* workspace,
                                   size_t workspace_bytes, cudaStream_t stream) {
-  if (kind < GPK_RBF || kind > GPK_MATERN52) return GPK_ERR_BAD_ARG;
+  if (kind < GPK_RBF || kind > GPK_RATIONAL_QUADRATIC) return GPK_ERR_BAD_ARG;
   if (n <= 0 || t < 0 || n > (1 << 20) || t > (1 << 20)) return GPK_ERR_BAD_ARG;
   if (d <= 0 || d > GPK_MAX_D || ldx < d || ldxt < d || !(n_ls == 1 || n_ls == d))
     return GPK_ERR_BAD_ARG;

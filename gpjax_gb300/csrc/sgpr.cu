@@ -307,7 +307,7 @@ __global__ void __launch_bounds__(256)
           const float df = sz[r][k] - xr[k];
           sq = fmaf(df, df, sq);
         }
-        const float v = gx < n ? kval<float>(kind, sq, s2) : 0.f;
+        const float v = gx < n ? kval<float>(kind, sq, s2, kshape<float>(kind, theta, n_ls)) : 0.f;
         tile[r][a] = v;
         if (i0 + r < m) {
           const float h = tf32_round(v);
@@ -435,7 +435,7 @@ __global__ void sg_combine(int m, int64_t ldm, const double* __restrict__ Kinv,
 __global__ void __launch_bounds__(256)
     sg_grad_kzz(int kind, int m, int d, int64_t ldm, const double* __restrict__ zs,
                 const double* __restrict__ GK, double* __restrict__ thK,
-                double* __restrict__ dzK) {
+                double* __restrict__ dzK, const double* __restrict__ theta, int n_ls) {
   const int i = blockIdx.x;
   __shared__ double red[(DMAXS * 2 + 1) * 8];
   double zi[DMAXS];
@@ -453,7 +453,7 @@ __global__ void __launch_bounds__(256)
       sq += dz[k] * dz[k];
     }
     double k1, c1;
-    kval_dcoef<double>(kind, sq, 1.0, k1, c1);
+    kval_dcoef<double>(kind, sq, 1.0, k1, c1, kshape<double>(kind, theta, n_ls));
     av += g * k1;
 #pragma unroll
     for (int k = 0; k < DMAXS; ++k) {
@@ -585,7 +585,7 @@ __global__ void __launch_bounds__(256)
           sq += dz[k] * dz[k];
         }
         T k1, c1;
-        kval_dcoef<T>(kind, sq, T(1), k1, c1);
+        kval_dcoef<T>(kind, sq, T(1), k1, c1, kshape<T>(kind, theta, n_ls));
         av += (double)(g * k1);
         const T gc = g * c1;
 #pragma unroll
@@ -912,13 +912,14 @@ gpk_status sgpr_run(int kind, int n, int m, int d, const double* x, int64_t ldx,
                                     b.Ht, b.Hh, b.Hl, b.gams, b.GK, b.red);
   GPK_LAUNCH_CHECK();
   if (want_grad) {
-    sg_grad_kzz<<<m, 256, 0, s>>>(kind, m, d, ldm, b.zs64, b.GK, b.thK, b.dzK);
+    sg_grad_kzz<<<m, 256, 0, s>>>(kind, m, d, ldm, b.zs64, b.GK, b.thK, b.dzK, theta, n_ls);
     GPK_LAUNCH_CHECK();
     if constexpr (mixed) {
       // G = H Phi + gamma d^T / s^2 on the tensor cores, reduced in the epilogue
       tc::TcParams p = sg_adj_params(n, m, d);
       p.n_true = n;
       p.kind = kind;
+      p.kaptr = kind == GPK_RATIONAL_QUADRATIC ? theta + n_ls + 3 : nullptr;
       p.xs = b.xs;
       p.zs = b.zs;
       p.avec = b.gams;
@@ -975,7 +976,7 @@ extern "C" gpk_status gpk_collapsed_elbo(int kind, int64_t n, int64_t m, int d, 
                                          double* out_elbo, double* out_grad, double* out_grad_z,
                                          int* info, void* workspace, size_t workspace_bytes,
                                          cudaStream_t stream) {
-  if (kind < GPK_RBF || kind > GPK_MATERN52) return GPK_ERR_BAD_ARG;
+  if (kind < GPK_RBF || kind > GPK_RATIONAL_QUADRATIC) return GPK_ERR_BAD_ARG;
   if (n <= 0 || m <= 0 || n > (int64_t)1 << 28 || m > 16384) return GPK_ERR_BAD_ARG;
   if (d <= 0 || d > DMAXS || ldx < d || ldz < d || !(n_ls == 1 || n_ls == d))
     return GPK_ERR_BAD_ARG;

@@ -214,13 +214,12 @@ struct Tile {
   static constexpr int TMEM_COLS = NBUF * BN;                  // a power of two >= 32
   static constexpr int HC = BN / 2;  // accumulator columns owned by one epilogue thread
   static constexpr int TLD = BN + 4; // staged output tile row stride (floats)
-  // K slices summed by one TMEM accumulator before the epilogue drains it:
-  // twelve MMAs (3 products x 4 K steps: 32 K elements for TF32, 64 for
-  // float16, whose MMAs take K = 16) -- the accumulation length the accuracy
-  // needs -- and, for the wide float16 tile, drains no more often than the
-  // epilogue's 16-column TMEM loads keep up with
-  static constexpr int SEG = TS == 1 || TS == 3 ? 2 : 1;
   static constexpr int KSTEP = F16 ? 16 : 8;  // K elements per MMA (32 bytes either way)
+  static constexpr int KS = BK / KSTEP;       // MMA K steps per K slice
+  // MMA K steps summed by one TMEM accumulator before the epilogue drains it
+  // (3 products each): the accumulation length the accuracy needs, and no more
+  // drains than the epilogue keeps up with
+  static constexpr int KPSEG = 4;
 };
 
 template <int STAGES_>
@@ -233,10 +232,13 @@ struct SmemCtl {
   int abort_flag;
 };
 
-// The tensor-core float32 accumulator rounds less carefully than an FMA, so
-// each accumulator only sums 32 K elements (Tile::SEG slices, 3 MMAs per 8);
-// the epilogue warps drain finished segments into round-to-nearest float32
-// registers while the MMA thread fills the next of NBUF TMEM buffers.
+// The tensor-core float32 accumulator truncates toward zero (measured on
+// positive products: a 12-MMA accumulator loses 3.3 units of 2^-24 of its
+// magnitude on average, whatever K; more on operands of wide dynamic range),
+// so each accumulator only sums Tile::KPSEG K steps, the hi*hi MMAs come after
+// the cross products, and the epilogue warps drain finished segments into
+// round-to-nearest float32 registers while the MMA thread fills the next of
+// NBUF TMEM buffers.
 constexpr int EPI_WARPS = 8;   // epilogue warps: two per TMEM lane quarter
 constexpr int EPI_THREADS = EPI_WARPS * 32;
 
@@ -305,7 +307,6 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                    const __grid_constant__ CUtensorMap tb_hi, const __grid_constant__ CUtensorMap tb_lo,
                    const __grid_constant__ TcParams p) {
   using TL = Tile<TS>;
-  constexpr int SEG_CHUNKS = TL::SEG;
   constexpr int BN = TL::BN, BK = TL::BK, STAGES = TL::STAGES, NBUF = TL::NBUF, HC = TL::HC,
                 TLD = TL::TLD, STAGE_BYTES = TL::STAGE_BYTES, A_BYTES = TL::A_BYTES,
                 B_BYTES = TL::B_BYTES;
@@ -331,7 +332,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   if (p.b_tri == TRI_UPPER) klo = max(klo, j0);
   klo = (klo / BK) * BK;
   const int nk = khi > klo ? (khi - klo + BK - 1) / BK : 0;
-  const int nseg = (nk + SEG_CHUNKS - 1) / SEG_CHUNKS;
+  const int nseg = (nk * TL::KS + TL::KPSEG - 1) / TL::KPSEG;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -388,39 +389,58 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   } else if (warp == 1) {
     if (lane == 0) {
       constexpr uint32_t idesc = TL::F16 ? idesc_f16(BM, BN) : idesc_tf32(BM, BN);
+      constexpr int KS = TL::KS, KP = TL::KPSEG;
+      const int nks = nk * KS;  // MMA K steps of this tile
       bool ok = true;
-      for (int kc = 0; kc < nk && ok; ++kc) {
-        const int seg = kc / SEG_CHUNKS, b = seg % NBUF;
+      int waited = 0;           // K slices whose full barrier has been passed
+      for (int seg = 0; seg < nseg && ok; ++seg) {
+        const int b = seg % NBUF;
         const uint32_t tacc = tmem + (uint32_t)(b * BN);
-        if (kc % SEG_CHUNKS == 0 && seg >= NBUF) {
+        if (seg >= NBUF) {
           ok = mbar_wait(&ctl->tempty[b], ((seg / NBUF) - 1) & 1, abort_flag, p.err);
           if (!ok) break;
           tc_fence_after();
         }
-        const int s = kc % STAGES;
-        ok = mbar_wait(&ctl->full[s], (kc / STAGES) & 1, abort_flag, p.err);
+        const int ks0 = seg * KP, ks1 = min(nks, ks0 + KP);
+        for (; waited <= (ks1 - 1) / KS && ok; ++waited)
+          ok = mbar_wait(&ctl->full[waited % STAGES], (waited / STAGES) & 1, abort_flag, p.err);
         if (!ok) break;
         tc_fence_after();
-        const uint32_t sb = smem_u32(tiles + s * STAGE_BYTES);
-        const uint64_t ahi = sdesc<TL::SWZ>(sb), alo = sdesc<TL::SWZ>(sb + A_BYTES);
-        const uint64_t bhi = sdesc<TL::SWZ>(sb + 2 * A_BYTES);
-        const uint64_t blo = sdesc<TL::SWZ>(sb + 2 * A_BYTES + B_BYTES);
-        const bool first = (kc % SEG_CHUNKS) == 0;
+        // The tensor core truncates each MMA's sum toward zero.  The cross
+        // products (about 2^-11 of the result) go first, so their truncation is
+        // negligible; then each hi*hi MMA truncates the running sum once.
 #pragma unroll
-        for (int k4 = 0; k4 < BK / TL::KSTEP; ++k4) {
-          const uint64_t off = (uint64_t)((k4 * 32) >> 4);  // 32 bytes per MMA K step
+        for (int q = 0; q < KP; ++q) {
+          const int ks = ks0 + q;
+          if (ks >= ks1) break;
+          const uint32_t sb = smem_u32(tiles + ((ks / KS) % STAGES) * STAGE_BYTES);
+          const uint64_t off = (uint64_t)(((ks % KS) * 32) >> 4);  // 32 bytes per MMA K step
+          const uint64_t ahi = sdesc<TL::SWZ>(sb) + off, alo = sdesc<TL::SWZ>(sb + A_BYTES) + off;
+          const uint64_t bhi = sdesc<TL::SWZ>(sb + 2 * A_BYTES) + off;
+          const uint64_t blo = sdesc<TL::SWZ>(sb + 2 * A_BYTES + B_BYTES) + off;
           if (TL::F16) {
-            mma_f16(tacc, alo + off, bhi + off, idesc, (first && k4 == 0) ? 0u : 1u);
-            mma_f16(tacc, ahi + off, blo + off, idesc, 1u);
-            mma_f16(tacc, ahi + off, bhi + off, idesc, 1u);
+            mma_f16(tacc, alo, bhi, idesc, q == 0 ? 0u : 1u);
+            mma_f16(tacc, ahi, blo, idesc, 1u);
           } else {
-            mma_tf32(tacc, alo + off, bhi + off, idesc, (first && k4 == 0) ? 0u : 1u);
-            mma_tf32(tacc, ahi + off, blo + off, idesc, 1u);
-            mma_tf32(tacc, ahi + off, bhi + off, idesc, 1u);
+            mma_tf32(tacc, alo, bhi, idesc, q == 0 ? 0u : 1u);
+            mma_tf32(tacc, ahi, blo, idesc, 1u);
           }
         }
-        mma_commit(&ctl->empty[s]);
-        if (kc % SEG_CHUNKS == SEG_CHUNKS - 1 || kc == nk - 1) mma_commit(&ctl->tfull[b]);
+#pragma unroll
+        for (int q = 0; q < KP; ++q) {
+          const int ks = ks0 + q;
+          if (ks >= ks1) break;
+          const uint32_t sb = smem_u32(tiles + ((ks / KS) % STAGES) * STAGE_BYTES);
+          const uint64_t off = (uint64_t)(((ks % KS) * 32) >> 4);
+          const uint64_t ahi = sdesc<TL::SWZ>(sb) + off, bhi = sdesc<TL::SWZ>(sb + 2 * A_BYTES) + off;
+          if (TL::F16)
+            mma_f16(tacc, ahi, bhi, idesc, 1u);
+          else
+            mma_tf32(tacc, ahi, bhi, idesc, 1u);
+        }
+        // release the K slices whose last K step this segment issued
+        for (int kc = ks0 / KS; (kc + 1) * KS <= ks1; ++kc) mma_commit(&ctl->empty[kc % STAGES]);
+        mma_commit(&ctl->tfull[b]);
       }
     }
     __syncwarp();
@@ -433,6 +453,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     const int r = q * 32 + lane;
     const int gi = i0 + r;  // row within the problem
     const int et = threadIdx.x - 64;
+    const float ka = p.kaptr ? (float)*p.kaptr : 1.f;  // kernel shape parameter
     if (MODE == MODE_GRAD || MODE == MODE_SGPR) {
       // column points and column coefficients of this tile
       const double* cvec = MODE == MODE_GRAD ? p.avec : p.bvec;
@@ -674,7 +695,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             sq = fmaf(df, df, sq);
           }
           float k1, c1;
-          kval_dcoef<float>(p.kind, sq, 1.f, k1, c1);
+          kval_dcoef<float>(p.kind, sq, 1.f, k1, c1, ka);
           pvar = fmaf(coef, k1, pvar);
           const float cc = coef * c1;
 #pragma unroll
@@ -759,7 +780,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             sq = fmaf(df, df, sq);
           }
           float k1, c1;
-          kval_dcoef<float>(p.kind, sq, 1.f, k1, c1);
+          kval_dcoef<float>(p.kind, sq, 1.f, k1, c1, ka);
           pvar = fmaf(g, k1, pvar);
           const float gc = g * c1;
 #pragma unroll

@@ -56,6 +56,7 @@ struct TcParams {
   const float* ra;
   const float* rb;
   int n_true, d, kind;
+  const double* kaptr;  // device pointer to the rational-quadratic alpha (kshape); null: 1
   const float* xs;
   const float* zs;
   const double* avec;

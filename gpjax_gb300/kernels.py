@@ -1,10 +1,12 @@
-"""Stationary kernels RBF, Matern32, Matern52 with ARD lengthscales
+"""Stationary kernels RBF, Matern32, Matern52, Matern12 and RationalQuadratic with ARD lengthscales
 (mirrors gpjax/kernels/base.py:42-149 and kernels/stationary/*.py).
 
 Pointwise definitions (on x/l, y/l):
   RBF       s2 exp(-|x-y|^2/2)                          rbf.py:40-44
   Matern32  s2 (1 + sqrt3 t) exp(-sqrt3 t)              matern32.py:41-54
   Matern52  s2 (1 + sqrt5 t + 5/3 t^2) exp(-sqrt5 t)    matern52.py:42-53
+  Matern12  s2 exp(-t)                                  matern12.py:44-48
+  RationalQuadratic  s2 (1 + |x-y|^2 / (2 alpha))^-alpha  rational_quadratic.py:76-83
 with t = sqrt(max(|x-y|^2, 1e-36)) (stationary/utils.py:56-67).
 """
 from __future__ import annotations
@@ -96,3 +98,32 @@ class Matern32(StationaryKernel):
 class Matern52(StationaryKernel):
     name = "Matérn52"
     kind = _lib.MATERN52
+
+
+class Matern12(StationaryKernel):
+    name = "Matérn12"
+    kind = _lib.MATERN12
+
+
+class RationalQuadratic(StationaryKernel):
+    """Rational quadratic kernel (kernels/stationary/rational_quadratic.py:40-83).
+
+    ``alpha`` is a fixed shape constant, as in the reference (stored as a plain
+    attribute there, not a trainable parameter); it travels to the library in
+    one more theta slot after the mean constant."""
+
+    name = "Rational Quadratic"
+    kind = _lib.RATIONAL_QUADRATIC
+
+    def __init__(self, active_dims=None, lengthscale=1.0, variance=1.0, alpha=1.0, n_dims=None,
+                 compute_engine: AbstractKernelComputation | None = None):
+        a = float(alpha.value) if hasattr(alpha, "value") else float(alpha)
+        if not a > 0:
+            raise ValueError("alpha must be > 0")
+        self.alpha = a
+        super().__init__(active_dims, lengthscale, variance, n_dims, compute_engine)
+
+    def theta_vector(self, device, obs_stddev=None, constant=None) -> torch.Tensor:
+        base = super().theta_vector(device, obs_stddev, constant)
+        return torch.cat([base, torch.full((1,), self.alpha, dtype=torch.float64,
+                                           device=base.device)])

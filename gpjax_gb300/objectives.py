@@ -26,7 +26,7 @@ class _ConjugateMLL(torch.autograd.Function):
         th = theta.detach().contiguous()
         xc, yc = x.detach().contiguous(), y.detach().reshape(-1).contiguous()
         out = torch.empty(1, dtype=torch.float64, device=dev)
-        grad = torch.zeros(n_ls + 3, dtype=torch.float64, device=dev)
+        grad = torch.zeros(th.numel(), dtype=torch.float64, device=dev)  # n_ls + 3 (+ RQ alpha)
         info = torch.zeros(1, dtype=torch.int32, device=dev)
         nbytes = _lib.lib().gpk_conjugate_mll_workspace_bytes(n, d, prec)
         ws = _lib.workspace(nbytes, dev)
@@ -57,6 +57,46 @@ def conjugate_mll(posterior, data, precision: str | None = None) -> torch.Tensor
     theta = kernel.theta_vector(dev, posterior.likelihood.obs_stddev.value, const)
     return _ConjugateMLL.apply(theta, x, data.y, kernel.kind, kernel.n_ls,
                                float(posterior.prior.jitter), precision_code(precision))
+
+
+class _ConjugateLOOCV(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, theta, x, y, kind, n_ls, jitter):
+        dev = _lib.require_cuda(x, y, theta)
+        n, d = x.shape
+        want_grad = bool(ctx.needs_input_grad[0])
+        th = theta.detach().contiguous()
+        xc, yc = x.detach().contiguous(), y.detach().reshape(-1).contiguous()
+        out = torch.empty(1, dtype=torch.float64, device=dev)
+        grad = torch.zeros(th.numel(), dtype=torch.float64, device=dev)  # n_ls + 3 (+ RQ alpha)
+        info = torch.zeros(1, dtype=torch.int32, device=dev)
+        ws = _lib.workspace(_lib.lib().gpk_conjugate_loocv_workspace_bytes(n, d), dev)
+        _lib.call("gpk_conjugate_loocv", kind, n, d, xc.data_ptr(), d, yc.data_ptr(),
+                  th.data_ptr(), n_ls, float(jitter), int(want_grad), out.data_ptr(),
+                  grad.data_ptr(), info.data_ptr(), ws.data_ptr(), ws.numel(),
+                  _lib.stream_ptr(dev))
+        ctx.save_for_backward(grad)
+        ctx.info = info
+        return out[0]
+
+    @staticmethod
+    def backward(ctx, g):
+        (grad,) = ctx.saved_tensors
+        return g * grad, None, None, None, None, None
+
+
+def conjugate_loocv(posterior, data) -> torch.Tensor:
+    """Leave-one-out predictive log-probability of a conjugate GP
+    (objectives.py:110-178), float64, differentiable w.r.t. the kernel,
+    likelihood and mean parameters; maximise it (minimise its negative) like the
+    marginal log-likelihood."""
+    kernel = posterior.prior.kernel
+    x = kernel.slice_input(data.X)
+    dev = _lib.require_cuda(x)
+    const = _mean_constant(posterior.prior.mean_function, dev)
+    theta = kernel.theta_vector(dev, posterior.likelihood.obs_stddev.value, const)
+    return _ConjugateLOOCV.apply(theta, x, data.y, kernel.kind, kernel.n_ls,
+                                 float(posterior.prior.jitter))
 
 
 def value_and_grad(objective, model, data, **kw):
@@ -102,7 +142,7 @@ class _CollapsedELBO(torch.autograd.Function):
         xc, yc = x.detach().contiguous(), y.detach().reshape(-1).contiguous()
         zc = z.detach().to(torch.float64).contiguous()
         out = torch.empty(1, dtype=torch.float64, device=dev)
-        grad = torch.zeros(n_ls + 3, dtype=torch.float64, device=dev)
+        grad = torch.zeros(th.numel(), dtype=torch.float64, device=dev)  # n_ls + 3 (+ RQ alpha)
         gz = torch.zeros((m, d), dtype=torch.float64, device=dev)
         info = torch.zeros(1, dtype=torch.int32, device=dev)
         nbytes = _lib.lib().gpk_collapsed_elbo_workspace_bytes(n, m, d, prec)
@@ -140,7 +180,7 @@ def cross_covariance_vjp(kind, n_ls, theta, x, y, G, need_x=False, need_y=False)
     """Cotangent of K(x, y) -> (d theta [n_ls + 3], d x, d y) through gpk_cross_covariance_vjp."""
     dev = _lib.require_cuda(x, y, G)
     n, m, d = x.shape[0], y.shape[0], x.shape[1]
-    gth = torch.zeros(n_ls + 3, dtype=torch.float64, device=dev)
+    gth = torch.zeros(theta.numel(), dtype=torch.float64, device=dev)  # n_ls + 3 (+ RQ alpha)
     gx = torch.zeros((n, d), dtype=torch.float64, device=dev) if need_x else None
     gy = torch.zeros((m, d), dtype=torch.float64, device=dev) if need_y else None
     Gc = G.detach().to(torch.float64).contiguous()

@@ -40,8 +40,18 @@ typedef enum {
   GPK_ERR_UNSUPPORTED = 6
 } gpk_status;
 
-/* stationary kernels: kernels/stationary/{rbf,matern32,matern52}.py */
-typedef enum { GPK_RBF = 0, GPK_MATERN32 = 1, GPK_MATERN52 = 2 } gpk_kernel_kind;
+/* stationary kernels: kernels/stationary/{rbf,matern32,matern52,matern12,
+ * rational_quadratic}.py.  GPK_RATIONAL_QUADRATIC reads its alpha from one
+ * more theta slot, theta[n_ls + 3] (after the mean constant); gradients keep
+ * the n_ls + 3 layout (alpha is a fixed constant of the reference's kernel,
+ * rational_quadratic.py:64). */
+typedef enum {
+  GPK_RBF = 0,
+  GPK_MATERN32 = 1,
+  GPK_MATERN52 = 2,
+  GPK_MATERN12 = 3,
+  GPK_RATIONAL_QUADRATIC = 4
+} gpk_kernel_kind;
 
 typedef enum { GPK_F64 = 0, GPK_F32 = 1 } gpk_dtype;
 
@@ -157,19 +167,38 @@ gpk_status gpk_conjugate_mll(int kind, int64_t n, int d,
                              void* workspace, size_t workspace_bytes,
                              cudaStream_t stream);
 
+/* Leave-one-out predictive log-probability and its gradient, float64
+ * (conjugate_loocv, gpjax/objectives.py:110-178):
+ *   loocv = sum_i log N(y_i; y_i - alpha_i / W_ii, 1 / W_ii),
+ *   alpha = Sigma^-1 (y - mean_constant), W = Sigma^-1,
+ *   Sigma = K(x, x) + (obs_stddev^2 + jitter) I.
+ * Arguments as gpk_conjugate_mll (theta layout, info); out_loocv: 1 device
+ * double; out_grad (if want_grad): device double [n_ls + 3].
+ * n <= 65536.  workspace: gpk_conjugate_loocv_workspace_bytes (about 4 n^2
+ * doubles: Sigma's factor, its inverse, Sigma^-1 and the cotangent). */
+size_t gpk_conjugate_loocv_workspace_bytes(int64_t n, int d);
+gpk_status gpk_conjugate_loocv(int kind, int64_t n, int d, const double* x, int64_t ldx,
+                               const double* y, const double* theta, int n_ls, double jitter,
+                               int want_grad, double* out_loocv, double* out_grad, int* info,
+                               void* workspace, size_t workspace_bytes, cudaStream_t stream);
+
 /* Allocation-free variant of gpk_conjugate_mll, float64 form only.
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory -- code running inside CUDA stream capture (cudaMalloc would break
  * the capture), host frameworks that pass a custom call no workspace, hosts
  * that forbid allocation after start-up -- the scratch is a static device
  * array of 8 MiB inside the library, which bounds the problem to
- * n <= gpk_conjugate_mll_noalloc_max_n() (512) and d <= 32; larger sizes return
- * GPK_ERR_UNSUPPORTED.  Every GPU that loads the library holds the array until
- * the process exits.  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress); make that first call before any stream
- * capture.  All calls share the one array: calls that overlap on the GPU
- * (different streams, or different host threads on the same device) race;
- * serialise them.  Arguments and results are those of gpk_conjugate_mll. */
+ * n <= gpk_conjugate_mll_noalloc_max_n() (512); a larger n returns
+ * GPK_ERR_UNSUPPORTED.  d is bounded as everywhere in the library (d <= 32,
+ * GPK_ERR_BAD_ARG beyond).  Every GPU that loads the library holds the array
+ * until the process exits.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) and keeps it for that device ordinal;
+ * make that first call before any stream capture.  Only the runtime's primary
+ * context is supported: after cudaDeviceReset, or with another context
+ * current, the kept address is stale.  All calls share the one array: calls
+ * that overlap on the GPU (different streams, or different host threads on the
+ * same device) race; serialise them.  Arguments and results are those of
+ * gpk_conjugate_mll. */
 size_t gpk_conjugate_mll_noalloc_max_n(void);
 gpk_status gpk_conjugate_mll_noalloc(int kind, int64_t n, int d,
                                      const double* x, int64_t ldx, const double* y,

@@ -44,8 +44,22 @@ import math
 import numpy as np
 import scipy.linalg as sla
 
-RBF, MATERN32, MATERN52 = 0, 1, 2
-KERNEL_NAMES = {RBF: "RBF", MATERN32: "Matern32", MATERN52: "Matern52"}
+RBF, MATERN32, MATERN52, MATERN12, RATIONAL_QUADRATIC = 0, 1, 2, 3, 4
+KERNEL_NAMES = {RBF: "RBF", MATERN32: "Matern32", MATERN52: "Matern52", MATERN12: "Matern12",
+                RATIONAL_QUADRATIC: "RationalQuadratic"}
+
+
+def rational_quadratic(alpha: float):
+    """Kernel code of a rational quadratic with shape alpha (the other kernels
+    are plain integer codes)."""
+    return (RATIONAL_QUADRATIC, float(alpha))
+
+
+def _kind(kind):
+    """(integer kernel code, rational-quadratic alpha or None)."""
+    if isinstance(kind, tuple):
+        return int(kind[0]), float(kind[1])
+    return int(kind), None
 DEFAULT_JITTER = 1e-6  # gpjax/gps.py:68,344 and variational_families.py:118
 _FLOOR = 1e-36  # gpjax/kernels/stationary/utils.py:67
 
@@ -66,9 +80,14 @@ def _sqdist(x: np.ndarray, y: np.ndarray, ls) -> np.ndarray:
 
 def kernel_from_sqdist(kind: int, sq: np.ndarray, variance: float) -> np.ndarray:
     """Pointwise kernel value from the scaled squared distance."""
+    kind, alpha = _kind(kind)
     if kind == RBF:  # rbf.py:43
         return variance * np.exp(-0.5 * sq)
+    if kind == RATIONAL_QUADRATIC:  # rational_quadratic.py:76-83
+        return variance * (1.0 + 0.5 * sq / alpha) ** (-alpha)
     tau = np.sqrt(np.maximum(sq, _FLOOR))  # utils.py:67
+    if kind == MATERN12:  # matern12.py:44-48
+        return variance * np.exp(-tau)
     if kind == MATERN32:  # matern32.py:48-53
         return variance * (1.0 + np.sqrt(3.0) * tau) * np.exp(-np.sqrt(3.0) * tau)
     if kind == MATERN52:  # matern52.py:46-52
@@ -146,6 +165,48 @@ def conjugate_mll_cholesky(kind, X, y, ls, variance, obs_stddev, mean_const=0.0,
     diff = y - mean_const
     z = sla.solve_triangular(L, diff, lower=True)
     return float(-0.5 * (n * np.log(2 * np.pi) + 2.0 * np.log(np.diag(L)).sum() + z @ z))
+
+
+def conjugate_loocv(kind, X, y, ls, variance, obs_stddev, mean_const=0.0,
+                    jitter=DEFAULT_JITTER) -> float:
+    """Leave-one-out log predictive probability (objectives.py:157-178): the
+    solve and inverse of Sigma = Kxx + I (obs_var + jitter) by LU, then the sum
+    of the per-point Normal log-densities."""
+    X = np.asarray(X, np.float64)
+    y = np.asarray(y, np.float64).reshape(-1, 1)
+    n = X.shape[0]
+    mx = np.ones((n, 1)) * mean_const  # :161
+    Sigma = gram(kind, X, ls, variance) + np.eye(n) * (obs_stddev**2 + jitter)  # :164-167
+    Sigma_inv_y = np.linalg.solve(Sigma, y - mx)  # :170
+    Sigma_inv_diag = np.diag(np.linalg.inv(Sigma))[:, None]  # :171-172
+    means = mx + (y - mx) - Sigma_inv_y / Sigma_inv_diag  # :174
+    stds = np.sqrt(1.0 / Sigma_inv_diag)  # :175
+    lp = -0.5 * np.log(2 * np.pi) - np.log(stds) - 0.5 * ((y - means) / stds) ** 2  # :177-178
+    return float(lp.sum())
+
+
+def conjugate_loocv_torch(kind, X, y, ls, variance, obs_stddev, mean_const=0.0,
+                          jitter=DEFAULT_JITTER):
+    """conjugate_loocv and its gradient w.r.t. (lengthscale, variance,
+    obs_stddev, constant) by torch float64 autograd of the same sequence."""
+    torch = _torch()
+    Xt = torch.as_tensor(np.asarray(X, np.float64))
+    yt = torch.as_tensor(np.asarray(y, np.float64).reshape(-1, 1))
+    n = Xt.shape[0]
+    ls_t, var_t, sd_t, c_t = _params(ls, variance, obs_stddev, mean_const, Xt.shape[1])
+    Sigma = _t_kernel(kind, Xt, Xt, ls_t, var_t) + torch.eye(n, dtype=torch.float64) * (
+        sd_t**2 + jitter)
+    diff = yt - c_t
+    siy = torch.linalg.solve(Sigma, diff)
+    sid = torch.diagonal(torch.linalg.inv(Sigma))[:, None]
+    means = c_t + diff - siy / sid
+    stds = torch.sqrt(1.0 / sid)
+    lp = -0.5 * math.log(2 * math.pi) - torch.log(stds) - 0.5 * ((yt - means) / stds) ** 2
+    val = lp.sum()
+    val.backward()
+    grads = {"lengthscale": ls_t.grad.numpy().copy(), "variance": float(var_t.grad),
+             "obs_stddev": float(sd_t.grad), "constant": float(c_t.grad)}
+    return float(val.detach()), grads
 
 
 def collapsed_elbo(kind, X, y, Z, ls, variance, obs_stddev, mean_const=0.0,
@@ -241,9 +302,14 @@ def _t_kernel(kind, x, y, ls, variance):
     xs = x / ls
     ys = y / ls
     sq = ((xs[:, None, :] - ys[None, :, :]) ** 2).sum(-1)
+    kind, alpha = _kind(kind)
     if kind == RBF:
         return variance * torch.exp(-0.5 * sq)
+    if kind == RATIONAL_QUADRATIC:
+        return variance * (1.0 + 0.5 * sq / alpha) ** (-alpha)
     tau = torch.sqrt(torch.clamp(sq, min=_FLOOR))
+    if kind == MATERN12:
+        return variance * torch.exp(-tau)
     if kind == MATERN32:
         return variance * (1.0 + math.sqrt(3.0) * tau) * torch.exp(-math.sqrt(3.0) * tau)
     return (variance * (1.0 + math.sqrt(5.0) * tau + 5.0 / 3.0 * tau**2)
@@ -328,19 +394,29 @@ def conjugate_mll_grad_lu(kind, X, y, ls, variance, obs_stddev, mean_const=0.0,
             sq += (xs[r0:r1, k, None] - xs[None, :, k]) ** 2
         return sq
 
+    code, ka = _kind(kind)
+
     def kval(sq):  # unit variance: rbf.py:43, matern32.py:48-53, matern52.py:46-52
-        if kind == RBF:
+        if code == RBF:
             return torch.exp(-0.5 * sq)
+        if code == RATIONAL_QUADRATIC:
+            return (1.0 + 0.5 * sq / ka) ** (-ka)
         tau = torch.sqrt(torch.clamp(sq, min=_FLOOR))
-        if kind == MATERN32:
+        if code == MATERN12:
+            return torch.exp(-tau)
+        if code == MATERN32:
             return (1.0 + r3 * tau) * torch.exp(-r3 * tau)
         return (1.0 + r5 * tau + 5.0 / 3.0 * tau * tau) * torch.exp(-r5 * tau)
 
     def dcoef(sq):  # dk/dl_k = s2 * dcoef * (x_k - y_k)^2 / l_k^3 (zero below the floor)
-        if kind == RBF:
+        if code == RBF:
             return torch.exp(-0.5 * sq)
+        if code == RATIONAL_QUADRATIC:
+            return (1.0 + 0.5 * sq / ka) ** (-ka - 1.0)
         tau = torch.sqrt(torch.clamp(sq, min=_FLOOR))
-        if kind == MATERN32:
+        if code == MATERN12:
+            c = torch.exp(-tau) / tau
+        elif code == MATERN32:
             c = 3.0 * torch.exp(-r3 * tau)
         else:
             c = 5.0 / 3.0 * (1.0 + r5 * tau) * torch.exp(-r5 * tau)

@@ -212,6 +212,22 @@ def test_objective_entry_points_reject_bad_arguments(built_lib):
                                          None) == 6
     assert lib.gpk_conjugate_mll_noalloc(0, 10, 2, _P, 2, _P, None, 1, 1e-6, 1, _P, _P, _P,
                                          None) == 1
+    # leave-one-out objective: argument checks before any device work
+    lws = lib.gpk_conjugate_loocv_workspace_bytes(50, 2)
+    assert lws > 0
+    assert lib.gpk_conjugate_loocv(5, 50, 2, _P, 2, _P, _P, 1, 1e-6, 1, _P, _P, _P, _P, lws,
+                                   None) == 1                            # unknown kernel
+    assert lib.gpk_conjugate_loocv(0, 50, 2, _P, 1, _P, _P, 1, 1e-6, 1, _P, _P, _P, _P, lws,
+                                   None) == 1                            # ldx < d
+    assert lib.gpk_conjugate_loocv(0, 50, 2, _P, 2, _P, _P, 3, 1e-6, 1, _P, _P, _P, _P, lws,
+                                   None) == 1                            # n_ls not 1 or d
+    assert lib.gpk_conjugate_loocv(0, 50, 2, _P, 2, _P, _P, 1, 1e-6, 1, _P, _P, _P, _P, lws - 1,
+                                   None) == 3                            # workspace too small
+    # d past the library-wide bound (32) is a bad argument, as for gpk_conjugate_mll
+    assert lib.gpk_conjugate_mll_noalloc(0, 10, 33, _P, 33, _P, _P, 1, 1e-6, 1, _P, _P, _P,
+                                         None) == 1
+    assert lib.gpk_conjugate_mll_noalloc(0, 10, 32, _P, 31, _P, _P, 1, 1e-6, 1, _P, _P, _P,
+                                         None) == 1                      # ldx < d
 
 
 def test_gemm_entry_point_rejects_bad_arguments(built_lib):

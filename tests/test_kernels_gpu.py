@@ -12,14 +12,21 @@ from oracle import gp_oracle as O
 pytestmark = pytest.mark.gpu
 
 
+def _kern(cls, ls, var):
+    if cls is K.RationalQuadratic:
+        return cls(lengthscale=ls, variance=var, alpha=0.7)
+    return cls(lengthscale=ls, variance=var)
+
+
 @pytest.mark.parametrize("cls,kind", [(K.RBF, O.RBF), (K.Matern32, O.MATERN32),
-                                      (K.Matern52, O.MATERN52)])
+                                      (K.Matern52, O.MATERN52), (K.Matern12, O.MATERN12),
+                                      (K.RationalQuadratic, O.rational_quadratic(0.7))])
 @pytest.mark.parametrize("n,m,d", [(1, 1, 1), (7, 3, 2), (65, 130, 8), (200, 33, 16)])
 def test_cross_covariance_parity(cuda_lib, cls, kind, n, m, d):
     rng = np.random.default_rng(n + m + d)
     x, y = rng.standard_normal((n, d)), rng.standard_normal((m, d))
     ls = np.exp(rng.uniform(-1, 1, d))
-    k = cls(lengthscale=ls, variance=0.7)
+    k = _kern(cls, ls, 0.7)
     out = k.cross_covariance(torch.as_tensor(x, device="cuda"),
                              torch.as_tensor(y, device="cuda")).cpu().numpy()
     ref = O.cross_covariance(kind, x, y, ls, 0.7)
@@ -76,3 +83,28 @@ def test_cholesky_not_pd_reports_info(cuda_lib):
     L, info = LA.cholesky_dense(A)
     assert int(info.item()) == 2
     assert torch.isnan(L[1, 1])
+
+
+@pytest.mark.parametrize("cls,kind", [(K.Matern12, O.MATERN12),
+                                      (K.RationalQuadratic, O.rational_quadratic(0.7))])
+def test_cross_covariance_vjp_added_kernels(cuda_lib, cls, kind):
+    """Gradient of sum(G * K(x, y)) w.r.t. lengthscales, variance and both inputs
+    against torch float64 autograd of the oracle's kernel."""
+    rng = np.random.default_rng(3)
+    x, y = rng.standard_normal((40, 3)), rng.standard_normal((25, 3))
+    ls = np.exp(rng.uniform(-0.5, 0.5, 3))
+    G = rng.standard_normal((40, 25))
+    k = _kern(cls, ls, 0.9)
+    k.lengthscale.to("cuda").requires_grad_(True)
+    k.variance.to("cuda").requires_grad_(True)
+    X = torch.as_tensor(x, device="cuda").requires_grad_(True)
+    Y = torch.as_tensor(y, device="cuda").requires_grad_(True)
+    (k.cross_covariance(X, Y) * torch.as_tensor(G, device="cuda")).sum().backward()
+    lt = torch.tensor(ls, requires_grad=True)
+    vt = torch.tensor(0.9, dtype=torch.float64, requires_grad=True)
+    xt = torch.tensor(x, requires_grad=True)
+    yt = torch.tensor(y, requires_grad=True)
+    (O._t_kernel(kind, xt, yt, lt, vt) * torch.as_tensor(G)).sum().backward()
+    for got, ref in ((k.lengthscale.value.grad, lt.grad), (k.variance.value.grad, vt.grad),
+                     (X.grad, xt.grad), (Y.grad, yt.grad)):
+        assert np.allclose(got.cpu().numpy(), ref.numpy(), rtol=1e-9, atol=1e-11)

@@ -146,3 +146,30 @@ def test_mll_mixed_dirty_workspace(cuda_lib, n):
     (v0, g0), (v1, g1) = results
     assert abs(v1 - ref) <= 1e-6 * abs(ref), (v1, ref)
     assert v1 == v0 and np.array_equal(g1, g0)
+
+
+@pytest.mark.parametrize("kind", [O.MATERN12, O.rational_quadratic(0.8)])
+@pytest.mark.parametrize("n,d", [(300, 3), (1100, 5)])
+def test_mll_added_kernels(cuda_lib, kind, n, d):
+    """Matern12 and RationalQuadratic: float64 form at the float64 tolerances;
+    mixed form at 1e-6 relative on the MLL and 1e-4 on the gradient norm."""
+    from gpjax_gb300 import kernels as K
+    rng = np.random.default_rng(n + d)
+    x = rng.standard_normal((n, d))
+    ls = np.exp(rng.uniform(np.log(0.5), np.log(3.0), d))
+    S = O.gram(kind, x, ls, 1.0) + (1e-6 + 1e-2) * np.eye(n)
+    y = (np.linalg.cholesky(S) @ rng.standard_normal(n))[:, None]
+    ref, gref = oracle(kind, x, y, ls, 1.0, 0.1, 0.05)
+    for prec, vtol, gtol in (("fp64", 1e-10, 1e-7), ("mixed", 1e-6, 1e-4)):
+        if isinstance(kind, tuple):
+            kern = K.RationalQuadratic(lengthscale=ls, variance=1.0, alpha=kind[1])
+        else:
+            kern = K.Matern12(lengthscale=ls, variance=1.0)
+        prior = gpx.gps.Prior(kernel=kern, mean_function=gpx.mean_functions.Constant(
+            gpx.parameters.Real(0.05)), jitter=1e-6)
+        post = to_cuda_params(prior * gpx.likelihoods.Gaussian(num_datapoints=n, obs_stddev=0.1))
+        val = gpx.objectives.conjugate_mll(post, gpx.Dataset(X=x, y=y), precision=prec)
+        val.backward()
+        g = grads_of(post)
+        assert abs(float(val.detach()) - ref) <= vtol * abs(ref), (prec, float(val), ref)
+        assert np.linalg.norm(g - gref) <= gtol * np.linalg.norm(gref), (prec, g, gref)

@@ -221,3 +221,78 @@ def test_lean_lu_port_matches_autograd(kind, ard):
                         [g2["variance"], g2["obs_stddev"], g2["constant"]]])
     assert abs(v1 - v2) <= 1e-12 * abs(v1)
     assert np.allclose(a, b, rtol=1e-12, atol=1e-12 * np.abs(a).max())
+
+
+@pytest.mark.parametrize("ard", [True, False])
+def test_matern12_and_rational_quadratic_match_an_independent_implementation(ard):
+    """Matern12 (matern12.py:44-48) against scikit-learn's Matern(nu=0.5), and the
+    isotropic RationalQuadratic (rational_quadratic.py:76-83) against
+    scikit-learn's RationalQuadratic (scalar length scale only)."""
+    gpk = pytest.importorskip("sklearn.gaussian_process.kernels")
+    rng = np.random.default_rng(9)
+    x, y = rng.standard_normal((40, 3)), rng.standard_normal((30, 3))
+    ls = np.array([0.4, 1.1, 2.5]) if ard else 0.8
+    ref = (gpk.ConstantKernel(1.7) * gpk.Matern(length_scale=ls, nu=0.5))(x, y)
+    assert np.allclose(O.cross_covariance(O.MATERN12, x, y, ls, 1.7), ref, rtol=1e-12, atol=1e-14)
+    if not ard:
+        for alpha in (0.5, 2.0):
+            ref = (gpk.ConstantKernel(1.7) * gpk.RationalQuadratic(length_scale=ls, alpha=alpha))(x, y)
+            got = O.cross_covariance(O.rational_quadratic(alpha), x, y, ls, 1.7)
+            assert np.allclose(got, ref, rtol=1e-12, atol=1e-14)
+
+
+@pytest.mark.parametrize("kind", [O.MATERN12, O.rational_quadratic(0.7)])
+@pytest.mark.parametrize("ard", [True, False])
+def test_added_kernels_lean_port_and_finite_differences(kind, ard):
+    """The lean port and autograd agree for the added kernels, and both match
+    central differences of the value."""
+    rng = np.random.default_rng(21)
+    n, d = 120, 3
+    x = rng.standard_normal((n, d))
+    y = rng.standard_normal((n, 1))
+    ls = np.exp(rng.uniform(-0.5, 0.5, d)) if ard else np.array(1.1)
+    v1, g1 = O.conjugate_mll_torch(kind, x, y, ls, 1.2, 0.3, 0.1)
+    v2, g2 = O.conjugate_mll_grad_lu(kind, x, y, ls, 1.2, 0.3, 0.1, block=64)
+    a = np.concatenate([np.atleast_1d(g1["lengthscale"]),
+                        [g1["variance"], g1["obs_stddev"], g1["constant"]]])
+    b = np.concatenate([np.atleast_1d(g2["lengthscale"]),
+                        [g2["variance"], g2["obs_stddev"], g2["constant"]]])
+    assert abs(v1 - v2) <= 1e-12 * abs(v1)
+    assert np.allclose(a, b, rtol=1e-10, atol=1e-10 * np.abs(a).max())
+    vec = np.concatenate([np.atleast_1d(ls), [1.2, 0.3, 0.1]])
+    nl = vec.size - 3
+
+    def f(v):
+        lsv = v[:nl] if ard else np.array(v[0])
+        return O.conjugate_mll(kind, x, y, lsv, v[nl], v[nl + 1], v[nl + 2])
+    fd = O.central_fd(f, vec, 1e-6)
+    assert np.allclose(a, fd, rtol=1e-5, atol=1e-6 * np.abs(fd).max())
+
+
+@pytest.mark.parametrize("kind", [O.RBF, O.MATERN52])
+def test_loocv_oracle_gradient_and_identity(kind):
+    """conjugate_loocv's autograd gradient matches central differences, and the
+    value equals the explicit leave-one-out sum (refit without point i, predict it)."""
+    rng = np.random.default_rng(5)
+    n, d = 25, 2
+    x = rng.uniform(-2, 2, (n, d))
+    y = (np.sin(x).sum(1) + 0.1 * rng.standard_normal(n))[:, None]
+    ls, var, sd, c = np.array([0.8, 1.3]), 1.1, 0.3, 0.2
+    v, g = O.conjugate_loocv_torch(kind, x, y, ls, var, sd, c)
+    assert abs(v - O.conjugate_loocv(kind, x, y, ls, var, sd, c)) < 1e-10 * abs(v)
+    vec = np.concatenate([ls, [var, sd, c]])
+    fd = O.central_fd(lambda p: O.conjugate_loocv(kind, x, y, p[:2], p[2], p[3], p[4]), vec, 1e-6)
+    gv = np.concatenate([g["lengthscale"], [g["variance"], g["obs_stddev"], g["constant"]]])
+    assert np.allclose(gv, fd, rtol=1e-5, atol=1e-7)
+    # brute force: for each i, the predictive density of y_i from the other n-1 points
+    S = O.gram(kind, x, ls, var) + np.eye(n) * (sd * sd + 1e-6)
+    tot = 0.0
+    for i in range(n):
+        keep = np.arange(n) != i
+        Sk = S[np.ix_(keep, keep)]
+        kv = S[i, keep]
+        w = np.linalg.solve(Sk, kv)
+        mu = c + w @ (y[keep, 0] - c)
+        var_i = S[i, i] - kv @ w
+        tot += -0.5 * np.log(2 * np.pi * var_i) - 0.5 * (y[i, 0] - mu) ** 2 / var_i
+    assert abs(tot - v) < 1e-9 * abs(v)

@@ -76,6 +76,29 @@ def test_no_alloc_matches_workspace_entry_point_twice(cuda_lib):
         assert torch.allclose(g, gref, rtol=1e-7, atol=1e-9), (g, gref)
 
 
+def test_no_alloc_takes_no_device_memory(cuda_lib):
+    """After a first call on the device (which loads the library's kernels),
+    further calls change neither torch's allocation count nor the device's
+    free memory."""
+    x, y, theta = _inputs(3, 256, 4, _lib.RBF)
+    _no_alloc(_lib.RBF, x, y, theta, 4)
+    torch.cuda.synchronize()
+    out = torch.empty(1, dtype=torch.float64, device="cuda")
+    grad = torch.empty(7, dtype=torch.float64, device="cuda")
+    info = torch.zeros(1, dtype=torch.int32, device="cuda")
+    lib = _lib.lib()
+    alloc0, free0 = torch.cuda.memory_allocated(), torch.cuda.mem_get_info()[0]
+    for _ in range(2):
+        st = lib.gpk_conjugate_mll_noalloc(_lib.RBF, 256, 4, x.data_ptr(), 4, y.data_ptr(),
+                                           theta.data_ptr(), 4, 1e-6, 1, out.data_ptr(),
+                                           grad.data_ptr(), info.data_ptr(), _lib.stream_ptr())
+        assert st == 0
+    torch.cuda.synchronize()
+    assert int(info.item()) == 0 and np.isfinite(float(out.item()))
+    assert torch.cuda.memory_allocated() == alloc0
+    assert torch.cuda.mem_get_info()[0] == free0
+
+
 def test_no_alloc_refuses_sizes_beyond_its_scratch(cuda_lib):
     lib = _lib.lib()
     fake = ctypes.c_void_p(0x1000)  # never dereferenced: the size check fails first
