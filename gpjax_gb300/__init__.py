@@ -5,13 +5,14 @@ objectives, gps, likelihoods, mean_functions, linalg, distributions,
 variational_families, Dataset.  All arithmetic runs in libgpk.so (CUDA,
 sm_103a) through its C ABI (include/gpk.h).
 """
-from . import (computations, config, distributions, gps, kernels, likelihoods, linalg,
+from . import (computations, config, distributions, fit, gps, kernels, likelihoods, linalg,
                mean_functions, objectives, parameters, variational_families)
 from ._lib import GPKError
 from .dataset import Dataset
 
 __version__ = "0.1.0"
 
-__all__ = ["Dataset", "GPKError", "computations", "config", "distributions", "gps", "kernels",
+__all__ = ["Dataset", "GPKError", "computations", "config", "distributions", "fit", "gps",
+           "kernels",
            "likelihoods", "linalg", "mean_functions", "objectives", "parameters",
            "variational_families"]

@@ -133,6 +133,43 @@ def ptr(t: torch.Tensor | None) -> int | None:
     return None if t is None else t.data_ptr()
 
 
+_RESIDENT: dict = {}  # device index -> uint8 buffer, while a resident_workspace() is open
+
+
 def workspace(nbytes: int, device: torch.device) -> torch.Tensor:
-    """Caller-owned workspace for one call (the library never allocates)."""
-    return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+    """Caller-owned workspace for one call (the library never allocates).  Inside
+    ``resident_workspace(device)`` every call gets the front of one buffer that
+    stays allocated between calls (grown when a call needs more)."""
+    nbytes = max(int(nbytes), 256)
+    idx = torch.device(device).index
+    if idx is None:
+        idx = torch.cuda.current_device()
+    if idx in _RESIDENT:
+        buf = _RESIDENT[idx]
+        if buf is None or buf.numel() < nbytes:
+            buf = _RESIDENT[idx] = None  # release the old buffer before growing
+            buf = _RESIDENT[idx] = torch.empty(nbytes, dtype=torch.uint8, device=device)
+        return buf[:nbytes]
+    return torch.empty(nbytes, dtype=torch.uint8, device=device)
+
+
+class resident_workspace:
+    """Keeps one workspace buffer on ``device`` for the library calls made inside
+    the block (repeated objective evaluations of a fit): calls on the device's
+    streams are stream-ordered, so they may share it; do not run concurrent
+    streams of library work inside the block."""
+
+    def __init__(self, device=None):
+        d = torch.device("cuda") if device is None else torch.device(device)
+        self.idx = d.index if d.index is not None else torch.cuda.current_device()
+
+    def __enter__(self):
+        self.owner = self.idx not in _RESIDENT
+        if self.owner:
+            _RESIDENT[self.idx] = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.owner:
+            _RESIDENT.pop(self.idx, None)
+        return False
