@@ -173,3 +173,19 @@ def test_mll_added_kernels(cuda_lib, kind, n, d):
         g = grads_of(post)
         assert abs(float(val.detach()) - ref) <= vtol * abs(ref), (prec, float(val), ref)
         assert np.linalg.norm(g - gref) <= gtol * np.linalg.norm(gref), (prec, g, gref)
+
+
+@pytest.mark.parametrize("precision,vtol,gtol", [("fp64", 1e-10, 1e-7), ("mixed", 1e-6, 1e-4)])
+def test_mll_c2_generator_n8192(cuda_lib, precision, vtol, gtol):
+    """The benchmark's generator (Matern-5/2 ARD, d = 8, X ~ N(0, I), log-uniform
+    lengthscales in [0.3, 3], noise 1e-2, y a float64 prior sample) at n = 8192,
+    both forms against the float64 oracle (the reference's LU op sequence)."""
+    import bench
+    n, d = 8192, 8
+    x, ls, eps = bench.c2_inputs(n, d, 1)
+    y = bench.c2_y_host(x, ls, eps)[:, None]
+    ref, g = O.conjugate_mll_grad_lu(O.MATERN52, x, y, ls, 1.0, 0.1, 0.0)
+    gref = np.concatenate([g["lengthscale"], [g["variance"], g["obs_stddev"], g["constant"]]])
+    val, gg = run(2, x, y, ls, 1.0, 0.1, 0.0, precision)
+    assert abs(val - ref) <= vtol * abs(ref), (precision, val, ref, abs(val - ref) / abs(ref))
+    assert np.linalg.norm(gg - gref) <= gtol * np.linalg.norm(gref), (precision, gg, gref)
