@@ -479,38 +479,53 @@ def ctypes_void_array(k):
 
 
 def run_c3(args):
-    """Precision stress (workload c3): exact-GP MLL + gradient at n = 65536, d = 16,
-    RBF ARD, X ~ U[0,1]^16, lengthscales log-U[0.1, 1], variance 1, noise 1e-3,
-    jitter 1e-6; mixed form timed over a few evaluations, the float64 form once as the
-    accuracy reference.  y = sum_j sin(2 pi x_j) / 4 + N(0, 1e-3) (a smooth target in
-    place of a float64 prior sample, which would need a second n = 65536 float64
-    factorisation)."""
+    """Precision stress (workload c3): exact GP at n = 65536, d = 16, RBF ARD,
+    X ~ U[0,1]^16, lengthscales log-U[0.1, 1], variance 1, noise 1e-3, jitter
+    1e-6, y = a float64 prior sample plus noise (drawn through the library's
+    float64 Gram and Cholesky), 4096 test points from the same X distribution.
+    Mixed form against the plain float64 form on the MLL, its gradient and the
+    predictive variance."""
     import torch
 
     from gpjax_gb300 import _lib
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
     lib = _lib.lib()
-    n, d = args.n or 65536, args.d or 16
+    n, d, t = args.n or 65536, args.d or 16, 4096
     rng = np.random.default_rng(args.seed)
     x = rng.uniform(0.0, 1.0, (n, d))
     ls = np.exp(rng.uniform(np.log(0.1), np.log(1.0), d))
-    y = np.sin(2 * np.pi * x).sum(axis=1) / 4 + np.sqrt(1e-3) * rng.standard_normal(n)
+    xt = rng.uniform(0.0, 1.0, (t, d))
+    eps = rng.standard_normal(n)
+    noise = 1e-3
     X = torch.as_tensor(x, device=dev)
-    Y = torch.as_tensor(y, device=dev)
-    theta = torch.tensor(list(ls) + [1.0, float(np.sqrt(1e-3)), 0.0], dtype=torch.float64,
+    XT = torch.as_tensor(xt, device=dev)
+    theta = torch.tensor(list(ls) + [1.0, float(np.sqrt(noise)), 0.0], dtype=torch.float64,
                          device=dev)
+    stream = torch.cuda.current_stream(dev)
+    # y = chol(K + (jitter + noise) I) eps, float64 (data generation, untimed)
+    t0 = time.perf_counter()
+    S = torch.empty((n, n), dtype=torch.float64, device=dev)
+    _lib.call("gpk_gram", _lib.RBF, n, d, X.data_ptr(), d, theta.data_ptr(), d, _lib.F64,
+              S.data_ptr(), n, stream.cuda_stream)
+    S.diagonal().add_(1e-6 + noise)
+    info = torch.zeros(1, dtype=torch.int32, device=dev)
+    _lib.call("gpk_lower_cholesky", n, _lib.F64, S.data_ptr(), n, None, info.data_ptr(),
+              stream.cuda_stream)
+    L = S
+    Y = torch.zeros(n, dtype=torch.float64, device=dev)
+    E = torch.as_tensor(eps, device=dev)
+    for r0 in range(0, n, 8192):  # row blocks of L (lower triangle, upper part zero)
+        Y[r0:r0 + 8192] = L[r0:r0 + 8192, :r0 + 8192] @ E[:r0 + 8192]
+    torch.cuda.synchronize(dev)
+    assert int(info.item()) == 0
+    del S, L
+    torch.cuda.empty_cache()
+    t_gen = time.perf_counter() - t0
     out = torch.zeros(1, dtype=torch.float64, device=dev)
     grad = torch.zeros(d + 3, dtype=torch.float64, device=dev)
-    info = torch.zeros(1, dtype=torch.int32, device=dev)
-    stream = torch.cuda.current_stream(dev)
 
-    def run(prec, steps, warm):
-        ws = _lib.workspace(lib.gpk_conjugate_mll_workspace_bytes(n, d, prec), dev)
-        call = lambda: _lib.call("gpk_conjugate_mll", _lib.RBF, n, d, X.data_ptr(), d,
-                                 Y.data_ptr(), theta.data_ptr(), d, 1e-6, prec, 1,
-                                 out.data_ptr(), grad.data_ptr(), info.data_ptr(),
-                                 ws.data_ptr(), ws.numel(), stream.cuda_stream)
+    def timed(call, steps, warm):
         for _ in range(warm):
             call()
         torch.cuda.synchronize(dev)
@@ -520,26 +535,56 @@ def run_c3(args):
             call()
         e1.record(stream)
         torch.cuda.synchronize(dev)
-        t = e0.elapsed_time(e1) / 1000.0 / steps
-        res = (float(out.item()), grad.cpu().numpy().copy(), int(info.item()), t)
+        return e0.elapsed_time(e1) / 1000.0 / steps
+
+    def mll(prec, steps, warm):
+        ws = _lib.workspace(lib.gpk_conjugate_mll_workspace_bytes(n, d, prec), dev)
+        tm = timed(lambda: _lib.call("gpk_conjugate_mll", _lib.RBF, n, d, X.data_ptr(), d,
+                                     Y.data_ptr(), theta.data_ptr(), d, 1e-6, prec, 1,
+                                     out.data_ptr(), grad.data_ptr(), info.data_ptr(),
+                                     ws.data_ptr(), ws.numel(), stream.cuda_stream), steps, warm)
+        res = (float(out.item()), grad.cpu().numpy().copy(), int(info.item()), tm)
         del ws
         torch.cuda.empty_cache()
         return res
 
-    mm, gm, im, tm = run(_lib.PREC_MIXED, max(1, min(args.steps, 3)), 1)
-    line = {"workload": "c3 precision stress: exact GP MLL + gradient, RBF ARD, "
-                        f"n={n}, d={d}, X~U[0,1]^{d}, noise 1e-3",
+    def predict(prec):
+        mean = torch.zeros(t, dtype=torch.float64, device=dev)
+        var = torch.zeros(t, dtype=torch.float64, device=dev)
+        ws = _lib.workspace(lib.gpk_predict_workspace_bytes(n, t, d, prec), dev)
+        tp = timed(lambda: _lib.call("gpk_predict", _lib.RBF, n, t, d, X.data_ptr(), d,
+                                     Y.data_ptr(), XT.data_ptr(), d, theta.data_ptr(), d, 1e-6,
+                                     1e-6, prec, mean.data_ptr(), var.data_ptr(), None, 0,
+                                     info.data_ptr(), ws.data_ptr(), ws.numel(),
+                                     stream.cuda_stream), 1, 0)
+        res = (mean.cpu().numpy(), var.cpu().numpy(), int(info.item()), tp)
+        del ws
+        torch.cuda.empty_cache()
+        return res
+
+    mm, gm, im, tm = mll(_lib.PREC_MIXED, max(1, min(args.steps, 3)), 1)
+    pm_mean, pm_var, ipm, tpm = predict(_lib.PREC_MIXED)
+    line = {"workload": "c3 precision stress: exact GP MLL + gradient + predictive variance, "
+                        f"RBF ARD, n={n}, d={d}, X~U[0,1]^{d}, lengthscales log-U[0.1,1], "
+                        f"noise 1e-3, y = float64 prior sample + noise, {t} test points",
             "metric": f"MLL+grad evals/s at n={n}", "unit": "evals/s", "n": n, "d": d,
+            "data": "synthetic", "y_generation_s": t_gen,
             "mixed": {"evals_per_s": 1.0 / tm, "ms_per_step": 1000.0 * tm, "mll": mm,
-                      "info": im},
-            "data": "synthetic"}
+                      "info": im, "predict_ms": 1000.0 * tpm, "predict_info": ipm}}
     if args.fp64_steps > 0:
-        m64, g64, i64, t64 = run(_lib.PREC_FP64, 1, 0)
-        line["fp64_form"] = {"evals_per_s": 1.0 / t64, "ms_per_step": 1000.0 * t64,
-                             "mll": m64, "info": i64}
+        m64, g64, i64, t64 = mll(_lib.PREC_FP64, 1, 0)
+        p64_mean, p64_var, ip64, tp64 = predict(_lib.PREC_FP64)
+        line["fp64_form"] = {"evals_per_s": 1.0 / t64, "ms_per_step": 1000.0 * t64, "mll": m64,
+                             "info": i64, "predict_ms": 1000.0 * tp64, "predict_info": ip64}
         line["speedup_vs_fp64"] = t64 / tm
         line["rel_err_mll_vs_fp64"] = abs(mm - m64) / abs(m64)
         line["rel_err_grad_vs_fp64"] = float(np.linalg.norm(gm - g64) / np.linalg.norm(g64))
+        line["max_rel_err_grad_component"] = float(np.max(np.abs(gm - g64) /
+                                                          np.maximum(np.abs(g64), 1e-300)))
+        line["max_rel_err_pred_var_vs_fp64"] = float(np.max(np.abs(pm_var - p64_var) /
+                                                            np.abs(p64_var)))
+        line["max_abs_err_pred_mean_vs_fp64"] = float(np.max(np.abs(pm_mean - p64_mean)))
+        line["pred_var_range_fp64"] = [float(p64_var.min()), float(p64_var.max())]
     print(json.dumps(line), flush=True)
 
 

@@ -44,6 +44,12 @@ SIGNATURES = {
     "gpk_solve_triangular_workspace_bytes": (_c_size, [_c_i64, _c_i64, _c_int]),
     "gpk_solve_triangular": (_c_int, [_c_i64, _c_i64, _c_int, _c_ptr, _c_i64, _c_ptr, _c_i64,
                                       _c_ptr, _c_size, _c_ptr]),
+    "gpk_solve_triangular_ex_workspace_bytes": (_c_size, [_c_i64, _c_i64, _c_int, _c_int]),
+    "gpk_solve_triangular_ex": (_c_int, [_c_i64, _c_i64, _c_int, _c_int, _c_int, _c_ptr, _c_i64,
+                                         _c_ptr, _c_i64, _c_ptr, _c_size, _c_ptr]),
+    "gpk_gemm_f64_workspace_bytes": (_c_size, [_c_int, _c_int, _c_i64, _c_i64, _c_i64]),
+    "gpk_gemm_f64": (_c_int, [_c_int, _c_int, _c_i64, _c_i64, _c_i64, _c_dbl, _c_ptr, _c_i64,
+                              _c_ptr, _c_i64, _c_dbl, _c_ptr, _c_i64, _c_ptr, _c_size, _c_ptr]),
     "gpk_logdet_triangular": (_c_int, [_c_i64, _c_int, _c_ptr, _c_i64, _c_ptr, _c_ptr]),
     "gpk_conjugate_mll_workspace_bytes": (_c_size, [_c_i64, _c_int, _c_int]),
     "gpk_conjugate_mll": (_c_int, [_c_int, _c_i64, _c_int, _c_ptr, _c_i64, _c_ptr, _c_ptr, _c_int,

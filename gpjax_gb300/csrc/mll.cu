@@ -556,45 +556,68 @@ __global__ void transpose_kernel(int rows, int cols, const T* __restrict__ src, 
 }
 
 template <typename T>
-static size_t solve_layout(int64_t n, int64_t nrhs, void* ws, T** M, T** V, T** scr, T** BT,
-                           int64_t* ld) {
+static size_t solve_layout(int64_t n, int64_t nrhs, bool upper, void* ws, T** M, T** V, T** scr,
+                           T** BT, T** LT, int64_t* ld) {
   Arena a(ws);
   *ld = pad_ld(n);
   *M = a.take<T>((size_t)n * *ld);
   *V = a.take<T>((size_t)n * *ld);
   *scr = a.take<T>((size_t)n * n / 2 + 64);
   *BT = a.take<T>((size_t)nrhs * *ld);
+  *LT = upper ? a.take<T>((size_t)n * *ld) : nullptr;  // lower copy U^T of an upper input
   return a.off + 256;
 }
 
-extern "C" size_t gpk_solve_triangular_workspace_bytes(int64_t n, int64_t nrhs, int dtype) {
+static size_t solve_ws(int64_t n, int64_t nrhs, int dtype, bool upper) {
   int64_t ld;
   if (dtype == GPK_F64) {
-    double *M, *V, *S, *B;
-    return solve_layout<double>(n, nrhs, nullptr, &M, &V, &S, &B, &ld);
+    double *M, *V, *S, *B, *LT;
+    return solve_layout<double>(n, nrhs, upper, nullptr, &M, &V, &S, &B, &LT, &ld);
   }
-  float *M, *V, *S, *B;
-  return solve_layout<float>(n, nrhs, nullptr, &M, &V, &S, &B, &ld);
+  float *M, *V, *S, *B, *LT;
+  return solve_layout<float>(n, nrhs, upper, nullptr, &M, &V, &S, &B, &LT, &ld);
 }
 
+extern "C" size_t gpk_solve_triangular_workspace_bytes(int64_t n, int64_t nrhs, int dtype) {
+  return solve_ws(n, nrhs, dtype, false);
+}
+
+extern "C" size_t gpk_solve_triangular_ex_workspace_bytes(int64_t n, int64_t nrhs, int dtype,
+                                                          int upper) {
+  return solve_ws(n, nrhs, dtype, upper != 0);
+}
+
+// op(T) X = B in place.  A lower input L gives M = L^-1 and V = L^-T by the
+// triangular inverse; an upper input U is first copied to the lower L = U^T,
+// so that U^-1 = L^-T (V) and U^-T = L^-1 (M).  X^T = B^T op^T, one NT GEMM
+// whose transposed output lands in B.
 template <typename T>
-static gpk_status solve_run(int n, int nrhs, const T* L, int64_t lda, T* B, int64_t ldb, void* ws,
-                            cudaStream_t s) {
-  T *M, *V, *scr, *BT;
+static gpk_status solve_run(int n, int nrhs, const T* L, int64_t lda, bool upper, bool trans,
+                            T* B, int64_t ldb, void* ws, cudaStream_t s) {
+  T *M, *V, *scr, *BT, *LT;
   int64_t ld;
-  solve_layout<T>(n, nrhs, ws, &M, &V, &scr, &BT, &ld);
-  GPK_CUDA_TRY(trtri_lower<T>(L, lda, n, M, ld, V, ld, scr, s));
+  solve_layout<T>(n, nrhs, upper, ws, &M, &V, &scr, &BT, &LT, &ld);
   dim3 tb(32, 8);
-  dim3 grid((unsigned)cdiv(nrhs, 32), (unsigned)cdiv(n, 32));
-  transpose_kernel<T><<<grid, tb, 0, s>>>(n, nrhs, B, ldb, BT, ld);
+  if (upper) {
+    transpose_kernel<T><<<dim3((unsigned)cdiv(n, 32), (unsigned)cdiv(n, 32)), tb, 0, s>>>(
+        n, n, L, lda, LT, ld);
+    GPK_LAUNCH_CHECK();
+    L = LT;
+    lda = ld;
+  }
+  GPK_CUDA_TRY(trtri_lower<T>(L, lda, n, M, ld, V, ld, scr, s));
+  // lower: T^-1 = M, T^-T = V ; upper (T = L^T): T^-1 = V, T^-T = M
+  const bool use_v = upper != trans;
+  transpose_kernel<T><<<dim3((unsigned)cdiv(nrhs, 32), (unsigned)cdiv(n, 32)), tb, 0, s>>>(
+      n, nrhs, B, ldb, BT, ld);
   GPK_LAUNCH_CHECK();
   GemmProb<T> p{};
   p.A = BT;
   p.lda = ld;
   p.M = nrhs;
-  p.B = M;
+  p.B = use_v ? V : M;
   p.ldb = ld;
-  p.b_tri = TRI_LOWER;
+  p.b_tri = use_v ? TRI_UPPER : TRI_LOWER;
   p.N = n;
   p.K = n;
   p.C = nullptr;
@@ -606,21 +629,105 @@ static gpk_status solve_run(int n, int nrhs, const T* L, int64_t lda, T* B, int6
   return GPK_OK;
 }
 
+static gpk_status solve_dispatch(int64_t n, int64_t nrhs, int dtype, bool upper, bool trans,
+                                 const void* L, int64_t lda, void* B, int64_t ldb,
+                                 void* workspace, size_t workspace_bytes, cudaStream_t stream) {
+  if (n < 0 || nrhs < 0 || n > (1 << 20) || lda < n || ldb < nrhs) return GPK_ERR_BAD_ARG;
+  if (dtype != GPK_F64 && dtype != GPK_F32) return GPK_ERR_BAD_ARG;
+  if (n == 0 || nrhs == 0) return GPK_OK;
+  if (!L || !B || !workspace) return GPK_ERR_BAD_ARG;
+  if (workspace_bytes < solve_ws(n, nrhs, dtype, upper)) return GPK_ERR_WORKSPACE;
+  if (dtype == GPK_F64)
+    return solve_run<double>((int)n, (int)nrhs, (const double*)L, lda, upper, trans, (double*)B,
+                             ldb, workspace, stream);
+  return solve_run<float>((int)n, (int)nrhs, (const float*)L, lda, upper, trans, (float*)B, ldb,
+                          workspace, stream);
+}
+
 extern "C" gpk_status gpk_solve_triangular(int64_t n, int64_t nrhs, int dtype, const void* L,
                                            int64_t lda, void* B, int64_t ldb, void* workspace,
                                            size_t workspace_bytes, cudaStream_t stream) {
-  if (n < 0 || nrhs < 0 || n > (1 << 20) || lda < n || ldb < nrhs) return GPK_ERR_BAD_ARG;
-  if (n == 0 || nrhs == 0) return GPK_OK;
-  if (!L || !B || !workspace) return GPK_ERR_BAD_ARG;
-  if (workspace_bytes < gpk_solve_triangular_workspace_bytes(n, nrhs, dtype))
+  return solve_dispatch(n, nrhs, dtype, false, false, L, lda, B, ldb, workspace, workspace_bytes,
+                        stream);
+}
+
+extern "C" gpk_status gpk_solve_triangular_ex(int64_t n, int64_t nrhs, int dtype, int upper,
+                                              int trans, const void* T, int64_t ldt, void* B,
+                                              int64_t ldb, void* workspace,
+                                              size_t workspace_bytes, cudaStream_t stream) {
+  return solve_dispatch(n, nrhs, dtype, upper != 0, trans != 0, T, ldt, B, ldb, workspace,
+                        workspace_bytes, stream);
+}
+
+// ---------------------------------------------------------------------------
+// float64 GEMM C = alpha op(A) op(B) + beta C (row-major), on the library's
+// NT kernel: operands that are not already in NT form are transposed into the
+// workspace first.
+// ---------------------------------------------------------------------------
+static size_t gemm64_layout(int64_t M, int64_t N, int64_t K, int transa, int transb, void* ws,
+                            double** At, double** Bt, int64_t* lda_t, int64_t* ldb_t) {
+  Arena a(ws);
+  *lda_t = pad_ld(K);
+  *ldb_t = pad_ld(K);
+  *At = transa ? a.take<double>((size_t)M * *lda_t) : nullptr;  // op(A) = A^T: A^T copy [M, K]
+  *Bt = transb ? nullptr : a.take<double>((size_t)N * *ldb_t);  // op(B) = B: B^T copy [N, K]
+  return a.off + 256;
+}
+
+extern "C" size_t gpk_gemm_f64_workspace_bytes(int transa, int transb, int64_t M, int64_t N,
+                                               int64_t K) {
+  double *a, *b;
+  int64_t la, lb;
+  return gemm64_layout(M, N, K, transa, transb, nullptr, &a, &b, &la, &lb);
+}
+
+extern "C" gpk_status gpk_gemm_f64(int transa, int transb, int64_t M, int64_t N, int64_t K,
+                                   double alpha, const double* A, int64_t lda, const double* B,
+                                   int64_t ldb, double beta, double* C, int64_t ldc,
+                                   void* workspace, size_t workspace_bytes, cudaStream_t s) {
+  if (M < 0 || N < 0 || K < 0 || M > (1 << 24) || N > (1 << 24) || K > (1 << 24))
+    return GPK_ERR_BAD_ARG;
+  if (lda < (transa ? M : K) || ldb < (transb ? K : N) || ldc < N) return GPK_ERR_BAD_ARG;
+  if (M == 0 || N == 0) return GPK_OK;
+  if (!A || !B || !C || !workspace) return GPK_ERR_BAD_ARG;
+  if (workspace_bytes < gpk_gemm_f64_workspace_bytes(transa, transb, M, N, K))
     return GPK_ERR_WORKSPACE;
-  if (dtype == GPK_F64)
-    return solve_run<double>((int)n, (int)nrhs, (const double*)L, lda, (double*)B, ldb, workspace,
-                             stream);
-  if (dtype == GPK_F32)
-    return solve_run<float>((int)n, (int)nrhs, (const float*)L, lda, (float*)B, ldb, workspace,
-                            stream);
-  return GPK_ERR_BAD_ARG;
+  double *At, *Bt;
+  int64_t la, lb;
+  gemm64_layout(M, N, K, transa, transb, workspace, &At, &Bt, &la, &lb);
+  dim3 tb(32, 8);
+  const double* An = A;
+  int64_t ldan = lda;
+  if (transa) {  // A stored [K, M]
+    transpose_kernel<double><<<dim3((unsigned)cdiv(M, 32), (unsigned)cdiv(K, 32)), tb, 0, s>>>(
+        (int)K, (int)M, A, lda, At, la);
+    GPK_LAUNCH_CHECK();
+    An = At;
+    ldan = la;
+  }
+  const double* Bn = B;
+  int64_t ldbn = ldb;
+  if (!transb) {  // B stored [K, N]
+    transpose_kernel<double><<<dim3((unsigned)cdiv(N, 32), (unsigned)cdiv(K, 32)), tb, 0, s>>>(
+        (int)K, (int)N, B, ldb, Bt, lb);
+    GPK_LAUNCH_CHECK();
+    Bn = Bt;
+    ldbn = lb;
+  }
+  GemmProb<double> p{};
+  p.A = An;
+  p.lda = ldan;
+  p.B = Bn;
+  p.ldb = ldbn;
+  p.C = C;
+  p.ldc = ldc;
+  p.M = (int)M;
+  p.N = (int)N;
+  p.K = (int)K;
+  p.alpha = alpha;
+  p.beta = beta;
+  GPK_CUDA_TRY(gemm_nt<double>(p, 1, s));
+  return GPK_OK;
 }
 
 template <typename T>

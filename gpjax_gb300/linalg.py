@@ -130,25 +130,48 @@ def lower_cholesky(A: LinearOperator) -> LinearOperator:
     return Triangular(L, lower=True)
 
 
-def _solve_lower(L: torch.Tensor, B: torch.Tensor) -> torch.Tensor:
-    dev = _lib.require_cuda(L, B)
-    L = L.detach().contiguous()
-    X = B.detach().to(L.dtype).contiguous().clone()
+def _solve(T: torch.Tensor, B: torch.Tensor, upper: bool, trans: bool) -> torch.Tensor:
+    dev = _lib.require_cuda(T, B)
+    T = T.detach().contiguous()
+    squeeze = B.ndim == 1
+    X = (B[:, None] if squeeze else B).detach().to(T.dtype).contiguous().clone()
     n, k = X.shape
-    nbytes = _lib.lib().gpk_solve_triangular_workspace_bytes(n, k, _dtype_code(L))
+    nbytes = _lib.lib().gpk_solve_triangular_ex_workspace_bytes(n, k, _dtype_code(T), int(upper))
     ws = _lib.workspace(nbytes, dev)
-    _lib.call("gpk_solve_triangular", n, k, _dtype_code(L), L.data_ptr(), L.stride(0),
-              X.data_ptr(), X.stride(0), ws.data_ptr(), ws.numel(), _lib.stream_ptr(dev))
-    return X
+    _lib.call("gpk_solve_triangular_ex", n, k, _dtype_code(T), int(upper), int(trans),
+              T.data_ptr(), T.stride(0), X.data_ptr(), X.stride(0), ws.data_ptr(), ws.numel(),
+              _lib.stream_ptr(dev))
+    return X[:, 0] if squeeze else X
 
 
-def solve_triangular(T: torch.Tensor, B: torch.Tensor, lower: bool = True) -> torch.Tensor:
-    """T X = B for triangular T (jsp.linalg.solve_triangular)."""
-    if lower:
-        return _solve_lower(T, B)
-    # U X = B  <=>  (P U P)(P X) = P B with P the reversal permutation; P U P is lower.
-    Tf = torch.flip(T, dims=(0, 1))
-    return torch.flip(_solve_lower(Tf, torch.flip(B, dims=(0,))), dims=(0,))
+def _solve_lower(L: torch.Tensor, B: torch.Tensor) -> torch.Tensor:
+    return _solve(L, B, upper=False, trans=False)
+
+
+def solve_triangular(T: torch.Tensor, B: torch.Tensor, lower: bool = True,
+                     trans: bool = False) -> torch.Tensor:
+    """op(T) X = B for triangular T (jsp.linalg.solve_triangular with ``lower``
+    and ``trans``), one library call."""
+    return _solve(T, B, upper=not lower, trans=trans)
+
+
+def matmul(A: torch.Tensor, B: torch.Tensor, transa: bool = False,
+           transb: bool = False, alpha: float = 1.0) -> torch.Tensor:
+    """alpha op(A) op(B) in float64 through the library's GEMM (gpk_gemm_f64)."""
+    dev = _lib.require_cuda(A, B)
+    A = A.detach().to(torch.float64).contiguous()
+    B = B.detach().to(torch.float64).contiguous()
+    M, K = (A.shape[1], A.shape[0]) if transa else (A.shape[0], A.shape[1])
+    KB, N = (B.shape[1], B.shape[0]) if transb else (B.shape[0], B.shape[1])
+    if K != KB:
+        raise ValueError(f"inner dimensions differ: {K} and {KB}")
+    C = torch.empty((M, N), dtype=torch.float64, device=dev)
+    nbytes = _lib.lib().gpk_gemm_f64_workspace_bytes(int(transa), int(transb), M, N, K)
+    ws = _lib.workspace(nbytes, dev)
+    _lib.call("gpk_gemm_f64", int(transa), int(transb), M, N, K, float(alpha), A.data_ptr(),
+              A.stride(0), B.data_ptr(), B.stride(0), 0.0, C.data_ptr(), N, ws.data_ptr(),
+              ws.numel(), _lib.stream_ptr(dev))
+    return C
 
 
 def solve(A: LinearOperator, b: torch.Tensor) -> torch.Tensor:
@@ -163,7 +186,7 @@ def solve(A: LinearOperator, b: torch.Tensor) -> torch.Tensor:
         res = solve_triangular(A.array, B, lower=A.lower)
     else:
         L, _ = cholesky_dense(A.to_dense(), check=True)
-        res = solve_triangular(L.transpose(0, 1).contiguous(), _solve_lower(L, B), lower=False)
+        res = solve_triangular(L, _solve_lower(L, B), trans=True)  # L^T x = L^-1 b
     return res[:, 0] if squeeze else res
 
 

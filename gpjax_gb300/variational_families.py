@@ -6,7 +6,7 @@ import torch
 
 from .distributions import GaussianDistribution
 from .likelihoods import Gaussian
-from .linalg import Dense, add_jitter, cholesky_dense, psd, solve_triangular
+from .linalg import Dense, add_jitter, cholesky_dense, matmul, psd, solve_triangular
 from .parameters import Real
 
 
@@ -31,35 +31,36 @@ class CollapsedVariationalGaussian(AbstractVariationalGaussian):
             raise TypeError("Likelihood must be Gaussian.")
 
     def predict(self, test_inputs: torch.Tensor, train_data) -> GaussianDistribution:
-        """SGPR predictive distribution (variational_families.py:786-870), composed
-        from the library's GPU cross-covariance, Cholesky and triangular solves."""
+        """SGPR predictive distribution (variational_families.py:786-870): every
+        product and solve is a library call -- cross-covariances and Grams,
+        Cholesky factors, triangular solves (including the transposed ones the
+        reference makes with cho_solve and solve_triangular(L.T)) and float64
+        GEMMs; torch only holds the tensors."""
         with torch.no_grad():
             t = test_inputs.to(train_data.X.device, torch.float64)
             x, y = train_data.X, train_data.y
             kernel = self.posterior.prior.kernel
             mean_function = self.posterior.prior.mean_function
-            sd = self.posterior.likelihood.obs_stddev.value.to(x.device).detach()
-            noise_var = sd**2
+            sd = float(self.posterior.likelihood.obs_stddev.value)
+            noise_var = sd * sd
             z = self.inducing_inputs.value.to(x.device).detach()
-            m = z.shape[0]
-            Kzx = kernel.cross_covariance(z, x).detach()
-            Kzz = add_jitter(kernel.gram(z).to_dense().detach(), self.jitter)
-            Lz, _ = cholesky_dense(Kzz, check=True)
-            Lz_inv_Kzx = solve_triangular(Lz, Kzx)
-            A = Lz_inv_Kzx / sd
-            AAT = A @ A.T
-            L, _ = cholesky_dense(torch.eye(m, dtype=torch.float64, device=x.device) + AAT,
-                                  check=True)
-            diff = y - mean_function(x)
-            tmp = solve_triangular(L, Lz_inv_Kzx @ diff)
-            Lz_inv_Kzx_diff = solve_triangular(L.T.contiguous(), tmp, lower=False)
-            Kzz_inv_Kzx_diff = solve_triangular(Lz.T.contiguous(), Lz_inv_Kzx_diff, lower=False)
-            Ktt = kernel.gram(t).to_dense().detach()
-            Kzt = kernel.cross_covariance(z, t).detach()
-            mut = mean_function(t)
-            Lz_inv_Kzt = solve_triangular(Lz, Kzt)
-            L_inv_Lz_inv_Kzt = solve_triangular(L, Lz_inv_Kzt)
-            mean = mut + (Kzt.T / noise_var) @ Kzz_inv_Kzx_diff
-            cov = Ktt - Lz_inv_Kzt.T @ Lz_inv_Kzt + L_inv_Lz_inv_Kzt.T @ L_inv_Lz_inv_Kzt
-            cov = add_jitter(cov, self.jitter)
+            Kzx = kernel.cross_covariance(z, x).detach()                       # :815
+            Kzz = add_jitter(kernel.gram(z).to_dense().detach(), self.jitter)   # :816-818
+            Lz, _ = cholesky_dense(Kzz, check=True)                             # :821
+            Lz_inv_Kzx = solve_triangular(Lz, Kzx)                              # :824
+            AAT = matmul(Lz_inv_Kzx, Lz_inv_Kzx, transb=True, alpha=1.0 / noise_var)  # :827-830
+            L, _ = cholesky_dense(add_jitter(AAT, 1.0), check=True)             # :833
+            diff = (y - mean_function(x)).reshape(-1, 1)                        # :835-836
+            v = matmul(Lz_inv_Kzx, diff)
+            v = solve_triangular(L, solve_triangular(L, v), trans=True)         # cho_solve :839
+            w = solve_triangular(Lz, v, trans=True)                             # Lz^-T :842
+            Ktt = kernel.gram(t).to_dense().detach()                            # :844
+            Kzt = kernel.cross_covariance(z, t).detach()                        # :845
+            Ktz = kernel.cross_covariance(t, z).detach()                        # Kzt^T
+            mut = mean_function(t)                                              # :846
+            Q = solve_triangular(Lz, Kzt)                                       # :849
+            R = solve_triangular(L, Q)                                          # :852
+            mean = mut.reshape(-1, 1) + matmul(Ktz, w, alpha=1.0 / noise_var)    # :855
+            cov = Ktt - matmul(Q, Q, transa=True) + matmul(R, R, transa=True)   # :858-862
+            cov = add_jitter(cov, self.jitter)                                  # :865
         return GaussianDistribution(mean.reshape(-1), psd(Dense(cov)))

@@ -142,6 +142,28 @@ gpk_status gpk_solve_triangular(int64_t n, int64_t nrhs, int dtype,
                                 void* workspace, size_t workspace_bytes,
                                 cudaStream_t stream);
 
+/* op(T) X = B in place for a triangular T [n, n] that is lower (upper = 0)
+ * or upper (upper = 1), op(T) = T (trans = 0) or T^T (trans = 1); B [n, nrhs]
+ * row-major.  The Triangular branch of solve with the lower / trans flags of
+ * jax.scipy.linalg.solve_triangular (linalg/operations.py:105-107;
+ * variational_families.py:839-852 solves against L^T).  workspace:
+ * gpk_solve_triangular_ex_workspace_bytes(n, nrhs, dtype, upper). */
+size_t gpk_solve_triangular_ex_workspace_bytes(int64_t n, int64_t nrhs, int dtype, int upper);
+gpk_status gpk_solve_triangular_ex(int64_t n, int64_t nrhs, int dtype, int upper, int trans,
+                                   const void* T, int64_t ldt, void* B, int64_t ldb,
+                                   void* workspace, size_t workspace_bytes, cudaStream_t stream);
+
+/* float64 C = alpha op(A) op(B) + beta C, row-major, op(A) [M, K], op(B)
+ * [K, N]: the dense products of the reference's predict paths (jnp.matmul at
+ * gps.py:520-522, variational_families.py:830-861).  workspace:
+ * gpk_gemm_f64_workspace_bytes (transposed operand copies, 256 bytes when
+ * none is needed). */
+size_t gpk_gemm_f64_workspace_bytes(int transa, int transb, int64_t M, int64_t N, int64_t K);
+gpk_status gpk_gemm_f64(int transa, int transb, int64_t M, int64_t N, int64_t K, double alpha,
+                        const double* A, int64_t lda, const double* B, int64_t ldb, double beta,
+                        double* C, int64_t ldc, void* workspace, size_t workspace_bytes,
+                        cudaStream_t stream);
+
 /* sum_i log L_ii in float64 (compensated), the Triangular branch of logdet
  * (linalg/operations.py:142-144); out is one device double. */
 gpk_status gpk_logdet_triangular(int64_t n, int dtype, const void* L, int64_t lda,

@@ -108,3 +108,33 @@ def test_cross_covariance_vjp_added_kernels(cuda_lib, cls, kind):
     for got, ref in ((k.lengthscale.value.grad, lt.grad), (k.variance.value.grad, vt.grad),
                      (X.grad, xt.grad), (Y.grad, yt.grad)):
         assert np.allclose(got.cpu().numpy(), ref.numpy(), rtol=1e-9, atol=1e-11)
+
+
+@pytest.mark.parametrize("upper", [False, True])
+@pytest.mark.parametrize("trans", [False, True])
+@pytest.mark.parametrize("n,k", [(1, 1), (65, 3), (300, 40)])
+def test_triangular_solve_variants(cuda_lib, upper, trans, n, k):
+    """op(T) X = B for lower / upper T and op = identity / transpose
+    (jax.scipy.linalg.solve_triangular's lower and trans flags)."""
+    rng = np.random.default_rng(n + k)
+    T = np.tril(rng.standard_normal((n, n))) + n * np.eye(n)
+    if upper:
+        T = T.T.copy()
+    B = rng.standard_normal((n, k))
+    X = LA.solve_triangular(torch.as_tensor(T, device="cuda"), torch.as_tensor(B, device="cuda"),
+                            lower=not upper, trans=trans).cpu().numpy()
+    ref = np.linalg.solve(T.T if trans else T, B)
+    assert np.allclose(X, ref, rtol=1e-11, atol=1e-12)
+
+
+@pytest.mark.parametrize("transa", [False, True])
+@pytest.mark.parametrize("transb", [False, True])
+@pytest.mark.parametrize("m,n,k", [(1, 1, 1), (70, 33, 129), (256, 300, 64)])
+def test_gemm_f64(cuda_lib, transa, transb, m, n, k):
+    rng = np.random.default_rng(m * n + k)
+    A = rng.standard_normal((k, m) if transa else (m, k))
+    B = rng.standard_normal((n, k) if transb else (k, n))
+    C = LA.matmul(torch.as_tensor(A, device="cuda"), torch.as_tensor(B, device="cuda"),
+                  transa=transa, transb=transb, alpha=0.5).cpu().numpy()
+    ref = 0.5 * (A.T if transa else A) @ (B.T if transb else B)
+    assert np.allclose(C, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
