@@ -75,6 +75,8 @@ SIGNATURES = {
     "gpk_gemm_tf32x3": (_c_int, [_c_i64, _c_i64, _c_i64, ctypes.c_float, _c_ptr, _c_i64, _c_ptr,
                                  _c_i64, ctypes.c_float, _c_ptr, _c_i64, _c_int, _c_ptr, _c_ptr,
                                  _c_size, _c_ptr]),
+    "gpk_selftest_wait_timeout_workspace_bytes": (_c_size, []),
+    "gpk_selftest_wait_timeout": (_c_int, [_c_ptr, _c_ptr, _c_size, _c_ptr]),
     "gpk_predict_workspace_bytes": (_c_size, [_c_i64, _c_i64, _c_int, _c_int]),
     "gpk_predict": (_c_int, [_c_int, _c_i64, _c_i64, _c_int, _c_ptr, _c_i64, _c_ptr, _c_ptr,
                              _c_i64, _c_ptr, _c_int, _c_dbl, _c_dbl, _c_int, _c_ptr, _c_ptr,

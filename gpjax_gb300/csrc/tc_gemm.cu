@@ -36,16 +36,17 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait: about two seconds of SM clock, or until another thread of the
-// CTA has given up (abort flag).  Returns false on timeout / abort.
+// Bounded wait: `limit` SM clocks (about two seconds by default), or until
+// another thread of the CTA has given up (abort flag).  Returns false on
+// timeout / abort; a timeout sets the abort flag and *err.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
-                                          int* err) {
+                                          int* err, long long limit) {
   const long long t0 = clock64();
   for (uint32_t it = 0;; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
     if ((it & 255u) == 255u) {
       if (*abort_flag) return false;
-      if (clock64() - t0 > 4000000000LL) {
+      if (clock64() - t0 > limit) {
         *abort_flag = 1;
         if (err) atomicExch(err, 1);
         return false;
@@ -53,6 +54,19 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volati
     }
   }
 }
+
+// Bounded wait that does not give up on the abort flag: for work this thread
+// started (its TMA copies, its MMAs), which must land before the CTA releases
+// its shared memory and tensor memory.
+__device__ __forceinline__ bool mbar_wait_own(uint64_t* bar, uint32_t parity, long long limit) {
+  const long long t0 = clock64();
+  for (uint32_t it = 0;; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((it & 255u) == 255u && clock64() - t0 > limit) return false;
+  }
+}
+
+constexpr long long kWaitCycles = 4000000000LL;  // ~2 s of SM clock
 
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
                                             uint64_t* bar) {
@@ -228,6 +242,7 @@ struct SmemCtl {
   uint64_t empty[STAGES_];
   uint64_t tfull[4];   // accumulator segment ready (MMA -> epilogue)
   uint64_t tempty[4];  // accumulator segment drained (epilogue -> MMA)
+  uint64_t mdone;      // MMAs issued before an abort have completed
   uint32_t tmem;
   int abort_flag;
 };
@@ -343,6 +358,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       mbar_init(&ctl->tfull[b], 1);
       mbar_init(&ctl->tempty[b], EPI_WARPS);  // one arrival per epilogue warp
     }
+    mbar_init(&ctl->mdone, 1);
     ctl->abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -360,6 +376,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   pdl_trigger();
   const uint32_t tmem = ctl->tmem;
   volatile int* abort_flag = &ctl->abort_flag;
+  const long long wlim = p.wait_cycles > 0 ? p.wait_cycles : kWaitCycles;
 
   if (warp == 0) {
     if (lane == 0 && nk > 0) {
@@ -369,7 +386,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       for (int kc = 0; kc < nk; ++kc) {
         const int s = kc % STAGES;
         if (kc >= STAGES) {
-          if (!mbar_wait(&ctl->empty[s], ((kc / STAGES) - 1) & 1, abort_flag, p.err)) break;
+          if (!mbar_wait(&ctl->empty[s], ((kc / STAGES) - 1) & 1, abort_flag, p.err, wlim)) break;
         }
         uint8_t* st = tiles + s * STAGE_BYTES;
         const int k = klo + kc * BK;
@@ -380,31 +397,35 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         tma_load_2d(st + 2 * A_BYTES + B_BYTES, &tb_lo, bx0 + k, by, &ctl->full[s]);
         ++issued;
       }
-      if (*abort_flag) {
-        // drain the copies this thread issued before returning
-        for (int kc = max(0, issued - STAGES); kc < issued; ++kc)
-          mbar_wait(&ctl->full[kc % STAGES], (kc / STAGES) & 1, abort_flag, nullptr);
-      }
+      // the copies of the last STAGES slices land before the CTA can exit (on
+      // the normal path the MMA thread has already waited for them; after an
+      // abort they may still be in flight)
+      for (int kc = max(0, issued - STAGES); kc < issued; ++kc)
+        mbar_wait_own(&ctl->full[kc % STAGES], (kc / STAGES) & 1, wlim);
     }
   } else if (warp == 1) {
     if (lane == 0) {
       constexpr uint32_t idesc = TL::F16 ? idesc_f16(BM, BN) : idesc_tf32(BM, BN);
       constexpr int KS = TL::KS, KP = TL::KPSEG;
       const int nks = nk * KS;  // MMA K steps of this tile
-      bool ok = true;
+      bool ok = true, issued_mma = false;
       int waited = 0;           // K slices whose full barrier has been passed
       for (int seg = 0; seg < nseg && ok; ++seg) {
         const int b = seg % NBUF;
         const uint32_t tacc = tmem + (uint32_t)(b * BN);
         if (seg >= NBUF) {
-          ok = mbar_wait(&ctl->tempty[b], ((seg / NBUF) - 1) & 1, abort_flag, p.err);
+          ok = mbar_wait(&ctl->tempty[b], ((seg / NBUF) - 1) & 1, abort_flag, p.err, wlim);
           if (!ok) break;
           tc_fence_after();
         }
         const int ks0 = seg * KP, ks1 = min(nks, ks0 + KP);
+        if (p.test_stall && seg == 0)  // self-test: wait on a barrier nothing arrives at
+          ok = mbar_wait(&ctl->mdone, 0, abort_flag, p.err, wlim);
         for (; waited <= (ks1 - 1) / KS && ok; ++waited)
-          ok = mbar_wait(&ctl->full[waited % STAGES], (waited / STAGES) & 1, abort_flag, p.err);
+          ok = mbar_wait(&ctl->full[waited % STAGES], (waited / STAGES) & 1, abort_flag, p.err,
+                         wlim);
         if (!ok) break;
+        issued_mma = true;
         tc_fence_after();
         // The tensor core truncates each MMA's sum toward zero.  The cross
         // products (about 2^-11 of the result) go first, so their truncation is
@@ -442,6 +463,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         for (int kc = ks0 / KS; (kc + 1) * KS <= ks1; ++kc) mma_commit(&ctl->empty[kc % STAGES]);
         mma_commit(&ctl->tfull[b]);
       }
+      if (!ok && issued_mma) {
+        // after an abort, the MMAs already issued finish before TMEM is freed
+        mma_commit(&ctl->mdone);
+        mbar_wait_own(&ctl->mdone, 0, wlim);
+      }
     }
     __syncwarp();
   } else {
@@ -477,7 +503,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     bool have = true;
     for (int seg = 0; seg < nseg; ++seg) {
       const int b = seg % NBUF;
-      have = __all_sync(0xffffffffu, mbar_wait(&ctl->tfull[b], (seg / NBUF) & 1, abort_flag, p.err));
+      have = __all_sync(0xffffffffu,
+                        mbar_wait(&ctl->tfull[b], (seg / NBUF) & 1, abort_flag, p.err, wlim));
       if (!have) break;
       tc_fence_after();
       const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN + hcol);
@@ -1131,6 +1158,43 @@ extern "C" gpk_status gpk_gemm_tf32x3(int64_t M, int64_t N, int64_t K, float alp
   p.alpha = alpha;
   p.err = err_flag;
   TcMat a{ahi, alo, M, K, ld}, b{bhi, blo, N, K, ld};
+  GPK_CUDA_TRY(tc_gemm_launch(tc::MODE_ADD_F32, a, b, p, 1, stream));
+  return GPK_OK;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI: self-test of the bounded waits.  One 256 x 256 x 256 GEMM whose MMA
+// thread waits on a barrier that nothing arrives at, with a 20M-cycle limit
+// (about 10 ms): the wait runs out, the CTA sets *err_flag, lets its own TMA
+// copies land, frees its tensor memory and returns -- the path a device-side
+// stall takes in any product call.
+// ---------------------------------------------------------------------------
+static constexpr int64_t kSelfTestN = 256;
+
+extern "C" size_t gpk_selftest_wait_timeout_workspace_bytes(void) {
+  return gpk_gemm_tf32x3_workspace_bytes(kSelfTestN, kSelfTestN, kSelfTestN) +
+         (size_t)kSelfTestN * kSelfTestN * 4 + 256;
+}
+
+extern "C" gpk_status gpk_selftest_wait_timeout(int* err_flag, void* workspace,
+                                                size_t workspace_bytes, cudaStream_t stream) {
+  if (!err_flag || !workspace || workspace_bytes < gpk_selftest_wait_timeout_workspace_bytes())
+    return GPK_ERR_BAD_ARG;
+  const int64_t n = kSelfTestN;
+  GPK_CUDA_TRY(cudaMemsetAsync(workspace, 0, workspace_bytes, stream));
+  float *ahi, *alo, *bhi, *blo;
+  int64_t ld;
+  const size_t g = gemm_ws_layout(n, n, n, workspace, &ahi, &alo, &bhi, &blo, &ld);
+  float* C = reinterpret_cast<float*>(static_cast<char*>(workspace) + ((g + 255) & ~size_t(255)));
+  tc::TcParams p{};
+  p.M = p.N = p.K = (int)n;
+  p.c0 = C;
+  p.ldc = n;
+  p.alpha = 1.f;
+  p.err = err_flag;
+  p.wait_cycles = 20000000LL;
+  p.test_stall = 1;
+  TcMat a{ahi, alo, n, n, ld}, b{bhi, blo, n, n, ld};
   GPK_CUDA_TRY(tc_gemm_launch(tc::MODE_ADD_F32, a, b, p, 1, stream));
   return GPK_OK;
 }

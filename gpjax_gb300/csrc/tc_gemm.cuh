@@ -64,6 +64,8 @@ struct TcParams {
   double* gpart;
   double* zpart;
   int* err;
+  long long wait_cycles;  // bound of every mbarrier wait in SM clocks; 0: about two seconds
+  int test_stall;         // self-test only: the MMA thread waits on a barrier nothing arrives at
 };
 
 }  // namespace tc

@@ -294,6 +294,16 @@ gpk_status gpk_gemm_tf32x3(int64_t M, int64_t N, int64_t K, float alpha,
                            int* err_flag, void* workspace, size_t workspace_bytes,
                            cudaStream_t stream);
 
+/* Self-test of the bounded device waits (no counterpart in the reference).
+ * Launches one small tensor-core GEMM whose MMA thread waits on a barrier that
+ * nothing arrives at, with a ~10 ms limit: the wait runs out and the kernel
+ * sets *err_flag (device int) to 1 and returns, leaving the context usable --
+ * the path every mbarrier wait of the library takes after its ~2 s bound.
+ * workspace: gpk_selftest_wait_timeout_workspace_bytes(). */
+size_t gpk_selftest_wait_timeout_workspace_bytes(void);
+gpk_status gpk_selftest_wait_timeout(int* err_flag, void* workspace, size_t workspace_bytes,
+                                     cudaStream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

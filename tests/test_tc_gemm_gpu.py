@@ -90,3 +90,24 @@ def test_split_tf32_cancellation_probe(cuda_lib):
     e_f32 = float(((A32 @ M32.T).double() - ref).norm() / ref.norm())
     print(f"cancellation probe: split-TF32 {e_tc:.3e}  float32 cuBLAS {e_f32:.3e}")
     assert e_tc < 50 * e_f32 + 1e-6
+
+
+def test_bounded_wait_runs_out_and_reports(cuda_lib):
+    """A device wait that can never be satisfied (the self-test's barrier that
+    nothing arrives at) gives up after its bound, reports through the error
+    flag and leaves the context usable: a normal GEMM right after it is exact."""
+    lib = _lib.lib()
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    ws = _lib.workspace(lib.gpk_selftest_wait_timeout_workspace_bytes(), torch.device("cuda"))
+    _lib.call("gpk_selftest_wait_timeout", err.data_ptr(), ws.data_ptr(), ws.numel(),
+              _lib.stream_ptr())
+    torch.cuda.synchronize()
+    assert int(err.item()) == 1
+    g = torch.Generator(device="cuda").manual_seed(5)
+    A = torch.randn(256, 128, device="cuda", generator=g)
+    B = torch.randn(192, 128, device="cuda", generator=g)
+    C = torch.zeros(256, 192, device="cuda")
+    gemm(A, B, C)
+    ref = A.double() @ B.double().T
+    assert float((C.double() - ref).abs().max()) <= 2e-5 * float(
+        (A.double().abs() @ B.double().abs().T).max())
