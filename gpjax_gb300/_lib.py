@@ -71,6 +71,10 @@ SIGNATURES = {
     "gpk_collapsed_elbo": (_c_int, [_c_int, _c_i64, _c_i64, _c_int, _c_ptr, _c_i64, _c_ptr,
                                     _c_ptr, _c_i64, _c_ptr, _c_int, _c_dbl, _c_int, _c_int,
                                     _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_size, _c_ptr]),
+    "gpk_collapsed_elbo_sharded": (_c_int, [_c_int, _c_i64, _c_i64, _c_i64, _c_int, _c_ptr, _c_i64,
+                                            _c_ptr, _c_ptr, _c_i64, _c_ptr, _c_int, _c_dbl,
+                                            _c_int, _c_int, _c_ptr, _c_ptr, _c_ptr, _c_ptr,
+                                            _c_ptr, _c_size, _c_ptr, _c_ptr, _c_ptr]),
     "gpk_gemm_tf32x3_workspace_bytes": (_c_size, [_c_i64, _c_i64, _c_i64]),
     "gpk_gemm_tf32x3": (_c_int, [_c_i64, _c_i64, _c_i64, ctypes.c_float, _c_ptr, _c_i64, _c_ptr,
                                  _c_i64, ctypes.c_float, _c_ptr, _c_i64, _c_int, _c_ptr, _c_ptr,
@@ -82,6 +86,9 @@ SIGNATURES = {
                              _c_i64, _c_ptr, _c_int, _c_dbl, _c_dbl, _c_int, _c_ptr, _c_ptr,
                              _c_ptr, _c_i64, _c_ptr, _c_ptr, _c_size, _c_ptr]),
 }
+
+# int (*gpk_allreduce_fn)(void* user, size_t byte_offset, int64_t count, cudaStream_t)
+ALLREDUCE_FN = ctypes.CFUNCTYPE(_c_int, _c_ptr, _c_size, _c_i64, _c_ptr)
 
 _LIB = None
 

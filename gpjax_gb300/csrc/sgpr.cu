@@ -727,8 +727,9 @@ __global__ void sg_zero(double* p, int count) {
 // Side stream for the Kzz chain (its Cholesky factor, inverse and K^-1 do not
 // depend on Phi or P, so they run beside the Phi generation and the P
 // product), forked from and joined back into the caller's stream.  The mutex
-// is held for a whole call's enqueue so that concurrent calls cannot
-// interleave their uses of the shared fork/join events.
+// is held from the fork to the join so that concurrent calls cannot
+// interleave their uses of the shared fork/join events (and is released
+// before a sharded call's exchanges, which may wait for other ranks).
 struct SgSide {
   cudaStream_t s = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
@@ -752,15 +753,42 @@ cudaError_t sg_side(SgSide** out) {
   return cudaSuccess;
 }
 
+// Sum of a float64 region of the workspace over the ranks of a sharded call
+// (gpk_collapsed_elbo_sharded); a no-op for a single-rank call.
+struct Exchange {
+  gpk_allreduce_fn fn = nullptr;
+  void* user = nullptr;
+  const void* ws = nullptr;
+  gpk_status sum(const double* p, int64_t count, cudaStream_t s) const {
+    if (!fn) return GPK_OK;
+    const size_t off = (size_t)(reinterpret_cast<const char*>(p) - static_cast<const char*>(ws));
+    return fn(user, off, count, s) == 0 ? GPK_OK : GPK_ERR_CUDA;
+  }
+};
+
+// Su = (Kzz + jitter I) + P / s from the summed P
+__global__ void sg_su(int m, int64_t ldm, const double* __restrict__ Kf,
+                      const double* __restrict__ P64, const double* __restrict__ theta, int n_ls,
+                      double jitter, double* __restrict__ Su) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (int64_t)m * m) return;
+  const int i = (int)(e / m), j = (int)(e % m);
+  const double sd = theta[n_ls + 1];
+  const int64_t o = (int64_t)i * ldm + j;
+  Su[o] = Kf[o] + (i == j ? jitter : 0.0) + P64[o] / (sd * sd);
+}
+
 template <typename T>
 gpk_status sgpr_run(int kind, int n, int m, int d, const double* x, int64_t ldx, const double* y,
                     const double* z, int64_t ldz, const double* theta, int n_ls, double jitter,
                     int want_grad, double* out_elbo, double* out_grad, double* out_gz, int* info,
-                    void* ws, cudaStream_t s) {
+                    void* ws, cudaStream_t s, const Exchange& ex = Exchange(),
+                    int64_t n_total = -1) {
   constexpr bool mixed = SgprBuf<T>::kMixed;
   SgprBuf<T> b;
   sgpr_layout<T>(n, m, d, ws, b);
   const int64_t ldm = b.ldm;
+  if (n_total < 0) n_total = n;
   sg_init<<<b.nb, 256, 0, s>>>(info, b.err, y, theta, n_ls, n, b.dv, b.ddpart);
   GPK_LAUNCH_CHECK();
   sg_zero<<<1, 64, 0, s>>>(b.red, 64);
@@ -770,7 +798,7 @@ gpk_status sgpr_run(int kind, int n, int m, int d, const double* x, int64_t ldx,
   GPK_CUDA_TRY(scale_inputs<double>(z, ldz, m, d, theta, n_ls, b.zs64, s));
   // Kzz chain on the side stream: K (float64, full), Lz = chol(K + jitter I),
   // Mz = Lz^-1, Vz = Mz^T, K^-1 = Vz Vz^T
-  std::lock_guard<std::mutex> lock(g_sg_mu);
+  std::unique_lock<std::mutex> lock(g_sg_mu);
   SgSide* side = nullptr;
   GPK_CUDA_TRY(sg_side(&side));
   const cudaStream_t ss = side->s;
@@ -866,9 +894,22 @@ gpk_status sgpr_run(int kind, int n, int m, int d, const double* x, int64_t ldx,
     }
   }
   GPK_CUDA_TRY(cudaStreamWaitEvent(s, side->join, 0));
+  lock.unlock();  // the side stream's events are not used past the join
   sg_reduce_P<T><<<(int)cdiv((int64_t)m * m, 256), 256, 0, s>>>(b.Pparts, b.nchunks, m, ldm, b.Kf,
                                                                   theta, n_ls, jitter, b.P64, b.Su);
   GPK_LAUNCH_CHECK();
+  GPK_CUDA_TRY(colsum(b.ddpart, b.nb, 2, b.ddds, false, b.colpart, s));
+  if (ex.fn) {
+    // the data-dependent statistics summed over the ranks' rows: P = Phi Phi^T,
+    // c = Phi d and Phi 1, (d^T d, 1^T d); then Su from the summed P
+    gpk_status st = ex.sum(b.P64, (int64_t)m * ldm, s);
+    if (st == GPK_OK) st = ex.sum(b.cv, 2 * (int64_t)m, s);
+    if (st == GPK_OK) st = ex.sum(b.ddds, 2, s);
+    if (st != GPK_OK) return st;
+    sg_su<<<(int)cdiv((int64_t)m * m, 256), 256, 0, s>>>(m, ldm, b.Kf, b.P64, theta, n_ls, jitter,
+                                                         b.Su);
+    GPK_LAUNCH_CHECK();
+  }
   GPK_CUDA_TRY(potrf_lower<double>(b.Su, ldm, m, b.ldU, info, nullptr, true, s));
   GPK_CUDA_TRY(trtri_lower<double>(b.Su, ldm, m, b.Mu, ldm, b.Vu, ldm, b.scr, s));
   {  // Su^-1 = Vu Vu^T (lower triangle, then mirrored)
@@ -944,10 +985,14 @@ gpk_status sgpr_run(int kind, int n, int m, int d, const double* x, int64_t ldx,
       GPK_CUDA_TRY(colsum(b.thP, (int64_t)ASPLIT * mt, d + 1, b.sth, false, b.colpart, s));
       GPK_CUDA_TRY(colsum(b.dzP, ASPLIT, (int64_t)m * d, b.gzs, false, b.colpart, s));
     }
+    // the Phi parts of the gradient sums over the ranks' rows; the Kzz part,
+    // identical on every rank, is added once after
+    gpk_status st = ex.sum(b.sth, d + 1, s);
+    if (st == GPK_OK) st = ex.sum(b.gzs, (int64_t)m * d, s);
+    if (st != GPK_OK) return st;
     GPK_CUDA_TRY(colsum(b.thK, m, d + 1, b.sth, true, b.colpart, s));
   }
-  GPK_CUDA_TRY(colsum(b.ddpart, b.nb, 2, b.ddds, false, b.colpart, s));
-  sg_finalize<<<1, 256, 0, s>>>(n, m, d, theta, n_ls, b.ldK, b.ldU, b.cv, b.gam, b.pgam, b.phi1,
+  sg_finalize<<<1, 256, 0, s>>>((int)n_total, m, d, theta, n_ls, b.ldK, b.ldU, b.cv, b.gam, b.pgam, b.phi1,
                                 b.red, b.sth, b.ddds, b.dzK, b.gzs, b.err, want_grad, info,
                                 out_elbo, out_grad, out_gz);
   GPK_LAUNCH_CHECK();
@@ -990,4 +1035,35 @@ extern "C" gpk_status gpk_collapsed_elbo(int kind, int64_t n, int64_t m, int d, 
                             want_grad, out_elbo, out_grad, out_grad_z, info, workspace, stream);
   return sgpr_run<float>(kind, (int)n, (int)m, d, x, ldx, y, z, ldz, theta, n_ls, jitter,
                          want_grad, out_elbo, out_grad, out_grad_z, info, workspace, stream);
+}
+
+extern "C" gpk_status gpk_collapsed_elbo_sharded(
+    int kind, int64_t n_local, int64_t n_total, int64_t m, int d, const double* x, int64_t ldx,
+    const double* y, const double* z, int64_t ldz, const double* theta, int n_ls, double jitter,
+    int precision, int want_grad, double* out_elbo, double* out_grad, double* out_grad_z,
+    int* info, void* workspace, size_t workspace_bytes, cudaStream_t stream,
+    gpk_allreduce_fn allreduce, void* user) {
+  if (kind < GPK_RBF || kind > GPK_RATIONAL_QUADRATIC) return GPK_ERR_BAD_ARG;
+  if (n_local <= 0 || n_total < n_local || m <= 0 || n_total > (int64_t)1 << 31 || m > 16384)
+    return GPK_ERR_BAD_ARG;
+  if (d <= 0 || d > DMAXS || ldx < d || ldz < d || !(n_ls == 1 || n_ls == d))
+    return GPK_ERR_BAD_ARG;
+  if (precision != GPK_PREC_FP64 && precision != GPK_PREC_MIXED) return GPK_ERR_BAD_ARG;
+  if (!x || !y || !z || !theta || !out_elbo || !info || !workspace || !allreduce)
+    return GPK_ERR_BAD_ARG;
+  if (want_grad && (!out_grad || !out_grad_z)) return GPK_ERR_BAD_ARG;
+  if (n_local > (int64_t)1 << 28) return GPK_ERR_BAD_ARG;
+  if (workspace_bytes < gpk_collapsed_elbo_workspace_bytes(n_local, m, d, precision))
+    return GPK_ERR_WORKSPACE;
+  Exchange ex;
+  ex.fn = allreduce;
+  ex.user = user;
+  ex.ws = workspace;
+  if (precision == GPK_PREC_FP64)
+    return sgpr_run<double>(kind, (int)n_local, (int)m, d, x, ldx, y, z, ldz, theta, n_ls, jitter,
+                            want_grad, out_elbo, out_grad, out_grad_z, info, workspace, stream, ex,
+                            n_total);
+  return sgpr_run<float>(kind, (int)n_local, (int)m, d, x, ldx, y, z, ldz, theta, n_ls, jitter,
+                         want_grad, out_elbo, out_grad, out_grad_z, info, workspace, stream, ex,
+                         n_total);
 }

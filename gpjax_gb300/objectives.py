@@ -131,9 +131,36 @@ def named_parameters(model) -> dict:
     return found
 
 
+def shard_rows(n: int, world: int, rank: int) -> slice:
+    """Rows of an n-row dataset that rank `rank` of `world` holds in a
+    data-parallel collapsed ELBO: contiguous, sizes differing by at most one."""
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError("need 0 <= rank < world")
+    base, extra = divmod(n, world)
+    start = rank * base + min(rank, extra)
+    return slice(start, start + base + (1 if rank < extra else 0))
+
+
+def allreduce_callback(workspace: torch.Tensor, group=None):
+    """The library's exchange hook for gpk_collapsed_elbo_sharded: sums the
+    float64 region at a byte offset of `workspace` over the process group, in
+    place (torch.distributed.all_reduce, ordered on the current stream).
+    Returns the ctypes callback (keep a reference while the call runs)."""
+    import torch.distributed as dist
+
+    def fn(user, offset, count, stream):
+        try:
+            view = workspace.narrow(0, int(offset), int(count) * 8).view(torch.float64)
+            dist.all_reduce(view, group=group)
+            return 0
+        except Exception:  # reported to the library as a failed exchange
+            return 1
+    return _lib.ALLREDUCE_FN(fn)
+
+
 class _CollapsedELBO(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, theta, z, x, y, kind, n_ls, jitter, prec):
+    def forward(ctx, theta, z, x, y, kind, n_ls, jitter, prec, group=None):
         dev = _lib.require_cuda(x, y, theta, z)
         n, d = x.shape
         m = z.shape[0]
@@ -147,10 +174,21 @@ class _CollapsedELBO(torch.autograd.Function):
         info = torch.zeros(1, dtype=torch.int32, device=dev)
         nbytes = _lib.lib().gpk_collapsed_elbo_workspace_bytes(n, m, d, prec)
         ws = _lib.workspace(nbytes, dev)
-        _lib.call("gpk_collapsed_elbo", kind, n, m, d, xc.data_ptr(), d, yc.data_ptr(),
-                  zc.data_ptr(), d, th.data_ptr(), n_ls, float(jitter), prec, int(want),
-                  out.data_ptr(), grad.data_ptr(), gz.data_ptr(), info.data_ptr(), ws.data_ptr(),
-                  ws.numel(), _lib.stream_ptr(dev))
+        if group is None:
+            _lib.call("gpk_collapsed_elbo", kind, n, m, d, xc.data_ptr(), d, yc.data_ptr(),
+                      zc.data_ptr(), d, th.data_ptr(), n_ls, float(jitter), prec, int(want),
+                      out.data_ptr(), grad.data_ptr(), gz.data_ptr(), info.data_ptr(),
+                      ws.data_ptr(), ws.numel(), _lib.stream_ptr(dev))
+        else:
+            import torch.distributed as dist
+            n_total = torch.tensor([n], dtype=torch.int64, device=dev)
+            dist.all_reduce(n_total, group=group)
+            cb = allreduce_callback(ws, group)
+            _lib.call("gpk_collapsed_elbo_sharded", kind, n, int(n_total.item()), m, d,
+                      xc.data_ptr(), d, yc.data_ptr(), zc.data_ptr(), d, th.data_ptr(), n_ls,
+                      float(jitter), prec, int(want), out.data_ptr(), grad.data_ptr(),
+                      gz.data_ptr(), info.data_ptr(), ws.data_ptr(), ws.numel(),
+                      _lib.stream_ptr(dev), cb, None)
         ctx.save_for_backward(grad, gz)
         ctx.info = info
         return out[0]
@@ -158,12 +196,18 @@ class _CollapsedELBO(torch.autograd.Function):
     @staticmethod
     def backward(ctx, g):
         grad, gz = ctx.saved_tensors
-        return g * grad, g * gz, None, None, None, None, None, None
+        return g * grad, g * gz, None, None, None, None, None, None, None
 
 
-def collapsed_elbo(variational_family, data, precision: str | None = None) -> torch.Tensor:
+def collapsed_elbo(variational_family, data, precision: str | None = None,
+                   process_group=None) -> torch.Tensor:
     """SGPR collapsed evidence lower bound (objectives.py:321-416), differentiable
-    w.r.t. the kernel, likelihood and mean parameters and the inducing inputs."""
+    w.r.t. the kernel, likelihood and mean parameters and the inducing inputs.
+
+    With ``process_group`` (a torch.distributed group, one GPU per rank),
+    ``data`` holds this rank's rows only (``shard_rows``): each rank forms its
+    statistics, one all-reduce sums them, and every rank returns the ELBO and
+    gradients of the whole dataset."""
     q = variational_family
     post = q.posterior
     kernel = post.prior.kernel
@@ -173,7 +217,7 @@ def collapsed_elbo(variational_family, data, precision: str | None = None) -> to
     const = _mean_constant(post.prior.mean_function, dev)
     theta = kernel.theta_vector(dev, post.likelihood.obs_stddev.value, const)
     return _CollapsedELBO.apply(theta, z, x, data.y, kernel.kind, kernel.n_ls, float(q.jitter),
-                                precision_code(precision))
+                                precision_code(precision), process_group)
 
 
 def cross_covariance_vjp(kind, n_ls, theta, x, y, G, need_x=False, need_y=False):

@@ -241,6 +241,28 @@ gpk_status gpk_collapsed_elbo(int kind, int64_t n, int64_t m, int d,
                               int* info, void* workspace, size_t workspace_bytes,
                               cudaStream_t stream);
 
+/* Data-parallel collapsed ELBO: each rank passes its own rows of x and y
+ * (n_local of n_total), the same z and theta, and a callback that sums a
+ * float64 region of its workspace over the ranks, in place, ordered on
+ * `stream` (an NCCL or gloo all-reduce; 0 on success).  The library calls it
+ * with the byte offset of the region inside `workspace` at two points: after
+ * the rank-local statistics (P = Phi Phi^T [m x ldm], c = Phi d and Phi 1 [2m],
+ * (d^T d, 1^T d) [2]) and, with want_grad, after the rank-local gradient sums
+ * (theta part [d + 1], z part [m x d]); the m x m algebra in between and after
+ * is replicated.  Every rank gets the full-data ELBO and gradients
+ * (objectives.py:321-416 over all n_total rows).  workspace:
+ * gpk_collapsed_elbo_workspace_bytes(n_local, m, d, precision).  No
+ * counterpart in the reference, which runs on one device. */
+typedef int (*gpk_allreduce_fn)(void* user, size_t byte_offset, int64_t count,
+                                cudaStream_t stream);
+gpk_status gpk_collapsed_elbo_sharded(int kind, int64_t n_local, int64_t n_total, int64_t m, int d,
+                                      const double* x, int64_t ldx, const double* y,
+                                      const double* z, int64_t ldz, const double* theta, int n_ls,
+                                      double jitter, int precision, int want_grad,
+                                      double* out_elbo, double* out_grad, double* out_grad_z,
+                                      int* info, void* workspace, size_t workspace_bytes,
+                                      cudaStream_t stream, gpk_allreduce_fn allreduce, void* user);
+
 /* ---------------------------------------------------------------------------
  * Batched MLL + gradient over independent GPs of different sizes (no single
  * reference counterpart: the reference evaluates conjugate_mll

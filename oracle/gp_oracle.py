@@ -236,6 +236,39 @@ def collapsed_elbo(kind, X, y, Z, ls, variance, obs_stddev, mean_const=0.0,
     return float((two_log_prob - two_trace) / 2.0)  # :416
 
 
+def sgpr_statistics(kind, X, y, Z, ls, variance, mean_const=0.0) -> dict:
+    """The data-dependent sums of the collapsed ELBO over the rows of (X, y):
+    P = Kzx Kxz, c = Kzx d, d^T d, sum_i k(x_i, x_i) and the row count.  Sums
+    over disjoint row blocks add up to the statistics of their union."""
+    X = np.asarray(X, np.float64)
+    d = np.asarray(y, np.float64).reshape(-1) - mean_const
+    Kzx = cross_covariance(kind, Z, X, ls, variance)
+    return {"P": Kzx @ Kzx.T, "c": Kzx @ d, "dd": float(d @ d),
+            "kdiag": float(diagonal(kind, X, ls, variance).sum()), "n": X.shape[0]}
+
+
+def collapsed_elbo_from_statistics(kind, stats, Z, ls, variance, obs_stddev,
+                                   jitter=DEFAULT_JITTER) -> float:
+    """collapsed_elbo (objectives.py:341-416) from the summed statistics, by the
+    reference's algebra: A A^T = Lz^-1 P Lz^-T / s, the quadratic term through
+    L^-1 A d = L^-1 Lz^-1 c / sqrt(s) and tr(A A^T) = tr(Lz^-1 P Lz^-T) / s."""
+    m = np.asarray(Z).shape[0]
+    s = obs_stddev**2
+    Kzz = add_jitter(gram(kind, Z, ls, variance), jitter)
+    Lz = np.linalg.cholesky(Kzz)
+    W = sla.solve_triangular(Lz, sla.solve_triangular(Lz, stats["P"], lower=True).T,
+                             lower=True) / s  # A A^T
+    L = np.linalg.cholesky(np.eye(m) + W)
+    log_det_B = 2.0 * np.sum(np.log(np.diag(L)))
+    u = sla.solve_triangular(L, sla.solve_triangular(Lz, stats["c"], lower=True) / np.sqrt(s),
+                             lower=True)
+    n = stats["n"]
+    quad = (stats["dd"] - u @ u) / s
+    two_log_prob = -n * np.log(2.0 * np.pi * s) - log_det_B - quad
+    two_trace = stats["kdiag"] / s - np.trace(W)
+    return float((two_log_prob - two_trace) / 2.0)
+
+
 def predict(kind, X, y, T, ls, variance, obs_stddev, mean_const=0.0,
             jitter=DEFAULT_JITTER, prior_jitter=DEFAULT_JITTER):
     """ConjugatePosterior.predict (gps.py:494-526); returns (mean [t], cov [t, t])."""

@@ -187,3 +187,88 @@ def test_collapsed_elbo_fp64_ill_conditioned_value(cuda_lib):
     ref = O.collapsed_elbo(0, x, y, Z, ls, 1.2, 0.3, 0.1)
     cond = np.linalg.cond(O.gram(0, Z, ls, 1.2) + 1e-6 * np.eye(m))
     assert abs(val - ref) <= max(1e-9, 1e-12 * cond) * abs(ref), (val, ref, cond)
+
+
+@pytest.mark.parametrize("precision,vtol,gtol", [("fp64", 1e-10, 1e-8), ("mixed", 1e-8, 1e-6)])
+def test_sharded_elbo_two_ranks_match_single(cuda_lib, precision, vtol, gtol):
+    """gpk_collapsed_elbo_sharded as two ranks -- two host threads, each on its
+    own stream with half the rows, exchanging through a host-side sum in the
+    callback (the device never waits on the other rank) -- against one
+    gpk_collapsed_elbo call on all rows."""
+    import threading
+
+    from gpjax_gb300 import _lib
+    from gpjax_gb300.objectives import shard_rows
+    lib = _lib.lib()
+    prec = _lib.PREC_FP64 if precision == "fp64" else _lib.PREC_MIXED
+    rng = np.random.default_rng(8)
+    n, m, d = 20000, 128, 4
+    x = rng.standard_normal((n, d))
+    y = np.sin(x).sum(1) + 0.1 * rng.standard_normal(n)
+    z = x[rng.choice(n, m, replace=False)]
+    ls = np.exp(rng.uniform(-0.5, 0.5, d))
+    dev = torch.device("cuda")
+    th = torch.tensor(list(ls) + [1.2, 0.2, 0.1], dtype=torch.float64, device=dev)
+    Z = torch.as_tensor(z, device=dev)
+
+    def outputs():
+        return (torch.zeros(1, dtype=torch.float64, device=dev),
+                torch.zeros(d + 3, dtype=torch.float64, device=dev),
+                torch.zeros((m, d), dtype=torch.float64, device=dev),
+                torch.zeros(1, dtype=torch.int32, device=dev))
+
+    X, Y = torch.as_tensor(x, device=dev), torch.as_tensor(y, device=dev)
+    e, g, gz, info = outputs()
+    ws = _lib.workspace(lib.gpk_collapsed_elbo_workspace_bytes(n, m, d, prec), dev)
+    _lib.call("gpk_collapsed_elbo", _lib.RBF, n, m, d, X.data_ptr(), d, Y.data_ptr(), Z.data_ptr(),
+              d, th.data_ptr(), d, 1e-6, prec, 1, e.data_ptr(), g.data_ptr(), gz.data_ptr(),
+              info.data_ptr(), ws.data_ptr(), ws.numel(), _lib.stream_ptr(dev))
+    torch.cuda.synchronize()
+    ref = (float(e.item()), g.cpu().numpy(), gz.cpu().numpy())
+    del ws
+
+    barrier = threading.Barrier(2)
+    slots, results, errors = {}, {}, []
+
+    def rank_main(r):
+        try:
+            rows = shard_rows(n, 2, r)
+            stream = torch.cuda.Stream(dev)
+            with torch.cuda.stream(stream):
+                Xr = torch.as_tensor(x[rows], device=dev)
+                Yr = torch.as_tensor(y[rows], device=dev)
+                er, gr, gzr, ir = outputs()
+                nl = Xr.shape[0]
+                wsr = _lib.workspace(lib.gpk_collapsed_elbo_workspace_bytes(nl, m, d, prec), dev)
+
+                def hostsum(user, off, count, s):
+                    view = wsr.narrow(0, int(off), int(count) * 8).view(torch.float64)
+                    slots[r] = view.cpu().numpy()          # waits for this rank's stream
+                    barrier.wait()
+                    tot = slots[0] + slots[1]
+                    barrier.wait()                          # both have read before the next round
+                    view.copy_(torch.as_tensor(tot, device=dev))
+                    return 0
+                cb = _lib.ALLREDUCE_FN(hostsum)
+                _lib.call("gpk_collapsed_elbo_sharded", _lib.RBF, nl, n, m, d, Xr.data_ptr(), d,
+                          Yr.data_ptr(), Z.data_ptr(), d, th.data_ptr(), d, 1e-6, prec, 1,
+                          er.data_ptr(), gr.data_ptr(), gzr.data_ptr(), ir.data_ptr(),
+                          wsr.data_ptr(), wsr.numel(), stream.cuda_stream, cb, None)
+                stream.synchronize()
+                assert int(ir.item()) == 0
+                results[r] = (float(er.item()), gr.cpu().numpy(), gzr.cpu().numpy())
+        except Exception as exc:  # surfaced below
+            errors.append(exc)
+            barrier.abort()
+
+    ts = [threading.Thread(target=rank_main, args=(r,)) for r in range(2)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join(timeout=300)
+    assert not errors, errors
+    for r in range(2):
+        val, gv, gzv = results[r]
+        assert abs(val - ref[0]) <= vtol * abs(ref[0]), (r, val, ref[0])
+        assert np.allclose(gv, ref[1], rtol=gtol, atol=gtol * np.abs(ref[1]).max())
+        assert np.allclose(gzv, ref[2], rtol=gtol, atol=gtol * np.abs(ref[2]).max())
