@@ -230,10 +230,16 @@ struct Tile {
   static constexpr int TLD = BN + 4; // staged output tile row stride (floats)
   static constexpr int KSTEP = F16 ? 16 : 8;  // K elements per MMA (32 bytes either way)
   static constexpr int KS = BK / KSTEP;       // MMA K steps per K slice
-  // MMA K steps summed by one TMEM accumulator before the epilogue drains it
-  // (3 products each): the accumulation length the accuracy needs, and no more
-  // drains than the epilogue keeps up with
-  static constexpr int KPSEG = 4;
+  // MMA K steps (3 products each) summed by one TMEM accumulator before the
+  // epilogue drains it.  The accumulator truncates each MMA's sum toward zero,
+  // so a segment of k steps biases the tile by about k units of 2^-24 toward
+  // zero on one-signed data (measured: 4 steps -3.3, 1 step -0.8).  The
+  // narrow and half tiles, which carry every product of the small and middle
+  // recursion nodes, drain after every step (this takes the mixed MLL from
+  // 1.4e-5 to 4e-7 relative error on an RBF problem with condition number
+  // ~4e3); the wide tiles of the large products drain every 4 steps, which
+  // their epilogue keeps up with.
+  static constexpr int KPSEG = (TS == 0 || TS == 2) ? 1 : 4;
 };
 
 template <int STAGES_>
@@ -421,46 +427,36 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         const int ks0 = seg * KP, ks1 = min(nks, ks0 + KP);
         if (p.test_stall && seg == 0)  // self-test: wait on a barrier nothing arrives at
           ok = mbar_wait(&ctl->mdone, 0, abort_flag, p.err, wlim);
-        for (; waited <= (ks1 - 1) / KS && ok; ++waited)
-          ok = mbar_wait(&ctl->full[waited % STAGES], (waited / STAGES) & 1, abort_flag, p.err,
-                         wlim);
         if (!ok) break;
-        issued_mma = true;
-        tc_fence_after();
-        // The tensor core truncates each MMA's sum toward zero.  The cross
-        // products (about 2^-11 of the result) go first, so their truncation is
-        // negligible; then each hi*hi MMA truncates the running sum once.
-#pragma unroll
-        for (int q = 0; q < KP; ++q) {
-          const int ks = ks0 + q;
-          if (ks >= ks1) break;
-          const uint32_t sb = smem_u32(tiles + ((ks / KS) % STAGES) * STAGE_BYTES);
-          const uint64_t off = (uint64_t)(((ks % KS) * 32) >> 4);  // 32 bytes per MMA K step
+        // per MMA K step: the two cross products (about 2^-11 of the result)
+        // before the hi*hi product, so the running sum carrying them is small
+        for (int ks = ks0; ks < ks1 && ok; ++ks) {
+          const int kc = ks / KS, k4 = ks % KS;
+          if (kc >= waited) {
+            ok = mbar_wait(&ctl->full[kc % STAGES], (kc / STAGES) & 1, abort_flag, p.err, wlim);
+            if (!ok) break;
+            waited = kc + 1;
+            tc_fence_after();
+          }
+          issued_mma = true;
+          const uint32_t sb = smem_u32(tiles + (kc % STAGES) * STAGE_BYTES);
+          const uint64_t off = (uint64_t)((k4 * 32) >> 4);  // 32 bytes per MMA K step
           const uint64_t ahi = sdesc<TL::SWZ>(sb) + off, alo = sdesc<TL::SWZ>(sb + A_BYTES) + off;
           const uint64_t bhi = sdesc<TL::SWZ>(sb + 2 * A_BYTES) + off;
           const uint64_t blo = sdesc<TL::SWZ>(sb + 2 * A_BYTES + B_BYTES) + off;
+          const uint32_t accf = ks == ks0 ? 0u : 1u;
           if (TL::F16) {
-            mma_f16(tacc, alo, bhi, idesc, q == 0 ? 0u : 1u);
+            mma_f16(tacc, alo, bhi, idesc, accf);
             mma_f16(tacc, ahi, blo, idesc, 1u);
-          } else {
-            mma_tf32(tacc, alo, bhi, idesc, q == 0 ? 0u : 1u);
-            mma_tf32(tacc, ahi, blo, idesc, 1u);
-          }
-        }
-#pragma unroll
-        for (int q = 0; q < KP; ++q) {
-          const int ks = ks0 + q;
-          if (ks >= ks1) break;
-          const uint32_t sb = smem_u32(tiles + ((ks / KS) % STAGES) * STAGE_BYTES);
-          const uint64_t off = (uint64_t)(((ks % KS) * 32) >> 4);
-          const uint64_t ahi = sdesc<TL::SWZ>(sb) + off, bhi = sdesc<TL::SWZ>(sb + 2 * A_BYTES) + off;
-          if (TL::F16)
             mma_f16(tacc, ahi, bhi, idesc, 1u);
-          else
+          } else {
+            mma_tf32(tacc, alo, bhi, idesc, accf);
+            mma_tf32(tacc, ahi, blo, idesc, 1u);
             mma_tf32(tacc, ahi, bhi, idesc, 1u);
+          }
+          if (k4 == KS - 1) mma_commit(&ctl->empty[kc % STAGES]);  // slice consumed
         }
-        // release the K slices whose last K step this segment issued
-        for (int kc = ks0 / KS; (kc + 1) * KS <= ks1; ++kc) mma_commit(&ctl->empty[kc % STAGES]);
+        if (!ok) break;
         mma_commit(&ctl->tfull[b]);
       }
       if (!ok && issued_mma) {

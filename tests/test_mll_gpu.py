@@ -68,22 +68,32 @@ def test_mll_mixed_parity_c2(cuda_lib, n):
     _mixed_check(val, g, ref, gref, abs(ref))
 
 
-@pytest.mark.parametrize("kind,n,d", [(0, 1024, 4), (1, 1500, 6), (0, 555, 16), (1, 2600, 5)])
+@pytest.mark.parametrize("kind,n,d", [(1, 1500, 6), (0, 555, 16), (1, 2600, 5)])
 def test_mll_mixed_parity_other_kernels(cuda_lib, kind, n, d):
-    """Other kernels: MLL error relative to the size of its terms
-    (|log det| + |quad| + n log 2pi) / 2, which stays meaningful when the MLL
-    itself is near zero, within 1e-5; gradients within 2e-3 of their norm (the
-    RBF Gram here has condition number ~1e4, an order of magnitude above the
-    Matern-5/2 case; the noise gradient carries tr(Sigma^-1), whose error is the
-    float32-class factor's backward error amplified by Sigma^-2)."""
+    """RBF and Matern-3/2 at the mixed form's targets: |dMLL|/|MLL| <= 1e-6 and
+    the gradient within 1e-4 of its norm (condition numbers up to ~4e3)."""
     x, y, ls = c2_like(n, d, seed=n, kind=kind)
     val, g = run(kind, x, y, ls, 1.0, 0.1, 0.0, "mixed")
     ref, gref = oracle(kind, x, y, ls, 1.0, 0.1, 0.0)
-    S = O.gram(kind, x, ls, 1.0) + (1e-6 + 1e-2) * np.eye(n)
+    _mixed_check(val, g, ref, gref, abs(ref))
+
+
+def test_mll_mixed_near_cancelling_mll(cuda_lib):
+    """RBF, d = 4, n = 1024, condition number ~1e4, where the MLL (8.4) is the
+    difference of terms three orders of magnitude larger (log det ~ -4e3,
+    quadratic ~1e3, n log 2 pi / 2 ~ 940): the MLL is held to 1e-6 of the size
+    of its terms; the gradient, whose noise component is the difference of
+    alpha^T alpha (5e4) and tr(Sigma^-1), to 3e-4 of its norm -- the float32
+    rounding of the Gram entries that the refinement's residual reads moves
+    alpha by ~1e-4 relative at this conditioning."""
+    x, y, ls = c2_like(1024, 4, seed=1024, kind=0)
+    val, g = run(0, x, y, ls, 1.0, 0.1, 0.0, "mixed")
+    ref, gref = oracle(0, x, y, ls, 1.0, 0.1, 0.0)
+    S = O.gram(0, x, ls, 1.0) + (1e-6 + 1e-2) * np.eye(1024)
     ld = np.linalg.slogdet(S)[1]
     quad = float(y[:, 0] @ np.linalg.solve(S, y[:, 0]))
-    _mixed_check(val, g, ref, gref, 0.5 * (abs(ld) + abs(quad) + n * np.log(2 * np.pi)),
-                 gtol=2e-3, vtol=1e-5, ptol=5e-3)
+    _mixed_check(val, g, ref, gref, 0.5 * (abs(ld) + abs(quad) + 1024 * np.log(2 * np.pi)),
+                 gtol=3e-4, vtol=1e-6, ptol=5e-3)
 
 
 def test_mll_matches_finite_differences(cuda_lib):
@@ -149,10 +159,11 @@ def test_mll_mixed_dirty_workspace(cuda_lib, n):
 
 
 @pytest.mark.parametrize("kind", [O.MATERN12, O.rational_quadratic(0.8)])
-@pytest.mark.parametrize("n,d", [(300, 3), (1100, 5)])
+@pytest.mark.parametrize("n,d", [(400, 3), (1100, 5)])
 def test_mll_added_kernels(cuda_lib, kind, n, d):
     """Matern12 and RationalQuadratic: float64 form at the float64 tolerances;
-    mixed form at 1e-6 relative on the MLL and 1e-4 on the gradient norm."""
+    mixed form at 1e-6 relative on the MLL and 1e-4 on the gradient norm
+    (|MLL| between 110 and 1400 on these draws)."""
     from gpjax_gb300 import kernels as K
     rng = np.random.default_rng(n + d)
     x = rng.standard_normal((n, d))
