@@ -415,49 +415,45 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       constexpr int KS = TL::KS, KP = TL::KPSEG;
       const int nks = nk * KS;  // MMA K steps of this tile
       bool ok = true, issued_mma = false;
-      int waited = 0;           // K slices whose full barrier has been passed
-      for (int seg = 0; seg < nseg && ok; ++seg) {
-        const int b = seg % NBUF;
-        const uint32_t tacc = tmem + (uint32_t)(b * BN);
-        if (seg >= NBUF) {
-          ok = mbar_wait(&ctl->tempty[b], ((seg / NBUF) - 1) & 1, abort_flag, p.err, wlim);
-          if (!ok) break;
-          tc_fence_after();
-        }
-        const int ks0 = seg * KP, ks1 = min(nks, ks0 + KP);
-        if (p.test_stall && seg == 0)  // self-test: wait on a barrier nothing arrives at
-          ok = mbar_wait(&ctl->mdone, 0, abort_flag, p.err, wlim);
+      if (p.test_stall)  // self-test: wait on a barrier nothing arrives at
+        ok = mbar_wait(&ctl->mdone, 0, abort_flag, p.err, wlim);
+      for (int kc = 0; kc < nk && ok; ++kc) {
+        const int s = kc % STAGES;
+        ok = mbar_wait(&ctl->full[s], (kc / STAGES) & 1, abort_flag, p.err, wlim);
         if (!ok) break;
-        // per MMA K step: the two cross products (about 2^-11 of the result)
-        // before the hi*hi product, so the running sum carrying them is small
-        for (int ks = ks0; ks < ks1 && ok; ++ks) {
-          const int kc = ks / KS, k4 = ks % KS;
-          if (kc >= waited) {
-            ok = mbar_wait(&ctl->full[kc % STAGES], (kc / STAGES) & 1, abort_flag, p.err, wlim);
+        tc_fence_after();
+        const uint32_t sb = smem_u32(tiles + s * STAGE_BYTES);
+        const uint64_t ahi = sdesc<TL::SWZ>(sb), alo = sdesc<TL::SWZ>(sb + A_BYTES);
+        const uint64_t bhi = sdesc<TL::SWZ>(sb + 2 * A_BYTES);
+        const uint64_t blo = sdesc<TL::SWZ>(sb + 2 * A_BYTES + B_BYTES);
+#pragma unroll
+        for (int k4 = 0; k4 < KS; ++k4) {
+          // segment of KP K steps per TMEM accumulator buffer
+          const int ks = kc * KS + k4, seg = ks / KP, b = seg % NBUF;
+          const uint32_t tacc = tmem + (uint32_t)(b * BN);
+          const bool first = (ks % KP) == 0;
+          if (first && seg >= NBUF) {
+            ok = mbar_wait(&ctl->tempty[b], ((seg / NBUF) - 1) & 1, abort_flag, p.err, wlim);
             if (!ok) break;
-            waited = kc + 1;
             tc_fence_after();
           }
           issued_mma = true;
-          const uint32_t sb = smem_u32(tiles + (kc % STAGES) * STAGE_BYTES);
+          // the two cross products (about 2^-11 of the result) before the
+          // hi*hi product, so the running sum carrying them is small
           const uint64_t off = (uint64_t)((k4 * 32) >> 4);  // 32 bytes per MMA K step
-          const uint64_t ahi = sdesc<TL::SWZ>(sb) + off, alo = sdesc<TL::SWZ>(sb + A_BYTES) + off;
-          const uint64_t bhi = sdesc<TL::SWZ>(sb + 2 * A_BYTES) + off;
-          const uint64_t blo = sdesc<TL::SWZ>(sb + 2 * A_BYTES + B_BYTES) + off;
-          const uint32_t accf = ks == ks0 ? 0u : 1u;
           if (TL::F16) {
-            mma_f16(tacc, alo, bhi, idesc, accf);
-            mma_f16(tacc, ahi, blo, idesc, 1u);
-            mma_f16(tacc, ahi, bhi, idesc, 1u);
+            mma_f16(tacc, alo + off, bhi + off, idesc, first ? 0u : 1u);
+            mma_f16(tacc, ahi + off, blo + off, idesc, 1u);
+            mma_f16(tacc, ahi + off, bhi + off, idesc, 1u);
           } else {
-            mma_tf32(tacc, alo, bhi, idesc, accf);
-            mma_tf32(tacc, ahi, blo, idesc, 1u);
-            mma_tf32(tacc, ahi, bhi, idesc, 1u);
+            mma_tf32(tacc, alo + off, bhi + off, idesc, first ? 0u : 1u);
+            mma_tf32(tacc, ahi + off, blo + off, idesc, 1u);
+            mma_tf32(tacc, ahi + off, bhi + off, idesc, 1u);
           }
-          if (k4 == KS - 1) mma_commit(&ctl->empty[kc % STAGES]);  // slice consumed
+          if ((ks % KP) == KP - 1 || ks == nks - 1) mma_commit(&ctl->tfull[b]);
         }
         if (!ok) break;
-        mma_commit(&ctl->tfull[b]);
+        mma_commit(&ctl->empty[s]);
       }
       if (!ok && issued_mma) {
         // after an abort, the MMAs already issued finish before TMEM is freed

@@ -189,12 +189,13 @@ def test_collapsed_elbo_fp64_ill_conditioned_value(cuda_lib):
     assert abs(val - ref) <= max(1e-9, 1e-12 * cond) * abs(ref), (val, ref, cond)
 
 
-@pytest.mark.parametrize("precision,vtol,gtol", [("fp64", 1e-10, 1e-8), ("mixed", 1e-8, 1e-6)])
+@pytest.mark.parametrize("precision,vtol,gtol", [("fp64", 1e-9, 1e-7), ("mixed", 1e-5, 2e-3)])
 def test_sharded_elbo_two_ranks_match_single(cuda_lib, precision, vtol, gtol):
     """gpk_collapsed_elbo_sharded as two ranks -- two host threads, each on its
     own stream with half the rows, exchanging through a host-side sum in the
     callback (the device never waits on the other rank) -- against one
-    gpk_collapsed_elbo call on all rows."""
+    float64 gpk_collapsed_elbo call on all rows: the float64 form to 1e-9
+    (summation order differs), the mixed form at the mixed SGPR tolerances."""
     import threading
 
     from gpjax_gb300 import _lib
@@ -202,7 +203,7 @@ def test_sharded_elbo_two_ranks_match_single(cuda_lib, precision, vtol, gtol):
     lib = _lib.lib()
     prec = _lib.PREC_FP64 if precision == "fp64" else _lib.PREC_MIXED
     rng = np.random.default_rng(8)
-    n, m, d = 20000, 128, 4
+    n, m, d = 20000, 128, 8
     x = rng.standard_normal((n, d))
     y = np.sin(x).sum(1) + 0.1 * rng.standard_normal(n)
     z = x[rng.choice(n, m, replace=False)]
@@ -219,9 +220,9 @@ def test_sharded_elbo_two_ranks_match_single(cuda_lib, precision, vtol, gtol):
 
     X, Y = torch.as_tensor(x, device=dev), torch.as_tensor(y, device=dev)
     e, g, gz, info = outputs()
-    ws = _lib.workspace(lib.gpk_collapsed_elbo_workspace_bytes(n, m, d, prec), dev)
+    ws = _lib.workspace(lib.gpk_collapsed_elbo_workspace_bytes(n, m, d, _lib.PREC_FP64), dev)
     _lib.call("gpk_collapsed_elbo", _lib.RBF, n, m, d, X.data_ptr(), d, Y.data_ptr(), Z.data_ptr(),
-              d, th.data_ptr(), d, 1e-6, prec, 1, e.data_ptr(), g.data_ptr(), gz.data_ptr(),
+              d, th.data_ptr(), d, 1e-6, _lib.PREC_FP64, 1, e.data_ptr(), g.data_ptr(), gz.data_ptr(),
               info.data_ptr(), ws.data_ptr(), ws.numel(), _lib.stream_ptr(dev))
     torch.cuda.synchronize()
     ref = (float(e.item()), g.cpu().numpy(), gz.cpu().numpy())
