@@ -493,19 +493,30 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 #pragma unroll
     for (int c = 0; c < HC; ++c) acc[c] = 0.f;
     bool have = true;
-    for (int seg = 0; seg < nseg; ++seg) {
+    // single-step segments of the half tile are drained two per round trip
+    constexpr int DR = (TL::KPSEG == 1 && HC == 32) ? 2 : 1;
+    for (int seg = 0; seg < nseg; seg += DR) {
       const int b = seg % NBUF;
-      have = __all_sync(0xffffffffu,
-                        mbar_wait(&ctl->tfull[b], (seg / NBUF) & 1, abort_flag, p.err, wlim));
+      const bool two = DR == 2 && seg + 1 < nseg;
+      const int b1 = (seg + 1) % NBUF;
+      bool ready = mbar_wait(&ctl->tfull[b], (seg / NBUF) & 1, abort_flag, p.err, wlim);
+      if (two && ready)
+        ready = mbar_wait(&ctl->tfull[b1], ((seg + 1) / NBUF) & 1, abort_flag, p.err, wlim);
+      have = __all_sync(0xffffffffu, ready);
       if (!have) break;
       tc_fence_after();
       const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN + hcol);
       if (HC == 32) {
-        uint32_t v0[32];
+        uint32_t v0[32], v1[32];
         tmem_ld32_nowait(tb, v0);
+        if (two) tmem_ld32_nowait(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b1 * BN + hcol), v1);
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
         for (int k = 0; k < 32; ++k) acc[k] += __uint_as_float(v0[k]);
+        if (two) {
+#pragma unroll
+          for (int k = 0; k < 32; ++k) acc[k] += __uint_as_float(v1[k]);
+        }
       } else if (HC == 64) {
         uint32_t v0[32], v1[32];
         tmem_ld32_nowait(tb, v0);
@@ -528,9 +539,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       }
       tc_fence_before();
       __syncwarp();
-      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(
-                                      smem_u32(&ctl->tempty[b]))
-                                  : "memory");
+      if (lane == 0) {
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&ctl->tempty[b]))
+                     : "memory");
+        if (two)
+          asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&ctl->tempty[b1]))
+                       : "memory");
+      }
     }
     if (p.ra) {
       // undo the float16 operands' power-of-two row scales (exact)
