@@ -50,12 +50,40 @@ __device__ __forceinline__ T kshape(int kind, const double* theta, int n_ls) {
   return kind == GPK_RATIONAL_QUADRATIC ? (T)theta[n_ls + 3] : T(1);
 }
 
+// The Matern-1/2 and rational-quadratic evaluations are out of line: kval and
+// kval_dcoef run once per matrix element inside the Gram, adjoint and GEMM
+// epilogue loops, and inlined (if-converted) extra branches there would cost
+// every kernel kind their exp, log1p and divisions.
+template <typename T>
+struct KvDc {
+  T k, c;
+};
+
+template <typename T>
+__device__ __noinline__ KvDc<T> kval_dcoef_m12(T sq, T s2) {
+  const bool above = sq > Consts<T>::floor_();
+  const T t = d_sqrt(above ? sq : Consts<T>::floor_());
+  KvDc<T> r;
+  r.k = s2 * d_exp(-t);
+  r.c = above ? r.k / t : T(0);  // -2 dk/dsq = s2 exp(-t) / t; zero below the floor
+  return r;
+}
+
+template <typename T>
+__device__ __noinline__ KvDc<T> kval_dcoef_rq(T sq, T s2, T ka) {
+  const T u = sq / (T(2) * ka);
+  KvDc<T> r;
+  r.k = s2 * d_exp(-ka * d_log1p(u));
+  r.c = r.k / (T(1) + u);  // -2 dk/dsq = s2 (1 + sq / (2 alpha))^-(alpha + 1)
+  return r;
+}
+
 template <typename T>
 __device__ __forceinline__ T kval(int kind, T sq, T s2, T ka = T(1)) {
   if (kind == GPK_RBF) return s2 * d_exp(T(-0.5) * sq);
-  if (kind == GPK_RATIONAL_QUADRATIC) return s2 * d_exp(-ka * d_log1p(sq / (T(2) * ka)));
+  if (kind >= GPK_MATERN12)
+    return kind == GPK_MATERN12 ? kval_dcoef_m12<T>(sq, s2).k : kval_dcoef_rq<T>(sq, s2, ka).k;
   T t = d_sqrt(sq > Consts<T>::floor_() ? sq : Consts<T>::floor_());
-  if (kind == GPK_MATERN12) return s2 * d_exp(-t);
   if (kind == GPK_MATERN32) {
     const T r3 = T(1.7320508075688772);
     return s2 * (T(1) + r3 * t) * d_exp(-r3 * t);
@@ -72,19 +100,13 @@ __device__ __forceinline__ void kval_dcoef(int kind, T sq, T s2, T& k, T& c, T k
     c = k;
     return;
   }
-  if (kind == GPK_RATIONAL_QUADRATIC) {
-    const T base = T(1) + sq / (T(2) * ka);
-    k = s2 * d_exp(-ka * d_log1p(sq / (T(2) * ka)));
-    c = k / base;  // -2 dk/dsq = s2 (1 + sq / (2 alpha))^-(alpha + 1)
+  if (kind >= GPK_MATERN12) {
+    const KvDc<T> r = kind == GPK_MATERN12 ? kval_dcoef_m12<T>(sq, s2) : kval_dcoef_rq<T>(sq, s2, ka);
+    k = r.k;
+    c = r.c;
     return;
   }
-  const bool above = sq > Consts<T>::floor_();
-  T t = d_sqrt(above ? sq : Consts<T>::floor_());
-  if (kind == GPK_MATERN12) {
-    k = s2 * d_exp(-t);
-    c = above ? k / t : T(0);  // -2 dk/dsq = s2 exp(-t) / t; zero below the floor
-    return;
-  }
+  T t = d_sqrt(sq > Consts<T>::floor_() ? sq : Consts<T>::floor_());
   if (kind == GPK_MATERN32) {
     const T r3 = T(1.7320508075688772);
     T e = s2 * d_exp(-r3 * t);
