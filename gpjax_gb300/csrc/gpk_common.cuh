@@ -1,6 +1,7 @@
 // Shared device helpers for the gpk library: pointwise stationary kernels and
 // their derivatives, status handling and small reductions.
 #pragma once
+#include <type_traits>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <math.h>
@@ -118,6 +119,40 @@ __device__ __forceinline__ void kval_dcoef(int kind, T sq, T s2, T& k, T& c, T k
   T e = s2 * d_exp(-r5 * t);
   k = (T(1) + r5 * t + T(5.0 / 3.0) * (t * t)) * e;
   c = T(5.0 / 3.0) * (T(1) + r5 * t) * e;
+}
+
+// kval_dcoef with the kernel kind fixed at compile time, for loops that
+// dispatch on the kind once outside (GEMM epilogues): each kind's loop holds
+// only its own arithmetic.
+template <int KIND, typename T>
+__device__ __forceinline__ void kval_dcoef_k(T sq, T s2, T& k, T& c, T ka = T(1)) {
+  if constexpr (KIND == GPK_RBF) {
+    k = s2 * d_exp(T(-0.5) * sq);
+    c = k;
+  } else if constexpr (KIND == GPK_MATERN12) {
+    const bool above = sq > Consts<T>::floor_();
+    const T t = d_sqrt(above ? sq : Consts<T>::floor_());
+    k = s2 * d_exp(-t);
+    c = above ? k / t : T(0);
+  } else if constexpr (KIND == GPK_RATIONAL_QUADRATIC) {
+    const T u = sq / (T(2) * ka);
+    k = s2 * d_exp(-ka * d_log1p(u));
+    c = k / (T(1) + u);
+  } else {
+    kval_dcoef<T>(KIND, sq, s2, k, c, ka);  // Matern-3/2, Matern-5/2
+  }
+}
+
+// Calls f(std::integral_constant<int, KIND>{}) for the runtime kind.
+template <typename F>
+__device__ __forceinline__ void with_kind(int kind, F&& f) {
+  switch (kind) {
+    case GPK_RBF: f(std::integral_constant<int, GPK_RBF>{}); break;
+    case GPK_MATERN32: f(std::integral_constant<int, GPK_MATERN32>{}); break;
+    case GPK_MATERN52: f(std::integral_constant<int, GPK_MATERN52>{}); break;
+    case GPK_MATERN12: f(std::integral_constant<int, GPK_MATERN12>{}); break;
+    default: f(std::integral_constant<int, GPK_RATIONAL_QUADRATIC>{}); break;
+  }
 }
 
 // float32 -> TF32 (10 explicit mantissa bits), round to nearest, ties away

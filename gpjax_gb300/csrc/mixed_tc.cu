@@ -795,6 +795,33 @@ cudaError_t to16(const float* hi, const float* lo, int64_t ld, int row0, int col
   return launch_status();
 }
 
+// Look-ahead in nodes whose right half is at least LA_MIN wide: only the rows
+// of L21 and the block of A22 that the right child's left half needs (its first
+// hq rows and columns) stay on the critical stream.  The other rows of L21 and
+// the rest of the trailing update run on a per-depth look-ahead stream while
+// that left half is factored; the right child waits for them before its L21.
+constexpr int LA_MIN = 2048;
+
+// Per-depth look-ahead streams (priority between the critical stream and the
+// side stream) and their events; created on first use and kept.
+struct LookAhead {
+  cudaStream_t s[kMaxDepth] = {};
+  cudaEvent_t fork[kMaxDepth] = {}, fork2[kMaxDepth] = {}, mid[kMaxDepth] = {},
+              done[kMaxDepth] = {};
+};
+
+cudaError_t la_streams(LookAhead& L, int depth) {
+  if (L.s[depth]) return cudaSuccess;
+  int least = 0, greatest = 0;
+  cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+  for (cudaEvent_t* ev : {&L.fork[depth], &L.fork2[depth], &L.mid[depth], &L.done[depth]})
+    if (e == cudaSuccess && !*ev) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+  // numerically lower is more urgent: one step below the critical stream
+  const int prio = greatest < least ? greatest + 1 : greatest;
+  if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&L.s[depth], cudaStreamNonBlocking, prio);
+  return e;
+}
+
 struct TcChol {
   float* A;
   int64_t ld;
@@ -811,6 +838,7 @@ struct TcChol {
   bool prev_kernel;   // the last operation enqueued on s was a kernel launch (PDL allowed)
   F16Set f16[kMaxDepth];
   int nf16;           // depths [0, nf16) have float16 buffers
+  LookAhead* la;      // null: no look-ahead
 };
 
 // A node of size sz at depth `depth`: [L11, M11] = chol_inv(A11) (left, size h),
@@ -822,7 +850,7 @@ struct TcChol {
 // 512 -> 18.0; with the fork before it: 0 -> 20.9, 128 -> 20.7, 512 -> 20.1,
 // 1024 -> 20.3, 4096 -> 21.0, measured before the float16 wide nodes).
 constexpr int TT_INLINE_MAX = 512;
-cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
+cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth, cudaEvent_t join = nullptr) {
   if (sz == LEAF) {
     PdlAttr attr(c.prev_kernel);
     cudaLaunchConfig_t cfg = {};
@@ -841,16 +869,41 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
   const int h2 = sz - h;
   cudaError_t e = chol_inv_rec(c, o, h, depth + 1);
   if (e != cudaSuccess) return e;
+  if (join) {  // the parent's look-ahead work on this node's A21 and A22
+    e = cudaStreamWaitEvent(c.s, join, 0);
+    c.prev_kernel = false;
+    if (e != cudaSuccess) return e;
+  }
   // wide nodes: split-float16 products on row-scaled float16 copies
   const bool f16 = h2 >= F16_MIN && depth < c.nf16;
   F16Set* f = f16 ? &c.f16[depth] : nullptr;
   TcMap fa, fm, fl, fv;  // float16 maps of this node's operand copies
-  {  // L21 = A21 M11^T, float64 diagonal track of A22
+  // look-ahead: rows [0, hq) of L21 and A22 are the right child's left half
+  const bool la = c.la && h2 >= LA_MIN;
+  const int hq = la ? ((h2 / 2 + LEAF - 1) / LEAF) * LEAF : h2;
+  const int hb = h2 - hq;
+  cudaStream_t ls = nullptr;
+  if (la) {
+    e = la_streams(*c.la, depth);
+    if (e != cudaSuccess) return e;
+    ls = c.la->s[depth];
+  }
+  if (f16) {
+    e = to16(c.Mh, c.Ml, c.ld, o, o, h, h, TRI_LOWER, f->mh, f->ml, f->rm, c.s);
+    if (e != cudaSuccess) return e;
+    c.prev_kernel = true;
+    if (!tc_make_map_f16(&fa, f->ah, f->al, h2, h, h) ||
+        !tc_make_map_f16(&fm, f->mh, f->ml, h, h, h) ||
+        !tc_make_map_f16(&fl, f->lh, f->ll, h2, h, h))
+      return cudaErrorInvalidValue;
+  }
+  // L21 = A21 M11^T on rows [r0, r0 + rows), float64 diagonal track of A22
+  auto l21 = [&](int r0, int rows, cudaStream_t st, bool pdl) -> cudaError_t {
     tc::TcParams p{};
-    p.M = h2;
+    p.M = rows;
     p.N = h;
     p.K = h;
-    p.a_row0 = o + h;  // A21 in the split copy of the trailing matrix
+    p.a_row0 = o + h + r0;  // A21 in the split copy of the trailing matrix
     p.a_col0 = o;
     p.b_row0 = o;
     p.b_col0 = o;
@@ -858,32 +911,75 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
     p.c0 = c.Lh;
     p.c1 = c.Ll;
     p.ldc = c.ld;
-    p.c_row0 = o + h;
+    p.c_row0 = o + h + r0;
     p.c_col0 = o;
     p.alpha = 1.f;
     p.dtrack = c.dtrack;
     p.err = c.err;
-    if (f16) {
-      e = to16(c.Ah, c.Al, c.ld, o + h, o, h2, h, TRI_NONE, f->ah, f->al, f->ra, c.s);
-      if (e == cudaSuccess)
-        e = to16(c.Mh, c.Ml, c.ld, o, o, h, h, TRI_LOWER, f->mh, f->ml, f->rm, c.s);
-      if (e != cudaSuccess) return e;
-      if (!tc_make_map_f16(&fa, f->ah, f->al, h2, h, h) ||
-          !tc_make_map_f16(&fm, f->mh, f->ml, h, h, h))
-        return cudaErrorInvalidValue;
-      p.a_row0 = p.a_col0 = p.b_row0 = p.b_col0 = 0;
-      p.force_shape = 4;
-      p.ra = f->ra;
-      p.rb = f->rm;
-      e = tc_gemm_run(tc::MODE_STORE_SPLIT, fa, fm, p, 1, c.s, true);
-      if (e == cudaSuccess)
-        e = to16(c.Lh, c.Ll, c.ld, o + h, o, h2, h, TRI_NONE, f->lh, f->ll, f->rl, c.s);
-      if (e == cudaSuccess && !tc_make_map_f16(&fl, f->lh, f->ll, h2, h, h))
-        e = cudaErrorInvalidValue;
-    } else {
-      e = tc_gemm_run(tc::MODE_STORE_SPLIT, c.mA, c.mM, p, 1, c.s, c.prev_kernel);
-    }
-    c.prev_kernel = true;
+    if (!f16) return tc_gemm_run(tc::MODE_STORE_SPLIT, c.mA, c.mM, p, 1, st, pdl);
+    const int64_t d0 = (int64_t)r0 * h;
+    cudaError_t ee = to16(c.Ah, c.Al, c.ld, o + h + r0, o, rows, h, TRI_NONE, f->ah + d0,
+                          f->al + d0, f->ra + r0, st);
+    if (ee != cudaSuccess) return ee;
+    p.a_row0 = r0;
+    p.a_col0 = p.b_row0 = p.b_col0 = 0;
+    p.force_shape = 4;
+    p.ra = f->ra + r0;
+    p.rb = f->rm;
+    ee = tc_gemm_run(tc::MODE_STORE_SPLIT, fa, fm, p, 1, st, true);
+    if (ee == cudaSuccess)
+      ee = to16(c.Lh, c.Ll, c.ld, o + h + r0, o, rows, h, TRI_NONE, f->lh + d0, f->ll + d0,
+                f->rl + r0, st);
+    return ee;
+  };
+  // A22 -= L21 L21^T on rows [r0, r0 + rows) x columns [c0, c0 + cols) of A22
+  // (lower tiles only when the block straddles the diagonal)
+  auto update = [&](int r0, int rows, int c0, int cols, int lower, cudaStream_t st,
+                    bool pdl) -> cudaError_t {
+    tc::TcParams p{};
+    p.M = rows;
+    p.N = cols;
+    p.K = h;
+    p.a_row0 = o + h + r0;
+    p.a_col0 = o;
+    p.b_row0 = o + h + c0;
+    p.b_col0 = o;
+    p.c_lower = lower;
+    p.c0 = c.A;
+    p.s0 = c.Ah;  // TF32 split copy of the updated A22
+    p.s1 = c.Al;
+    p.ldc = c.ld;
+    p.c_row0 = o + h + r0;
+    p.c_col0 = o + h + c0;
+    p.alpha = -1.f;
+    p.err = c.err;
+    if (!f16) return tc_gemm_run(tc::MODE_ADD_F32, c.mL, c.mL, p, 1, st, pdl);
+    p.a_row0 = r0;
+    p.b_row0 = c0;
+    p.a_col0 = p.b_col0 = 0;
+    p.force_shape = 4;
+    p.ra = f->rl + r0;
+    p.rb = f->rl + c0;
+    return tc_gemm_run(tc::MODE_ADD_F32, fl, fl, p, 1, st, pdl);
+  };
+  if (la) {  // the rest of L21 on the look-ahead stream, beside its first rows
+    e = cudaEventRecord(c.la->fork[depth], c.s);
+    c.prev_kernel = false;
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ls, c.la->fork[depth], 0);
+    if (e == cudaSuccess) e = l21(hq, hb, ls, false);
+    if (e == cudaSuccess) e = cudaEventRecord(c.la->mid[depth], ls);
+    if (e != cudaSuccess) return e;
+  }
+  e = l21(0, hq, c.s, c.prev_kernel);
+  c.prev_kernel = true;
+  if (e != cudaSuccess) return e;
+  if (la) {  // the trailing update below the right child's left half, look-ahead stream
+    e = cudaEventRecord(c.la->fork2[depth], c.s);
+    c.prev_kernel = false;
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ls, c.la->fork2[depth], 0);
+    if (e == cudaSuccess) e = update(hq, hb, 0, hq, 0, ls, false);
+    if (e == cudaSuccess) e = update(hq, hb, hq, hb, 1, ls, true);
+    if (e == cudaSuccess) e = cudaEventRecord(c.la->done[depth], ls);
     if (e != cudaSuccess) return e;
   }
   // T^T = (L21 M11)^T; T[i, j] = sum_c L21[i, c] V11[j, c].  Large nodes run it
@@ -898,6 +994,7 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
       cudaError_t ee = cudaEventRecord(c.efork, c.s);
       c.prev_kernel = false;
       if (ee == cudaSuccess) ee = cudaStreamWaitEvent(c.side, c.efork, 0);
+      if (ee == cudaSuccess && la) ee = cudaStreamWaitEvent(c.side, c.la->mid[depth], 0);
       if (ee != cudaSuccess) return ee;
     }
     tc::TcParams p{};
@@ -941,40 +1038,16 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth) {
     e = tt();
     if (e != cudaSuccess) return e;
   }
-  {  // A22 -= L21 L21^T (lower tiles)
-    tc::TcParams p{};
-    p.M = h2;
-    p.N = h2;
-    p.K = h;
-    p.a_row0 = o + h;
-    p.a_col0 = o;
-    p.b_row0 = o + h;
-    p.b_col0 = o;
-    p.c_lower = 1;
-    p.c0 = c.A;
-    p.s0 = c.Ah;  // TF32 split copy of the updated A22
-    p.s1 = c.Al;
-    p.ldc = c.ld;
-    p.c_row0 = o + h;
-    p.c_col0 = o + h;
-    p.alpha = -1.f;
-    p.err = c.err;
-    if (f16) {
-      p.a_row0 = p.a_col0 = p.b_row0 = p.b_col0 = 0;
-      p.force_shape = 4;
-      p.ra = p.rb = f->rl;
-      e = tc_gemm_run(tc::MODE_ADD_F32, fl, fl, p, 1, c.s, c.prev_kernel);
-    } else {
-      e = tc_gemm_run(tc::MODE_ADD_F32, c.mL, c.mL, p, 1, c.s, c.prev_kernel);
-    }
-    c.prev_kernel = true;
-    if (e != cudaSuccess) return e;
-  }
+  // A22 -= L21 L21^T: the whole lower triangle, or with look-ahead its block
+  // [0, hq) x [0, hq) only
+  e = update(0, hq, 0, hq, 1, c.s, c.prev_kernel);
+  c.prev_kernel = true;
+  if (e != cudaSuccess) return e;
   if (!tt_inline) {
     e = tt();
     if (e != cudaSuccess) return e;
   }
-  e = chol_inv_rec(c, o + h, h2, depth + 1);
+  e = chol_inv_rec(c, o + h, h2, depth + 1, la ? c.la->done[depth] : nullptr);
   if (e != cudaSuccess) return e;
   if (f16) {  // M22 into the A21 copy's storage (free since L21)
     e = to16(c.Mh, c.Ml, c.ld, o + h, o + h, h2, h2, TRI_LOWER, f->ah, f->al, f->ra, c.s);
@@ -1177,6 +1250,7 @@ struct SideCtx {
   cudaStream_t hp = nullptr;    // highest priority: the critical path
   cudaStream_t side = nullptr;  // lowest priority: work that fills idle SMs
   cudaEvent_t estart = nullptr, efork = nullptr, ejoin = nullptr, edone = nullptr;
+  LookAhead la;                 // the recursion's look-ahead streams
 };
 constexpr int kMaxDevices = 64;
 std::mutex g_side_mu;
@@ -1289,6 +1363,7 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
   c.side = sc->side;
   c.efork = sc->efork;
   c.ejoin = sc->ejoin;
+  c.la = &sc->la;
   GPK_CUDA_TRY(cudaEventRecord(sc->estart, s));
   GPK_CUDA_TRY(cudaStreamWaitEvent(hs, sc->estart, 0));
   leaf_zero_kernel<<<dim3(cdiv(LEAF * 24, 256), np / LEAF), 256, 0, hs>>>(b.Mh, b.Ml, b.Vh, b.Vl,

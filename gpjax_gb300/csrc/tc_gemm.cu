@@ -708,6 +708,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       for (int k = 0; k < DM; ++k) glh[k] = gll[k] = 0.f;
       double gnoise = 0.0;
       float gvh = 0.f, gvl = 0.f;
+      with_kind(p.kind, [&](auto kind_c) {  // one loop per kernel kind
+        constexpr int KIND = decltype(kind_c)::value;
 #pragma unroll
       for (int cb = 0; cb < HC / 32; ++cb) {
         float pl[DM];
@@ -729,7 +731,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             sq = fmaf(df, df, sq);
           }
           float k1, c1;
-          kval_dcoef<float>(p.kind, sq, 1.f, k1, c1, ka);
+          kval_dcoef_k<KIND, float>(sq, 1.f, k1, c1, ka);
           pvar = fmaf(coef, k1, pvar);
           const float cc = coef * c1;
 #pragma unroll
@@ -742,6 +744,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         for (int kk = 0; kk < DM; ++kk) ff_add(glh[kk], gll[kk], pl[kk]);
         ff_add(gvh, gvl, pvar);
       }
+      });
       // the diagonal's noise term, outside the column loop (float64 there
       // would run for every element of an if-converted branch)
       {
@@ -796,6 +799,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 #pragma unroll
       for (int k = 0; k < DM; ++k) glh[k] = gll[k] = gzh[k] = gzl[k] = 0.f;
       float gvh = 0.f, gvl = 0.f;
+      with_kind(p.kind, [&](auto kind_c) {  // one loop per kernel kind
+        constexpr int KIND = decltype(kind_c)::value;
 #pragma unroll 1
       for (int cb = 0; cb < HC / 32; ++cb) {
         float pl[DM], pz[DM];
@@ -814,7 +819,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             sq = fmaf(df, df, sq);
           }
           float k1, c1;
-          kval_dcoef<float>(p.kind, sq, 1.f, k1, c1, ka);
+          kval_dcoef_k<KIND, float>(sq, 1.f, k1, c1, ka);
           pvar = fmaf(g, k1, pvar);
           const float gc = g * c1;
 #pragma unroll
@@ -832,6 +837,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         }
         ff_add(gvh, gvl, pvar);
       }
+      });
       // per-row z partials: the two threads of a row combine in a fixed order
       if (hcol != 0) {
 #pragma unroll
