@@ -59,6 +59,13 @@ SIGNATURES = {
     "gpk_conjugate_mll_batched": (_c_int, [_c_int, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr,
                                            _c_ptr, _c_ptr, _c_dbl, _c_int, _c_ptr, _c_ptr,
                                            _c_ptr, _c_ptr, _c_size, _c_ptr]),
+    "gpk_batch_plan_create": (_c_int, [_c_int, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr,
+                                       _c_ptr, _c_ptr, _c_dbl, _c_int, _c_ptr, _c_ptr, _c_ptr,
+                                       _c_int, _c_ptr]),
+    "gpk_batch_plan_workspace_bytes": (_c_size, [_c_ptr]),
+    "gpk_batch_plan_config": (_c_int, [_c_ptr, _c_i64]),
+    "gpk_batch_plan_execute": (_c_int, [_c_ptr, _c_ptr, _c_size, _c_ptr]),
+    "gpk_batch_plan_destroy": (_c_int, [_c_ptr]),
     "gpk_conjugate_loocv_workspace_bytes": (_c_size, [_c_i64, _c_int]),
     "gpk_conjugate_loocv": (_c_int, [_c_int, _c_i64, _c_int, _c_ptr, _c_i64, _c_ptr, _c_ptr,
                                      _c_int, _c_dbl, _c_int, _c_ptr, _c_ptr, _c_ptr, _c_ptr,

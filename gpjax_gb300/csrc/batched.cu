@@ -1,0 +1,934 @@
+// Persistent batched exact-GP marginal log-likelihood and gradient: many
+// independent GPs of uneven n (Bayesian-optimisation candidates, multi-start
+// hyperparameter fits) in ONE launch.  Per instance the quantity is the one of
+// mll.cu -- conjugate_mll (gpjax/objectives.py:36-107) and its gradient
+// 1/2 tr((alpha alpha^T - Sigma^-1) dSigma/dtheta) -- in float32 with float64
+// pivots (a float-float diagonal track), float-float residuals for two rounds
+// of refinement of alpha and float64 sums.
+//
+// Schedule.  A plan (built once, outside any stream capture) holds the
+// instance descriptors on the device, a queue of instance indices sorted by n
+// (largest first) and a tile configuration per instance chosen by the
+// autotuner.  Each execution zeroes the queue head and launches one grid of
+// one CTA per SM; a CTA takes the next queue entry with an atomic add and runs
+// the whole instance in its workspace slot, then takes the next.  The largest
+// instances start first and the small ones fill in behind them, so the SMs
+// finish together.  CTAs never wait on one another.
+//
+// Per instance (padded to n_pad, a multiple of 128, with an identity block):
+//   Gram: lower 128-blocks of Sigma (float32) and its float64 diagonal;
+//   chol_inv(o, sz): [L11, M11] = chol_inv(A11); L21 = A21 M11^T;
+//                    A22 -= L21 L21^T; [L22, M22] = chol_inv(A22);
+//                    T = L21 M11; M21 = -M22 T       (M = L^-1)
+//     with 128 x 128 leaves factored and inverted by leaf_chol_inv_body;
+//   alpha = M^T M diff, refined twice against float-float residuals;
+//   W = M^T M tile by tile, reduced at once against dK/dtheta (adjoint).
+// Every product runs on the CUDA cores as 128 x 128 output tiles, one per half
+// of the CTA (256 threads, 8 x 8 outputs per thread, K slices double-buffered
+// through shared memory); the autotuner picks the K-slice depth per n range.
+#include <algorithm>
+#include <climits>
+#include <map>
+#include <mutex>
+#include <vector>
+#include "gpk_internal.cuh"
+#include "simt_tile.cuh"
+#include "leaf_chol.cuh"
+#include "mll_finalize.cuh"
+
+namespace gpk {
+namespace {
+
+constexpr int BNT = LEAF_NT;  // threads per CTA (the leaf's 512)
+constexpr int HT = 256;       // threads of one half: one 128 x 128 output tile
+constexpr int TT = 128;       // output tile edge = leaf size
+constexpr int SLD = TT + 4;   // staged K-slice rows (16-byte aligned)
+constexpr int WLD = TT + 1;   // W tile rows in shared memory
+constexpr int BDM = 16;       // input dimension bound of the batched kernel
+constexpr int XLD = BDM + 1;  // staged input rows
+constexpr int NP_MAX = 4096;  // largest padded instance
+constexpr int NCFG = 2;       // tile configurations: K slices of 16 or 32
+
+// floats of one half's shared memory: the K-slice double buffer or the W
+// tile, then the staged inputs of the tile's rows and columns
+__host__ __device__ constexpr int half_stage_floats(int bk) {
+  return 4 * bk * SLD > TT * WLD ? 4 * bk * SLD : TT * WLD;
+}
+__host__ __device__ constexpr int half_floats() {
+  return half_stage_floats(32) + 2 * TT * XLD + 2 * TT;
+}
+
+struct BatchInst {
+  const double* x;
+  const double* y;
+  const double* theta;
+  double* out_mll;
+  double* out_grad;
+  int* info;
+  int64_t ldx;
+  int n, d, kind, n_ls, cfg, pad_;
+};
+
+struct BatchArgs {
+  const BatchInst* inst;
+  const int* queue;  // instance indices, largest n first
+  int* head;         // next queue position, zeroed before each launch
+  int count;
+  char* ws;          // one slot per CTA
+  size_t slot_bytes;
+  int np_max;        // the slot layout's matrix size
+  int want_grad;
+  double jitter;
+  int force_cfg;     // >= 0: every instance with this configuration (autotuner trials)
+};
+
+struct Slot {
+  float *A, *L, *M, *xs;
+  double *dtrack, *logdiag, *diff, *alpha;
+  float *rf, *zf;
+};
+
+__host__ __device__ inline size_t al256(size_t b) { return (b + 255) & ~size_t(255); }
+
+// Slot of a CTA for instances up to np (matrices with leading dimension of
+// the instance's own n_pad, so smaller instances use the front of each array).
+__host__ __device__ inline size_t slot_layout(int np, char* base, Slot* s) {
+  const size_t mat = al256((size_t)np * np * sizeof(float));
+  const size_t vd = al256((size_t)np * sizeof(double)), vf = al256((size_t)np * sizeof(float));
+  const size_t xsb = al256((size_t)np * BDM * sizeof(float));
+  if (s) {
+    char* p = base;
+    s->A = reinterpret_cast<float*>(p);
+    s->L = reinterpret_cast<float*>(p += mat);
+    s->M = reinterpret_cast<float*>(p += mat);
+    s->xs = reinterpret_cast<float*>(p += mat);
+    s->dtrack = reinterpret_cast<double*>(p += xsb);
+    s->logdiag = reinterpret_cast<double*>(p += vd);
+    s->diff = reinterpret_cast<double*>(p += vd);
+    s->alpha = reinterpret_cast<double*>(p += vd);
+    s->rf = reinterpret_cast<float*>(p += vd);
+    s->zf = reinterpret_cast<float*>(p += vf);
+  }
+  return 3 * mat + xsb + 4 * vd + 2 * vf;
+}
+
+// ---------------------------------------------------------------------------
+// One 128 x 128 output tile on one half of the CTA:
+//   acc[u][v] = sum_{k in [klo, khi)} A(i, k) B(j, k)
+// for rows i = i0 + ty*4 + (u & 3) + 64 (u >> 2) and columns likewise with tx.
+// Operand element (m, k) sits at P[m * ld + k] (KM = false: rows hold K) or
+// P[k * ld + m] (KM = true).  K slices of BK are loaded into registers one
+// slice ahead and stored into the other half of a double buffer.
+// ---------------------------------------------------------------------------
+template <int BK, bool KM>
+__device__ __forceinline__ void slice_load(const float* __restrict__ P, int ld, int r0, int k0,
+                                           int ht, float4 (&r)[BK / 8]) {
+#pragma unroll
+  for (int v = 0; v < BK / 8; ++v) {
+    const int e = ht + v * HT;
+    if constexpr (KM) {
+      const int k = e / (TT / 4), m = 4 * (e % (TT / 4));
+      r[v] = *reinterpret_cast<const float4*>(P + (int64_t)(k0 + k) * ld + r0 + m);
+    } else {
+      const int m = e / (BK / 4), k = 4 * (e % (BK / 4));
+      r[v] = *reinterpret_cast<const float4*>(P + (int64_t)(r0 + m) * ld + k0 + k);
+    }
+  }
+}
+
+template <int BK, bool KM>
+__device__ __forceinline__ void slice_store(float* S, int ht, const float4 (&r)[BK / 8]) {
+#pragma unroll
+  for (int v = 0; v < BK / 8; ++v) {
+    const int e = ht + v * HT;
+    if constexpr (KM) {
+      const int k = e / (TT / 4), m = 4 * (e % (TT / 4));
+      *reinterpret_cast<float4*>(S + k * SLD + m) = r[v];
+    } else {
+      const int m = e / (BK / 4), k = 4 * (e % (BK / 4));
+      S[(k + 0) * SLD + m] = r[v].x;
+      S[(k + 1) * SLD + m] = r[v].y;
+      S[(k + 2) * SLD + m] = r[v].z;
+      S[(k + 3) * SLD + m] = r[v].w;
+    }
+  }
+}
+
+__device__ __forceinline__ void half_sync(int half) { bar_sync_n(8 + half, HT); }
+
+template <int BK, bool AKM, bool BKM>
+__device__ __forceinline__ void tile_mma(const float* __restrict__ A, int lda,
+                                         const float* __restrict__ B, int ldb, int i0, int j0,
+                                         int klo, int khi, float* S, int ht, int half,
+                                         float (&acc)[8][8]) {
+  float* As = S;                 // [2][BK][SLD]
+  float* Bs = S + 2 * BK * SLD;  // [2][BK][SLD]
+  const int ty = ht >> 4, tx = ht & 15;
+  if (klo >= khi) return;
+  float4 ra[BK / 8], rb[BK / 8];
+  slice_load<BK, AKM>(A, lda, i0, klo, ht, ra);
+  slice_load<BK, BKM>(B, ldb, j0, klo, ht, rb);
+  slice_store<BK, AKM>(As, ht, ra);
+  slice_store<BK, BKM>(Bs, ht, rb);
+  half_sync(half);
+  int st = 0;
+  for (int k0 = klo; k0 < khi; k0 += BK) {
+    const bool more = k0 + BK < khi;
+    if (more) {
+      slice_load<BK, AKM>(A, lda, i0, k0 + BK, ht, ra);
+      slice_load<BK, BKM>(B, ldb, j0, k0 + BK, ht, rb);
+    }
+    const float* as = As + st * BK * SLD;
+    const float* bs = Bs + st * BK * SLD;
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      const float4 a0 = *reinterpret_cast<const float4*>(as + kk * SLD + ty * 4);
+      const float4 a1 = *reinterpret_cast<const float4*>(as + kk * SLD + 64 + ty * 4);
+      const float4 b0 = *reinterpret_cast<const float4*>(bs + kk * SLD + tx * 4);
+      const float4 b1 = *reinterpret_cast<const float4*>(bs + kk * SLD + 64 + tx * 4);
+      const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+#pragma unroll
+        for (int v = 0; v < 8; ++v) acc[u][v] = fmaf(av[u], bv[v], acc[u][v]);
+    }
+    if (more) {
+      slice_store<BK, AKM>(As + (st ^ 1) * BK * SLD, ht, ra);
+      slice_store<BK, BKM>(Bs + (st ^ 1) * BK * SLD, ht, rb);
+    }
+    half_sync(half);
+    st ^= 1;
+  }
+}
+
+__device__ __forceinline__ int tile_row(int ht, int u) { return (ht >> 4) * 4 + (u & 3) + ((u >> 2) << 6); }
+__device__ __forceinline__ int tile_col(int ht, int v) { return (ht & 15) * 4 + (v & 3) + ((v >> 2) << 6); }
+
+// A product over tm x tn output tiles (the lower ones when lower): the two
+// halves take alternate tiles.  kr(i0, j0, klo, khi) gives a tile's K range
+// (the triangles of the operands), ep(i0, j0, ht, acc, S) consumes it (S: the
+// half's shared memory, free until the half's next barrier).
+template <int BK, bool AKM, bool BKM, class KR, class EP>
+__device__ void product(int tm, int tn, bool lower, const float* A, int lda, const float* B,
+                        int ldb, KR kr, EP ep, float* smem) {
+  const int half = threadIdx.x / HT, ht = threadIdx.x % HT;
+  float* S = smem + half * half_floats();
+  const int nt = lower ? tm * (tm + 1) / 2 : tm * tn;
+  for (int t = half; t < nt; t += 2) {
+    int I, J;
+    if (lower) {
+      tri_index(t, I, J);
+    } else {
+      I = t / tn;
+      J = t % tn;
+    }
+    int klo, khi;
+    kr(I * TT, J * TT, klo, khi);
+    float acc[8][8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+#pragma unroll
+      for (int v = 0; v < 8; ++v) acc[u][v] = 0.f;
+    tile_mma<BK, AKM, BKM>(A, lda, B, ldb, I * TT, J * TT, klo, khi, S, ht, half, acc);
+    ep(I * TT, J * TT, ht, acc, S);
+  }
+  __syncthreads();
+}
+
+// C tile (rows i0.., columns j0..) = alpha acc (+ C when add), float4 rows
+__device__ __forceinline__ void put_tile(float* C, int ldc, int i0, int j0, int ht,
+                                         const float (&acc)[8][8], float alpha, bool add) {
+#pragma unroll
+  for (int u = 0; u < 8; ++u) {
+    const int64_t row = (int64_t)(i0 + tile_row(ht, u)) * ldc;
+#pragma unroll
+    for (int vb = 0; vb < 2; ++vb) {
+      float* c = C + row + j0 + tile_col(ht, 4 * vb);
+      float4 v = make_float4(alpha * acc[u][4 * vb], alpha * acc[u][4 * vb + 1],
+                             alpha * acc[u][4 * vb + 2], alpha * acc[u][4 * vb + 3]);
+      if (add) {
+        const float4 o = *reinterpret_cast<const float4*>(c);
+        v.x += o.x;
+        v.y += o.y;
+        v.z += o.z;
+        v.w += o.w;
+      }
+      *reinterpret_cast<float4*>(c) = v;
+    }
+  }
+}
+
+// The leaf's M blocks as plain float32 (its V = M^T blocks are not kept).
+struct LeafOutPlain {
+  float* M;
+  int64_t ldm;
+  int o;
+  __device__ void put_m(const float* Ms, int r0, int nr, int c0, int nc, int t, int nth) const {
+    const int q4 = nc / 4;
+    for (int e = t; e < nr * q4; e += nth) {
+      const int i = r0 + e / q4, c = c0 + 4 * (e % q4);
+      *reinterpret_cast<float4*>(M + (int64_t)(o + i) * ldm + o + c) =
+          *reinterpret_cast<const float4*>(Ms + i * LEAF_LDT + c);
+    }
+  }
+  __device__ void put_v(const float*, int, int, int, int, int, int) const {}
+};
+
+// dtrack[o + r] -= sum_k L[o + r][c0 + k]^2 (k < w) for rows r < rows: one
+// warp per row, float-float squares, float64 total.
+__device__ void track_rows(const float* L, int ld, int o, int rows, int c0, int w,
+                           double* dtrack) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int r = warp; r < rows; r += BNT / 32) {
+    const float* row = L + (int64_t)(o + r) * ld + c0;
+    float hi = 0.f, lo = 0.f;
+    for (int k = lane * 4; k < w; k += 128) {
+      const float4 v = *reinterpret_cast<const float4*>(row + k);
+      ff_sub_sq(hi, lo, v.x);
+      ff_sub_sq(hi, lo, v.y);
+      ff_sub_sq(hi, lo, v.z);
+      ff_sub_sq(hi, lo, v.w);
+    }
+    const double s = warp_sum((double)hi + (double)lo);
+    if (lane == 0) dtrack[o + r] += s;
+  }
+}
+
+// The two halves of an inner node of the recursive Cholesky + inverse of the
+// block at (o, o), size sz (a multiple of 128), h = the left child's size:
+//   before the right child: L21 = A21 M11^T into L (strictly below the
+//     diagonal blocks), the float64 diagonal track, A22 -= L21 L21^T;
+//   after it: T = L21 M11, stored transposed in L's unused upper part, and
+//     M21 = -M22 T into M (M = L^-1).
+template <int BK>
+__device__ void node_down(const Slot& S, int ld, int o, int h, int h2, float* smem) {
+  float* A21 = S.A + (int64_t)(o + h) * ld + o;
+  float* L21 = S.L + (int64_t)(o + h) * ld + o;
+  const float* M11 = S.M + (int64_t)o * ld + o;
+  // L21 = A21 M11^T: M11[j][k] = 0 for k > j
+  product<BK, false, false>(
+      h2 / TT, h / TT, false, A21, ld, M11, ld,
+      [&](int, int j0, int& klo, int& khi) { klo = 0; khi = min(h, j0 + TT); },
+      [&](int i0, int j0, int ht, const float (&acc)[8][8], float*) {
+        put_tile(L21, ld, i0, j0, ht, acc, 1.f, false);
+      },
+      smem);
+  track_rows(S.L, ld, o + h, h2, o, h, S.dtrack);
+  // A22 -= L21 L21^T (lower tiles)
+  float* A22 = S.A + (int64_t)(o + h) * ld + o + h;
+  product<BK, false, false>(
+      h2 / TT, h2 / TT, true, L21, ld, L21, ld,
+      [&](int, int, int& klo, int& khi) { klo = 0; khi = h; },
+      [&](int i0, int j0, int ht, const float (&acc)[8][8], float*) {
+        put_tile(A22, ld, i0, j0, ht, acc, -1.f, true);
+      },
+      smem);
+  __syncthreads();  // track_rows' dtrack writes before the leaves read them
+}
+
+template <int BK>
+__device__ void node_up(const Slot& S, int ld, int o, int h, int h2, float* smem) {
+  const float* L21 = S.L + (int64_t)(o + h) * ld + o;
+  const float* M11 = S.M + (int64_t)o * ld + o;
+  // T = L21 M11 (h2 x h; M11[k][j] = 0 for k < j), stored transposed:
+  // Tt[j][i] at L[(o + j) * ld + o + h + i]
+  float* Tt = S.L + (int64_t)o * ld + o + h;
+  product<BK, false, true>(
+      h2 / TT, h / TT, false, L21, ld, M11, ld,
+      [&](int, int j0, int& klo, int& khi) { klo = j0; khi = h; },
+      [&](int i0, int j0, int ht, const float (&acc)[8][8], float*) {
+#pragma unroll
+        for (int v = 0; v < 8; ++v) {
+          float* c = Tt + (int64_t)(j0 + tile_col(ht, v)) * ld + i0;
+#pragma unroll
+          for (int ub = 0; ub < 2; ++ub)
+            *reinterpret_cast<float4*>(c + tile_row(ht, 4 * ub)) =
+                make_float4(acc[4 * ub][v], acc[4 * ub + 1][v], acc[4 * ub + 2][v],
+                            acc[4 * ub + 3][v]);
+        }
+      },
+      smem);
+  // M21 = -M22 T: M22[i][k] = 0 for k > i; T(k, j) = Tt[j][k]
+  const float* M22 = S.M + (int64_t)(o + h) * ld + o + h;
+  float* M21 = S.M + (int64_t)(o + h) * ld + o;
+  product<BK, false, false>(
+      h2 / TT, h / TT, false, M22, ld, Tt, ld,
+      [&](int i0, int, int& klo, int& khi) { klo = 0; khi = min(h2, i0 + TT); },
+      [&](int i0, int j0, int ht, const float (&acc)[8][8], float*) {
+        put_tile(M21, ld, i0, j0, ht, acc, -1.f, false);
+      },
+      smem);
+}
+
+// Post-order walk of the recursion with an explicit stack (every thread
+// takes the same path): leaves at 128, left child of size
+// h = 128 * ceil(sz / 256), right child sz - h.
+template <int BK>
+__device__ void chol_inv(const Slot& S, int ld, int np, int* info, float* smem) {
+  constexpr int DEPTH = 8;  // np <= 4096: at most 6 levels
+  int so[DEPTH], ss[DEPTH], sst[DEPTH];
+  int top = 0;
+  so[0] = 0;
+  ss[0] = np;
+  sst[0] = 0;
+  while (top >= 0) {
+    const int o = so[top], sz = ss[top];
+    if (sz == TT) {
+      leaf_chol_inv_body(S.A, ld, o, S.dtrack, S.logdiag, info, LeafOutPlain{S.M, ld, o}, smem);
+      __syncthreads();
+      --top;
+      continue;
+    }
+    const int h = ((sz / 2 + TT - 1) / TT) * TT, h2 = sz - h;
+    if (sst[top] == 0) {
+      sst[top] = 1;
+      ++top;
+      so[top] = o;
+      ss[top] = h;
+      sst[top] = 0;
+    } else if (sst[top] == 1) {
+      node_down<BK>(S, ld, o, h, h2, smem);
+      sst[top] = 2;
+      ++top;
+      so[top] = o + h;
+      ss[top] = h2;
+      sst[top] = 0;
+    } else {
+      node_up<BK>(S, ld, o, h, h2, smem);
+      --top;
+    }
+  }
+}
+
+// z = M r (lower), one warp per row, float accumulation
+__device__ void gemv_lower(const float* M, int ld, int np, const float* r, float* z) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int i = warp; i < np; i += BNT / 32) {
+    const float* row = M + (int64_t)i * ld;
+    float s = 0.f;
+    for (int k = lane * 4; k <= i; k += 128) {
+      const float4 m = *reinterpret_cast<const float4*>(row + k);
+      const float4 v = *reinterpret_cast<const float4*>(r + k);
+      s = fmaf(m.x, v.x, s);
+      s = fmaf(m.y, v.y, s);
+      s = fmaf(m.z, v.z, s);
+      s = fmaf(m.w, v.w, s);  // entries past i are zeros of M
+    }
+    s = warp_sum(s);
+    if (lane == 0) z[i] = s;
+  }
+}
+
+// alpha (+)= M^T z, one thread per column (coalesced rows of M)
+__device__ void gemv_upper_t(const float* M, int ld, int np, const float* z, double* alpha,
+                             bool accumulate) {
+  for (int j = threadIdx.x; j < np; j += BNT) {
+    float s = 0.f;
+    for (int i = j; i < np; ++i) s = fmaf(M[(int64_t)i * ld + j], z[i], s);
+    alpha[j] = accumulate ? alpha[j] + (double)s : (double)s;
+  }
+}
+
+// rf = rhs as float32 (rhs: float64, zeros past n)
+__device__ void to_float(const double* rhs, int np, float* rf) {
+  for (int i = threadIdx.x; i < np; i += BNT) rf[i] = (float)rhs[i];
+}
+
+// alpha (+)= M^T M rhs
+__device__ void solve_apply(const Slot& S, int ld, int np, const double* rhs, bool accumulate) {
+  to_float(rhs, np, S.rf);
+  __syncthreads();
+  gemv_lower(S.M, ld, np, S.rf, S.zf);
+  __syncthreads();
+  gemv_upper_t(S.M, ld, np, S.zf, S.alpha, accumulate);
+  __syncthreads();
+}
+
+// float-float accumulation (hi, lo) += a (two-sum, not contracted)
+__device__ __forceinline__ void ff_add_b(float& hi, float& lo, float a) {
+  const float s = __fadd_rn(hi, a);
+  const float bb = __fsub_rn(s, hi);
+  lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(a, bb)));
+  hi = s;
+}
+
+// r = diff - Sigma alpha for rows < n (zeros past n) into rres (float64),
+// Sigma regenerated from the scaled inputs, products summed in float-float.
+// ah / al: alpha split into float hi / lo parts (shared memory).
+__device__ void residual(const BatchInst& I, const Slot& S, int np, float s2, float ka,
+                         double noise_diag, const float* ah, const float* al, double* rres) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n = I.n, d = I.d;
+  for (int i = warp; i < np; i += BNT / 32) {
+    if (i >= n) {
+      if (lane == 0) rres[i] = 0.0;
+      continue;
+    }
+    float xi[BDM];
+#pragma unroll
+    for (int k = 0; k < BDM; ++k) xi[k] = k < d ? S.xs[i * d + k] : 0.f;
+    float sh = 0.f, sl = 0.f;
+    for (int j = lane; j < n; j += 32) {
+      float sq = 0.f;
+#pragma unroll
+      for (int k = 0; k < BDM; ++k) {
+        if (k < d) {
+          const float df = xi[k] - S.xs[j * d + k];
+          sq = fmaf(df, df, sq);
+        }
+      }
+      const float kv = kval<float>(I.kind, sq, s2, ka);
+      const float p = kv * ah[j];
+      const float pe = fmaf(kv, ah[j], -p);
+      ff_add_b(sh, sl, p);
+      sl = fmaf(kv, al[j], sl + pe);
+    }
+    double s = warp_sum((double)sh + (double)sl);
+    if (lane == 0) {
+      s += noise_diag * S.alpha[i];  // the noise and jitter on the diagonal
+      rres[i] = S.diff[i] - s;
+    }
+  }
+}
+
+// The adjoint: W = M^T M (lower tiles, M[k][i] = 0 for k < i), contracted at
+// once with (alpha alpha^T - W) o dK/dtheta (unit variance).  Each thread sums
+// its elements of a tile in float32 (64 terms); the tile's sums go, per warp
+// and in float64, into the warp's own slots of wred (fixed order: the result
+// is reproducible).  sg[d + 2] (shared memory) receives the lengthscale sums,
+// the variance sum and the noise sum.
+template <int BK>
+__device__ void adjoint(const BatchInst& I, const Slot& S, int ld, int np, float ka,
+                        const float* ah, double* sg, double* wred, float* smem) {
+  const int d = I.d, n = I.n;
+  constexpr int NW = BNT / 32;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int e = threadIdx.x; e < (d + 2) * NW; e += BNT) wred[e] = 0.0;
+  __syncthreads();
+  product<BK, true, true>(
+      np / TT, np / TT, true, S.M, ld, S.M, ld,
+      [&](int i0, int, int& klo, int& khi) { klo = i0; khi = np; },
+      [&](int i0, int j0, int ht, const float (&acc)[8][8], float* Sh) {
+        const int half = threadIdx.x / HT;
+        float* Ws = Sh;                              // [TT][WLD]
+        float* sxi = Sh + half_stage_floats(32);     // [TT][XLD]
+        float* sxj = sxi + TT * XLD;
+        float* sai = sxj + TT * XLD;                 // alpha of the tile's rows
+        float* saj = sai + TT;                       // and columns
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+#pragma unroll
+          for (int v = 0; v < 8; ++v) Ws[tile_row(ht, u) * WLD + tile_col(ht, v)] = acc[u][v];
+        for (int e = ht; e < TT * BDM; e += HT) {
+          const int r = e / BDM, k = e % BDM;
+          sxi[r * XLD + k] = (i0 + r < n && k < d) ? S.xs[(i0 + r) * d + k] : 0.f;
+          sxj[r * XLD + k] = (j0 + r < n && k < d) ? S.xs[(j0 + r) * d + k] : 0.f;
+        }
+        for (int e = ht; e < TT; e += HT) {
+          sai[e] = ah[i0 + e];
+          saj[e] = ah[j0 + e];
+        }
+        half_sync(half);
+        with_kind(I.kind, [&](auto kind_c) {
+          constexpr int KIND = decltype(kind_c)::value;
+          float pl[BDM];
+#pragma unroll
+          for (int k = 0; k < BDM; ++k) pl[k] = 0.f;
+          float pvar = 0.f, pnoise = 0.f;
+#pragma unroll 2
+          for (int m = 0; m < TT * TT / HT; ++m) {
+            const int e = ht + m * HT, r = e >> 7, c = e & 127;
+            const int gi = i0 + r, gj = j0 + c;
+            if (gi >= n || gj >= n || gj > gi) continue;
+            const float w = Ws[r * WLD + c];
+            const float coef = (gi == gj ? 1.f : 2.f) * (sai[r] * saj[c] - w);
+            float sq = 0.f;
+#pragma unroll
+            for (int k = 0; k < BDM; ++k) {
+              const float df = sxi[r * XLD + k] - sxj[c * XLD + k];
+              sq = fmaf(df, df, sq);
+            }
+            float k1, c1;
+            kval_dcoef_k<KIND, float>(sq, 1.f, k1, c1, ka);
+            pvar = fmaf(coef, k1, pvar);
+            const float cc = coef * c1;
+#pragma unroll
+            for (int k = 0; k < BDM; ++k) {
+              const float df = sxi[r * XLD + k] - sxj[c * XLD + k];
+              pl[k] = fmaf(cc, df * df, pl[k]);
+            }
+            if (gi == gj) pnoise += fmaf(sai[r], sai[r], -w);
+          }
+          for (int s2 = 0; s2 < d + 2; ++s2) {
+            float v = pnoise;
+            if (s2 == d) v = pvar;
+#pragma unroll
+            for (int k = 0; k < BDM; ++k)
+              if (k == s2) v = pl[k];
+            const double t = warp_sum((double)v);
+            if (lane == 0) wred[s2 * NW + warp] += t;
+          }
+        });
+        half_sync(half);  // the staging area is the next tile's K buffer
+      },
+      smem);
+  for (int s = threadIdx.x; s < d + 2; s += BNT) {
+    double t = 0.0;
+    for (int w = 0; w < NW; ++w) t += wred[s * NW + w];
+    sg[s] = t;
+  }
+  __syncthreads();
+}
+
+template <int BK>
+__device__ void run_instance(const BatchArgs& a, const BatchInst& I, const Slot& S,
+                             float* smem, double* sred) {
+  const int n = I.n, d = I.d;
+  const int np = ((n + TT - 1) / TT) * TT;
+  const int ld = np;
+  const double* th = I.theta;
+  const double s2d = th[I.n_ls], sd = th[I.n_ls + 1], cst = th[I.n_ls + 2];
+  const float s2 = (float)s2d;
+  const float ka = kshape<float>(I.kind, th, I.n_ls);
+  const double noise_diag = a.jitter + sd * sd;
+  if (threadIdx.x == 0) *I.info = INT_MAX;
+  // scaled inputs, diff, diagonal track, zeroed diagonal blocks of M
+  for (int e = threadIdx.x; e < n * d; e += BNT) {
+    const int i = e / d, k = e % d;
+    const double l = I.n_ls == 1 ? th[0] : th[k];
+    S.xs[e] = (float)(I.x[(int64_t)i * I.ldx + k] / l);
+  }
+  for (int i = threadIdx.x; i < np; i += BNT) {
+    S.diff[i] = i < n ? I.y[i] - cst : 0.0;
+    S.dtrack[i] = i < n ? s2d + noise_diag : 1.0;
+  }
+  for (int e = threadIdx.x; e < np * TT; e += BNT) {
+    const int i = e / TT, c = e % TT;
+    S.M[(int64_t)i * ld + (i / TT) * TT + c] = 0.f;
+  }
+  __syncthreads();
+  // Gram: lower 128-blocks (diagonal blocks in full), identity past n
+  {
+    const int nb = np / TT, nt = nb * (nb + 1) / 2;
+    for (int t = 0; t < nt; ++t) {
+      int bi, bj;
+      tri_index(t, bi, bj);
+      for (int e = threadIdx.x; e < TT * TT; e += BNT) {
+        const int i = bi * TT + e / TT, j = bj * TT + e % TT;
+        float v;
+        if (i >= n || j >= n) {
+          v = i == j ? 1.f : 0.f;
+        } else {
+          float sq = 0.f;
+          for (int k = 0; k < d; ++k) {
+            const float df = S.xs[i * d + k] - S.xs[j * d + k];
+            sq = fmaf(df, df, sq);
+          }
+          v = kval<float>(I.kind, sq, s2, ka);
+          if (i == j) v = (float)((double)v + noise_diag);
+        }
+        S.A[(int64_t)i * ld + j] = v;
+      }
+    }
+  }
+  __syncthreads();
+  chol_inv<BK>(S, ld, np, I.info, smem);
+  __syncthreads();
+  const bool failed = *(volatile int*)I.info != INT_MAX;
+  __syncthreads();
+  double* sg = sred;                       // [GPK_MAX_D + 2]
+  double* red = sred + GPK_MAX_D + 2;      // [(GPK_MAX_D + 2) * 16]
+  if (!failed) {
+    // alpha = Sigma^-1 diff, refined twice
+    solve_apply(S, ld, np, S.diff, false);
+    float* ah = smem;          // [np] alpha hi
+    float* al = smem + np;     // [np] alpha lo
+    double* rres = reinterpret_cast<double*>(smem + 2 * np);  // [np]
+    for (int it = 0; it < 2; ++it) {
+      for (int i = threadIdx.x; i < np; i += BNT) {
+        const double v = S.alpha[i];
+        const float hi = (float)v;
+        ah[i] = hi;
+        al[i] = (float)(v - (double)hi);
+      }
+      __syncthreads();
+      residual(I, S, np, s2, ka, noise_diag, ah, al, rres);
+      __syncthreads();
+      solve_apply(S, ld, np, rres, true);
+    }
+    if (a.want_grad) {
+      // alpha hi parts for the adjoint, kept past the K buffers of both halves
+      float* ahg = smem + 2 * half_floats();
+      for (int i = threadIdx.x; i < np; i += BNT) ahg[i] = (float)S.alpha[i];
+      __syncthreads();
+      adjoint<BK>(I, S, ld, np, ka, ahg, sg, red, smem);
+    }
+  }
+  // sums and the outputs
+  const double logdet =
+      2.0 * block_ksum(n, [&](int i) { return failed ? 0.0 : S.logdiag[i]; });
+  const double quad = block_ksum(n, [&](int i) { return failed ? 0.0 : S.diff[i] * S.alpha[i]; });
+  const double asum = block_ksum(n, [&](int i) { return failed ? 0.0 : S.alpha[i]; });
+  if (threadIdx.x == 0) {
+    if (failed || !a.want_grad)
+      for (int s = 0; s < d + 2; ++s) sg[s] = 0.0;
+    finalize_outputs(n, d, th, I.n_ls, a.jitter, logdet, quad, asum, sg, a.want_grad, I.info,
+                     I.out_mll, a.want_grad ? I.out_grad : nullptr);
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(BNT, 1) batch_mll_kernel(const __grid_constant__ BatchArgs a) {
+  extern __shared__ __align__(16) float smem[];
+  __shared__ int s_job;
+  __shared__ double s_red[(GPK_MAX_D + 2) * 17];
+  Slot S;
+  slot_layout(a.np_max, a.ws + (size_t)blockIdx.x * a.slot_bytes, &S);
+  for (;;) {
+    if (threadIdx.x == 0) s_job = atomicAdd(a.head, 1);
+    __syncthreads();
+    const int q = s_job;
+    __syncthreads();
+    if (q >= a.count) break;
+    const BatchInst I = a.inst[a.queue[q]];
+    const int cfg = a.force_cfg >= 0 ? a.force_cfg : I.cfg;
+    if (cfg == 0)
+      run_instance<16>(a, I, S, smem, s_red);
+    else
+      run_instance<32>(a, I, S, smem, s_red);
+  }
+}
+
+size_t batch_smem_bytes(int np_max) {
+  // two halves, plus alpha for the adjoint; the leaf and the refinement
+  // vectors fit inside
+  const size_t halves = (size_t)2 * half_floats() * sizeof(float);
+  const size_t leaf = leaf_smem_bytes();
+  const size_t refine = (size_t)np_max * (2 * sizeof(float) + sizeof(double));
+  return std::max(std::max(halves + (size_t)np_max * sizeof(float), leaf), refine);
+}
+
+}  // namespace
+}  // namespace gpk
+
+using namespace gpk;
+
+// ---------------------------------------------------------------------------
+// Plans
+// ---------------------------------------------------------------------------
+struct gpk_batch_plan_s {
+  int device = 0;
+  int count = 0;
+  int np_max = 0;
+  int want_grad = 1;
+  double jitter = 0.0;
+  int grid = 0;
+  size_t slot_bytes = 0;
+  size_t smem = 0;
+  BatchInst* d_inst = nullptr;  // device copies of the descriptors
+  int* d_queue = nullptr;       // size-sorted instance indices
+  int* d_head = nullptr;
+  std::vector<int> cfg_of_bucket;  // chosen configuration per n_pad / 128 bucket
+};
+
+namespace {
+// Autotuner results, kept for the process: (device, n_pad) -> configuration.
+std::mutex g_tune_mu;
+std::map<std::pair<int, int>, int> g_tune;
+
+cudaError_t launch_batch(const gpk_batch_plan_s& P, void* ws, int force_cfg, int count,
+                         const int* queue, cudaStream_t s) {
+  BatchArgs a{};
+  a.inst = P.d_inst;
+  a.queue = queue;
+  a.head = P.d_head;
+  a.count = count;
+  a.ws = static_cast<char*>(ws);
+  a.slot_bytes = P.slot_bytes;
+  a.np_max = P.np_max;
+  a.want_grad = P.want_grad;
+  a.jitter = P.jitter;
+  a.force_cfg = force_cfg;
+  cudaError_t e = cudaMemsetAsync(P.d_head, 0, sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  const int grid = std::min(P.grid, std::max(count, 1));
+  batch_mll_kernel<<<grid, BNT, P.smem, s>>>(a);
+  return launch_status();
+}
+
+// Times every configuration on up to one grid of the plan's instances of
+// each n_pad (their outputs are overwritten by the next execution) and
+// keeps the faster per (device, n_pad).
+gpk_status autotune(gpk_batch_plan_s& P, const std::vector<int>& np_of, const std::vector<int>& order) {
+  std::map<int, std::vector<int>> by_np;
+  for (int i : order) by_np[np_of[i]].push_back(i);
+  std::vector<int> todo;
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    for (auto& kv : by_np)
+      if (!g_tune.count({P.device, kv.first})) todo.push_back(kv.first);
+  }
+  if (todo.empty()) return GPK_OK;
+  const size_t ws_bytes = P.slot_bytes * (size_t)P.grid;
+  void* ws = nullptr;
+  int* dq = nullptr;
+  cudaStream_t s = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  gpk_status st = GPK_OK;
+  if (cudaMalloc(&ws, ws_bytes) != cudaSuccess || cudaMalloc(&dq, sizeof(int) * P.count) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+    st = GPK_ERR_CUDA;
+  for (size_t b = 0; st == GPK_OK && b < todo.size(); ++b) {
+    std::vector<int>& ids = by_np[todo[b]];
+    const int m = std::min((int)ids.size(), P.grid);
+    if (cudaMemcpy(dq, ids.data(), sizeof(int) * m, cudaMemcpyHostToDevice) != cudaSuccess) {
+      st = GPK_ERR_CUDA;
+      break;
+    }
+    float best = 0.f;
+    int best_cfg = 0;
+    for (int cfg = 0; cfg < NCFG && st == GPK_OK; ++cfg) {
+      float ms = 0.f;
+      for (int rep = 0; rep < 2; ++rep) {  // the first run warms up
+        if (cudaEventRecord(e0, s) != cudaSuccess || launch_batch(P, ws, cfg, m, dq, s) != cudaSuccess ||
+            cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+          st = GPK_ERR_CUDA;
+          break;
+        }
+      }
+      if (st == GPK_OK && (cfg == 0 || ms < best)) {
+        best = ms;
+        best_cfg = cfg;
+      }
+    }
+    if (st == GPK_OK) {
+      std::lock_guard<std::mutex> lock(g_tune_mu);
+      g_tune[{P.device, todo[b]}] = best_cfg;
+    }
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (s) cudaStreamDestroy(s);
+  if (dq) cudaFree(dq);
+  if (ws) cudaFree(ws);
+  return st;
+}
+}  // namespace
+
+extern "C" gpk_status gpk_batch_plan_create(int count, const int* kind, const int64_t* n,
+                                            const int* d, const double* const* x,
+                                            const int64_t* ldx, const double* const* y,
+                                            const double* const* theta, const int* n_ls,
+                                            double jitter, int want_grad,
+                                            double* const* out_mll, double* const* out_grad,
+                                            int* info, int autotune_flag, gpk_batch_plan* plan) {
+  if (!plan) return GPK_ERR_BAD_ARG;
+  *plan = nullptr;
+  if (count <= 0 || !kind || !n || !d || !x || !ldx || !y || !theta || !n_ls || !out_mll ||
+      !info || (want_grad && !out_grad) || !(jitter >= 0.0))
+    return GPK_ERR_BAD_ARG;
+  int np_max = 0;
+  std::vector<int> np_of(count);
+  std::vector<BatchInst> hv(count);
+  for (int i = 0; i < count; ++i) {
+    if (kind[i] < GPK_RBF || kind[i] > GPK_RATIONAL_QUADRATIC || n[i] <= 0 || d[i] <= 0 ||
+        ldx[i] < d[i] || (n_ls[i] != 1 && n_ls[i] != d[i]) || !x[i] || !y[i] || !theta[i] ||
+        !out_mll[i] || (want_grad && !out_grad[i]))
+      return GPK_ERR_BAD_ARG;
+    if (n[i] > NP_MAX || d[i] > BDM) return GPK_ERR_UNSUPPORTED;
+    np_of[i] = (int)((n[i] + TT - 1) / TT) * TT;
+    np_max = std::max(np_max, np_of[i]);
+    hv[i] = BatchInst{x[i], y[i], theta[i], out_mll[i], want_grad ? out_grad[i] : nullptr,
+                      info + i, ldx[i], (int)n[i], d[i], kind[i], n_ls[i], 0, 0};
+  }
+  std::vector<int> order(count);
+  for (int i = 0; i < count; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return n[a] > n[b]; });
+  auto* P = new gpk_batch_plan_s;
+  auto fail = [&](gpk_status st) {
+    gpk_batch_plan_destroy(P);
+    return st;
+  };
+  if (cudaGetDevice(&P->device) != cudaSuccess) return fail(GPK_ERR_CUDA);
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, P->device) != cudaSuccess)
+    return fail(GPK_ERR_CUDA);
+  P->count = count;
+  P->np_max = np_max;
+  P->want_grad = want_grad ? 1 : 0;
+  P->jitter = jitter;
+  P->smem = batch_smem_bytes(np_max);
+  P->slot_bytes = al256(slot_layout(np_max, nullptr, nullptr));
+  if (cudaFuncSetAttribute(batch_mll_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)P->smem) != cudaSuccess)
+    return fail(GPK_ERR_CUDA);
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_mll_kernel, BNT, P->smem) !=
+          cudaSuccess ||
+      per_sm < 1)
+    return fail(GPK_ERR_UNSUPPORTED);
+  P->grid = sms * per_sm;
+  if (cudaMalloc(&P->d_inst, sizeof(BatchInst) * count) != cudaSuccess ||
+      cudaMalloc(&P->d_queue, sizeof(int) * count) != cudaSuccess ||
+      cudaMalloc(&P->d_head, sizeof(int)) != cudaSuccess)
+    return fail(GPK_ERR_CUDA);
+  if (cudaMemcpy(P->d_inst, hv.data(), sizeof(BatchInst) * count, cudaMemcpyHostToDevice) !=
+          cudaSuccess ||
+      cudaMemcpy(P->d_queue, order.data(), sizeof(int) * count, cudaMemcpyHostToDevice) !=
+          cudaSuccess)
+    return fail(GPK_ERR_CUDA);
+  if (autotune_flag) {
+    const gpk_status st = autotune(*P, np_of, order);
+    if (st != GPK_OK) return fail(st);
+  }
+  // configurations per instance from the tuned table (K slices of 32 where untuned)
+  bool changed = false;
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    for (int i = 0; i < count; ++i) {
+      auto it = g_tune.find({P->device, np_of[i]});
+      const int cfg = it != g_tune.end() ? it->second : 1;
+      if (hv[i].cfg != cfg) {
+        hv[i].cfg = cfg;
+        changed = true;
+      }
+    }
+  }
+  if (changed && cudaMemcpy(P->d_inst, hv.data(), sizeof(BatchInst) * count,
+                            cudaMemcpyHostToDevice) != cudaSuccess)
+    return fail(GPK_ERR_CUDA);
+  *plan = P;
+  return GPK_OK;
+}
+
+extern "C" size_t gpk_batch_plan_workspace_bytes(gpk_batch_plan plan) {
+  return plan ? plan->slot_bytes * (size_t)plan->grid : 0;
+}
+
+extern "C" int gpk_batch_plan_config(gpk_batch_plan plan, int64_t n) {
+  if (!plan || n <= 0 || n > NP_MAX) return -1;
+  const int np = (int)((n + TT - 1) / TT) * TT;
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  auto it = g_tune.find({plan->device, np});
+  return it != g_tune.end() ? it->second : 1;
+}
+
+extern "C" gpk_status gpk_batch_plan_execute(gpk_batch_plan plan, void* workspace,
+                                             size_t workspace_bytes, cudaStream_t stream) {
+  if (!plan || !workspace) return GPK_ERR_BAD_ARG;
+  if (workspace_bytes < gpk_batch_plan_workspace_bytes(plan)) return GPK_ERR_WORKSPACE;
+  GPK_CUDA_TRY(launch_batch(*plan, workspace, -1, plan->count, plan->d_queue, stream));
+  return GPK_OK;
+}
+
+extern "C" gpk_status gpk_batch_plan_destroy(gpk_batch_plan plan) {
+  if (!plan) return GPK_OK;
+  if (plan->d_inst) cudaFree(plan->d_inst);
+  if (plan->d_queue) cudaFree(plan->d_queue);
+  if (plan->d_head) cudaFree(plan->d_head);
+  delete plan;
+  return GPK_OK;
+}

@@ -188,6 +188,45 @@ __device__ __forceinline__ void ff_add(float& hi, float& lo, float a) {
   hi = s;
 }
 
+// Packed float32 pairs (sm_100 and later): one instruction for two lanes'
+// worth of add / sub / mul / fma, each element rounded as its scalar form.
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 f2_pack(float a, float b) {
+  f32x2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ float f2_lo(f32x2 v) {
+  float a, b;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+  return a;
+}
+__device__ __forceinline__ float f2_hi(f32x2 v) {
+  float a, b;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+  return b;
+}
+__device__ __forceinline__ f32x2 f2_add(f32x2 a, f32x2 b) {
+  f32x2 r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f32x2 f2_sub(f32x2 a, f32x2 b) {
+  f32x2 r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f32x2 f2_mul(f32x2 a, f32x2 b) {
+  f32x2 r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f32x2 f2_fma(f32x2 a, f32x2 b, f32x2 c) {
+  f32x2 r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+
 __device__ __forceinline__ float tf32_rna(float x) {
   uint32_t r;
   asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
@@ -710,13 +749,20 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       float gvh = 0.f, gvl = 0.f;
       with_kind(p.kind, [&](auto kind_c) {  // one loop per kernel kind
         constexpr int KIND = decltype(kind_c)::value;
+        // coordinates in pairs: packed float32x2 arithmetic halves the
+        // per-element instruction count of the distance and of the
+        // lengthscale sums, which bound this epilogue
+        constexpr int DP = DM / 2;
+        f32x2 xi2[DP];
+#pragma unroll
+        for (int kp = 0; kp < DP; ++kp) xi2[kp] = f2_pack(xi[2 * kp], xi[2 * kp + 1]);
 #pragma unroll
       for (int cb = 0; cb < HC / 32; ++cb) {
-        float pl[DM];
+        f32x2 pl2[DP];
 #pragma unroll
-        for (int k = 0; k < DM; ++k) pl[k] = 0.f;
+        for (int kp = 0; kp < DP; ++kp) pl2[kp] = f2_pack(0.f, 0.f);
         float pvar = 0.f;
-#pragma unroll
+#pragma unroll 8
         for (int k = 0; k < 32; ++k) {
           const int c = hcol + cb * 32 + k;
           const int gj = j0 + c;
@@ -724,24 +770,29 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
           const float w = otile[r * GLD + c];
           const float f = (gi == gj) ? 1.f : 2.f;
           const float coef = f * (ai * ga[c] - w);
-          float sq = 0.f;
+          const f32x2* gx2 = reinterpret_cast<const f32x2*>(gx + c * DM);
+          f32x2 dsq2[DP];
+          f32x2 s2 = f2_pack(0.f, 0.f);
 #pragma unroll
-          for (int kk = 0; kk < DM; ++kk) {
-            const float df = xi[kk] - gx[c * DM + kk];
-            sq = fmaf(df, df, sq);
+          for (int kp = 0; kp < DP; ++kp) {
+            const f32x2 df = f2_sub(xi2[kp], gx2[kp]);
+            dsq2[kp] = f2_mul(df, df);
+            s2 = f2_add(s2, dsq2[kp]);
           }
+          const float sq = f2_lo(s2) + f2_hi(s2);
           float k1, c1;
           kval_dcoef_k<KIND, float>(sq, 1.f, k1, c1, ka);
           pvar = fmaf(coef, k1, pvar);
           const float cc = coef * c1;
+          const f32x2 cc2 = f2_pack(cc, cc);
 #pragma unroll
-          for (int kk = 0; kk < DM; ++kk) {
-            const float df = xi[kk] - gx[c * DM + kk];
-            pl[kk] = fmaf(cc, df * df, pl[kk]);
-          }
+          for (int kp = 0; kp < DP; ++kp) pl2[kp] = f2_fma(cc2, dsq2[kp], pl2[kp]);
         }
 #pragma unroll
-        for (int kk = 0; kk < DM; ++kk) ff_add(glh[kk], gll[kk], pl[kk]);
+        for (int kp = 0; kp < DP; ++kp) {
+          ff_add(glh[2 * kp], gll[2 * kp], f2_lo(pl2[kp]));
+          ff_add(glh[2 * kp + 1], gll[2 * kp + 1], f2_hi(pl2[kp]));
+        }
         ff_add(gvh, gvl, pvar);
       }
       });
@@ -801,39 +852,49 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       float gvh = 0.f, gvl = 0.f;
       with_kind(p.kind, [&](auto kind_c) {  // one loop per kernel kind
         constexpr int KIND = decltype(kind_c)::value;
+        // coordinates in pairs (packed float32x2 arithmetic, as in MODE_GRAD)
+        constexpr int DP = DM / 2;
+        f32x2 zi2[DP];
+#pragma unroll
+        for (int kp = 0; kp < DP; ++kp) zi2[kp] = f2_pack(zi[2 * kp], zi[2 * kp + 1]);
 #pragma unroll 1
       for (int cb = 0; cb < HC / 32; ++cb) {
-        float pl[DM], pz[DM];
+        f32x2 pl2[DP], pz2[DP];
 #pragma unroll
-        for (int k = 0; k < DM; ++k) pl[k] = pz[k] = 0.f;
+        for (int kp = 0; kp < DP; ++kp) pl2[kp] = pz2[kp] = f2_pack(0.f, 0.f);
         float pvar = 0.f;
 #pragma unroll 4
         for (int k = 0; k < 32; ++k) {
           const int c = hcol + cb * 32 + k;
           if (!row_ok || j0 + c >= p.n_true) continue;
           const float g = fmaf(ai, ga[c], otile[r * GLD + c]);
-          float sq = 0.f;
+          const f32x2* gx2 = reinterpret_cast<const f32x2*>(gx + c * DM);
+          f32x2 df2[DP];
+          f32x2 s2 = f2_pack(0.f, 0.f);
 #pragma unroll
-          for (int kk = 0; kk < DM; ++kk) {
-            const float df = zi[kk] - gx[c * DM + kk];
-            sq = fmaf(df, df, sq);
+          for (int kp = 0; kp < DP; ++kp) {
+            df2[kp] = f2_sub(zi2[kp], gx2[kp]);
+            s2 = f2_fma(df2[kp], df2[kp], s2);
           }
+          const float sq = f2_lo(s2) + f2_hi(s2);
           float k1, c1;
           kval_dcoef_k<KIND, float>(sq, 1.f, k1, c1, ka);
           pvar = fmaf(g, k1, pvar);
           const float gc = g * c1;
+          const f32x2 gc2 = f2_pack(gc, gc);
 #pragma unroll
-          for (int kk = 0; kk < DM; ++kk) {
-            const float df = zi[kk] - gx[c * DM + kk];
-            const float t = gc * df;
-            pz[kk] += t;
-            pl[kk] = fmaf(t, df, pl[kk]);
+          for (int kp = 0; kp < DP; ++kp) {
+            const f32x2 t = f2_mul(gc2, df2[kp]);
+            pz2[kp] = f2_add(pz2[kp], t);
+            pl2[kp] = f2_fma(t, df2[kp], pl2[kp]);
           }
         }
 #pragma unroll
-        for (int kk = 0; kk < DM; ++kk) {
-          ff_add(glh[kk], gll[kk], pl[kk]);
-          ff_add(gzh[kk], gzl[kk], pz[kk]);
+        for (int kp = 0; kp < DP; ++kp) {
+          ff_add(glh[2 * kp], gll[2 * kp], f2_lo(pl2[kp]));
+          ff_add(glh[2 * kp + 1], gll[2 * kp + 1], f2_hi(pl2[kp]));
+          ff_add(gzh[2 * kp], gzl[2 * kp], f2_lo(pz2[kp]));
+          ff_add(gzh[2 * kp + 1], gzl[2 * kp + 1], f2_hi(pz2[kp]));
         }
         ff_add(gvh, gvl, pvar);
       }

@@ -236,6 +236,77 @@ def cross_covariance_vjp(kind, n_ls, theta, x, y, G, need_x=False, need_y=False)
     return gth, gx, gy
 
 
+class BatchPlan:
+    """Many independent GPs of uneven n (conjugate_mll, gpjax/objectives.py:36-107,
+    and its gradient per instance) evaluated by ONE persistent kernel launch per
+    :meth:`execute`: the plan sorts the instances by n into a device queue, and
+    one CTA per SM pulls instances from it and runs each to completion
+    (``gpk_batch_plan_*`` in include/gpk.h).  With ``autotune`` the plan times
+    the library's tile configurations on its own instances for every padded n
+    not tuned before in this process.
+
+    kinds: kernel codes; xs: [n_i, d_i] float64 CUDA tensors (n_i <= 4096,
+    d_i <= 16); ys: [n_i]; thetas: the theta layout ``[lengthscale (n_ls[i]),
+    variance, obs_stddev, constant]`` (``alpha`` last for RationalQuadratic).
+    The tensors are read at every execution (update them in place between
+    executions, e.g. for multi-start fits); results land in ``self.mll``,
+    ``self.grads`` and ``self.info``.  ``execute`` is stream-ordered and can be
+    captured in a CUDA graph.
+    """
+
+    def __init__(self, kinds, xs, ys, thetas, n_ls, jitter: float = 1e-6,
+                 want_grad: bool = True, autotune: bool = True):
+        import ctypes
+
+        B = len(xs)
+        dev = _lib.require_cuda(*xs)
+        self.device = dev
+        self.xs = [x.detach().contiguous() for x in xs]
+        self.ys = [y.detach().reshape(-1).contiguous() for y in ys]
+        self.thetas = [t.detach().contiguous() for t in thetas]
+        self.mll = torch.full((B,), float("nan"), dtype=torch.float64, device=dev)
+        self.grads = [torch.zeros(int(nl) + 3 + (1 if int(k) == _lib.RATIONAL_QUADRATIC else 0),
+                                  dtype=torch.float64, device=dev)
+                      for nl, k in zip(n_ls, kinds)]
+        self.info = torch.zeros(B, dtype=torch.int32, device=dev)
+        i32, i64, ptr = ctypes.c_int * B, ctypes.c_int64 * B, ctypes.c_void_p * B
+        handle = ctypes.c_void_p()
+        _lib.call("gpk_batch_plan_create", B, i32(*[int(k) for k in kinds]),
+                  i64(*[x.shape[0] for x in self.xs]), i32(*[x.shape[1] for x in self.xs]),
+                  ptr(*[x.data_ptr() for x in self.xs]), i64(*[x.shape[1] for x in self.xs]),
+                  ptr(*[y.data_ptr() for y in self.ys]), ptr(*[t.data_ptr() for t in self.thetas]),
+                  i32(*[int(v) for v in n_ls]), float(jitter), int(want_grad),
+                  ptr(*[self.mll.data_ptr() + 8 * i for i in range(B)]),
+                  ptr(*[g.data_ptr() for g in self.grads]), self.info.data_ptr(), int(autotune),
+                  ctypes.byref(handle))
+        self._handle = handle
+        lib = _lib.lib()
+        self.workspace = torch.empty(max(int(lib.gpk_batch_plan_workspace_bytes(handle)), 256),
+                                     dtype=torch.uint8, device=dev)
+
+    def config(self, n: int) -> int:
+        """Tile configuration the autotuner chose for instances of size n."""
+        return int(_lib.lib().gpk_batch_plan_config(self._handle, int(n)))
+
+    def execute(self):
+        """One launch over all instances; returns (mll, grads, info)."""
+        _lib.call("gpk_batch_plan_execute", self._handle, self.workspace.data_ptr(),
+                  self.workspace.numel(), _lib.stream_ptr(self.device))
+        return self.mll, self.grads, self.info
+
+    def close(self):
+        if getattr(self, "_handle", None) is not None and self._handle.value:
+            torch.cuda.synchronize(self.device)
+            _lib.lib().gpk_batch_plan_destroy(self._handle)
+            self._handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # interpreter shutdown
+            pass
+
+
 def conjugate_mll_batched(kinds, xs, ys, thetas, n_ls, jitter: float = 1e-6,
                           want_grad: bool = True):
     """conjugate_mll (gpjax/objectives.py:36-107) and its gradient for a batch of

@@ -285,6 +285,38 @@ gpk_status gpk_conjugate_mll_batched(int count, const int* kind, const int64_t* 
                                      cudaStream_t stream);
 
 /* ---------------------------------------------------------------------------
+ * Persistent batched MLL + gradient through a plan (no single counterpart:
+ * conjugate_mll, gpjax/objectives.py:36-107, and jax.value_and_grad of it per
+ * instance, as the reference would vmap or loop over independent GPs).
+ * gpk_batch_plan_create records the instances (same arguments and result
+ * locations as gpk_conjugate_mll_batched; the device arrays are read at each
+ * execution, so their contents may change between executions), sorts them
+ * by n (largest first) into a device queue and, when autotune != 0, times the
+ * tile configurations on the plan's own instances for every n_pad not yet
+ * tuned on this device (results kept for the process).  It allocates a few
+ * bytes per instance of device memory and synchronises the device: call it
+ * outside stream capture.  gpk_batch_plan_execute zeroes the queue head and
+ * launches ONE persistent kernel (one CTA per SM pulls instances from the
+ * queue and runs each to completion), so an execution can be captured in a
+ * CUDA graph.  Float32 compute with float64 pivots, float-float refinement of
+ * alpha and float64 sums.  n <= 4096, d <= 16 (else GPK_ERR_UNSUPPORTED).
+ * gpk_batch_plan_config returns the configuration chosen for instances of
+ * size n (0: K slices of 16, 1: of 32) or -1.
+ * ------------------------------------------------------------------------- */
+typedef struct gpk_batch_plan_s* gpk_batch_plan;
+gpk_status gpk_batch_plan_create(int count, const int* kind, const int64_t* n, const int* d,
+                                 const double* const* x, const int64_t* ldx,
+                                 const double* const* y, const double* const* theta,
+                                 const int* n_ls, double jitter, int want_grad,
+                                 double* const* out_mll, double* const* out_grad, int* info,
+                                 int autotune, gpk_batch_plan* plan);
+size_t gpk_batch_plan_workspace_bytes(gpk_batch_plan plan);
+int gpk_batch_plan_config(gpk_batch_plan plan, int64_t n);
+gpk_status gpk_batch_plan_execute(gpk_batch_plan plan, void* workspace, size_t workspace_bytes,
+                                  cudaStream_t stream);
+gpk_status gpk_batch_plan_destroy(gpk_batch_plan plan);
+
+/* ---------------------------------------------------------------------------
  * Prediction: ConjugatePosterior.predict (gpjax/gps.py:443-526).
  * mean [t] and var [t] float64 (var = diag of the predictive covariance,
  * GaussianDistribution.variance, distributions.py:79-81); cov [t, t] float64

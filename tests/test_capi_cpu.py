@@ -124,6 +124,38 @@ def test_batched_mll_rejects_bad_arguments(built_lib):
                                          0, None) == 1
 
 
+def test_batch_plan_rejects_bad_arguments(built_lib):
+    """Plan creation checks every instance on the host before touching the
+    device; a null plan is refused by execute and harmless elsewhere."""
+    from gpjax_gb300 import _lib
+    lib = _lib.lib()
+    P = ctypes.c_void_p(0x1000)
+    ptr1 = (ctypes.c_void_p * 1)(P)
+    i32 = lambda *v: (ctypes.c_int * len(v))(*v)
+    i64 = lambda *v: (ctypes.c_int64 * len(v))(*v)
+    out = ctypes.c_void_p()
+
+    def create(count=1, kind=0, n=100, d=2, ldx=2, nls=2, jitter=1e-6):
+        return lib.gpk_batch_plan_create(count, i32(kind), i64(n), i32(d), ptr1, i64(ldx), ptr1,
+                                         ptr1, i32(nls), jitter, 1, ptr1, ptr1, P, 0,
+                                         ctypes.byref(out))
+    assert create(count=0) == 1
+    assert create(kind=7) == 1
+    assert create(n=0) == 1
+    assert create(ldx=1) == 1
+    assert create(nls=3) == 1
+    assert create(jitter=-1.0) == 1
+    assert create(n=4097) == 6          # GPK_ERR_UNSUPPORTED: one CTA per instance up to 4096
+    assert create(d=17, ldx=17, nls=17) == 6
+    assert out.value is None
+    assert lib.gpk_batch_plan_create(1, i32(0), i64(100), i32(2), ptr1, i64(2), ptr1, ptr1,
+                                     i32(2), 1e-6, 1, ptr1, ptr1, P, 0, None) == 1
+    assert lib.gpk_batch_plan_workspace_bytes(None) == 0
+    assert lib.gpk_batch_plan_config(None, 100) == -1
+    assert lib.gpk_batch_plan_execute(None, P, 1 << 20, None) == 1
+    assert lib.gpk_batch_plan_destroy(None) == 0
+
+
 # ---------------------------------------------------------------------------
 # Argument checks of the remaining entry points: every case below is refused
 # on the host before any device work (fake pointers are never dereferenced)
