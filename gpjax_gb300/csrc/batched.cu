@@ -45,7 +45,7 @@ constexpr int TT = 128;       // output tile edge = leaf size
 constexpr int SLD = TT + 4;   // staged K-slice rows (16-byte aligned)
 constexpr int WLD = TT + 1;   // W tile rows in shared memory
 constexpr int BDM = 16;       // input dimension bound of the batched kernel
-constexpr int XLD = BDM + 1;  // staged input rows
+constexpr int XLD = BDM + 2;  // staged input rows (pairs stay 8-byte aligned)
 constexpr int NP_MAX = 4096;  // largest padded instance
 constexpr int NCFG = 2;       // tile configurations: K slices of 16 or 32
 
@@ -492,6 +492,57 @@ __device__ void residual(const BatchInst& I, const Slot& S, int np, float s2, fl
   }
 }
 
+// One W tile (shared memory, row stride WLD) contracted against dK/dtheta:
+// coordinates in DP pairs (packed float32x2 arithmetic), per-thread float32
+// sums over its 64 elements, then per warp in float64 into wred[slot][warp].
+template <int KIND, int DP>
+__device__ __forceinline__ void adj_tile(int ht, int i0, int j0, int n, int d, float ka,
+                                         const float* Ws, const float* sxi, const float* sxj,
+                                         const float* sai, const float* saj, double* wred,
+                                         int warp, int lane) {
+  constexpr int NW = BNT / 32;
+  f32x2 pl2[DP];
+#pragma unroll
+  for (int kp = 0; kp < DP; ++kp) pl2[kp] = f2_pack(0.f, 0.f);
+  float pvar = 0.f, pnoise = 0.f;
+#pragma unroll 2
+  for (int m = 0; m < TT * TT / HT; ++m) {
+    const int e = ht + m * HT, r = e >> 7, c = e & 127;
+    const int gi = i0 + r, gj = j0 + c;
+    if (gi >= n || gj >= n || gj > gi) continue;
+    const float w = Ws[r * WLD + c];
+    const float coef = (gi == gj ? 1.f : 2.f) * (sai[r] * saj[c] - w);
+    const f32x2* xi2 = reinterpret_cast<const f32x2*>(sxi + r * XLD);
+    const f32x2* xj2 = reinterpret_cast<const f32x2*>(sxj + c * XLD);
+    f32x2 dsq2[DP];
+    f32x2 s2 = f2_pack(0.f, 0.f);
+#pragma unroll
+    for (int kp = 0; kp < DP; ++kp) {
+      const f32x2 df = f2_sub(xi2[kp], xj2[kp]);
+      dsq2[kp] = f2_mul(df, df);
+      s2 = f2_add(s2, dsq2[kp]);
+    }
+    float k1, c1;
+    kval_dcoef_k<KIND, float>(f2_lo(s2) + f2_hi(s2), 1.f, k1, c1, ka);
+    pvar = fmaf(coef, k1, pvar);
+    const float cc = coef * c1;
+    const f32x2 cc2 = f2_pack(cc, cc);
+#pragma unroll
+    for (int kp = 0; kp < DP; ++kp) pl2[kp] = f2_fma(cc2, dsq2[kp], pl2[kp]);
+    if (gi == gj) pnoise += fmaf(sai[r], sai[r], -w);
+  }
+  for (int s = 0; s < d + 2; ++s) {
+    float v = s == d ? pvar : pnoise;
+#pragma unroll
+    for (int kp = 0; kp < DP; ++kp) {  // (pairs past d hold the zero padding)
+      if (s < d && 2 * kp == s) v = f2_lo(pl2[kp]);
+      if (s < d && 2 * kp + 1 == s) v = f2_hi(pl2[kp]);
+    }
+    const double t = warp_sum((double)v);
+    if (lane == 0) wred[s * NW + warp] += t;
+  }
+}
+
 // The adjoint: W = M^T M (lower tiles, M[k][i] = 0 for k < i), contracted at
 // once with (alpha alpha^T - W) o dK/dtheta (unit variance).  Each thread sums
 // its elements of a tile in float32 (64 terms); the tile's sums go, per warp
@@ -532,43 +583,13 @@ __device__ void adjoint(const BatchInst& I, const Slot& S, int ld, int np, float
         half_sync(half);
         with_kind(I.kind, [&](auto kind_c) {
           constexpr int KIND = decltype(kind_c)::value;
-          float pl[BDM];
-#pragma unroll
-          for (int k = 0; k < BDM; ++k) pl[k] = 0.f;
-          float pvar = 0.f, pnoise = 0.f;
-#pragma unroll 2
-          for (int m = 0; m < TT * TT / HT; ++m) {
-            const int e = ht + m * HT, r = e >> 7, c = e & 127;
-            const int gi = i0 + r, gj = j0 + c;
-            if (gi >= n || gj >= n || gj > gi) continue;
-            const float w = Ws[r * WLD + c];
-            const float coef = (gi == gj ? 1.f : 2.f) * (sai[r] * saj[c] - w);
-            float sq = 0.f;
-#pragma unroll
-            for (int k = 0; k < BDM; ++k) {
-              const float df = sxi[r * XLD + k] - sxj[c * XLD + k];
-              sq = fmaf(df, df, sq);
-            }
-            float k1, c1;
-            kval_dcoef_k<KIND, float>(sq, 1.f, k1, c1, ka);
-            pvar = fmaf(coef, k1, pvar);
-            const float cc = coef * c1;
-#pragma unroll
-            for (int k = 0; k < BDM; ++k) {
-              const float df = sxi[r * XLD + k] - sxj[c * XLD + k];
-              pl[k] = fmaf(cc, df * df, pl[k]);
-            }
-            if (gi == gj) pnoise += fmaf(sai[r], sai[r], -w);
-          }
-          for (int s2 = 0; s2 < d + 2; ++s2) {
-            float v = pnoise;
-            if (s2 == d) v = pvar;
-#pragma unroll
-            for (int k = 0; k < BDM; ++k)
-              if (k == s2) v = pl[k];
-            const double t = warp_sum((double)v);
-            if (lane == 0) wred[s2 * NW + warp] += t;
-          }
+          const int dp = (d + 1) / 2;
+          if (dp <= 2)
+            adj_tile<KIND, 2>(ht, i0, j0, n, d, ka, Ws, sxi, sxj, sai, saj, wred, warp, lane);
+          else if (dp <= 4)
+            adj_tile<KIND, 4>(ht, i0, j0, n, d, ka, Ws, sxi, sxj, sai, saj, wred, warp, lane);
+          else
+            adj_tile<KIND, 8>(ht, i0, j0, n, d, ka, Ws, sxi, sxj, sai, saj, wred, warp, lane);
         });
         half_sync(half);  // the staging area is the next tile's K buffer
       },
