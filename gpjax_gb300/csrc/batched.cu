@@ -18,8 +18,8 @@
 // Per instance (padded to n_pad, a multiple of 128, with an identity block):
 //   Gram: lower 128-blocks of Sigma (float32) and its float64 diagonal;
 //   factor: right-looking over 128-wide panels, each diagonal block factored
-//     and inverted by leaf_chol_inv_body, the panel below X = A_panel M_kk^T,
-//     A22 -= X X^T;
+//     and inverted by leaf_chol_inv_body, the panel below solved by
+//     substitution, A22 -= X X^T;
 //   inverse: M = L^-1 by the recursive merge M21 = -M22 (L21 M11);
 //   alpha = M^T M diff, refined twice against float-float residuals;
 //   W = M^T M tile by tile, reduced at once against dK/dtheta (adjoint).
@@ -332,14 +332,75 @@ __device__ void node_up(const Slot& S, int ld, int o, int h, int h2, float* smem
       smem);
 }
 
+// X L_kk^T = A_panel for the R rows below a diagonal block: forward
+// substitution, one thread per row, 32 columns at a time in registers (the
+// solved columns of the row are read back from X).  L_kk comes from the
+// leaf's shared memory, still in place: LT[k][i] = L[i][k] below the
+// diagonal (zeros on and above it) and Rl[i] = 1 / L[i][i].  Substitution is
+// backward stable; X = A_panel M_kk^T with the leaf's inverse is not, and on
+// a smooth RBF instance (n = 1068, d = 2, condition number 8.8e6) the
+// product form drove a later pivot negative.
+__device__ void panel_solve(const float* __restrict__ Ap, float* __restrict__ Xp, int ld, int R,
+                            const float* leaf_smem) {
+  constexpr int LDT = LEAF_LDT, PB = 32;
+  const float* LT = leaf_smem;
+  const float* Rl = leaf_smem + 2 * LEAF * LEAF_LDT + 64 * LEAF_TLD + 4 * LEAF;
+  for (int row = threadIdx.x; row < R; row += BNT) {
+    const float* ar = Ap + (int64_t)row * ld;
+    float* xr = Xp + (int64_t)row * ld;
+    for (int cb = 0; cb < LEAF / PB; ++cb) {
+      const int c0 = cb * PB;
+      float a[PB];
+#pragma unroll
+      for (int g = 0; g < PB / 4; ++g) {
+        const float4 v = *reinterpret_cast<const float4*>(ar + c0 + 4 * g);
+        a[4 * g] = v.x;
+        a[4 * g + 1] = v.y;
+        a[4 * g + 2] = v.z;
+        a[4 * g + 3] = v.w;
+      }
+      for (int m = 0; m < c0; ++m) {  // the solved columns
+        const float xm = xr[m];
+#pragma unroll
+        for (int g = 0; g < PB / 4; ++g) {
+          const float4 l = *reinterpret_cast<const float4*>(LT + m * LDT + c0 + 4 * g);
+          a[4 * g] = fmaf(-xm, l.x, a[4 * g]);
+          a[4 * g + 1] = fmaf(-xm, l.y, a[4 * g + 1]);
+          a[4 * g + 2] = fmaf(-xm, l.z, a[4 * g + 2]);
+          a[4 * g + 3] = fmaf(-xm, l.w, a[4 * g + 3]);
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < PB; ++j) {  // within the block
+        const float xj = a[j] * Rl[c0 + j];
+        a[j] = xj;
+#pragma unroll
+        for (int g = 0; g < PB / 4; ++g) {
+          if (4 * g + 3 > j) {
+            const float4 l = *reinterpret_cast<const float4*>(LT + (c0 + j) * LDT + c0 + 4 * g);
+            if (4 * g + 0 > j) a[4 * g] = fmaf(-xj, l.x, a[4 * g]);
+            if (4 * g + 1 > j) a[4 * g + 1] = fmaf(-xj, l.y, a[4 * g + 1]);
+            if (4 * g + 2 > j) a[4 * g + 2] = fmaf(-xj, l.z, a[4 * g + 2]);
+            a[4 * g + 3] = fmaf(-xj, l.w, a[4 * g + 3]);
+          }
+        }
+      }
+#pragma unroll
+      for (int g = 0; g < PB / 4; ++g)
+        *reinterpret_cast<float4*>(xr + c0 + 4 * g) =
+            make_float4(a[4 * g], a[4 * g + 1], a[4 * g + 2], a[4 * g + 3]);
+    }
+  }
+}
+
 // Cholesky + inverse of the padded matrix.
 //  * Factor: right-looking over 128-wide panels.  The leaf factors and inverts
 //    the diagonal block (pivots from the float64 diagonal track); the panel
-//    below is X = A_panel M_kk^T (the leaf's accurate 128 x 128 inverse), the
-//    diagonal track loses X's row sums of squares, and A22 -= X X^T.  (The
+//    below is solved by substitution against L_kk (panel_solve), the
+//    diagonal track loses its row sums of squares, and A22 -= X X^T.  (The
 //    recursive form L21 = A21 M11^T with a recursively formed M11 amplified
-//    rounding by the condition number of L11: on ill-conditioned RBF instances
-//    its log-determinant erred ~10x more than this panel form.)
+//    rounding by the condition number of L11: on ill-conditioned RBF
+//    instances its log-determinant erred ~10x more than this panel form.)
 //  * Inverse: M = L^-1 by the recursion's merge step, post-order over the
 //    tree with 128 leaves and left child h = 128 * ceil(sz / 256):
 //    T = L21 M11, M21 = -M22 T (node_up), every thread on the same path.
@@ -351,14 +412,8 @@ __device__ void chol_inv(const Slot& S, int ld, int np, int* info, float* smem) 
     const int R = np - o - TT;
     if (R <= 0) break;
     float* Lp = S.L + (int64_t)(o + TT) * ld + o;
-    const float* Mkk = S.M + (int64_t)o * ld + o;
-    product<BK, false, false>(
-        R / TT, 1, false, S.A + (int64_t)(o + TT) * ld + o, ld, Mkk, ld,
-        [&](int, int, int& klo, int& khi) { klo = 0; khi = TT; },
-        [&](int i0, int j0, int ht, const float (&acc)[8][8], float*) {
-          put_tile(Lp, ld, i0, j0, ht, acc, 1.f, false);
-        },
-        smem);
+    panel_solve(S.A + (int64_t)(o + TT) * ld + o, Lp, ld, R, smem);
+    __syncthreads();
     track_rows(S.L, ld, o + TT, R, o, TT, S.dtrack);
     float* A22 = S.A + (int64_t)(o + TT) * ld + o + TT;
     product<BK, false, false>(

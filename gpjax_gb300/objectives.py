@@ -141,6 +141,45 @@ def shard_rows(n: int, world: int, rank: int) -> slice:
     return slice(start, start + base + (1 if rank < extra else 0))
 
 
+def partition_instances(ns, world: int) -> list:
+    """Independent GPs split over `world` ranks for a data-parallel batched
+    evaluation (each rank builds a BatchPlan over its share; no collective but
+    the gather of the results).  Cost of an instance ~ n^3: largest first, each
+    to the rank with the least cost so far (ties to the lower rank).  Returns
+    one sorted index list per rank; deterministic, so every rank computes the
+    same split."""
+    if world < 1:
+        raise ValueError("need world >= 1")
+    load = [0.0] * world
+    parts = [[] for _ in range(world)]
+    for i in sorted(range(len(ns)), key=lambda i: (-int(ns[i]), i)):
+        r = min(range(world), key=lambda q: (load[q], q))
+        parts[r].append(i)
+        load[r] += float(ns[i]) ** 3
+    return [sorted(p) for p in parts]
+
+
+def gather_instance_results(mll: torch.Tensor, indices, count: int, group=None) -> torch.Tensor:
+    """All ranks' per-instance MLL values into one [count] float64 tensor in
+    the original order (torch.distributed.all_gather of each rank's share,
+    padded to the longest share)."""
+    import torch.distributed as dist
+
+    world = dist.get_world_size(group)
+    sizes = [None] * world
+    dist.all_gather_object(sizes, (len(indices), list(indices)), group=group)
+    width = max(s[0] for s in sizes) if sizes else 0
+    buf = torch.full((width,), float("nan"), dtype=torch.float64, device=mll.device)
+    buf[:len(indices)] = mll[:len(indices)]
+    bufs = [torch.empty_like(buf) for _ in range(world)]
+    dist.all_gather(bufs, buf, group=group)
+    out = torch.full((count,), float("nan"), dtype=torch.float64, device=mll.device)
+    for (k, idx), b in zip(sizes, bufs):
+        if k:
+            out[torch.as_tensor(idx, device=mll.device)] = b[:k]
+    return out
+
+
 def allreduce_callback(workspace: torch.Tensor, group=None):
     """The library's exchange hook for gpk_collapsed_elbo_sharded: sums the
     float64 region at a byte offset of `workspace` over the process group, in
