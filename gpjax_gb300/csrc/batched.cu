@@ -23,9 +23,10 @@
 //   inverse: M = L^-1 by the recursive merge M21 = -M22 (L21 M11);
 //   alpha = M^T M diff, refined twice against float-float residuals;
 //   W = M^T M tile by tile, reduced at once against dK/dtheta (adjoint).
-// Every product runs on the CUDA cores as 128 x 128 output tiles, one per half
-// of the CTA (256 threads, 8 x 8 outputs per thread, K slices double-buffered
-// through shared memory); the autotuner picks the K-slice depth per n range.
+// Every product runs on the CUDA cores as 128 x 128 output tiles, one at a
+// time on the whole CTA (512 threads, 8 x 4 outputs per thread, K slices
+// double-buffered through shared memory); the autotuner picks the K-slice
+// depth per n range.
 #include <algorithm>
 #include <climits>
 #include <map>
@@ -40,23 +41,20 @@ namespace gpk {
 namespace {
 
 constexpr int BNT = LEAF_NT;  // threads per CTA (the leaf's 512)
-constexpr int HT = 256;       // threads of one half: one 128 x 128 output tile
 constexpr int TT = 128;       // output tile edge = leaf size
 constexpr int SLD = TT + 4;   // staged K-slice rows (16-byte aligned)
-constexpr int WLD = TT + 1;   // W tile rows in shared memory
+constexpr int WLD = TT + 4;   // W tile rows in shared memory (float4 rows)
 constexpr int BDM = 16;       // input dimension bound of the batched kernel
 constexpr int XLD = BDM + 2;  // staged input rows (pairs stay 8-byte aligned)
 constexpr int NP_MAX = 4096;  // largest padded instance
 constexpr int NCFG = 2;       // tile configurations: K slices of 16 or 32
 
-// floats of one half's shared memory: the K-slice double buffer or the W
-// tile, then the staged inputs of the tile's rows and columns
-__host__ __device__ constexpr int half_stage_floats(int bk) {
-  return 4 * bk * SLD > TT * WLD ? 4 * bk * SLD : TT * WLD;
+// floats of the product staging area: the K-slice double buffer (or the W
+// tile), then the staged inputs and alphas of a tile's rows and columns
+__host__ __device__ constexpr int stage_floats() {
+  return 4 * 32 * SLD > TT * WLD ? 4 * 32 * SLD : TT * WLD;
 }
-__host__ __device__ constexpr int half_floats() {
-  return half_stage_floats(32) + 2 * TT * XLD + 2 * TT;
-}
+__host__ __device__ constexpr int prod_floats() { return stage_floats() + 2 * TT * XLD + 2 * TT; }
 
 struct BatchInst {
   const double* x;
@@ -113,19 +111,21 @@ __host__ __device__ inline size_t slot_layout(int np, char* base, Slot* s) {
 }
 
 // ---------------------------------------------------------------------------
-// One 128 x 128 output tile on one half of the CTA:
+// One 128 x 128 output tile on the whole CTA (512 threads, 8 x 4 outputs each):
 //   acc[u][v] = sum_{k in [klo, khi)} A(i, k) B(j, k)
-// for rows i = i0 + ty*4 + (u & 3) + 64 (u >> 2) and columns likewise with tx.
-// Operand element (m, k) sits at P[m * ld + k] (KM = false: rows hold K) or
-// P[k * ld + m] (KM = true).  K slices of BK are loaded into registers one
-// slice ahead and stored into the other half of a double buffer.
+// for rows i = i0 + tile_row(u) (ty*4 + (u & 3) + 64 (u >> 2)) and columns
+// j = j0 + tx*4 + v, with ty = tid / 32 and tx = tid % 32 (a warp shares its
+// rows: the A fragment loads are broadcasts).  Operand element (m, k) sits at
+// P[m * ld + k] (KM = false: rows hold K) or P[k * ld + m] (KM = true).  K
+// slices of BK are loaded into registers one slice ahead and stored into the
+// other half of a double buffer.
 // ---------------------------------------------------------------------------
 template <int BK, bool KM>
 __device__ __forceinline__ void slice_load(const float* __restrict__ P, int ld, int r0, int k0,
-                                           int ht, float4 (&r)[BK / 8]) {
+                                           float4 (&r)[BK / 16]) {
 #pragma unroll
-  for (int v = 0; v < BK / 8; ++v) {
-    const int e = ht + v * HT;
+  for (int v = 0; v < BK / 16; ++v) {
+    const int e = threadIdx.x + v * BNT;
     if constexpr (KM) {
       const int k = e / (TT / 4), m = 4 * (e % (TT / 4));
       r[v] = *reinterpret_cast<const float4*>(P + (int64_t)(k0 + k) * ld + r0 + m);
@@ -137,10 +137,10 @@ __device__ __forceinline__ void slice_load(const float* __restrict__ P, int ld, 
 }
 
 template <int BK, bool KM>
-__device__ __forceinline__ void slice_store(float* S, int ht, const float4 (&r)[BK / 8]) {
+__device__ __forceinline__ void slice_store(float* S, const float4 (&r)[BK / 16]) {
 #pragma unroll
-  for (int v = 0; v < BK / 8; ++v) {
-    const int e = ht + v * HT;
+  for (int v = 0; v < BK / 16; ++v) {
+    const int e = threadIdx.x + v * BNT;
     if constexpr (KM) {
       const int k = e / (TT / 4), m = 4 * (e % (TT / 4));
       *reinterpret_cast<float4*>(S + k * SLD + m) = r[v];
@@ -154,29 +154,26 @@ __device__ __forceinline__ void slice_store(float* S, int ht, const float4 (&r)[
   }
 }
 
-__device__ __forceinline__ void half_sync(int half) { bar_sync_n(8 + half, HT); }
-
 template <int BK, bool AKM, bool BKM>
 __device__ __forceinline__ void tile_mma(const float* __restrict__ A, int lda,
                                          const float* __restrict__ B, int ldb, int i0, int j0,
-                                         int klo, int khi, float* S, int ht, int half,
-                                         float (&acc)[8][8]) {
+                                         int klo, int khi, float* S, float (&acc)[8][4]) {
   float* As = S;                 // [2][BK][SLD]
   float* Bs = S + 2 * BK * SLD;  // [2][BK][SLD]
-  const int ty = ht >> 4, tx = ht & 15;
+  const int ty = threadIdx.x >> 5, tx = threadIdx.x & 31;
   if (klo >= khi) return;
-  float4 ra[BK / 8], rb[BK / 8];
-  slice_load<BK, AKM>(A, lda, i0, klo, ht, ra);
-  slice_load<BK, BKM>(B, ldb, j0, klo, ht, rb);
-  slice_store<BK, AKM>(As, ht, ra);
-  slice_store<BK, BKM>(Bs, ht, rb);
-  half_sync(half);
+  float4 ra[BK / 16], rb[BK / 16];
+  slice_load<BK, AKM>(A, lda, i0, klo, ra);
+  slice_load<BK, BKM>(B, ldb, j0, klo, rb);
+  slice_store<BK, AKM>(As, ra);
+  slice_store<BK, BKM>(Bs, rb);
+  __syncthreads();
   int st = 0;
   for (int k0 = klo; k0 < khi; k0 += BK) {
     const bool more = k0 + BK < khi;
     if (more) {
-      slice_load<BK, AKM>(A, lda, i0, k0 + BK, ht, ra);
-      slice_load<BK, BKM>(B, ldb, j0, k0 + BK, ht, rb);
+      slice_load<BK, AKM>(A, lda, i0, k0 + BK, ra);
+      slice_load<BK, BKM>(B, ldb, j0, k0 + BK, rb);
     }
     const float* as = As + st * BK * SLD;
     const float* bs = Bs + st * BK * SLD;
@@ -185,37 +182,36 @@ __device__ __forceinline__ void tile_mma(const float* __restrict__ A, int lda,
       const float4 a0 = *reinterpret_cast<const float4*>(as + kk * SLD + ty * 4);
       const float4 a1 = *reinterpret_cast<const float4*>(as + kk * SLD + 64 + ty * 4);
       const float4 b0 = *reinterpret_cast<const float4*>(bs + kk * SLD + tx * 4);
-      const float4 b1 = *reinterpret_cast<const float4*>(bs + kk * SLD + 64 + tx * 4);
       const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-      const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+      const float bv[4] = {b0.x, b0.y, b0.z, b0.w};
 #pragma unroll
       for (int u = 0; u < 8; ++u)
 #pragma unroll
-        for (int v = 0; v < 8; ++v) acc[u][v] = fmaf(av[u], bv[v], acc[u][v]);
+        for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(av[u], bv[v], acc[u][v]);
     }
     if (more) {
-      slice_store<BK, AKM>(As + (st ^ 1) * BK * SLD, ht, ra);
-      slice_store<BK, BKM>(Bs + (st ^ 1) * BK * SLD, ht, rb);
+      slice_store<BK, AKM>(As + (st ^ 1) * BK * SLD, ra);
+      slice_store<BK, BKM>(Bs + (st ^ 1) * BK * SLD, rb);
     }
-    half_sync(half);
+    __syncthreads();
     st ^= 1;
   }
 }
 
-__device__ __forceinline__ int tile_row(int ht, int u) { return (ht >> 4) * 4 + (u & 3) + ((u >> 2) << 6); }
-__device__ __forceinline__ int tile_col(int ht, int v) { return (ht & 15) * 4 + (v & 3) + ((v >> 2) << 6); }
+__device__ __forceinline__ int tile_row(int u) {
+  return (threadIdx.x >> 5) * 4 + (u & 3) + ((u >> 2) << 6);
+}
+__device__ __forceinline__ int tile_col(int v) { return (threadIdx.x & 31) * 4 + v; }
 
-// A product over tm x tn output tiles (the lower ones when lower): the two
-// halves take alternate tiles.  kr(i0, j0, klo, khi) gives a tile's K range
-// (the triangles of the operands), ep(i0, j0, ht, acc, S) consumes it (S: the
-// half's shared memory, free until the half's next barrier).
+// A product over tm x tn output tiles (the lower ones when lower), one tile
+// at a time on the whole CTA.  kr(i0, j0, klo, khi) gives a tile's K range
+// (the triangles of the operands), ep(i0, j0, acc, S) consumes it (S: the
+// staging area, free until the next barrier).
 template <int BK, bool AKM, bool BKM, class KR, class EP>
 __device__ void product(int tm, int tn, bool lower, const float* A, int lda, const float* B,
                         int ldb, KR kr, EP ep, float* smem) {
-  const int half = threadIdx.x / HT, ht = threadIdx.x % HT;
-  float* S = smem + half * half_floats();
   const int nt = lower ? tm * (tm + 1) / 2 : tm * tn;
-  for (int t = half; t < nt; t += 2) {
+  for (int t = 0; t < nt; ++t) {
     int I, J;
     if (lower) {
       tri_index(t, I, J);
@@ -225,37 +221,33 @@ __device__ void product(int tm, int tn, bool lower, const float* A, int lda, con
     }
     int klo, khi;
     kr(I * TT, J * TT, klo, khi);
-    float acc[8][8];
+    float acc[8][4];
 #pragma unroll
     for (int u = 0; u < 8; ++u)
 #pragma unroll
-      for (int v = 0; v < 8; ++v) acc[u][v] = 0.f;
-    tile_mma<BK, AKM, BKM>(A, lda, B, ldb, I * TT, J * TT, klo, khi, S, ht, half, acc);
-    ep(I * TT, J * TT, ht, acc, S);
+      for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
+    tile_mma<BK, AKM, BKM>(A, lda, B, ldb, I * TT, J * TT, klo, khi, smem, acc);
+    ep(I * TT, J * TT, acc, smem);
   }
   __syncthreads();
 }
 
 // C tile (rows i0.., columns j0..) = alpha acc (+ C when add), float4 rows
-__device__ __forceinline__ void put_tile(float* C, int ldc, int i0, int j0, int ht,
-                                         const float (&acc)[8][8], float alpha, bool add) {
+__device__ __forceinline__ void put_tile(float* C, int ldc, int i0, int j0,
+                                         const float (&acc)[8][4], float alpha, bool add) {
 #pragma unroll
   for (int u = 0; u < 8; ++u) {
-    const int64_t row = (int64_t)(i0 + tile_row(ht, u)) * ldc;
-#pragma unroll
-    for (int vb = 0; vb < 2; ++vb) {
-      float* c = C + row + j0 + tile_col(ht, 4 * vb);
-      float4 v = make_float4(alpha * acc[u][4 * vb], alpha * acc[u][4 * vb + 1],
-                             alpha * acc[u][4 * vb + 2], alpha * acc[u][4 * vb + 3]);
-      if (add) {
-        const float4 o = *reinterpret_cast<const float4*>(c);
-        v.x += o.x;
-        v.y += o.y;
-        v.z += o.z;
-        v.w += o.w;
-      }
-      *reinterpret_cast<float4*>(c) = v;
+    float* c = C + (int64_t)(i0 + tile_row(u)) * ldc + j0 + tile_col(0);
+    float4 v = make_float4(alpha * acc[u][0], alpha * acc[u][1], alpha * acc[u][2],
+                           alpha * acc[u][3]);
+    if (add) {
+      const float4 o = *reinterpret_cast<const float4*>(c);
+      v.x += o.x;
+      v.y += o.y;
+      v.z += o.z;
+      v.w += o.w;
     }
+    *reinterpret_cast<float4*>(c) = v;
   }
 }
 
@@ -308,13 +300,13 @@ __device__ void node_up(const Slot& S, int ld, int o, int h, int h2, float* smem
   product<BK, false, true>(
       h2 / TT, h / TT, false, L21, ld, M11, ld,
       [&](int, int j0, int& klo, int& khi) { klo = j0; khi = h; },
-      [&](int i0, int j0, int ht, const float (&acc)[8][8], float*) {
+      [&](int i0, int j0, const float (&acc)[8][4], float*) {
 #pragma unroll
-        for (int v = 0; v < 8; ++v) {
-          float* c = Tt + (int64_t)(j0 + tile_col(ht, v)) * ld + i0;
+        for (int v = 0; v < 4; ++v) {
+          float* c = Tt + (int64_t)(j0 + tile_col(v)) * ld + i0;
 #pragma unroll
           for (int ub = 0; ub < 2; ++ub)
-            *reinterpret_cast<float4*>(c + tile_row(ht, 4 * ub)) =
+            *reinterpret_cast<float4*>(c + tile_row(4 * ub)) =
                 make_float4(acc[4 * ub][v], acc[4 * ub + 1][v], acc[4 * ub + 2][v],
                             acc[4 * ub + 3][v]);
         }
@@ -326,8 +318,8 @@ __device__ void node_up(const Slot& S, int ld, int o, int h, int h2, float* smem
   product<BK, false, false>(
       h2 / TT, h / TT, false, M22, ld, Tt, ld,
       [&](int i0, int, int& klo, int& khi) { klo = 0; khi = min(h2, i0 + TT); },
-      [&](int i0, int j0, int ht, const float (&acc)[8][8], float*) {
-        put_tile(M21, ld, i0, j0, ht, acc, -1.f, false);
+      [&](int i0, int j0, const float (&acc)[8][4], float*) {
+        put_tile(M21, ld, i0, j0, acc, -1.f, false);
       },
       smem);
 }
@@ -419,8 +411,8 @@ __device__ void chol_inv(const Slot& S, int ld, int np, int* info, float* smem) 
     product<BK, false, false>(
         R / TT, R / TT, true, Lp, ld, Lp, ld,
         [&](int, int, int& klo, int& khi) { klo = 0; khi = TT; },
-        [&](int i0, int j0, int ht, const float (&acc)[8][8], float*) {
-          put_tile(A22, ld, i0, j0, ht, acc, -1.f, true);
+        [&](int i0, int j0, const float (&acc)[8][4], float*) {
+          put_tile(A22, ld, i0, j0, acc, -1.f, true);
         },
         smem);
     __syncthreads();  // track_rows' dtrack writes before the next leaf reads them
@@ -547,7 +539,7 @@ __device__ void residual(const BatchInst& I, const Slot& S, int np, float s2, fl
 // coordinates in DP pairs (packed float32x2 arithmetic), per-thread float32
 // sums over its 64 elements, then per warp in float64 into wred[slot][warp].
 template <int KIND, int DP>
-__device__ __forceinline__ void adj_tile(int ht, int i0, int j0, int n, int d, float ka,
+__device__ __forceinline__ void adj_tile(int i0, int j0, int n, int d, float ka,
                                          const float* Ws, const float* sxi, const float* sxj,
                                          const float* sai, const float* saj, double* wred,
                                          int warp, int lane) {
@@ -557,8 +549,8 @@ __device__ __forceinline__ void adj_tile(int ht, int i0, int j0, int n, int d, f
   for (int kp = 0; kp < DP; ++kp) pl2[kp] = f2_pack(0.f, 0.f);
   float pvar = 0.f, pnoise = 0.f;
 #pragma unroll 2
-  for (int m = 0; m < TT * TT / HT; ++m) {
-    const int e = ht + m * HT, r = e >> 7, c = e & 127;
+  for (int m = 0; m < TT * TT / BNT; ++m) {
+    const int e = threadIdx.x + m * BNT, r = e >> 7, c = e & 127;
     const int gi = i0 + r, gj = j0 + c;
     if (gi >= n || gj >= n || gj > gi) continue;
     const float w = Ws[r * WLD + c];
@@ -611,38 +603,37 @@ __device__ void adjoint(const BatchInst& I, const Slot& S, int ld, int np, float
   product<BK, true, true>(
       np / TT, np / TT, true, S.M, ld, S.M, ld,
       [&](int i0, int, int& klo, int& khi) { klo = i0; khi = np; },
-      [&](int i0, int j0, int ht, const float (&acc)[8][8], float* Sh) {
-        const int half = threadIdx.x / HT;
-        float* Ws = Sh;                              // [TT][WLD]
-        float* sxi = Sh + half_stage_floats(32);     // [TT][XLD]
+      [&](int i0, int j0, const float (&acc)[8][4], float* Sh) {
+        float* Ws = Sh;                          // [TT][WLD]
+        float* sxi = Sh + stage_floats();        // [TT][XLD]
         float* sxj = sxi + TT * XLD;
-        float* sai = sxj + TT * XLD;                 // alpha of the tile's rows
-        float* saj = sai + TT;                       // and columns
+        float* sai = sxj + TT * XLD;             // alpha of the tile's rows
+        float* saj = sai + TT;                   // and columns
 #pragma unroll
         for (int u = 0; u < 8; ++u)
-#pragma unroll
-          for (int v = 0; v < 8; ++v) Ws[tile_row(ht, u) * WLD + tile_col(ht, v)] = acc[u][v];
-        for (int e = ht; e < TT * BDM; e += HT) {
+          *reinterpret_cast<float4*>(Ws + tile_row(u) * WLD + tile_col(0)) =
+              make_float4(acc[u][0], acc[u][1], acc[u][2], acc[u][3]);
+        for (int e = threadIdx.x; e < TT * BDM; e += BNT) {
           const int r = e / BDM, k = e % BDM;
           sxi[r * XLD + k] = (i0 + r < n && k < d) ? S.xs[(i0 + r) * d + k] : 0.f;
           sxj[r * XLD + k] = (j0 + r < n && k < d) ? S.xs[(j0 + r) * d + k] : 0.f;
         }
-        for (int e = ht; e < TT; e += HT) {
+        for (int e = threadIdx.x; e < TT; e += BNT) {
           sai[e] = ah[i0 + e];
           saj[e] = ah[j0 + e];
         }
-        half_sync(half);
+        __syncthreads();
         with_kind(I.kind, [&](auto kind_c) {
           constexpr int KIND = decltype(kind_c)::value;
           const int dp = (d + 1) / 2;
           if (dp <= 2)
-            adj_tile<KIND, 2>(ht, i0, j0, n, d, ka, Ws, sxi, sxj, sai, saj, wred, warp, lane);
+            adj_tile<KIND, 2>(i0, j0, n, d, ka, Ws, sxi, sxj, sai, saj, wred, warp, lane);
           else if (dp <= 4)
-            adj_tile<KIND, 4>(ht, i0, j0, n, d, ka, Ws, sxi, sxj, sai, saj, wred, warp, lane);
+            adj_tile<KIND, 4>(i0, j0, n, d, ka, Ws, sxi, sxj, sai, saj, wred, warp, lane);
           else
-            adj_tile<KIND, 8>(ht, i0, j0, n, d, ka, Ws, sxi, sxj, sai, saj, wred, warp, lane);
+            adj_tile<KIND, 8>(i0, j0, n, d, ka, Ws, sxi, sxj, sai, saj, wred, warp, lane);
         });
-        half_sync(half);  // the staging area is the next tile's K buffer
+        __syncthreads();  // the staging area is the next tile's K buffer
       },
       smem);
   for (int s = threadIdx.x; s < d + 2; s += BNT) {
@@ -731,7 +722,7 @@ __device__ void run_instance(const BatchArgs& a, const BatchInst& I, const Slot&
     }
     if (a.want_grad) {
       // alpha hi parts for the adjoint, kept past the K buffers of both halves
-      float* ahg = smem + 2 * half_floats();
+      float* ahg = smem + prod_floats();
       for (int i = threadIdx.x; i < np; i += BNT) ahg[i] = (float)S.alpha[i];
       __syncthreads();
       adjoint<BK>(I, S, ld, np, ka, ahg, sg, red, smem);
@@ -779,12 +770,12 @@ __global__ void __launch_bounds__(BNT, 1) batch_mll_kernel(const __grid_constant
 }
 
 size_t batch_smem_bytes(int np_max) {
-  // two halves, plus alpha for the adjoint; the leaf and the refinement
-  // vectors fit inside
-  const size_t halves = (size_t)2 * half_floats() * sizeof(float);
+  // the largest of: the product staging area plus alpha for the adjoint, the
+  // leaf, the refinement vectors
+  const size_t prod = (size_t)prod_floats() * sizeof(float);
   const size_t leaf = leaf_smem_bytes();
   const size_t refine = (size_t)np_max * (2 * sizeof(float) + sizeof(double));
-  return std::max(std::max(halves + (size_t)np_max * sizeof(float), leaf), refine);
+  return std::max(std::max(prod + (size_t)np_max * sizeof(float), leaf), refine);
 }
 
 }  // namespace
