@@ -163,16 +163,8 @@ __device__ __forceinline__ f32x2 f2_pack(float a, float b) {
   asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
   return r;
 }
-__device__ __forceinline__ float f2_lo(f32x2 v) {
-  float a, b;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
-  return a;
-}
-__device__ __forceinline__ float f2_hi(f32x2 v) {
-  float a, b;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
-  return b;
-}
+__device__ __forceinline__ float f2_lo(f32x2 v) { return __uint_as_float((unsigned)v); }
+__device__ __forceinline__ float f2_hi(f32x2 v) { return __uint_as_float((unsigned)(v >> 32)); }
 __device__ __forceinline__ f32x2 f2_add(f32x2 a, f32x2 b) {
   f32x2 r;
   asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));

@@ -935,6 +935,77 @@ cudaError_t side_ctx(SideCtx** out) {
 }
 }  // namespace
 
+// Predictive mean and variance on the factor of the mixed form
+// (ConjugatePosterior.predict, gpjax/gps.py:443-526, without the full
+// covariance): Ktx in TF32 hi/lo, Q^T = Ktx M^T as one split-TF32 GEMM whose
+// epilogue only sums the squares of each row of Q^T (the float64 diagonal
+// track, nothing stored), mean = m + Ktx alpha with the refined alpha.
+struct TcPredict {
+  int t;
+  const double* xt;
+  int64_t ldxt;
+  double prior_jitter;
+  double* mean;
+  double* var;
+  float *Kh, *Kl, *ts;  // [t_pad][np] x 2, [t][d]
+  double* vacc;         // [t_pad]: minus the row sums of squares of Q^T
+};
+
+__global__ void pred_tc_info_kernel(int* info) {
+  if (*info == INT_MAX) *info = 0;
+}
+
+size_t predict_tc_extra_bytes(int64_t np, int64_t t, int d) {
+  const int64_t tp = ((t + LEAF - 1) / LEAF) * LEAF;
+  return 2 * (size_t)tp * np * sizeof(float) + (size_t)t * d * sizeof(float) +
+         (size_t)tp * sizeof(double) + 4 * 1024;
+}
+
+// Kh/Kl[i][k] = TF32 split of k(t_i, x_k) for i < t, k < n; zeros elsewhere
+__global__ void __launch_bounds__(256)
+    ktx_split_kernel(int kind, int t, int tp, int n, int np, int d, const float* __restrict__ ts,
+                     const float* __restrict__ xs, const double* __restrict__ theta, int n_ls,
+                     float* __restrict__ Kh, float* __restrict__ Kl) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (int64_t)tp * np) return;
+  const int i = (int)(e / np), k = (int)(e % np);
+  float v = 0.f;
+  if (i < t && k < n) {
+    float sq = 0.f;
+    for (int c = 0; c < d; ++c) {
+      const float df = ts[(int64_t)i * d + c] - xs[(int64_t)k * d + c];
+      sq = fmaf(df, df, sq);
+    }
+    v = kval<float>(kind, sq, (float)theta[n_ls], kshape<float>(kind, theta, n_ls));
+  }
+  const float hi = tf32_rna_f(v);
+  Kh[e] = hi;
+  Kl[e] = tf32_rna_f(v - hi);
+}
+
+// mean_i = m + sum_k Ktx[i][k] alpha_k (float64 sums), var_i = s2 + prior
+// jitter - |Q^T row i|^2; NaN when the factorisation failed
+__global__ void __launch_bounds__(256)
+    pred_tc_finish_kernel(int t, int n, int np, const float* __restrict__ Kh,
+                          const float* __restrict__ Kl, const double* __restrict__ alpha,
+                          const double* __restrict__ vacc, const double* __restrict__ theta,
+                          int n_ls, double prior_jitter, const int* __restrict__ info,
+                          double* __restrict__ mean, double* __restrict__ var) {
+  const int i = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (i >= t) return;
+  double s = 0.0;
+  for (int k = lane; k < n; k += 32)
+    s += ((double)Kh[(int64_t)i * np + k] + (double)Kl[(int64_t)i * np + k]) * alpha[k];
+  s = warp_sum(s);
+  if (lane == 0) {
+    const bool bad = *info != 0 && *info != INT_MAX;
+    const double nan = __longlong_as_double(0x7ff8000000000000ULL);
+    mean[i] = bad ? nan : theta[n_ls + 2] + s;
+    var[i] = bad ? nan : theta[n_ls] + prior_jitter + vacc[i];
+  }
+}
+
 size_t mll_tc_workspace_bytes(int64_t n, int d) {
   TcBuffers b;
   return tc_layout(n, d, nullptr, b);
@@ -944,7 +1015,8 @@ bool mll_tc_supported(int d) { return d <= tc::GRAD_DMAX; }
 
 gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, const double* y,
                       const double* theta, int n_ls, double jitter, int refine, int want_grad,
-                      double* out_mll, double* out_grad, int* info, void* ws, cudaStream_t s) {
+                      double* out_mll, double* out_grad, int* info, void* ws, cudaStream_t s,
+                      const TcPredict* pred) {
   TcBuffers b;
   tc_layout(n, d, ws, b);
   const int np = b.npad;
@@ -1060,6 +1132,36 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
     if (st != GPK_OK) return st;
   }
   prof_mark(3, hs);
+  if (pred) {  // predictive mean and variance instead of the adjoint
+    const int t = pred->t, tp = (int)(((int64_t)t + LEAF - 1) / LEAF * LEAF);
+    GPK_CUDA_TRY(scale_inputs<float>(pred->xt, pred->ldxt, t, d, theta, n_ls, pred->ts, hs));
+    ktx_split_kernel<<<(unsigned)cdiv((int64_t)tp * np, 256), 256, 0, hs>>>(
+        kind, t, tp, n, np, d, pred->ts, b.xs, theta, n_ls, pred->Kh, pred->Kl);
+    GPK_LAUNCH_CHECK();
+    GPK_CUDA_TRY(cudaMemsetAsync(pred->vacc, 0, sizeof(double) * tp, hs));
+    TcMap mK;
+    if (!tc_make_map(&mK, pred->Kh, pred->Kl, tp, np, np)) return GPK_ERR_UNSUPPORTED;
+    tc::TcParams pq{};  // Q^T[i, j] = sum_k Ktx[i, k] M[j, k], M[j, k] = 0 for k > j
+    pq.M = tp;
+    pq.N = np;
+    pq.K = np;
+    pq.b_tri = TRI_LOWER;
+    pq.alpha = 1.f;
+    pq.dtrack = pred->vacc;
+    pq.err = b.err;
+    GPK_CUDA_TRY(tc_gemm_run(tc::MODE_STORE_SPLIT, mK, c.mM, pq, 1, hs));
+    GPK_CUDA_TRY(cudaEventRecord(sc->edone, hs));
+    GPK_CUDA_TRY(cudaStreamWaitEvent(s, sc->edone, 0));
+    tc_check_err<<<1, 1, 0, s>>>(b.err, info);
+    GPK_LAUNCH_CHECK();
+    pred_tc_finish_kernel<<<(unsigned)cdiv((int64_t)t * 32, 256), 256, 0, s>>>(
+        t, n, np, pred->Kh, pred->Kl, b.alpha, pred->vacc, theta, n_ls, pred->prior_jitter, info,
+        pred->mean, pred->var);
+    GPK_LAUNCH_CHECK();
+    pred_tc_info_kernel<<<1, 1, 0, s>>>(info);
+    GPK_LAUNCH_CHECK();
+    return GPK_OK;
+  }
   // the adjoint: W = V V^T tiles contracted with (alpha alpha^T - W) x dK/dtheta
   // in the GEMM epilogue
   tc::TcParams pg{};
@@ -1107,6 +1209,35 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
                                    out_mll, out_grad, s, b.fin));
   prof_mark(6, s);
   return GPK_OK;
+}
+
+size_t predict_tc_workspace_bytes(int64_t n, int64_t t, int d) {
+  TcBuffers b;
+  const size_t base = tc_layout(n, d, nullptr, b);
+  return ((base + 1023) & ~size_t(1023)) + predict_tc_extra_bytes(b.npad, t, d);
+}
+
+gpk_status predict_run_tc(int kind, int n, int t, int d, const double* x, int64_t ldx,
+                          const double* y, const double* xt, int64_t ldxt, const double* theta,
+                          int n_ls, double jitter, double prior_jitter, double* mean, double* var,
+                          int* info, void* ws, cudaStream_t s) {
+  TcBuffers b;
+  const size_t base = (tc_layout(n, d, nullptr, b) + 1023) & ~size_t(1023);
+  const int64_t tp = ((int64_t)t + LEAF - 1) / LEAF * LEAF;
+  char* p = static_cast<char*>(ws) + base;
+  TcPredict pr{};
+  pr.t = t;
+  pr.xt = xt;
+  pr.ldxt = ldxt;
+  pr.prior_jitter = prior_jitter;
+  pr.mean = mean;
+  pr.var = var;
+  pr.Kh = reinterpret_cast<float*>(p);
+  pr.Kl = pr.Kh + tp * b.npad;
+  pr.vacc = reinterpret_cast<double*>(pr.Kl + tp * b.npad);
+  pr.ts = reinterpret_cast<float*>(pr.vacc + tp);
+  return mll_run_tc(kind, n, d, x, ldx, y, theta, n_ls, jitter, 2, 0, nullptr, nullptr, info, ws,
+                    s, &pr);
 }
 
 }  // namespace gpk

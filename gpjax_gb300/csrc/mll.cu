@@ -34,9 +34,11 @@ void prof_mark(int k, cudaStream_t s) {
 // mixed_tc.cu
 size_t mll_tc_workspace_bytes(int64_t n, int d);
 bool mll_tc_supported(int d);
+struct TcPredict;
 gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, const double* y,
                       const double* theta, int n_ls, double jitter, int refine, int want_grad,
-                      double* out_mll, double* out_grad, int* info, void* ws, cudaStream_t s);
+                      double* out_mll, double* out_grad, int* info, void* ws, cudaStream_t s,
+                      const TcPredict* pred = nullptr);
 
 // Carves caller-provided workspace into 256-byte aligned regions.
 struct Arena {

@@ -6,10 +6,19 @@
 // mean is formed as Ktx alpha with the same refined alpha as the marginal
 // likelihood, the variance as k(t, t) - |Q^T row|^2 + prior_jitter, and the
 // full covariance only when requested (the reference always forms it).
+#include <algorithm>
 #include <climits>
 #include "gpk_internal.cuh"
 
 namespace gpk {
+
+// mixed_tc.cu: mean and variance on the tensor-core factorisation
+bool mll_tc_supported(int d);
+size_t predict_tc_workspace_bytes(int64_t n, int64_t t, int d);
+gpk_status predict_run_tc(int kind, int n, int t, int d, const double* x, int64_t ldx,
+                          const double* y, const double* xt, int64_t ldxt, const double* theta,
+                          int n_ls, double jitter, double prior_jitter, double* mean, double* var,
+                          int* info, void* ws, cudaStream_t s);
 
 namespace {
 
@@ -209,7 +218,9 @@ extern "C" size_t gpk_predict_workspace_bytes(int64_t n, int64_t t, int d, int p
     return pred_layout<double>(n, t, d, true, nullptr, b);
   }
   PredBuffers<float> b;
-  return pred_layout<float>(n, t, d, true, nullptr, b);
+  const size_t simt = pred_layout<float>(n, t, d, true, nullptr, b);
+  // mean and variance only: the tensor-core factorisation and Q^T product
+  return mll_tc_supported(d) ? std::max(simt, predict_tc_workspace_bytes(n, t, d)) : simt;
 }
 
 extern "C" gpk_status gpk_predict(int kind, int64_t n, int64_t t, int d, const double* x,
@@ -230,6 +241,9 @@ extern "C" gpk_status gpk_predict(int kind, int64_t n, int64_t t, int d, const d
   if (precision == GPK_PREC_FP64)
     return predict_run<double>(kind, (int)n, (int)t, d, x, ldx, y, xt, ldxt, theta, n_ls, jitter,
                                prior_jitter, 1, mean, var, cov, ldcov, info, workspace, stream);
+  if (!cov && mll_tc_supported(d))
+    return predict_run_tc(kind, (int)n, (int)t, d, x, ldx, y, xt, ldxt, theta, n_ls, jitter,
+                          prior_jitter, mean, var, info, workspace, stream);
   return predict_run<float>(kind, (int)n, (int)t, d, x, ldx, y, xt, ldxt, theta, n_ls, jitter,
                             prior_jitter, 2, mean, var, cov, ldcov, info, workspace, stream);
 }

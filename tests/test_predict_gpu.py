@@ -35,3 +35,26 @@ def test_predict_mixed(cuda_lib):
     mean, cov = O.predict(2, x, y, xt, ls, 1.0, 0.1, 0.0)
     assert np.allclose(dist.mean.cpu().numpy(), mean, rtol=1e-4, atol=1e-4 * np.abs(mean).max())
     assert np.allclose(dist.variance.cpu().numpy(), np.diag(cov), atol=1e-4)
+
+
+@pytest.mark.parametrize("kind,n,t,d", [(2, 1500, 300, 8), (0, 4500, 257, 4), (1, 700, 1, 3)])
+def test_predict_mean_variance_tensor_core_path(cuda_lib, kind, n, t, d):
+    """Mean and variance without the covariance run on the mixed form's
+    tensor-core factorisation (Q^T = Ktx M^T as one split-TF32 GEMM whose
+    epilogue keeps only the row sums of squares); n = 4500 includes the
+    split-float16 wide nodes."""
+    rng = np.random.default_rng(n + t + kind)
+    x = rng.uniform(-2, 2, size=(n, d))
+    y = np.sin(2 * x).sum(1, keepdims=True) + 0.1 * rng.standard_normal((n, 1))
+    xt = rng.uniform(-2.2, 2.2, size=(t, d))
+    ls = np.exp(rng.uniform(np.log(0.5), np.log(1.5), d))
+    post = make_posterior(kind, ls, 1.3, 0.1, 0.2)
+    dist = post.predict(torch.as_tensor(xt, device="cuda"), gpx.Dataset(X=x, y=y),
+                        precision="mixed", full_covariance=False)
+    mean, cov = O.predict(kind, x, y, xt, ls, 1.3, 0.1, 0.2)
+    m = dist.mean.cpu().numpy()
+    v = dist.variance.cpu().numpy()
+    merr = np.max(np.abs(m - mean)) / np.max(np.abs(mean))
+    verr = np.max(np.abs(v - np.diag(cov)))
+    print("mean rel", merr, "var abs", verr)
+    assert merr <= 2e-6 and verr <= 2e-6, (merr, verr)
