@@ -64,32 +64,39 @@ struct BatchInst {
   double* out_grad;
   int* info;
   int64_t ldx;
-  int n, d, kind, n_ls, cfg, pad_;
+  int64_t slot_off;   // byte offset of the instance's slot in the workspace
+  int64_t tpart_off;  // first of its ntiles * (d + 2) per-tile gradient partials
+  int n, d, kind, n_ls, cfg, ntiles;
 };
 
+// Per-execution counters (zeroed before each launch): the queue head, then
+// per instance "published" (its M and alpha are final), the next unclaimed
+// adjoint tile and the number of finished tiles.
 struct BatchArgs {
   const BatchInst* inst;
   const int* queue;  // instance indices, largest n first
-  int* head;         // next queue position, zeroed before each launch
+  int* head;         // next queue position
+  int* published;    // [count]
+  int* next_tile;    // [count]
+  int* tiles_done;   // [count]
+  double* tpart;     // per-tile gradient partials
   int count;
-  char* ws;          // one slot per CTA
-  size_t slot_bytes;
-  int np_max;        // the slot layout's matrix size
+  char* ws;          // one slot per instance
   int want_grad;
   double jitter;
   int force_cfg;     // >= 0: every instance with this configuration (autotuner trials)
+  long long wait_cycles;  // bound on an idle CTA's wait for published tiles
 };
 
 struct Slot {
   float *A, *L, *M, *xs;
   double *dtrack, *logdiag, *diff, *alpha;
-  float *rf, *zf;
+  float *rf, *zf, *ahf;  // ahf: alpha in float32 (the adjoint tiles' operand)
 };
 
 __host__ __device__ inline size_t al256(size_t b) { return (b + 255) & ~size_t(255); }
 
-// Slot of a CTA for instances up to np (matrices with leading dimension of
-// the instance's own n_pad, so smaller instances use the front of each array).
+// Slot of one instance of padded size np (matrices with leading dimension np).
 __host__ __device__ inline size_t slot_layout(int np, char* base, Slot* s) {
   const size_t mat = al256((size_t)np * np * sizeof(float));
   const size_t vd = al256((size_t)np * sizeof(double)), vf = al256((size_t)np * sizeof(float));
@@ -106,8 +113,9 @@ __host__ __device__ inline size_t slot_layout(int np, char* base, Slot* s) {
     s->alpha = reinterpret_cast<double*>(p += vd);
     s->rf = reinterpret_cast<float*>(p += vd);
     s->zf = reinterpret_cast<float*>(p += vf);
+    s->ahf = reinterpret_cast<float*>(p += vf);
   }
-  return 3 * mat + xsb + 4 * vd + 2 * vf;
+  return 3 * mat + xsb + 4 * vd + 3 * vf;
 }
 
 // ---------------------------------------------------------------------------
@@ -592,61 +600,106 @@ __device__ __forceinline__ void adj_tile(int i0, int j0, int n, int d, float ka,
 // and in float64, into the warp's own slots of wred (fixed order: the result
 // is reproducible).  sg[d + 2] (shared memory) receives the lengthscale sums,
 // the variance sum and the noise sum.
+// One adjoint tile t (lower tiles of W = M^T M, M[k][i] = 0 for k < i) of an
+// instance whose M and alpha are final, on any CTA: the W tile contracted
+// with (alpha alpha^T - W) o dK/dtheta in the epilogue, its d + 2 partial
+// sums written to tpart[t] (per-warp float64 sums added in a fixed order, so
+// the result does not depend on which CTA ran the tile).  Returns true on
+// the CTA that finished the instance's last tile.
 template <int BK>
-__device__ void adjoint(const BatchInst& I, const Slot& S, int ld, int np, float ka,
-                        const float* ah, double* sg, double* wred, float* smem) {
-  const int d = I.d, n = I.n;
+__device__ bool adjoint_tile(const BatchArgs& a, int id, const BatchInst& I, const Slot& S,
+                             int t, float* smem, double* wred) {
+  const int d = I.d, n = I.n, np = ((n + TT - 1) / TT) * TT, ld = np;
   constexpr int NW = BNT / 32;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const float ka = kshape<float>(I.kind, I.theta, I.n_ls);
+  int bi, bj;
+  tri_index(t, bi, bj);
+  const int i0 = bi * TT, j0 = bj * TT;
   for (int e = threadIdx.x; e < (d + 2) * NW; e += BNT) wred[e] = 0.0;
-  __syncthreads();
-  product<BK, true, true>(
-      np / TT, np / TT, true, S.M, ld, S.M, ld,
-      [&](int i0, int, int& klo, int& khi) { klo = i0; khi = np; },
-      [&](int i0, int j0, const float (&acc)[8][4], float* Sh) {
-        float* Ws = Sh;                          // [TT][WLD]
-        float* sxi = Sh + stage_floats();        // [TT][XLD]
-        float* sxj = sxi + TT * XLD;
-        float* sai = sxj + TT * XLD;             // alpha of the tile's rows
-        float* saj = sai + TT;                   // and columns
+  float acc[8][4];
 #pragma unroll
-        for (int u = 0; u < 8; ++u)
-          *reinterpret_cast<float4*>(Ws + tile_row(u) * WLD + tile_col(0)) =
-              make_float4(acc[u][0], acc[u][1], acc[u][2], acc[u][3]);
-        for (int e = threadIdx.x; e < TT * BDM; e += BNT) {
-          const int r = e / BDM, k = e % BDM;
-          sxi[r * XLD + k] = (i0 + r < n && k < d) ? S.xs[(i0 + r) * d + k] : 0.f;
-          sxj[r * XLD + k] = (j0 + r < n && k < d) ? S.xs[(j0 + r) * d + k] : 0.f;
-        }
-        for (int e = threadIdx.x; e < TT; e += BNT) {
-          sai[e] = ah[i0 + e];
-          saj[e] = ah[j0 + e];
-        }
-        __syncthreads();
-        with_kind(I.kind, [&](auto kind_c) {
-          constexpr int KIND = decltype(kind_c)::value;
-          const int dp = (d + 1) / 2;
-          if (dp <= 2)
-            adj_tile<KIND, 2>(i0, j0, n, d, ka, Ws, sxi, sxj, sai, saj, wred, warp, lane);
-          else if (dp <= 4)
-            adj_tile<KIND, 4>(i0, j0, n, d, ka, Ws, sxi, sxj, sai, saj, wred, warp, lane);
-          else
-            adj_tile<KIND, 8>(i0, j0, n, d, ka, Ws, sxi, sxj, sai, saj, wred, warp, lane);
-        });
-        __syncthreads();  // the staging area is the next tile's K buffer
-      },
-      smem);
-  for (int s = threadIdx.x; s < d + 2; s += BNT) {
-    double t = 0.0;
-    for (int w = 0; w < NW; ++w) t += wred[s * NW + w];
-    sg[s] = t;
+  for (int u = 0; u < 8; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
+  tile_mma<BK, true, true>(S.M, ld, S.M, ld, i0, j0, i0, np, smem, acc);
+  float* Ws = smem;                          // [TT][WLD]
+  float* sxi = smem + stage_floats();        // [TT][XLD]
+  float* sxj = sxi + TT * XLD;
+  float* sai = sxj + TT * XLD;               // alpha of the tile's rows
+  float* saj = sai + TT;                     // and columns
+#pragma unroll
+  for (int u = 0; u < 8; ++u)
+    *reinterpret_cast<float4*>(Ws + tile_row(u) * WLD + tile_col(0)) =
+        make_float4(acc[u][0], acc[u][1], acc[u][2], acc[u][3]);
+  for (int e = threadIdx.x; e < TT * BDM; e += BNT) {
+    const int r = e / BDM, k = e % BDM;
+    sxi[r * XLD + k] = (i0 + r < n && k < d) ? S.xs[(i0 + r) * d + k] : 0.f;
+    sxj[r * XLD + k] = (j0 + r < n && k < d) ? S.xs[(j0 + r) * d + k] : 0.f;
   }
+  for (int e = threadIdx.x; e < TT; e += BNT) {
+    sai[e] = S.ahf[i0 + e];
+    saj[e] = S.ahf[j0 + e];
+  }
+  __syncthreads();
+  with_kind(I.kind, [&](auto kind_c) {
+    constexpr int KIND = decltype(kind_c)::value;
+    const int dp = (d + 1) / 2;
+    if (dp <= 2)
+      adj_tile<KIND, 2>(i0, j0, n, d, ka, Ws, sxi, sxj, sai, saj, wred, warp, lane);
+    else if (dp <= 4)
+      adj_tile<KIND, 4>(i0, j0, n, d, ka, Ws, sxi, sxj, sai, saj, wred, warp, lane);
+    else
+      adj_tile<KIND, 8>(i0, j0, n, d, ka, Ws, sxi, sxj, sai, saj, wred, warp, lane);
+  });
+  __syncthreads();
+  double* tp = a.tpart + I.tpart_off + (int64_t)t * (d + 2);
+  for (int s = threadIdx.x; s < d + 2; s += BNT) {
+    double v = 0.0;
+    for (int w = 0; w < NW; ++w) v += wred[s * NW + w];
+    tp[s] = v;
+  }
+  __shared__ int s_last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();  // the partials before the count
+    s_last = atomicAdd(&a.tiles_done[id], 1) == I.ntiles - 1;
+  }
+  __syncthreads();
+  return s_last;
+}
+
+// The outputs of an instance from its slot (any CTA): log-determinant,
+// quadratic form and alpha sum in compensated float64, the gradient slots
+// summed over the tiles' partials in tile order.
+__device__ void finish_instance(const BatchArgs& a, const BatchInst& I, const Slot& S,
+                                bool failed, double* sg) {
+  const int n = I.n, d = I.d;
+  const bool grad = a.want_grad && !failed;
+  __threadfence();  // every tile's partials (written on other SMs) before reading them
+  for (int s = threadIdx.x; s < d + 2; s += BNT) {
+    double v = 0.0;
+    if (grad)
+      for (int t = 0; t < I.ntiles; ++t) v += a.tpart[I.tpart_off + (int64_t)t * (d + 2) + s];
+    sg[s] = v;
+  }
+  __syncthreads();
+  const double logdet =
+      2.0 * block_ksum(n, [&](int i) { return failed ? 0.0 : S.logdiag[i]; });
+  const double quad = block_ksum(n, [&](int i) { return failed ? 0.0 : S.diff[i] * S.alpha[i]; });
+  const double asum = block_ksum(n, [&](int i) { return failed ? 0.0 : S.alpha[i]; });
+  if (threadIdx.x == 0)
+    finalize_outputs(n, d, I.theta, I.n_ls, a.jitter, logdet, quad, asum, sg, a.want_grad,
+                     I.info, I.out_mll, a.want_grad ? I.out_grad : nullptr);
   __syncthreads();
 }
 
+// Everything of an instance before its adjoint, on the CTA that took it from
+// the queue: Gram, factor and inverse, alpha refined twice.  Returns true if
+// the factorisation failed.
 template <int BK>
-__device__ void run_instance(const BatchArgs& a, const BatchInst& I, const Slot& S,
-                             float* smem, double* sred) {
+__device__ bool instance_front(const BatchArgs& a, const BatchInst& I, const Slot& S,
+                               float* smem) {
   const int n = I.n, d = I.d;
   const int np = ((n + TT - 1) / TT) * TT;
   const int ld = np;
@@ -700,72 +753,145 @@ __device__ void run_instance(const BatchArgs& a, const BatchInst& I, const Slot&
   __syncthreads();
   const bool failed = *(volatile int*)I.info != INT_MAX;
   __syncthreads();
-  double* sg = sred;                       // [GPK_MAX_D + 2]
-  double* red = sred + GPK_MAX_D + 2;      // [(GPK_MAX_D + 2) * 16]
-  if (!failed) {
-    // alpha = Sigma^-1 diff, refined twice
-    solve_apply(S, ld, np, S.diff, false);
-    float* ah = smem;          // [np] alpha hi
-    float* al = smem + np;     // [np] alpha lo
-    double* rres = reinterpret_cast<double*>(smem + 2 * np);  // [np]
-    for (int it = 0; it < 2; ++it) {
-      for (int i = threadIdx.x; i < np; i += BNT) {
-        const double v = S.alpha[i];
-        const float hi = (float)v;
-        ah[i] = hi;
-        al[i] = (float)(v - (double)hi);
-      }
-      __syncthreads();
-      residual(I, S, np, s2, ka, noise_diag, ah, al, rres);
-      __syncthreads();
-      solve_apply(S, ld, np, rres, true);
+  if (failed) return true;
+  // alpha = Sigma^-1 diff, refined twice
+  solve_apply(S, ld, np, S.diff, false);
+  float* ah = smem;          // [np] alpha hi
+  float* al = smem + np;     // [np] alpha lo
+  double* rres = reinterpret_cast<double*>(smem + 2 * np);  // [np]
+  for (int it = 0; it < 2; ++it) {
+    for (int i = threadIdx.x; i < np; i += BNT) {
+      const double v = S.alpha[i];
+      const float hi = (float)v;
+      ah[i] = hi;
+      al[i] = (float)(v - (double)hi);
     }
-    if (a.want_grad) {
-      // alpha hi parts for the adjoint, kept past the K buffers of both halves
-      float* ahg = smem + prod_floats();
-      for (int i = threadIdx.x; i < np; i += BNT) ahg[i] = (float)S.alpha[i];
-      __syncthreads();
-      adjoint<BK>(I, S, ld, np, ka, ahg, sg, red, smem);
-    }
+    __syncthreads();
+    residual(I, S, np, s2, ka, noise_diag, ah, al, rres);
+    __syncthreads();
+    solve_apply(S, ld, np, rres, true);
   }
-  // sums and the outputs
-  const double logdet =
-      2.0 * block_ksum(n, [&](int i) { return failed ? 0.0 : S.logdiag[i]; });
-  const double quad = block_ksum(n, [&](int i) { return failed ? 0.0 : S.diff[i] * S.alpha[i]; });
-  const double asum = block_ksum(n, [&](int i) { return failed ? 0.0 : S.alpha[i]; });
-  if (threadIdx.x == 0) {
-    if (failed || !a.want_grad)
-      for (int s = 0; s < d + 2; ++s) sg[s] = 0.0;
-    finalize_outputs(n, d, th, I.n_ls, a.jitter, logdet, quad, asum, sg, a.want_grad, I.info,
-                     I.out_mll, a.want_grad ? I.out_grad : nullptr);
-  }
+  for (int i = threadIdx.x; i < np; i += BNT) S.ahf[i] = (float)S.alpha[i];
   __syncthreads();
+  return false;
 }
 
+// One CTA per SM.  A CTA first works through the adjoint tiles of the last
+// instance it prepared; then takes the next instance from the size-sorted
+// queue (Gram, factor, inverse, alpha) and publishes it; when the queue is
+// empty it takes unclaimed adjoint tiles of any published instance, waiting
+// (at most wait_cycles in total) while some instance is still being prepared.
+// Whoever finishes an instance's last tile writes its outputs.  An idle CTA
+// that stops waiting changes nothing but speed: the owner of an instance
+// claims all of its tiles that nobody else has.
 __global__ void __launch_bounds__(BNT, 1) batch_mll_kernel(const __grid_constant__ BatchArgs a) {
   extern __shared__ __align__(16) float smem[];
-  __shared__ int s_job;
   __shared__ double s_red[(GPK_MAX_D + 2) * 17];
   // the slot's pointers and the instance's descriptor live in shared memory
   // (read where used) rather than in ~40 registers for the whole instance
   __shared__ Slot s_slot;
   __shared__ BatchInst s_inst;
-  if (threadIdx.x == 0) slot_layout(a.np_max, a.ws + (size_t)blockIdx.x * a.slot_bytes, &s_slot);
+  __shared__ int s_mode, s_id, s_tile, s_own;
+  __shared__ long long s_wait0;
+  if (threadIdx.x == 0) {
+    s_own = -1;
+    s_wait0 = -1;
+  }
   for (;;) {
     if (threadIdx.x == 0) {
-      const int q = atomicAdd(a.head, 1);
-      s_job = q;
-      if (q < a.count) s_inst = a.inst[a.queue[q]];
+      int mode = 0, id = -1, tile = -1;
+      // 1) the tiles of the instance this CTA prepared
+      if (s_own >= 0) {
+        const int t = atomicAdd(&a.next_tile[s_own], 1);
+        if (t < a.inst[s_own].ntiles) {
+          mode = 2;
+          id = s_own;
+          tile = t;
+        } else {
+          s_own = -1;
+        }
+      }
+      // 2) the next instance of the queue
+      if (mode == 0) {
+        const int q = atomicAdd(a.head, 1);
+        if (q < a.count) {
+          mode = 1;
+          id = a.queue[q];
+        }
+      }
+      // 3) unclaimed tiles of published instances
+      if (mode == 0) {
+        bool all_published = true;
+        for (int i = 0; i < a.count && mode == 0; ++i) {
+          if (!*(volatile int*)&a.published[i]) {
+            all_published = false;
+            continue;
+          }
+          if (*(volatile int*)&a.next_tile[i] >= a.inst[i].ntiles) continue;
+          const int t = atomicAdd(&a.next_tile[i], 1);
+          if (t < a.inst[i].ntiles) {
+            mode = 2;
+            id = i;
+            tile = t;
+          }
+        }
+        if (mode == 0) {
+          if (all_published) {
+            mode = 3;  // nothing left anywhere
+          } else {
+            const long long now = clock64();
+            if (s_wait0 < 0) s_wait0 = now;
+            mode = now - s_wait0 > a.wait_cycles ? 3 : 4;
+          }
+        }
+      }
+      if (mode == 2) __threadfence();  // the instance's slot after its "published" flag
+      if (id >= 0) {
+        s_inst = a.inst[id];
+        const int np = ((s_inst.n + TT - 1) / TT) * TT;
+        slot_layout(np, a.ws + s_inst.slot_off, &s_slot);
+      }
+      s_mode = mode;
+      s_id = id;
+      s_tile = tile;
     }
     __syncthreads();
-    const int q = s_job;
-    if (q >= a.count) break;
+    const int mode = s_mode;
+    if (mode == 3) break;
+    if (mode == 4) {
+      if (threadIdx.x == 0) __nanosleep(2000);
+      __syncthreads();
+      continue;
+    }
+    const int id = s_id;
     const int cfg = a.force_cfg >= 0 ? a.force_cfg : s_inst.cfg;
-    if (cfg == 0)
-      run_instance<16>(a, s_inst, s_slot, smem, s_red);
-    else
-      run_instance<32>(a, s_inst, s_slot, smem, s_red);
-    __syncthreads();  // everyone is done with s_job / s_inst before thread 0 rewrites them
+    if (mode == 1) {
+      const bool failed = cfg == 0 ? instance_front<16>(a, s_inst, s_slot, smem)
+                                   : instance_front<32>(a, s_inst, s_slot, smem);
+      const bool tiles = !failed && a.want_grad && s_inst.ntiles > 0;
+      if (!tiles) finish_instance(a, s_inst, s_slot, failed, s_red);
+      if (threadIdx.x == 0) {
+        if (!tiles) atomicExch(&a.next_tile[id], 1 << 30);  // no tiles to claim
+        __threadfence();  // the slot's M and alpha before the flag
+        atomicExch(&a.published[id], 1);
+        s_own = tiles ? id : -1;
+      }
+    } else {
+      const bool last = cfg == 0 ? adjoint_tile<16>(a, id, s_inst, s_slot, s_tile, smem, s_red)
+                                 : adjoint_tile<32>(a, id, s_inst, s_slot, s_tile, smem, s_red);
+      if (last) finish_instance(a, s_inst, s_slot, false, s_red + GPK_MAX_D + 2 + 16 * 18);
+    }
+    __syncthreads();  // everyone is done with the shared descriptors before thread 0 rewrites them
+  }
+}
+
+// The queued instances of a partial launch (autotuner trial): not yet
+// published, tiles claimed from 0.
+__global__ void batch_reset_kernel(const int* queue, int count, int* published, int* next_tile) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < count) {
+    published[queue[q]] = 0;
+    next_tile[queue[q]] = 0;
   }
 }
 
@@ -793,12 +919,12 @@ struct gpk_batch_plan_s {
   int want_grad = 1;
   double jitter = 0.0;
   int grid = 0;
-  size_t slot_bytes = 0;
+  size_t ws_bytes = 0;          // one slot per instance
   size_t smem = 0;
   BatchInst* d_inst = nullptr;  // device copies of the descriptors
   int* d_queue = nullptr;       // size-sorted instance indices
-  int* d_head = nullptr;
-  std::vector<int> cfg_of_bucket;  // chosen configuration per n_pad / 128 bucket
+  int* d_state = nullptr;       // head, published[count], next_tile[count], tiles_done[count]
+  double* d_tpart = nullptr;    // per-tile gradient partials
 };
 
 namespace {
@@ -806,21 +932,39 @@ namespace {
 std::mutex g_tune_mu;
 std::map<std::pair<int, int>, int> g_tune;
 
+// Wait bound of an idle CTA for instances still being prepared (~2 s of SM
+// clock; an execution takes tens of milliseconds).
+constexpr long long kIdleWaitCycles = 4000000000LL;
+
 cudaError_t launch_batch(const gpk_batch_plan_s& P, void* ws, int force_cfg, int count,
                          const int* queue, cudaStream_t s) {
   BatchArgs a{};
   a.inst = P.d_inst;
   a.queue = queue;
-  a.head = P.d_head;
+  a.head = P.d_state;
+  a.published = P.d_state + 1;
+  a.next_tile = a.published + P.count;
+  a.tiles_done = a.next_tile + P.count;
+  a.tpart = P.d_tpart;
   a.count = count;
   a.ws = static_cast<char*>(ws);
-  a.slot_bytes = P.slot_bytes;
-  a.np_max = P.np_max;
   a.want_grad = P.want_grad;
   a.jitter = P.jitter;
   a.force_cfg = force_cfg;
-  cudaError_t e = cudaMemsetAsync(P.d_head, 0, sizeof(int), s);
+  a.wait_cycles = kIdleWaitCycles;
+  // instances outside the queue (autotuner trials) count as published with
+  // no tiles: 1 in published[], a huge next_tile
+  cudaError_t e = cudaMemsetAsync(P.d_state, 0, sizeof(int) * (1 + 3 * (size_t)P.count), s);
+  if (e == cudaSuccess && count < P.count) {
+    e = cudaMemsetAsync(a.published, 0x01, sizeof(int) * P.count, s);  // any non-zero word
+    if (e == cudaSuccess) e = cudaMemsetAsync(a.next_tile, 0x7f, sizeof(int) * P.count, s);
+  }
   if (e != cudaSuccess) return e;
+  if (count < P.count) {  // the trial's instances: not published, tiles from 0
+    batch_reset_kernel<<<(count + 255) / 256, 256, 0, s>>>(queue, count, a.published, a.next_tile);
+    e = launch_status();
+    if (e != cudaSuccess) return e;
+  }
   const int grid = std::min(P.grid, std::max(count, 1));
   batch_mll_kernel<<<grid, BNT, P.smem, s>>>(a);
   return launch_status();
@@ -839,7 +983,7 @@ gpk_status autotune(gpk_batch_plan_s& P, const std::vector<int>& np_of, const st
       if (!g_tune.count({P.device, kv.first})) todo.push_back(kv.first);
   }
   if (todo.empty()) return GPK_OK;
-  const size_t ws_bytes = P.slot_bytes * (size_t)P.grid;
+  const size_t ws_bytes = P.ws_bytes;
   void* ws = nullptr;
   int* dq = nullptr;
   cudaStream_t s = nullptr;
@@ -910,8 +1054,30 @@ extern "C" gpk_status gpk_batch_plan_create(int count, const int* kind, const in
     if (n[i] > NP_MAX || d[i] > BDM) return GPK_ERR_UNSUPPORTED;
     np_of[i] = (int)((n[i] + TT - 1) / TT) * TT;
     np_max = std::max(np_max, np_of[i]);
-    hv[i] = BatchInst{x[i], y[i], theta[i], out_mll[i], want_grad ? out_grad[i] : nullptr,
-                      info + i, ldx[i], (int)n[i], d[i], kind[i], n_ls[i], 0, 0};
+    hv[i] = BatchInst{};
+    hv[i].x = x[i];
+    hv[i].y = y[i];
+    hv[i].theta = theta[i];
+    hv[i].out_mll = out_mll[i];
+    hv[i].out_grad = want_grad ? out_grad[i] : nullptr;
+    hv[i].info = info + i;
+    hv[i].ldx = ldx[i];
+    hv[i].n = (int)n[i];
+    hv[i].d = d[i];
+    hv[i].kind = kind[i];
+    hv[i].n_ls = n_ls[i];
+  }
+  // one workspace slot per instance; the adjoint's lower 128-tiles and their
+  // partial sums
+  size_t ws_bytes = 0;
+  int64_t tpart = 0;
+  for (int i = 0; i < count; ++i) {
+    const int nb = np_of[i] / TT;
+    hv[i].slot_off = (int64_t)ws_bytes;
+    ws_bytes += al256(slot_layout(np_of[i], nullptr, nullptr));
+    hv[i].ntiles = want_grad ? nb * (nb + 1) / 2 : 0;
+    hv[i].tpart_off = tpart;
+    tpart += (int64_t)hv[i].ntiles * (d[i] + 2);
   }
   std::vector<int> order(count);
   for (int i = 0; i < count; ++i) order[i] = i;
@@ -930,7 +1096,7 @@ extern "C" gpk_status gpk_batch_plan_create(int count, const int* kind, const in
   P->want_grad = want_grad ? 1 : 0;
   P->jitter = jitter;
   P->smem = batch_smem_bytes(np_max);
-  P->slot_bytes = al256(slot_layout(np_max, nullptr, nullptr));
+  P->ws_bytes = ws_bytes;
   if (cudaFuncSetAttribute(batch_mll_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)P->smem) != cudaSuccess)
     return fail(GPK_ERR_CUDA);
@@ -942,7 +1108,8 @@ extern "C" gpk_status gpk_batch_plan_create(int count, const int* kind, const in
   P->grid = sms * per_sm;
   if (cudaMalloc(&P->d_inst, sizeof(BatchInst) * count) != cudaSuccess ||
       cudaMalloc(&P->d_queue, sizeof(int) * count) != cudaSuccess ||
-      cudaMalloc(&P->d_head, sizeof(int)) != cudaSuccess)
+      cudaMalloc(&P->d_state, sizeof(int) * (1 + 3 * (size_t)count)) != cudaSuccess ||
+      cudaMalloc(&P->d_tpart, sizeof(double) * (size_t)std::max<int64_t>(tpart, 1)) != cudaSuccess)
     return fail(GPK_ERR_CUDA);
   if (cudaMemcpy(P->d_inst, hv.data(), sizeof(BatchInst) * count, cudaMemcpyHostToDevice) !=
           cudaSuccess ||
@@ -974,7 +1141,7 @@ extern "C" gpk_status gpk_batch_plan_create(int count, const int* kind, const in
 }
 
 extern "C" size_t gpk_batch_plan_workspace_bytes(gpk_batch_plan plan) {
-  return plan ? plan->slot_bytes * (size_t)plan->grid : 0;
+  return plan ? plan->ws_bytes : 0;
 }
 
 extern "C" int gpk_batch_plan_config(gpk_batch_plan plan, int64_t n) {
@@ -997,7 +1164,8 @@ extern "C" gpk_status gpk_batch_plan_destroy(gpk_batch_plan plan) {
   if (!plan) return GPK_OK;
   if (plan->d_inst) cudaFree(plan->d_inst);
   if (plan->d_queue) cudaFree(plan->d_queue);
-  if (plan->d_head) cudaFree(plan->d_head);
+  if (plan->d_state) cudaFree(plan->d_state);
+  if (plan->d_tpart) cudaFree(plan->d_tpart);
   delete plan;
   return GPK_OK;
 }
