@@ -140,3 +140,39 @@ def test_autotuner_picks_a_configuration_per_size(cuda_lib):
     assert plan.config(256) in (0, 1) and plan.config(1024) in (0, 1)
     assert plan.config(5000) == -1
     plan.close()
+
+
+def test_plan_rational_quadratic_and_value_only(cuda_lib):
+    """The rational quadratic (alpha in theta[n_ls + 3]) and a plan without
+    gradients (no adjoint tiles: every instance finishes on its owner)."""
+    dev = torch.device("cuda")
+    rng = np.random.default_rng(7)
+    insts, kinds = [], []
+    for k, (n, d) in enumerate([(300, 3), (900, 5), (129, 2)]):
+        x = rng.uniform(-1.0, 1.0, (n, d))
+        ls = np.exp(rng.uniform(np.log(0.3), np.log(2.0), d))
+        alpha = float(np.exp(rng.uniform(np.log(0.5), np.log(3.0))))
+        y = np.sin(3 * x).sum(axis=1) + 0.1 * rng.standard_normal(n)
+        insts.append((x, y, ls, 1.2, 0.1, 0.05, alpha))
+        kinds.append(_lib.RATIONAL_QUADRATIC)
+    xs = [torch.as_tensor(i[0], device=dev) for i in insts]
+    ys = [torch.as_tensor(i[1], device=dev) for i in insts]
+    ths = [torch.as_tensor(np.concatenate([i[2], [i[3], i[4], i[5], i[6]]]), device=dev)
+           for i in insts]
+    for want in (True, False):
+        plan = BatchPlan(kinds, xs, ys, ths, [len(i[2]) for i in insts], want_grad=want,
+                         autotune=False)
+        mll, grads, info = plan.execute()
+        torch.cuda.synchronize()
+        assert np.all(info.cpu().numpy() == 0)
+        for k, (x, y, ls, var, sd, c, alpha) in enumerate(insts):
+            kern = O.rational_quadratic(alpha)
+            ref = O.conjugate_mll(kern, x, y[:, None], ls, var, sd, c)
+            assert abs(float(mll[k]) - ref) <= MLL_RTOL * abs(ref), (k, float(mll[k]), ref)
+            if want:
+                _, g = O.conjugate_mll_torch(kern, x, y[:, None], ls, var, sd, c, lu=False)
+                gref = np.concatenate([np.atleast_1d(g["lengthscale"]),
+                                       [g["variance"], g["obs_stddev"], g["constant"]]])
+                gk = grads[k].cpu().numpy()[:len(gref)]
+                assert np.linalg.norm(gk - gref) <= GRAD_RTOL * np.linalg.norm(gref)
+        plan.close()
