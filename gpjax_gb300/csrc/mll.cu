@@ -676,9 +676,8 @@ extern "C" gpk_status gpk_logdet_triangular(int64_t n, int dtype, const void* L,
 // ---------------------------------------------------------------------------
 // Allocation-free float64 marginal log-likelihood for small problems.
 //
-// Callers that cannot allocate device memory (code running inside CUDA stream
-// capture, where cudaMalloc would break the capture; host frameworks that
-// hand a custom call no workspace; embedded or real-time hosts that forbid
+// Callers that cannot allocate device memory (host frameworks that hand a
+// custom call no workspace; embedded or real-time hosts that forbid
 // allocation after start-up) use this entry point instead of
 // gpk_conjugate_mll: its scratch is a file-scope device array, so the call
 // allocates nothing.  The array holds kNoallocBytes (8 MiB), enough for

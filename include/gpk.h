@@ -206,16 +206,15 @@ gpk_status gpk_conjugate_loocv(int kind, int64_t n, int d, const double* x, int6
 
 /* Allocation-free variant of gpk_conjugate_mll, float64 form only.
  * No counterpart in the reference.  For callers that cannot allocate device
- * memory -- code running inside CUDA stream capture (cudaMalloc would break
- * the capture), host frameworks that pass a custom call no workspace, hosts
- * that forbid allocation after start-up -- the scratch is a static device
- * array of 8 MiB inside the library, which bounds the problem to
+ * memory -- host frameworks that pass a custom call no workspace, hosts that
+ * forbid allocation after start-up -- the scratch is a static device array
+ * of 8 MiB inside the library, which bounds the problem to
  * n <= gpk_conjugate_mll_noalloc_max_n() (512); a larger n returns
  * GPK_ERR_UNSUPPORTED.  d is bounded as everywhere in the library (d <= 32,
  * GPK_ERR_BAD_ARG beyond).  Every GPU that loads the library holds the array
  * until the process exits.  The first call on a device looks up the array's
- * device address (cudaGetSymbolAddress) and keeps it for that device ordinal;
- * make that first call before any stream capture.  Only the runtime's primary
+ * device address (cudaGetSymbolAddress) and keeps it for that device
+ * ordinal.  Only the runtime's primary
  * context is supported: after cudaDeviceReset, or with another context
  * current, the kept address is stale.  All calls share the one array: calls
  * that overlap on the GPU (different streams, or different host threads on the

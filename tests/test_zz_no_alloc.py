@@ -1,8 +1,8 @@
 """GPU: the allocation-free marginal log-likelihood entry point.
 
 gpk_conjugate_mll_noalloc serves callers that cannot allocate device memory
-(work captured into a CUDA graph, custom calls that receive no workspace,
-hosts that forbid allocation after start-up): its scratch is a fixed 8 MiB
+(custom calls that receive no workspace, hosts that forbid allocation after
+start-up): its scratch is a fixed 8 MiB
 device array inside the library, so it takes no workspace and handles
 n <= 512.  This test calls it through the C ABI and compares it with
 gpk_conjugate_mll (which takes caller-allocated workspace) on the same inputs,
