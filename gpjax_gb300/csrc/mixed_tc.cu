@@ -494,8 +494,6 @@ struct TcChol {
   F16Set f16[kMaxDepth];
   int nf16;           // depths [0, nf16) have float16 buffers
   LookAhead* la;      // null: no look-ahead
-  cudaStream_t m21s;  // non-null: the top node's M21 product runs on this stream
-  cudaEvent_t m21fork, m21done;
 };
 
 // A node of size sz at depth `depth`: [L11, M11] = chol_inv(A11) (left, size h),
@@ -706,30 +704,19 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth, cudaEvent_t join =
   }
   e = chol_inv_rec(c, o + h, h2, depth + 1, la ? c.la->done[depth] : nullptr);
   if (e != cudaSuccess) return e;
-  // the top node's M21 on its own stream (see M21_DEFER_MIN)
-  const bool defer = depth == 0 && c.m21s != nullptr;
-  cudaStream_t ms = defer ? c.m21s : c.s;
-  bool mpdl = c.prev_kernel;
-  if (defer) {
-    e = cudaEventRecord(c.m21fork, c.s);
-    c.prev_kernel = false;
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(ms, c.m21fork, 0);
-    if (e != cudaSuccess) return e;
-    mpdl = false;
-  }
   if (f16) {  // M22 into the A21 copy's storage (free since L21)
-    e = to16(c.Mh, c.Ml, c.ld, o + h, o + h, h2, h2, TRI_LOWER, f->ah, f->al, f->ra, ms);
+    e = to16(c.Mh, c.Ml, c.ld, o + h, o + h, h2, h2, TRI_LOWER, f->ah, f->al, f->ra, c.s);
     if (e == cudaSuccess && (!tc_make_map_f16(&fa, f->ah, f->al, h2, h2, h2) ||
                              !tc_make_map_f16(&fm, f->mh, f->ml, h, h2, h2)))
       e = cudaErrorInvalidValue;
     if (e != cudaSuccess) return e;
-    mpdl = true;
+    c.prev_kernel = true;
   }
   if (!tt_inline) {
     // the latest T^T on the side stream is this node's or a later one:
     // either way this node's is complete when it is
-    e = cudaStreamWaitEvent(ms, c.ejoin, 0);
-    mpdl = false;
+    e = cudaStreamWaitEvent(c.s, c.ejoin, 0);
+    c.prev_kernel = false;
     if (e != cudaSuccess) return e;
   }
   {  // M21 = -M22 T ; M21[i, j] = sum_c M22[i, c] TT[j, c]; V12 = M21^T
@@ -757,12 +744,11 @@ cudaError_t chol_inv_rec(TcChol& c, int o, int sz, int depth, cudaEvent_t join =
       p.force_shape = 4;
       p.ra = f->ra;
       p.rb = f->rm;
-      e = tc_gemm_run(tc::MODE_STORE_SPLIT, fa, fm, p, 1, ms, mpdl);
+      e = tc_gemm_run(tc::MODE_STORE_SPLIT, fa, fm, p, 1, c.s, c.prev_kernel);
     } else {
-      e = tc_gemm_run(tc::MODE_STORE_SPLIT, c.mM, c.mTT[depth], p, 1, ms, mpdl);
+      e = tc_gemm_run(tc::MODE_STORE_SPLIT, c.mM, c.mTT[depth], p, 1, c.s, c.prev_kernel);
     }
-    if (!defer) c.prev_kernel = true;
-    if (e == cudaSuccess && defer) e = cudaEventRecord(c.m21done, ms);
+    c.prev_kernel = true;
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -817,77 +803,6 @@ __global__ void __launch_bounds__(256)
   if (lane == 0) vscale[r] = inv;
 }
 
-// The top node's M21 = -M22 (L21 M11) is needed only by the full M and V
-// (the adjoint, predict), not by the rest of the factor; from this n_pad on it
-// runs on its own stream while alpha is solved in block form through M11,
-// L21 and M22:  z1 = M11 x1,  z2 = M22 (x2 - L21 z1),  a2 = V22 z2,
-// a1 = V11 (z1 - L21^T a2).
-constexpr int M21_DEFER_MIN = 4096;
-constexpr int kSolveChunks = 16;  // row chunks of the column GEMV with L21
-
-// y_i = base_i - sum_k (Th + Tl)[i][k] x_k, dense rows of length cols (a
-// multiple of 4): one warp per row, float4 loads, float64 warp sum
-__global__ void __launch_bounds__(256)
-    gemv_rect_sub_kernel(const float* __restrict__ Th, const float* __restrict__ Tl, int64_t ld,
-                         int rows, int cols, const float* __restrict__ x,
-                         const double* __restrict__ base, double* __restrict__ y) {
-  const int i = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-  const int lane = threadIdx.x & 31;
-  if (i >= rows) return;
-  const float* rh = Th + (int64_t)i * ld;
-  const float* rl = Tl + (int64_t)i * ld;
-  float s0 = 0.f, s1 = 0.f;
-#pragma unroll 4
-  for (int c = 4 * lane; c < cols; c += 128) {
-    const float4 h = *reinterpret_cast<const float4*>(rh + c);
-    const float4 l = *reinterpret_cast<const float4*>(rl + c);
-    const float4 xv = *reinterpret_cast<const float4*>(x + c);
-    s0 = fmaf(h.x + l.x, xv.x, s0);
-    s1 = fmaf(h.y + l.y, xv.y, s1);
-    s0 = fmaf(h.z + l.z, xv.z, s0);
-    s1 = fmaf(h.w + l.w, xv.w, s1);
-  }
-  const double sd = warp_sum((double)s0 + (double)s1);
-  if (lane == 0) y[i] = base[i] - sd;
-}
-
-// part[c][j] = sum over rows i of chunk c of (Th + Tl)[i][j] x_i: one thread
-// per column (coalesced rows), chunks of rows across blockIdx.y
-__global__ void __launch_bounds__(256)
-    gemvt_rect_part_kernel(const float* __restrict__ Th, const float* __restrict__ Tl, int64_t ld,
-                           int rows, int cols, const float* __restrict__ x,
-                           double* __restrict__ part) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= cols) return;
-  const int per = (rows + kSolveChunks - 1) / kSolveChunks;
-  const int i0 = blockIdx.y * per, i1 = min(rows, i0 + per);
-  float s0 = 0.f, s1 = 0.f;
-  int i = i0;
-  for (; i + 1 < i1; i += 2) {
-    s0 = fmaf(Th[(int64_t)i * ld + j] + Tl[(int64_t)i * ld + j], x[i], s0);
-    s1 = fmaf(Th[(int64_t)(i + 1) * ld + j] + Tl[(int64_t)(i + 1) * ld + j], x[i + 1], s1);
-  }
-  if (i < i1) s0 = fmaf(Th[(int64_t)i * ld + j] + Tl[(int64_t)i * ld + j], x[i], s0);
-  part[(int64_t)blockIdx.y * cols + j] = (double)s0 + (double)s1;
-}
-
-// y_j = base_j - sum_c part[c][j] (chunks in order)
-__global__ void gemvt_finish_kernel(int cols, const double* __restrict__ part,
-                                    const double* __restrict__ base, double* __restrict__ y) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= cols) return;
-  double s = 0.0;
-  for (int c = 0; c < kSolveChunks; ++c) s += part[(int64_t)c * cols + j];
-  y[j] = base[j] - s;
-}
-
-// y (+)= w
-__global__ void vec_add_kernel(int n, const double* __restrict__ w, double* __restrict__ y,
-                               int accumulate) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) y[i] = accumulate ? y[i] + w[i] : w[i];
-}
-
 struct TcBuffers {
   int npad;
   int64_t ld;
@@ -900,7 +815,6 @@ struct TcBuffers {
   F16Set f16[kMaxDepth];  // float16 operand copies of the wide nodes, per depth
   int nf16;
   double *diff, *z, *alpha, *r, *logdiag, *dtrack, *rpart, *gpart, *rbuf, *cbuf, *fin;
-  double *w, *tpart;  // block solve: a vector of n_pad, column partials [kSolveChunks][n_pad]
   int* err;
 };
 
@@ -970,8 +884,6 @@ size_t tc_layout(int64_t n, int d, void* ws, TcBuffers& b) {
   b.rbuf = (double*)take((size_t)(b.npad / LEAF) * n * 8);  // residual partials, by tile
   b.cbuf = (double*)take((size_t)(b.npad / LEAF) * n * 8);
   b.fin = (double*)take(mll_finalize_scratch_doubles(d) * 8);
-  b.w = (double*)take((size_t)b.npad * 8);
-  b.tpart = (double*)take((size_t)kSolveChunks * b.npad * 8);
   const size_t tm = (size_t)b.npad / LEAF;
   b.gpart = (double*)take(tm * (tm + 1) / 2 * (d + 2) * 8);  // one row per adjoint tile
   b.err = (int*)take(64);
@@ -994,8 +906,6 @@ struct SideCtx {
   cudaStream_t side = nullptr;  // lowest priority: work that fills idle SMs
   cudaEvent_t estart = nullptr, efork = nullptr, ejoin = nullptr, edone = nullptr;
   LookAhead la;                 // the recursion's look-ahead streams
-  cudaStream_t m21 = nullptr;   // the top node's M21 (priority of the critical path)
-  cudaEvent_t m21fork = nullptr, m21done = nullptr;
 };
 constexpr int kMaxDevices = 64;
 std::mutex g_side_mu;
@@ -1016,8 +926,7 @@ cudaError_t side_ctx(SideCtx** out) {
     e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
     if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&sc.hp, cudaStreamNonBlocking, greatest);
     if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&sc.side, cudaStreamNonBlocking, least);
-    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&sc.m21, cudaStreamNonBlocking, greatest);
-    for (cudaEvent_t* ev : {&sc.estart, &sc.efork, &sc.ejoin, &sc.edone, &sc.m21fork, &sc.m21done})
+    for (cudaEvent_t* ev : {&sc.estart, &sc.efork, &sc.ejoin, &sc.edone})
       if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
     if (e != cudaSuccess) return e;
   }
@@ -1182,10 +1091,6 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
   c.efork = sc->efork;
   c.ejoin = sc->ejoin;
   c.la = &sc->la;
-  const bool defer_m21 = np >= M21_DEFER_MIN;
-  c.m21s = defer_m21 ? sc->m21 : nullptr;
-  c.m21fork = sc->m21fork;
-  c.m21done = sc->m21done;
   GPK_CUDA_TRY(cudaEventRecord(sc->estart, s));
   GPK_CUDA_TRY(cudaStreamWaitEvent(hs, sc->estart, 0));
   leaf_zero_kernel<<<dim3(cdiv(LEAF * 24, 256), np / LEAF), 256, 0, hs>>>(b.Mh, b.Ml, b.Vh, b.Vl,
@@ -1198,52 +1103,20 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
   GPK_LAUNCH_CHECK();
   c.prev_kernel = true;
   GPK_CUDA_TRY(chol_inv_rec(c, 0, np, 0));
-  if (!defer_m21) prof_mark(2, hs);
+  prof_mark(2, hs);
   // alpha = Sigma^-1 (y - m), refined against float64 residuals from the
   // mirrored upper triangle of the Gram matrix
-  const int ht = ((np / 2 + LEAF - 1) / LEAF) * LEAF, ht2 = np - ht;  // the top node's halves
-  // y (+)= op(T block) x on rows / columns [r0, r0 + m) of a triangle
-  auto gemv_blk = [&](const float* Th, const float* Tl, int r0, int m, int lower,
-                      const double* x, double* y, int accumulate) -> gpk_status {
-    to_f32_kernel<<<(int)cdiv(m, 256), 256, 0, hs>>>(m, x, b.vf);
+  const int gb = (int)cdiv((int64_t)np * 32, 256), gv = (int)cdiv(np, 256);
+  auto gemv = [&](const float* Th, const float* Tl, int lower, const double* x, double* y,
+                  int accumulate) -> gpk_status {
+    to_f32_kernel<<<gv, 256, 0, hs>>>(np, x, b.vf);
     GPK_LAUNCH_CHECK();
-    const int64_t off = (int64_t)r0 * b.ld + r0;
-    gemv_split_kernel<<<(int)cdiv((int64_t)m * 32, 256), 256, 0, hs>>>(
-        Th + off, Tl + off, b.ld, m, lower, b.vf, y, accumulate);
+    gemv_split_kernel<<<gb, 256, 0, hs>>>(Th, Tl, b.ld, np, lower, b.vf, y, accumulate);
     GPK_LAUNCH_CHECK();
     return GPK_OK;
   };
-  // alpha (+)= Sigma^-1 x: V (M x), or in block form through M11, L21, M22
-  // while the top node's M21 is still being formed
-  auto solve = [&](const double* x, int accumulate) -> gpk_status {
-    if (!defer_m21) {
-      gpk_status st = gemv_blk(b.Mh, b.Ml, 0, np, 1, x, b.z, 0);
-      return st == GPK_OK ? gemv_blk(b.Vh, b.Vl, 0, np, 0, b.z, b.alpha, accumulate) : st;
-    }
-    const float* L21h = b.Lh + (int64_t)ht * b.ld;
-    const float* L21l = b.Ll + (int64_t)ht * b.ld;
-    gpk_status st = gemv_blk(b.Mh, b.Ml, 0, ht, 1, x, b.z, 0);  // z1 = M11 x1
-    if (st != GPK_OK) return st;
-    to_f32_kernel<<<(int)cdiv(ht, 256), 256, 0, hs>>>(ht, b.z, b.vf);
-    GPK_LAUNCH_CHECK();
-    gemv_rect_sub_kernel<<<(int)cdiv((int64_t)ht2 * 32, 256), 256, 0, hs>>>(  // w = x2 - L21 z1
-        L21h, L21l, b.ld, ht2, ht, b.vf, x + ht, b.w);
-    GPK_LAUNCH_CHECK();
-    st = gemv_blk(b.Mh, b.Ml, ht, ht2, 1, b.w, b.z + ht, 0);  // z2 = M22 w
-    if (st == GPK_OK) st = gemv_blk(b.Vh, b.Vl, ht, ht2, 0, b.z + ht, b.w, 0);  // a2 = V22 z2
-    if (st != GPK_OK) return st;
-    vec_add_kernel<<<(int)cdiv(ht2, 256), 256, 0, hs>>>(ht2, b.w, b.alpha + ht, accumulate);
-    GPK_LAUNCH_CHECK();
-    to_f32_kernel<<<(int)cdiv(ht2, 256), 256, 0, hs>>>(ht2, b.w, b.vf);
-    GPK_LAUNCH_CHECK();
-    gemvt_rect_part_kernel<<<dim3((unsigned)cdiv(ht, 256), kSolveChunks), 256, 0, hs>>>(
-        L21h, L21l, b.ld, ht2, ht, b.vf, b.tpart);
-    GPK_LAUNCH_CHECK();
-    gemvt_finish_kernel<<<(int)cdiv(ht, 256), 256, 0, hs>>>(ht, b.tpart, b.z, b.z);  // z1 - L21^T a2
-    GPK_LAUNCH_CHECK();
-    return gemv_blk(b.Vh, b.Vl, 0, ht, 0, b.z, b.alpha, accumulate);  // a1 = V11 (...)
-  };
-  gpk_status st = solve(b.diff, 0);
+  gpk_status st = gemv(b.Mh, b.Ml, 1, b.diff, b.z, 0);
+  if (st == GPK_OK) st = gemv(b.Vh, b.Vl, 0, b.z, b.alpha, 0);
   if (st != GPK_OK) return st;
   for (int it = 0; it < refine; ++it) {
     const int tn = (int)cdiv(n, RU_T);
@@ -1254,14 +1127,9 @@ gpk_status mll_run_tc(int kind, int n, int d, const double* x, int64_t ldx, cons
                                                              b.diff, b.alpha, b.rbuf, b.cbuf,
                                                              b.r);
     GPK_LAUNCH_CHECK();
-    st = solve(b.r, 1);
+    st = gemv(b.Mh, b.Ml, 1, b.r, b.z, 0);
+    if (st == GPK_OK) st = gemv(b.Vh, b.Vl, 0, b.z, b.alpha, 1);
     if (st != GPK_OK) return st;
-  }
-  if (defer_m21) {
-    // the full M and V for what follows; the factor phase then ends here (the
-    // alpha solve ran beside the top node's M21 and is timed inside it)
-    GPK_CUDA_TRY(cudaStreamWaitEvent(hs, sc->m21done, 0));
-    prof_mark(2, hs);
   }
   prof_mark(3, hs);
   if (pred) {  // predictive mean and variance instead of the adjoint
