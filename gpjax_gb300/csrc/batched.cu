@@ -36,6 +36,7 @@
 #include "simt_tile.cuh"
 #include "leaf_chol.cuh"
 #include "mll_finalize.cuh"
+#include "tc_ptx.cuh"
 
 namespace gpk {
 namespace {
@@ -47,7 +48,8 @@ constexpr int WLD = TT + 4;   // W tile rows in shared memory (float4 rows)
 constexpr int BDM = 16;       // input dimension bound of the batched kernel
 constexpr int XLD = BDM + 2;  // staged input rows (pairs stay 8-byte aligned)
 constexpr int NP_MAX = 4096;  // largest padded instance
-constexpr int NCFG = 2;       // tile configurations: K slices of 16 or 32
+constexpr int NCFG = 3;       // tile configurations: K slices of 16 or 32 (CUDA cores),
+                              // K slices of 32 on the tensor cores
 
 // floats of the product staging area: the K-slice double buffer (or the W
 // tile), then the staged inputs and alphas of a tile's rows and columns
@@ -163,9 +165,10 @@ __device__ __forceinline__ void slice_store(float* S, const float4 (&r)[BK / 16]
 }
 
 template <int BK, bool AKM, bool BKM>
-__device__ __forceinline__ void tile_mma(const float* __restrict__ A, int lda,
-                                         const float* __restrict__ B, int ldb, int i0, int j0,
-                                         int klo, int khi, float* S, float (&acc)[8][4]) {
+__device__ __forceinline__ void tile_mma_simt(const float* __restrict__ A, int lda,
+                                              const float* __restrict__ B, int ldb, int i0,
+                                              int j0, int klo, int khi, float* S,
+                                              float (&acc)[8][4]) {
   float* As = S;                 // [2][BK][SLD]
   float* Bs = S + 2 * BK * SLD;  // [2][BK][SLD]
   const int ty = threadIdx.x >> 5, tx = threadIdx.x & 31;
@@ -210,6 +213,274 @@ __device__ __forceinline__ int tile_row(int u) {
   return (threadIdx.x >> 5) * 4 + (u & 3) + ((u >> 2) << 6);
 }
 __device__ __forceinline__ int tile_col(int v) { return (threadIdx.x & 31) * 4 + v; }
+
+// ---------------------------------------------------------------------------
+// The same 128 x 128 tile on the tensor cores (configuration TC_BK): K slices
+// of 32 float32 elements are split into TF32 hi / lo by all 512 threads and
+// stored in the 128B-swizzled K-major layout the MMA reads (two stages of
+// A_hi, A_lo, B_hi, B_lo, 64 KB each, 1024-byte aligned); thread 0 issues
+// the slice's 3 products (A_lo B_hi, A_hi B_lo, A_hi B_hi) x 4 K steps of
+// tcgen05.mma kind::tf32 into one of two TMEM accumulators and commits to
+// that accumulator's mbarrier; every thread then adds its 32 accumulator
+// columns to float32 registers (round to nearest: one slice, 12 MMAs, per
+// TMEM accumulation), while the next slice is staged and issued.  The
+// finished tile goes through shared memory into the CUDA-core fragment
+// layout of tile_mma_simt, so every epilogue is shared.  Waits are bounded
+// (kTcWait cycles); a timeout sets the CTA's error flag, after which no
+// wait is attempted and the instance reports info = -1.
+// ---------------------------------------------------------------------------
+constexpr int TC_BK = 0;        // template value of the tensor-core configuration
+constexpr int TC_STAGE = 65536; // bytes of one stage
+constexpr long long kTcWait = 4000000000LL;
+
+struct TcState {
+  uint64_t bar[2];  // MMA completion, one per accumulator
+  uint32_t n[2];    // completions consumed so far (parity = n & 1)
+  uint32_t issued[2];  // commits made
+  uint32_t tmem;    // base of 256 TMEM columns (two 128-column accumulators)
+  int err;          // a wait timed out
+};
+__device__ __forceinline__ TcState& tc_state() {
+  __shared__ TcState st;
+  return st;
+}
+
+// element (r, k) of a 128-row, 32-column float32 K slice in the 128B swizzle
+__device__ __forceinline__ uint32_t sw128(int r, int k) {
+  return (uint32_t)(r * 128 + ((((k >> 2) ^ (r & 7))) << 4) + ((k & 3) << 2));
+}
+
+// Element e (0..1023) of a slice, four floats: rows m..m+3 of column k when
+// the operand is stored K-major in memory (KM: a warp covers 8 columns x 16
+// rows, 64-byte segments, so that its swizzled scalar stores spread over 16
+// banks), else columns k..k+3 of row m (a warp covers 4 whole rows).
+__device__ __forceinline__ void tc_km_index(int e, int& k, int& m) {
+  const int w = e >> 5, l = e & 31;
+  k = (w & 3) * 8 + (l & 7);
+  m = (w >> 2) * 16 + 4 * (l >> 3);
+}
+
+template <bool KM>
+__device__ __forceinline__ void tc_load(const float* __restrict__ P, int ld, int r0, int k0,
+                                        float4 (&r)[2]) {
+#pragma unroll
+  for (int v = 0; v < 2; ++v) {
+    const int e = threadIdx.x + v * BNT;
+    if constexpr (KM) {
+      int k, m;
+      tc_km_index(e, k, m);
+      r[v] = *reinterpret_cast<const float4*>(P + (int64_t)(k0 + k) * ld + r0 + m);
+    } else {
+      const int m = e >> 3, k = 4 * (e & 7);
+      r[v] = *reinterpret_cast<const float4*>(P + (int64_t)(r0 + m) * ld + k0 + k);
+    }
+  }
+}
+
+__device__ __forceinline__ float4 tf32_hi4(float4 x) {
+  return make_float4(tf32_rna_f(x.x), tf32_rna_f(x.y), tf32_rna_f(x.z), tf32_rna_f(x.w));
+}
+
+template <bool KM>
+__device__ __forceinline__ void tc_store(char* hi, char* lo, const float4 (&r)[2]) {
+#pragma unroll
+  for (int v = 0; v < 2; ++v) {
+    const int e = threadIdx.x + v * BNT;
+    const float4 h = tf32_hi4(r[v]);
+    const float4 l = tf32_hi4(make_float4(r[v].x - h.x, r[v].y - h.y, r[v].z - h.z, r[v].w - h.w));
+    if constexpr (KM) {  // four rows of one column k
+      int k, m;
+      tc_km_index(e, k, m);
+      const float hv[4] = {h.x, h.y, h.z, h.w}, lv[4] = {l.x, l.y, l.z, l.w};
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const uint32_t o = sw128(m + u, k);
+        *reinterpret_cast<float*>(hi + o) = hv[u];
+        *reinterpret_cast<float*>(lo + o) = lv[u];
+      }
+    } else {  // one 16-byte chunk of row m
+      const int m = e >> 3, k = 4 * (e & 7);
+      const uint32_t o = sw128(m, k);
+      *reinterpret_cast<float4*>(hi + o) = h;
+      *reinterpret_cast<float4*>(lo + o) = l;
+    }
+  }
+}
+
+__device__ __forceinline__ void tc_wait(int b) {
+  TcState& st = tc_state();
+  if (*(volatile int*)&st.err) return;
+  if (!tc::mbar_wait_own(&st.bar[b], st.n[b] & 1u, kTcWait)) st.err = 1;
+}
+
+// The tensor-core staging region: the start of the dynamic shared memory,
+// 1024-byte aligned for the swizzle.  It overlaps the CUDA-core staging area
+// and the leaf's storage, neither of which is live during a tile product (the
+// epilogue runs after the tile has been moved to registers).  Kept within the
+// leaf's footprint so that the L1 share of the SM does not shrink.
+__host__ __device__ constexpr size_t tc_region_bytes() { return 1024 + 2 * (size_t)TC_STAGE; }
+
+// Kernel start (every thread): barriers, counters, 256 TMEM columns.
+__device__ void tc_setup() {
+  TcState& st = tc_state();
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&st.bar[0], 1);
+    tc::mbar_init(&st.bar[1], 1);
+    st.n[0] = st.n[1] = 0;
+    st.issued[0] = st.issued[1] = 0;
+    st.err = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if ((threadIdx.x >> 5) == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     tc::smem_u32(&st.tmem)),
+                 "r"(256)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+}
+
+// Kernel end (every thread): after a timeout, the commits not yet seen are
+// waited for (bounded) before the TMEM columns are released.
+__device__ void tc_teardown() {
+  TcState& st = tc_state();
+  __syncthreads();
+  if (threadIdx.x == 0 && st.err) {
+    for (int b = 0; b < 2; ++b)
+      while (st.n[b] < st.issued[b] && tc::mbar_wait_own(&st.bar[b], st.n[b] & 1u, kTcWait))
+        st.n[b] += 1;
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if ((threadIdx.x >> 5) == 0) {
+    tc::tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(st.tmem), "r"(256)
+                 : "memory");
+  }
+}
+
+template <bool AKM, bool BKM>
+__device__ void tile_mma_tc(const float* __restrict__ A, int lda, const float* __restrict__ B,
+                            int ldb, int i0, int j0, int klo, int khi, float* S,
+                            float (&acc)[8][4]) {
+  TcState& st = tc_state();
+  char* base =
+      reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(S) + 1023) & ~uintptr_t(1023));
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nsl = (khi - klo) / 32;
+  float c32[32];
+#pragma unroll
+  for (int k = 0; k < 32; ++k) c32[k] = 0.f;
+  // K slices are loaded into registers two slices ahead (ra[q], rb[q] hold
+  // slice sl + 2 while slice sl + 1 is split and stored), so a load has a
+  // whole slice of work to land behind
+  float4 ra0[2], rb0[2], ra1[2], rb1[2];
+  auto stage = [&](int sl, const float4(&qa)[2], const float4(&qb)[2]) {
+    // smem of slice sl, the MMAs issued and committed
+    char* sb = base + (sl & 1) * TC_STAGE;
+    tc_store<AKM>(sb, sb + 16384, qa);
+    tc_store<BKM>(sb + 32768, sb + 49152, qb);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tc::tc_fence_before();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tc::tc_fence_after();
+      const uint32_t a = tc::smem_u32(sb);
+      const uint64_t ahi = tc::sdesc<128>(a), alo = tc::sdesc<128>(a + 16384);
+      const uint64_t bhi = tc::sdesc<128>(a + 32768), blo = tc::sdesc<128>(a + 49152);
+      const uint32_t tacc = st.tmem + (uint32_t)((sl & 1) * 128);
+      constexpr uint32_t idesc = tc::idesc_tf32(128, 128);
+      // the small cross products first, the hi x hi products last: the
+      // accumulator's roundings at the size of the result happen 4 times
+      // per slice instead of 12
+#pragma unroll
+      for (int ks = 0; ks < 4; ++ks)
+        tc::mma_tf32(tacc, alo + 2 * ks, bhi + 2 * ks, idesc, ks ? 1u : 0u);
+#pragma unroll
+      for (int ks = 0; ks < 4; ++ks) tc::mma_tf32(tacc, ahi + 2 * ks, blo + 2 * ks, idesc, 1u);
+#pragma unroll
+      for (int ks = 0; ks < 4; ++ks) tc::mma_tf32(tacc, ahi + 2 * ks, bhi + 2 * ks, idesc, 1u);
+      tc::mma_commit(&st.bar[sl & 1]);
+      st.issued[sl & 1] += 1;
+    }
+  };
+  auto drain = [&](int sl) {
+    const int b = sl & 1;
+    tc_wait(b);
+    tc::tc_fence_after();
+    const uint32_t ta =
+        st.tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(b * 128 + 32 * (warp >> 2));
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {  // two 16-column loads: fewer live registers
+      uint32_t v[16];
+      tc::tmem_ld16_nowait(ta + 16 * h, v);
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+      for (int k = 0; k < 16; ++k) c32[16 * h + k] += __uint_as_float(v[k]);
+    }
+    tc::tc_fence_before();
+    __syncthreads();  // the accumulator is read: the next MMAs into it may start
+    if (threadIdx.x == 0) st.n[b] += 1;
+  };
+  // iteration sl: slice sl is staged, the other register set holds slice
+  // sl + 1; a stage is rewritten only after the slice that last read it
+  // (sl - 1) was drained
+  if (nsl > 0) {
+    tc_load<AKM>(A, lda, i0, klo, ra0);
+    tc_load<BKM>(B, ldb, j0, klo, rb0);
+  }
+  if (nsl > 1) {
+    tc_load<AKM>(A, lda, i0, klo + 32, ra1);
+    tc_load<BKM>(B, ldb, j0, klo + 32, rb1);
+  }
+  if (nsl > 0) stage(0, ra0, rb0);
+  for (int sl = 0; sl < nsl; sl += 2) {
+    if (sl + 2 < nsl) {
+      tc_load<AKM>(A, lda, i0, klo + 32 * (sl + 2), ra0);
+      tc_load<BKM>(B, ldb, j0, klo + 32 * (sl + 2), rb0);
+    }
+    if (sl + 1 < nsl) stage(sl + 1, ra1, rb1);
+    drain(sl);
+    if (sl + 1 < nsl) {
+      if (sl + 3 < nsl) {
+        tc_load<AKM>(A, lda, i0, klo + 32 * (sl + 3), ra1);
+        tc_load<BKM>(B, ldb, j0, klo + 32 * (sl + 3), rb1);
+      }
+      if (sl + 2 < nsl) stage(sl + 2, ra0, rb0);
+      drain(sl + 1);
+    }
+  }
+  // the tile through shared memory into the CUDA-core fragment layout
+  float* Cs = reinterpret_cast<float*>(base);
+  const int r = 32 * (warp & 3) + lane, c0 = 32 * (warp >> 2);
+#pragma unroll
+  for (int q = 0; q < 8; ++q)
+    *reinterpret_cast<float4*>(Cs + r * SLD + c0 + 4 * q) =
+        make_float4(c32[4 * q], c32[4 * q + 1], c32[4 * q + 2], c32[4 * q + 3]);
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < 8; ++u) {
+    const float4 t = *reinterpret_cast<const float4*>(Cs + tile_row(u) * SLD + tile_col(0));
+    acc[u][0] = t.x;
+    acc[u][1] = t.y;
+    acc[u][2] = t.z;
+    acc[u][3] = t.w;
+  }
+  __syncthreads();
+}
+
+template <int BK, bool AKM, bool BKM>
+__device__ __forceinline__ void tile_mma(const float* __restrict__ A, int lda,
+                                         const float* __restrict__ B, int ldb, int i0, int j0,
+                                         int klo, int khi, float* S, float (&acc)[8][4]) {
+  if constexpr (BK == TC_BK)
+    tile_mma_tc<AKM, BKM>(A, lda, B, ldb, i0, j0, klo, khi, S, acc);
+  else
+    tile_mma_simt<BK, AKM, BKM>(A, lda, B, ldb, i0, j0, klo, khi, S, acc);
+}
 
 // A product over tm x tn output tiles (the lower ones when lower), one tile
 // at a time on the whole CTA.  kr(i0, j0, klo, khi) gives a tile's K range
@@ -797,6 +1068,7 @@ __global__ void __launch_bounds__(BNT, 1) batch_mll_kernel(const __grid_constant
     s_own = -1;
     s_wait0 = -1;
   }
+  tc_setup();
   for (;;) {
     if (threadIdx.x == 0) {
       int mode = 0, id = -1, tile = -1;
@@ -866,8 +1138,14 @@ __global__ void __launch_bounds__(BNT, 1) batch_mll_kernel(const __grid_constant
     const int id = s_id;
     const int cfg = a.force_cfg >= 0 ? a.force_cfg : s_inst.cfg;
     if (mode == 1) {
-      const bool failed = cfg == 0 ? instance_front<16>(a, s_inst, s_slot, smem)
-                                   : instance_front<32>(a, s_inst, s_slot, smem);
+      bool failed = cfg == 0   ? instance_front<16>(a, s_inst, s_slot, smem)
+                    : cfg == 1 ? instance_front<32>(a, s_inst, s_slot, smem)
+                               : instance_front<TC_BK>(a, s_inst, s_slot, smem);
+      if (tc_state().err) {  // a tensor-core wait timed out: the instance fails
+        __syncthreads();
+        if (threadIdx.x == 0) *s_inst.info = -1;
+        failed = true;
+      }
       const bool tiles = !failed && a.want_grad && s_inst.ntiles > 0;
       if (!tiles) finish_instance(a, s_inst, s_slot, failed, s_red);
       if (threadIdx.x == 0) {
@@ -877,12 +1155,16 @@ __global__ void __launch_bounds__(BNT, 1) batch_mll_kernel(const __grid_constant
         s_own = tiles ? id : -1;
       }
     } else {
-      const bool last = cfg == 0 ? adjoint_tile<16>(a, id, s_inst, s_slot, s_tile, smem, s_red)
-                                 : adjoint_tile<32>(a, id, s_inst, s_slot, s_tile, smem, s_red);
+      const bool last =
+          cfg == 0   ? adjoint_tile<16>(a, id, s_inst, s_slot, s_tile, smem, s_red)
+          : cfg == 1 ? adjoint_tile<32>(a, id, s_inst, s_slot, s_tile, smem, s_red)
+                     : adjoint_tile<TC_BK>(a, id, s_inst, s_slot, s_tile, smem, s_red);
+      if (tc_state().err && threadIdx.x == 0) atomicExch(s_inst.info, -1);
       if (last) finish_instance(a, s_inst, s_slot, false, s_red + GPK_MAX_D + 2 + 16 * 18);
     }
     __syncthreads();  // everyone is done with the shared descriptors before thread 0 rewrites them
   }
+  tc_teardown();
 }
 
 // The queued instances of a partial launch (autotuner trial): not yet
@@ -896,12 +1178,12 @@ __global__ void batch_reset_kernel(const int* queue, int count, int* published, 
 }
 
 size_t batch_smem_bytes(int np_max) {
-  // the largest of: the product staging area plus alpha for the adjoint, the
+  // the largest of: the product staging area, the tensor-core region, the
   // leaf, the refinement vectors
-  const size_t prod = (size_t)prod_floats() * sizeof(float);
+  const size_t prod = std::max((size_t)prod_floats() * sizeof(float), tc_region_bytes());
   const size_t leaf = leaf_smem_bytes();
   const size_t refine = (size_t)np_max * (2 * sizeof(float) + sizeof(double));
-  return std::max(std::max(prod + (size_t)np_max * sizeof(float), leaf), refine);
+  return std::max(std::max(prod, leaf), refine);
 }
 
 }  // namespace
@@ -925,6 +1207,7 @@ struct gpk_batch_plan_s {
   int* d_queue = nullptr;       // size-sorted instance indices
   int* d_state = nullptr;       // head, published[count], next_tile[count], tiles_done[count]
   double* d_tpart = nullptr;    // per-tile gradient partials
+  int force_cfg = -1;           // >= 0: every instance runs this configuration
 };
 
 namespace {
@@ -1152,11 +1435,19 @@ extern "C" int gpk_batch_plan_config(gpk_batch_plan plan, int64_t n) {
   return it != g_tune.end() ? it->second : 1;
 }
 
+extern "C" int gpk_batch_plan_config_count(void) { return NCFG; }
+
+extern "C" gpk_status gpk_batch_plan_force_config(gpk_batch_plan plan, int cfg) {
+  if (!plan || cfg < -1 || cfg >= NCFG) return GPK_ERR_BAD_ARG;
+  plan->force_cfg = cfg;
+  return GPK_OK;
+}
+
 extern "C" gpk_status gpk_batch_plan_execute(gpk_batch_plan plan, void* workspace,
                                              size_t workspace_bytes, cudaStream_t stream) {
   if (!plan || !workspace) return GPK_ERR_BAD_ARG;
   if (workspace_bytes < gpk_batch_plan_workspace_bytes(plan)) return GPK_ERR_WORKSPACE;
-  GPK_CUDA_TRY(launch_batch(*plan, workspace, -1, plan->count, plan->d_queue, stream));
+  GPK_CUDA_TRY(launch_batch(*plan, workspace, plan->force_cfg, plan->count, plan->d_queue, stream));
   return GPK_OK;
 }
 

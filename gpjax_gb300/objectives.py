@@ -327,6 +327,16 @@ class BatchPlan:
         """Tile configuration the autotuner chose for instances of size n."""
         return int(_lib.lib().gpk_batch_plan_config(self._handle, int(n)))
 
+    @staticmethod
+    def config_count() -> int:
+        """Number of tile configurations (the last one runs on the tensor cores)."""
+        return int(_lib.lib().gpk_batch_plan_config_count())
+
+    def force_config(self, cfg: int):
+        """Run every instance of later executions with configuration ``cfg``
+        (``-1``: the tuned configurations again)."""
+        _lib.call("gpk_batch_plan_force_config", self._handle, int(cfg))
+
     def execute(self):
         """One launch over all instances; returns (mll, grads, info)."""
         _lib.call("gpk_batch_plan_execute", self._handle, self.workspace.data_ptr(),

@@ -300,7 +300,11 @@ gpk_status gpk_conjugate_mll_batched(int count, const int* kind, const int64_t* 
  * CUDA graph.  Float32 compute with float64 pivots, float-float refinement of
  * alpha and float64 sums.  n <= 4096, d <= 16 (else GPK_ERR_UNSUPPORTED).
  * gpk_batch_plan_config returns the configuration chosen for instances of
- * size n (0: K slices of 16, 1: of 32) or -1.
+ * size n (0: K slices of 16 on the CUDA cores, 1: of 32, 2: K slices of 32 on
+ * the tcgen05 tensor cores in split TF32) or -1; gpk_batch_plan_config_count
+ * gives the number of configurations.  gpk_batch_plan_force_config runs every
+ * instance of later executions with configuration cfg (-1: the tuned ones
+ * again); GPK_ERR_BAD_ARG outside [-1, count).
  * ------------------------------------------------------------------------- */
 typedef struct gpk_batch_plan_s* gpk_batch_plan;
 gpk_status gpk_batch_plan_create(int count, const int* kind, const int64_t* n, const int* d,
@@ -311,6 +315,8 @@ gpk_status gpk_batch_plan_create(int count, const int* kind, const int64_t* n, c
                                  int autotune, gpk_batch_plan* plan);
 size_t gpk_batch_plan_workspace_bytes(gpk_batch_plan plan);
 int gpk_batch_plan_config(gpk_batch_plan plan, int64_t n);
+int gpk_batch_plan_config_count(void);
+gpk_status gpk_batch_plan_force_config(gpk_batch_plan plan, int cfg);
 gpk_status gpk_batch_plan_execute(gpk_batch_plan plan, void* workspace, size_t workspace_bytes,
                                   cudaStream_t stream);
 gpk_status gpk_batch_plan_destroy(gpk_batch_plan plan);

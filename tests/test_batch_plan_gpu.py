@@ -137,8 +137,39 @@ def test_plan_reports_a_failed_instance_and_keeps_the_others(cuda_lib):
 def test_autotuner_picks_a_configuration_per_size(cuda_lib):
     insts = [_instance((_lib.RBF, n, 3, False), 120 + k) for k, n in enumerate([256, 256, 1024])]
     plan = _plan(insts, autotune=True)
-    assert plan.config(256) in (0, 1) and plan.config(1024) in (0, 1)
+    ncfg = BatchPlan.config_count()
+    assert plan.config(256) in range(ncfg) and plan.config(1024) in range(ncfg)
     assert plan.config(5000) == -1
+    plan.close()
+
+
+@pytest.mark.parametrize("cfg", [0, 1, 2])
+def test_every_configuration_matches_oracle(cuda_lib, cfg):
+    """Each tile configuration forced on every instance (2: the products on the
+    tcgen05 tensor cores in split TF32) meets the same tolerances, and going
+    back to the tuned configurations changes no result beyond them."""
+    insts = [_instance(s, 200 + k) for k, s in enumerate(SPECS)]
+    plan = _plan(insts, autotune=False)
+    plan.force_config(cfg)
+    mll, grads, info = plan.execute()
+    torch.cuda.synchronize()
+    mll, info = mll.cpu().numpy().copy(), info.cpu().numpy()
+    assert np.all(info == 0), info
+    for k, inst in enumerate(insts):
+        ref, gref = _oracle(inst)
+        g = grads[k].cpu().numpy()
+        rel = abs(mll[k] - ref) / abs(ref)
+        grel = np.linalg.norm(g - gref) / np.linalg.norm(gref)
+        assert rel <= MLL_RTOL, (cfg, k, SPECS[k], mll[k], ref, rel)
+        assert grel <= GRAD_RTOL, (cfg, k, SPECS[k], g, gref, grel)
+        print("cfg", cfg, "instance", k, SPECS[k], "mll rel", rel, "grad rel", grel)
+    plan.force_config(-1)
+    mll2, _, info2 = plan.execute()
+    torch.cuda.synchronize()
+    assert np.all(info2.cpu().numpy() == 0)
+    np.testing.assert_allclose(mll2.cpu().numpy(), mll, rtol=2 * MLL_RTOL)
+    with pytest.raises(_lib.GPKError):
+        plan.force_config(BatchPlan.config_count())
     plan.close()
 
 

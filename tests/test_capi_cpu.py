@@ -154,6 +154,8 @@ def test_batch_plan_rejects_bad_arguments(built_lib):
     assert lib.gpk_batch_plan_config(None, 100) == -1
     assert lib.gpk_batch_plan_execute(None, P, 1 << 20, None) == 1
     assert lib.gpk_batch_plan_destroy(None) == 0
+    assert lib.gpk_batch_plan_config_count() == 3
+    assert lib.gpk_batch_plan_force_config(None, 0) == 1
 
 
 # ---------------------------------------------------------------------------
