@@ -374,10 +374,10 @@ __device__ void tile_mma_tc(const float* __restrict__ A, int lda, const float* _
   float c32[32];
 #pragma unroll
   for (int k = 0; k < 32; ++k) c32[k] = 0.f;
-  // K slices are loaded into registers two slices ahead (ra[q], rb[q] hold
-  // slice sl + 2 while slice sl + 1 is split and stored), so a load has a
-  // whole slice of work to land behind
-  float4 ra0[2], rb0[2], ra1[2], rb1[2];
+  // K slices are loaded into registers one slice ahead (a second register
+  // set, two slices ahead, measured slower: its spills reached every path
+  // of the kernel)
+  float4 ra[2], rb[2];
   auto stage = [&](int sl, const float4(&qa)[2], const float4(&qb)[2]) {
     // smem of slice sl, the MMAs issued and committed
     char* sb = base + (sl & 1) * TC_STAGE;
@@ -425,33 +425,18 @@ __device__ void tile_mma_tc(const float* __restrict__ A, int lda, const float* _
     __syncthreads();  // the accumulator is read: the next MMAs into it may start
     if (threadIdx.x == 0) st.n[b] += 1;
   };
-  // iteration sl: slice sl is staged, the other register set holds slice
-  // sl + 1; a stage is rewritten only after the slice that last read it
-  // (sl - 1) was drained
   if (nsl > 0) {
-    tc_load<AKM>(A, lda, i0, klo, ra0);
-    tc_load<BKM>(B, ldb, j0, klo, rb0);
+    tc_load<AKM>(A, lda, i0, klo, ra);
+    tc_load<BKM>(B, ldb, j0, klo, rb);
+    stage(0, ra, rb);
   }
-  if (nsl > 1) {
-    tc_load<AKM>(A, lda, i0, klo + 32, ra1);
-    tc_load<BKM>(B, ldb, j0, klo + 32, rb1);
-  }
-  if (nsl > 0) stage(0, ra0, rb0);
-  for (int sl = 0; sl < nsl; sl += 2) {
-    if (sl + 2 < nsl) {
-      tc_load<AKM>(A, lda, i0, klo + 32 * (sl + 2), ra0);
-      tc_load<BKM>(B, ldb, j0, klo + 32 * (sl + 2), rb0);
+  for (int sl = 0; sl < nsl; ++sl) {
+    if (sl + 1 < nsl) {  // the next slice's stage was last read by slice sl - 1, drained below
+      tc_load<AKM>(A, lda, i0, klo + 32 * (sl + 1), ra);
+      tc_load<BKM>(B, ldb, j0, klo + 32 * (sl + 1), rb);
+      stage(sl + 1, ra, rb);
     }
-    if (sl + 1 < nsl) stage(sl + 1, ra1, rb1);
     drain(sl);
-    if (sl + 1 < nsl) {
-      if (sl + 3 < nsl) {
-        tc_load<AKM>(A, lda, i0, klo + 32 * (sl + 3), ra1);
-        tc_load<BKM>(B, ldb, j0, klo + 32 * (sl + 3), rb1);
-      }
-      if (sl + 2 < nsl) stage(sl + 2, ra0, rb0);
-      drain(sl + 1);
-    }
   }
   // the tile through shared memory into the CUDA-core fragment layout
   float* Cs = reinterpret_cast<float*>(base);
@@ -723,32 +708,84 @@ __device__ void chol_inv(const Slot& S, int ld, int np, int* info, float* smem) 
   }
 }
 
-// z = M r (lower), one warp per row, float accumulation
+__device__ __forceinline__ float dot4(float4 m, float4 v, float s) {
+  return fmaf(m.w, v.w, fmaf(m.z, v.z, fmaf(m.y, v.y, fmaf(m.x, v.x, s))));
+}
+
+// z = M r (lower), one warp per row, float accumulation.  The two GEMVs of a
+// solve read M from memory (np^2 / 2 floats each) with one CTA per SM, so
+// they are written for bytes in flight: four independent 16-byte loads per
+// lane before the first FMA.
 __device__ void gemv_lower(const float* M, int ld, int np, const float* r, float* z) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int i = warp; i < np; i += BNT / 32) {
     const float* row = M + (int64_t)i * ld;
-    float s = 0.f;
-    for (int k = lane * 4; k <= i; k += 128) {
-      const float4 m = *reinterpret_cast<const float4*>(row + k);
-      const float4 v = *reinterpret_cast<const float4*>(r + k);
-      s = fmaf(m.x, v.x, s);
-      s = fmaf(m.y, v.y, s);
-      s = fmaf(m.z, v.z, s);
-      s = fmaf(m.w, v.w, s);  // entries past i are zeros of M
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    int k = lane * 4;
+    // entries past i inside the float4 that holds i are zeros of M's
+    // diagonal block; every load starts at k <= i
+    for (; k + 384 <= i; k += 512) {
+      const float4 m0 = *reinterpret_cast<const float4*>(row + k);
+      const float4 m1 = *reinterpret_cast<const float4*>(row + k + 128);
+      const float4 m2 = *reinterpret_cast<const float4*>(row + k + 256);
+      const float4 m3 = *reinterpret_cast<const float4*>(row + k + 384);
+      s0 = dot4(m0, *reinterpret_cast<const float4*>(r + k), s0);
+      s1 = dot4(m1, *reinterpret_cast<const float4*>(r + k + 128), s1);
+      s2 = dot4(m2, *reinterpret_cast<const float4*>(r + k + 256), s2);
+      s3 = dot4(m3, *reinterpret_cast<const float4*>(r + k + 384), s3);
     }
-    s = warp_sum(s);
+    for (; k <= i; k += 128)
+      s0 = dot4(*reinterpret_cast<const float4*>(row + k), *reinterpret_cast<const float4*>(r + k),
+                s0);
+    const float s = warp_sum((s0 + s1) + (s2 + s3));
     if (lane == 0) z[i] = s;
   }
 }
 
-// alpha (+)= M^T z, one thread per column (coalesced rows of M)
+// alpha (+)= M^T z by 128-column chunks: warp w takes rows c0 + w, c0 + w +
+// 16, ... (a float4 of 4 columns per lane, four rows in flight), the 16
+// warps' partial sums meet in shared memory (red: 16 x 128 floats).  Rows of
+// the diagonal block reach past the diagonal into its zeros.
 __device__ void gemv_upper_t(const float* M, int ld, int np, const float* z, double* alpha,
-                             bool accumulate) {
-  for (int j = threadIdx.x; j < np; j += BNT) {
-    float s = 0.f;
-    for (int i = j; i < np; ++i) s = fmaf(M[(int64_t)i * ld + j], z[i], s);
-    alpha[j] = accumulate ? alpha[j] + (double)s : (double)s;
+                             bool accumulate, float* red) {
+  constexpr int NW = BNT / 32;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int c0 = 0; c0 < np; c0 += TT) {
+    const float* col = M + c0 + 4 * lane;
+    float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f), a1 = a0;
+    int i = c0 + warp;
+    for (; i + 3 * NW < np; i += 4 * NW) {
+      const float4 m0 = *reinterpret_cast<const float4*>(col + (int64_t)i * ld);
+      const float4 m1 = *reinterpret_cast<const float4*>(col + (int64_t)(i + NW) * ld);
+      const float4 m2 = *reinterpret_cast<const float4*>(col + (int64_t)(i + 2 * NW) * ld);
+      const float4 m3 = *reinterpret_cast<const float4*>(col + (int64_t)(i + 3 * NW) * ld);
+      const float z0 = z[i], z1 = z[i + NW], z2 = z[i + 2 * NW], z3 = z[i + 3 * NW];
+      a0.x = fmaf(m0.x, z0, a0.x); a0.y = fmaf(m0.y, z0, a0.y);
+      a0.z = fmaf(m0.z, z0, a0.z); a0.w = fmaf(m0.w, z0, a0.w);
+      a1.x = fmaf(m1.x, z1, a1.x); a1.y = fmaf(m1.y, z1, a1.y);
+      a1.z = fmaf(m1.z, z1, a1.z); a1.w = fmaf(m1.w, z1, a1.w);
+      a0.x = fmaf(m2.x, z2, a0.x); a0.y = fmaf(m2.y, z2, a0.y);
+      a0.z = fmaf(m2.z, z2, a0.z); a0.w = fmaf(m2.w, z2, a0.w);
+      a1.x = fmaf(m3.x, z3, a1.x); a1.y = fmaf(m3.y, z3, a1.y);
+      a1.z = fmaf(m3.z, z3, a1.z); a1.w = fmaf(m3.w, z3, a1.w);
+    }
+    for (; i < np; i += NW) {
+      const float4 m0 = *reinterpret_cast<const float4*>(col + (int64_t)i * ld);
+      const float z0 = z[i];
+      a0.x = fmaf(m0.x, z0, a0.x); a0.y = fmaf(m0.y, z0, a0.y);
+      a0.z = fmaf(m0.z, z0, a0.z); a0.w = fmaf(m0.w, z0, a0.w);
+    }
+    *reinterpret_cast<float4*>(red + warp * TT + 4 * lane) =
+        make_float4(a0.x + a1.x, a0.y + a1.y, a0.z + a1.z, a0.w + a1.w);
+    __syncthreads();
+    if (threadIdx.x < TT) {
+      float s = 0.f;
+#pragma unroll
+      for (int w = 0; w < NW; ++w) s += red[w * TT + threadIdx.x];
+      const int j = c0 + threadIdx.x;
+      alpha[j] = accumulate ? alpha[j] + (double)s : (double)s;
+    }
+    __syncthreads();
   }
 }
 
@@ -757,13 +794,14 @@ __device__ void to_float(const double* rhs, int np, float* rf) {
   for (int i = threadIdx.x; i < np; i += BNT) rf[i] = (float)rhs[i];
 }
 
-// alpha (+)= M^T M rhs
-__device__ void solve_apply(const Slot& S, int ld, int np, const double* rhs, bool accumulate) {
+// alpha (+)= M^T M rhs (red: 16 x 128 floats of shared memory)
+__device__ void solve_apply(const Slot& S, int ld, int np, const double* rhs, bool accumulate,
+                            float* red) {
   to_float(rhs, np, S.rf);
   __syncthreads();
   gemv_lower(S.M, ld, np, S.rf, S.zf);
   __syncthreads();
-  gemv_upper_t(S.M, ld, np, S.zf, S.alpha, accumulate);
+  gemv_upper_t(S.M, ld, np, S.zf, S.alpha, accumulate, red);
   __syncthreads();
 }
 
@@ -1026,10 +1064,11 @@ __device__ bool instance_front(const BatchArgs& a, const BatchInst& I, const Slo
   __syncthreads();
   if (failed) return true;
   // alpha = Sigma^-1 diff, refined twice
-  solve_apply(S, ld, np, S.diff, false);
   float* ah = smem;          // [np] alpha hi
   float* al = smem + np;     // [np] alpha lo
   double* rres = reinterpret_cast<double*>(smem + 2 * np);  // [np]
+  float* red = smem + 4 * np;  // [16][128] GEMV partial sums
+  solve_apply(S, ld, np, S.diff, false, red);
   for (int it = 0; it < 2; ++it) {
     for (int i = threadIdx.x; i < np; i += BNT) {
       const double v = S.alpha[i];
@@ -1040,7 +1079,7 @@ __device__ bool instance_front(const BatchArgs& a, const BatchInst& I, const Slo
     __syncthreads();
     residual(I, S, np, s2, ka, noise_diag, ah, al, rres);
     __syncthreads();
-    solve_apply(S, ld, np, rres, true);
+    solve_apply(S, ld, np, rres, true, red);
   }
   for (int i = threadIdx.x; i < np; i += BNT) S.ahf[i] = (float)S.alpha[i];
   __syncthreads();
@@ -1182,7 +1221,8 @@ size_t batch_smem_bytes(int np_max) {
   // leaf, the refinement vectors
   const size_t prod = std::max((size_t)prod_floats() * sizeof(float), tc_region_bytes());
   const size_t leaf = leaf_smem_bytes();
-  const size_t refine = (size_t)np_max * (2 * sizeof(float) + sizeof(double));
+  const size_t refine =
+      (size_t)np_max * (2 * sizeof(float) + sizeof(double)) + (size_t)16 * TT * sizeof(float);
   return std::max(std::max(prod, leaf), refine);
 }
 
