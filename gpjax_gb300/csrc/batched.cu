@@ -931,7 +931,10 @@ __device__ bool adjoint_tile(const BatchArgs& a, int id, const BatchInst& I, con
   for (int u = 0; u < 8; ++u)
 #pragma unroll
     for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
-  tile_mma<BK, true, true>(S.M, ld, S.M, ld, i0, j0, i0, np, smem, acc);
+  if constexpr (BK == TC_BK)  // MT = M^T in the slot's A: K along rows
+    tile_mma<BK, false, false>(S.A, ld, S.A, ld, i0, j0, i0, np, smem, acc);
+  else
+    tile_mma<BK, true, true>(S.M, ld, S.M, ld, i0, j0, i0, np, smem, acc);
   float* Ws = smem;                          // [TT][WLD]
   float* sxi = smem + stage_floats();        // [TT][XLD]
   float* sxj = sxi + TT * XLD;
@@ -1003,6 +1006,40 @@ __device__ void finish_instance(const BatchArgs& a, const BatchInst& I, const Sl
   __syncthreads();
 }
 
+// MT = M^T into the slot's A (dead after the factorisation): the lower
+// 128-blocks of M become the upper blocks of MT, diagonal blocks with their
+// zeros.  The tensor-core adjoint then reads both operands of W = M^T M
+// along rows (K-major in memory, 16-byte stores while staging) instead of
+// transposing each K slice.  One block at a time through shared memory
+// (rows of 129 floats: both the row-wise writes and the column-wise reads
+// are free of bank conflicts).
+__device__ void transpose_m(const Slot& S, int ld, int np, float* smem) {
+  constexpr int TLD = TT + 1;
+  const int nb = np / TT, nt = nb * (nb + 1) / 2;
+  for (int t = 0; t < nt; ++t) {
+    int bi, bj;
+    tri_index(t, bi, bj);
+    const float* src = S.M + (int64_t)bi * TT * ld + bj * TT;
+    for (int e = threadIdx.x; e < TT * TT / 4; e += BNT) {
+      const int r = e / (TT / 4), c = 4 * (e % (TT / 4));
+      const float4 v = *reinterpret_cast<const float4*>(src + (int64_t)r * ld + c);
+      smem[r * TLD + c] = v.x;
+      smem[r * TLD + c + 1] = v.y;
+      smem[r * TLD + c + 2] = v.z;
+      smem[r * TLD + c + 3] = v.w;
+    }
+    __syncthreads();
+    float* dst = S.A + (int64_t)bj * TT * ld + bi * TT;
+    for (int e = threadIdx.x; e < TT * TT / 4; e += BNT) {
+      const int c = e / (TT / 4), r = 4 * (e % (TT / 4));
+      *reinterpret_cast<float4*>(dst + (int64_t)c * ld + r) =
+          make_float4(smem[r * TLD + c], smem[(r + 1) * TLD + c], smem[(r + 2) * TLD + c],
+                      smem[(r + 3) * TLD + c]);
+    }
+    __syncthreads();
+  }
+}
+
 // Everything of an instance before its adjoint, on the CTA that took it from
 // the queue: Gram, factor and inverse, alpha refined twice.  Returns true if
 // the factorisation failed.
@@ -1063,6 +1100,9 @@ __device__ bool instance_front(const BatchArgs& a, const BatchInst& I, const Slo
   const bool failed = *(volatile int*)I.info != INT_MAX;
   __syncthreads();
   if (failed) return true;
+  if constexpr (BK == TC_BK) {
+    if (a.want_grad) transpose_m(S, ld, np, smem);
+  }
   // alpha = Sigma^-1 diff, refined twice
   float* ah = smem;          // [np] alpha hi
   float* al = smem + np;     // [np] alpha lo
