@@ -215,22 +215,25 @@ __device__ __forceinline__ int tile_row(int u) {
 __device__ __forceinline__ int tile_col(int v) { return (threadIdx.x & 31) * 4 + v; }
 
 // ---------------------------------------------------------------------------
-// The same 128 x 128 tile on the tensor cores (configuration TC_BK): K slices
-// of 32 float32 elements are split into TF32 hi / lo by all 512 threads and
-// stored in the 128B-swizzled K-major layout the MMA reads (two stages of
-// A_hi, A_lo, B_hi, B_lo, 64 KB each, 1024-byte aligned); thread 0 issues
-// the slice's 3 products (A_lo B_hi, A_hi B_lo, A_hi B_hi) x 4 K steps of
-// tcgen05.mma kind::tf32 into one of two TMEM accumulators and commits to
-// that accumulator's mbarrier; every thread then adds its 32 accumulator
-// columns to float32 registers (round to nearest: one slice, 12 MMAs, per
-// TMEM accumulation), while the next slice is staged and issued.  The
-// finished tile goes through shared memory into the CUDA-core fragment
-// layout of tile_mma_simt, so every epilogue is shared.  Waits are bounded
-// (kTcWait cycles); a timeout sets the CTA's error flag, after which no
-// wait is attempted and the instance reports info = -1.
+// The same 128 x 128 tile on the tensor cores (configuration TC_BK).  K
+// slices of 32 float32 elements are copied from memory by cp.async into one
+// of two raw stages (32 KB each, two slices in flight), then split into TF32
+// hi / lo by all 512 threads and stored into the 128B-swizzled K-major layout
+// the MMA reads (one split stage of A_hi, A_lo, B_hi, B_lo, 64 KB, 1024-byte
+// aligned).  Thread 0 issues the slice's 3 products (A_lo B_hi, A_hi B_lo,
+// then A_hi B_hi) x 4 K steps of tcgen05.mma kind::tf32 into one of two TMEM
+// accumulators and commits to that accumulator's mbarrier; while they run,
+// every thread adds the previous slice's accumulator (its 32 columns) to
+// float32 registers (round to nearest: 12 MMAs per TMEM accumulation) and
+// the next raw slice lands.  The finished tile goes through shared memory
+// into the CUDA-core fragment layout of tile_mma_simt, so every epilogue is
+// shared.  Waits on the MMA barriers are bounded (kTcWait cycles); a timeout
+// sets the CTA's error flag, after which no wait is attempted and the
+// instance reports info = -1.
 // ---------------------------------------------------------------------------
 constexpr int TC_BK = 0;        // template value of the tensor-core configuration
-constexpr int TC_STAGE = 65536; // bytes of one stage
+constexpr int TC_STAGE = 65536; // bytes of the split stage
+constexpr int TC_RAW = 32768;   // bytes of one raw stage (A, then B)
 constexpr long long kTcWait = 4000000000LL;
 
 struct TcState {
@@ -250,29 +253,34 @@ __device__ __forceinline__ uint32_t sw128(int r, int k) {
   return (uint32_t)(r * 128 + ((((k >> 2) ^ (r & 7))) << 4) + ((k & 3) << 2));
 }
 
-// Element e (0..1023) of a slice, four floats: rows m..m+3 of column k when
-// the operand is stored K-major in memory (KM: a warp covers 8 columns x 16
-// rows, 64-byte segments, so that its swizzled scalar stores spread over 16
-// banks), else columns k..k+3 of row m (a warp covers 4 whole rows).
-__device__ __forceinline__ void tc_km_index(int e, int& k, int& m) {
-  const int w = e >> 5, l = e & 31;
-  k = (w & 3) * 8 + (l & 7);
-  m = (w >> 2) * 16 + 4 * (l >> 3);
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(tc::smem_u32(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
+// Raw copy of one operand's K slice (1024 16-byte chunks, two per thread):
+// rows of 32 floats (KM = false: raw[m * 32 + k]) or rows of 128 (KM = true:
+// raw[k * 128 + m]), both as they lie in memory (a warp copies 512
+// contiguous bytes per row group).
 template <bool KM>
-__device__ __forceinline__ void tc_load(const float* __restrict__ P, int ld, int r0, int k0,
-                                        float4 (&r)[2]) {
+__device__ __forceinline__ void tc_copy(const float* __restrict__ P, int ld, int r0, int k0,
+                                        float* raw) {
 #pragma unroll
   for (int v = 0; v < 2; ++v) {
     const int e = threadIdx.x + v * BNT;
     if constexpr (KM) {
-      int k, m;
-      tc_km_index(e, k, m);
-      r[v] = *reinterpret_cast<const float4*>(P + (int64_t)(k0 + k) * ld + r0 + m);
+      const int k = e >> 5, m = 4 * (e & 31);
+      cp_async16(raw + k * TT + m, P + (int64_t)(k0 + k) * ld + r0 + m);
     } else {
       const int m = e >> 3, k = 4 * (e & 7);
-      r[v] = *reinterpret_cast<const float4*>(P + (int64_t)(r0 + m) * ld + k0 + k);
+      cp_async16(raw + m * 32 + k, P + (int64_t)(r0 + m) * ld + k0 + k);
     }
   }
 }
@@ -281,36 +289,40 @@ __device__ __forceinline__ float4 tf32_hi4(float4 x) {
   return make_float4(tf32_rna_f(x.x), tf32_rna_f(x.y), tf32_rna_f(x.z), tf32_rna_f(x.w));
 }
 
+// Split of a raw slice into the swizzled hi / lo buffers: each thread forms
+// four consecutive k of one row m and stores them as one 16-byte chunk
+// (KM: lanes run over m, so the four column reads and the swizzled stores
+// are free of bank conflicts).
 template <bool KM>
-__device__ __forceinline__ void tc_store(char* hi, char* lo, const float4 (&r)[2]) {
+__device__ __forceinline__ void tc_split(const float* raw, char* hi, char* lo) {
 #pragma unroll
   for (int v = 0; v < 2; ++v) {
     const int e = threadIdx.x + v * BNT;
-    const float4 h = tf32_hi4(r[v]);
-    const float4 l = tf32_hi4(make_float4(r[v].x - h.x, r[v].y - h.y, r[v].z - h.z, r[v].w - h.w));
-    if constexpr (KM) {  // four rows of one column k
-      int k, m;
-      tc_km_index(e, k, m);
-      const float hv[4] = {h.x, h.y, h.z, h.w}, lv[4] = {l.x, l.y, l.z, l.w};
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const uint32_t o = sw128(m + u, k);
-        *reinterpret_cast<float*>(hi + o) = hv[u];
-        *reinterpret_cast<float*>(lo + o) = lv[u];
-      }
-    } else {  // one 16-byte chunk of row m
-      const int m = e >> 3, k = 4 * (e & 7);
-      const uint32_t o = sw128(m, k);
-      *reinterpret_cast<float4*>(hi + o) = h;
-      *reinterpret_cast<float4*>(lo + o) = l;
+    int m, k;
+    float4 x;
+    if constexpr (KM) {
+      m = e & (TT - 1);
+      k = 4 * (e >> 7);
+      x = make_float4(raw[k * TT + m], raw[(k + 1) * TT + m], raw[(k + 2) * TT + m],
+                      raw[(k + 3) * TT + m]);
+    } else {
+      m = e >> 3;
+      k = 4 * (e & 7);
+      x = *reinterpret_cast<const float4*>(raw + m * 32 + k);
     }
+    const float4 h = tf32_hi4(x);
+    const float4 l = tf32_hi4(make_float4(x.x - h.x, x.y - h.y, x.z - h.z, x.w - h.w));
+    const uint32_t o = sw128(m, k);
+    *reinterpret_cast<float4*>(hi + o) = h;
+    *reinterpret_cast<float4*>(lo + o) = l;
   }
 }
 
-__device__ __forceinline__ void tc_wait(int b) {
+// Wait for the n-th completion (from 0) of accumulator b's barrier.
+__device__ __forceinline__ void tc_wait(int b, uint32_t n) {
   TcState& st = tc_state();
   if (*(volatile int*)&st.err) return;
-  if (!tc::mbar_wait_own(&st.bar[b], st.n[b] & 1u, kTcWait)) st.err = 1;
+  if (!tc::mbar_wait_own(&st.bar[b], n & 1u, kTcWait)) st.err = 1;
 }
 
 // The tensor-core staging region: the start of the dynamic shared memory,
@@ -318,7 +330,9 @@ __device__ __forceinline__ void tc_wait(int b) {
 // and the leaf's storage, neither of which is live during a tile product (the
 // epilogue runs after the tile has been moved to registers).  Kept within the
 // leaf's footprint so that the L1 share of the SM does not shrink.
-__host__ __device__ constexpr size_t tc_region_bytes() { return 1024 + 2 * (size_t)TC_STAGE; }
+__host__ __device__ constexpr size_t tc_region_bytes() {
+  return 1024 + (size_t)TC_STAGE + 2 * (size_t)TC_RAW;
+}
 
 // Kernel start (every thread): barriers, counters, 256 TMEM columns.
 __device__ void tc_setup() {
@@ -369,26 +383,59 @@ __device__ void tile_mma_tc(const float* __restrict__ A, int lda, const float* _
   TcState& st = tc_state();
   char* base =
       reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(S) + 1023) & ~uintptr_t(1023));
+  char* sp = base;  // split stage: A_hi, A_lo, B_hi, B_lo
+  auto raw = [&](int sl) {  // raw stage of slice sl
+    return reinterpret_cast<float*>(base + TC_STAGE + (sl & 1) * TC_RAW);
+  };
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nsl = (khi - klo) / 32;
+  // completions consumed per accumulator (the same in every thread; two
+  // scalars, not an array indexed at run time, which would live in memory)
+  uint32_t nb0 = st.n[0], nb1 = st.n[1];
   float c32[32];
 #pragma unroll
   for (int k = 0; k < 32; ++k) c32[k] = 0.f;
-  // K slices are loaded into registers one slice ahead (a second register
-  // set, two slices ahead, measured slower: its spills reached every path
-  // of the kernel)
-  float4 ra[2], rb[2];
-  auto stage = [&](int sl, const float4(&qa)[2], const float4(&qb)[2]) {
-    // smem of slice sl, the MMAs issued and committed
-    char* sb = base + (sl & 1) * TC_STAGE;
-    tc_store<AKM>(sb, sb + 16384, qa);
-    tc_store<BKM>(sb + 32768, sb + 49152, qb);
+  auto copy = [&](int sl) {  // raw stage sl & 1; one commit group per call
+    if (sl < nsl) {
+      float* r = raw(sl);
+      tc_copy<AKM>(A, lda, i0, klo + 32 * sl, r);
+      tc_copy<BKM>(B, ldb, j0, klo + 32 * sl, r + TT * 32);
+    }
+    cp_async_commit();
+  };
+  auto drain = [&](int b) {  // accumulator b, complete, into c32
+    const uint32_t ta =
+        st.tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(b * 128 + 32 * (warp >> 2));
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {  // two 16-column loads: fewer live registers
+      uint32_t v[16];
+      tc::tmem_ld16_nowait(ta + 16 * h, v);
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+      for (int k = 0; k < 16; ++k) c32[16 * h + k] += __uint_as_float(v[k]);
+    }
+  };
+  if (nsl > 0) {
+    copy(0);
+    copy(1);
+  }
+  for (int sl = 0; sl < nsl; ++sl) {
+    cp_async_wait<1>();  // this thread's copies of slice sl have landed
+    __syncthreads();     // everyone's; the accumulator drained last iteration is free
+    if (sl > 0) {        // the MMAs of slice sl - 1 read the split stage: wait for them
+      tc_wait((sl - 1) & 1, ((sl - 1) & 1) ? nb1 : nb0);
+      tc::tc_fence_after();
+    }
+    const float* r = raw(sl);
+    tc_split<AKM>(r, sp, sp + 16384);
+    tc_split<BKM>(r + TT * 32, sp + 32768, sp + 49152);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     tc::tc_fence_before();
-    __syncthreads();
+    __syncthreads();  // the split stage is written; raw stage sl & 1 is free
+    copy(sl + 2);
     if (threadIdx.x == 0) {
       tc::tc_fence_after();
-      const uint32_t a = tc::smem_u32(sb);
+      const uint32_t a = tc::smem_u32(sp);
       const uint64_t ahi = tc::sdesc<128>(a), alo = tc::sdesc<128>(a + 16384);
       const uint64_t bhi = tc::sdesc<128>(a + 32768), blo = tc::sdesc<128>(a + 49152);
       const uint32_t tacc = st.tmem + (uint32_t)((sl & 1) * 128);
@@ -406,37 +453,25 @@ __device__ void tile_mma_tc(const float* __restrict__ A, int lda, const float* _
       tc::mma_commit(&st.bar[sl & 1]);
       st.issued[sl & 1] += 1;
     }
-  };
-  auto drain = [&](int sl) {
-    const int b = sl & 1;
-    tc_wait(b);
-    tc::tc_fence_after();
-    const uint32_t ta =
-        st.tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(b * 128 + 32 * (warp >> 2));
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {  // two 16-column loads: fewer live registers
-      uint32_t v[16];
-      tc::tmem_ld16_nowait(ta + 16 * h, v);
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-      for (int k = 0; k < 16; ++k) c32[16 * h + k] += __uint_as_float(v[k]);
+    if (sl > 0) {  // slice sl - 1's accumulator, complete since the wait above
+      drain((sl - 1) & 1);
+      if ((sl - 1) & 1) ++nb1; else ++nb0;
+      tc::tc_fence_before();  // ordered before the next barrier, after which it is rewritten
     }
-    tc::tc_fence_before();
-    __syncthreads();  // the accumulator is read: the next MMAs into it may start
-    if (threadIdx.x == 0) st.n[b] += 1;
-  };
-  if (nsl > 0) {
-    tc_load<AKM>(A, lda, i0, klo, ra);
-    tc_load<BKM>(B, ldb, j0, klo, rb);
-    stage(0, ra, rb);
   }
-  for (int sl = 0; sl < nsl; ++sl) {
-    if (sl + 1 < nsl) {  // the next slice's stage was last read by slice sl - 1, drained below
-      tc_load<AKM>(A, lda, i0, klo + 32 * (sl + 1), ra);
-      tc_load<BKM>(B, ldb, j0, klo + 32 * (sl + 1), rb);
-      stage(sl + 1, ra, rb);
-    }
-    drain(sl);
+  cp_async_wait<0>();
+  if (nsl > 0) {
+    const int b = (nsl - 1) & 1;
+    tc_wait(b, b ? nb1 : nb0);
+    tc::tc_fence_after();
+    drain(b);
+    if (b) ++nb1; else ++nb0;
+    tc::tc_fence_before();
+  }
+  __syncthreads();  // every thread past its waits and loads: the counters, and the stages
+  if (threadIdx.x == 0) {
+    st.n[0] = nb0;
+    st.n[1] = nb1;
   }
   // the tile through shared memory into the CUDA-core fragment layout
   float* Cs = reinterpret_cast<float*>(base);
