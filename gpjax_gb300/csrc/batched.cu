@@ -17,9 +17,9 @@
 //
 // Per instance (padded to n_pad, a multiple of 128, with an identity block):
 //   Gram: lower 128-blocks of Sigma (float32) and its float64 diagonal;
-//   factor: right-looking over 128-wide panels, each diagonal block factored
-//     and inverted by leaf_chol_inv_body, the panel below solved by
-//     substitution, A22 -= X X^T;
+//   factor: left-looking over 128-wide block columns: the column updated by
+//     one product over all earlier panels, its diagonal block factored and
+//     inverted by leaf_chol_inv_body, the panel below solved by substitution;
 //   inverse: M = L^-1 by the recursive merge M21 = -M22 (L21 M11);
 //   alpha = M^T M diff, refined twice against float-float residuals;
 //   W = M^T M tile by tile, reduced at once against dK/dtheta (adjoint).
@@ -376,7 +376,7 @@ __device__ void tc_teardown() {
   }
 }
 
-template <bool AKM, bool BKM>
+template <bool AKM, bool BKM, bool ACC_IN>
 __device__ void tile_mma_tc(const float* __restrict__ A, int lda, const float* __restrict__ B,
                             int ldb, int i0, int j0, int klo, int khi, float* S,
                             float (&acc)[8][4]) {
@@ -393,8 +393,27 @@ __device__ void tile_mma_tc(const float* __restrict__ A, int lda, const float* _
   // scalars, not an array indexed at run time, which would live in memory)
   uint32_t nb0 = st.n[0], nb1 = st.n[1];
   float c32[32];
+  if constexpr (ACC_IN) {  // the incoming accumulator (fragment layout) to the row layout
+    float* Cs = reinterpret_cast<float*>(base);
 #pragma unroll
-  for (int k = 0; k < 32; ++k) c32[k] = 0.f;
+    for (int u = 0; u < 8; ++u)
+      *reinterpret_cast<float4*>(Cs + tile_row(u) * SLD + tile_col(0)) =
+          make_float4(acc[u][0], acc[u][1], acc[u][2], acc[u][3]);
+    __syncthreads();
+    const float* row = Cs + (32 * (warp & 3) + lane) * SLD + 32 * (warp >> 2);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const float4 t = *reinterpret_cast<const float4*>(row + 4 * q);
+      c32[4 * q] = t.x;
+      c32[4 * q + 1] = t.y;
+      c32[4 * q + 2] = t.z;
+      c32[4 * q + 3] = t.w;
+    }
+    __syncthreads();
+  } else {
+#pragma unroll
+    for (int k = 0; k < 32; ++k) c32[k] = 0.f;
+  }
   auto copy = [&](int sl) {  // raw stage sl & 1; one commit group per call
     if (sl < nsl) {
       float* r = raw(sl);
@@ -492,23 +511,25 @@ __device__ void tile_mma_tc(const float* __restrict__ A, int lda, const float* _
   __syncthreads();
 }
 
-template <int BK, bool AKM, bool BKM>
+// acc += the tile's product (ACC_IN: acc holds a starting value; else zeros)
+template <int BK, bool AKM, bool BKM, bool ACC_IN = false>
 __device__ __forceinline__ void tile_mma(const float* __restrict__ A, int lda,
                                          const float* __restrict__ B, int ldb, int i0, int j0,
                                          int klo, int khi, float* S, float (&acc)[8][4]) {
   if constexpr (BK == TC_BK)
-    tile_mma_tc<AKM, BKM>(A, lda, B, ldb, i0, j0, klo, khi, S, acc);
+    tile_mma_tc<AKM, BKM, ACC_IN>(A, lda, B, ldb, i0, j0, klo, khi, S, acc);
   else
     tile_mma_simt<BK, AKM, BKM>(A, lda, B, ldb, i0, j0, klo, khi, S, acc);
 }
 
 // A product over tm x tn output tiles (the lower ones when lower), one tile
 // at a time on the whole CTA.  kr(i0, j0, klo, khi) gives a tile's K range
-// (the triangles of the operands), ep(i0, j0, acc, S) consumes it (S: the
-// staging area, free until the next barrier).
-template <int BK, bool AKM, bool BKM, class KR, class EP>
-__device__ void product(int tm, int tn, bool lower, const float* A, int lda, const float* B,
-                        int ldb, KR kr, EP ep, float* smem) {
+// (the triangles of the operands), init(i0, j0, acc) the accumulator's
+// starting value when ACC_IN (else zeros), ep(i0, j0, acc, S) consumes it (S:
+// the staging area, free until the next barrier).
+template <int BK, bool AKM, bool BKM, bool ACC_IN, class KR, class IN, class EP>
+__device__ void product_from(int tm, int tn, bool lower, const float* A, int lda,
+                             const float* B, int ldb, KR kr, IN init, EP ep, float* smem) {
   const int nt = lower ? tm * (tm + 1) / 2 : tm * tn;
   for (int t = 0; t < nt; ++t) {
     int I, J;
@@ -521,14 +542,25 @@ __device__ void product(int tm, int tn, bool lower, const float* A, int lda, con
     int klo, khi;
     kr(I * TT, J * TT, klo, khi);
     float acc[8][4];
+    if constexpr (ACC_IN) {
+      init(I * TT, J * TT, acc);
+    } else {
 #pragma unroll
-    for (int u = 0; u < 8; ++u)
+      for (int u = 0; u < 8; ++u)
 #pragma unroll
-      for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
-    tile_mma<BK, AKM, BKM>(A, lda, B, ldb, I * TT, J * TT, klo, khi, smem, acc);
+        for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
+    }
+    tile_mma<BK, AKM, BKM, ACC_IN>(A, lda, B, ldb, I * TT, J * TT, klo, khi, smem, acc);
     ep(I * TT, J * TT, acc, smem);
   }
   __syncthreads();
+}
+
+template <int BK, bool AKM, bool BKM, class KR, class EP>
+__device__ void product(int tm, int tn, bool lower, const float* A, int lda, const float* B,
+                        int ldb, KR kr, EP ep, float* smem) {
+  product_from<BK, AKM, BKM, false>(
+      tm, tn, lower, A, lda, B, ldb, kr, [](int, int, float(&)[8][4]) {}, ep, smem);
 }
 
 // C tile (rows i0.., columns j0..) = alpha acc (+ C when add), float4 rows
@@ -685,19 +717,53 @@ __device__ void panel_solve(const float* __restrict__ Ap, float* __restrict__ Xp
 }
 
 // Cholesky + inverse of the padded matrix.
-//  * Factor: right-looking over 128-wide panels.  The leaf factors and inverts
-//    the diagonal block (pivots from the float64 diagonal track); the panel
-//    below is solved by substitution against L_kk (panel_solve), the
-//    diagonal track loses its row sums of squares, and A22 -= X X^T.  (The
-//    recursive form L21 = A21 M11^T with a recursively formed M11 amplified
-//    rounding by the condition number of L11: on ill-conditioned RBF
-//    instances its log-determinant erred ~10x more than this panel form.)
+//  * Factor: left-looking over 128-wide block columns.  Block column o is
+//    brought up to date by ONE product, A[o:, o:o+128] -= L[o:, :o]
+//    L[o:o+128, :o]^T (K = o: every earlier panel at once, each output tile
+//    read and written once); the leaf then factors and inverts the diagonal
+//    block (pivots from the float64 diagonal track), the panel below is
+//    solved by substitution against L_kk (panel_solve) and the diagonal
+//    track loses its row sums of squares.  (The right-looking order,
+//    A22 -= X X^T after every panel, rewrote the trailing matrix once per
+//    panel: its read-modify-write traffic bound the factor with one CTA per
+//    SM.  The recursive form L21 = A21 M11^T with a recursively formed M11
+//    amplified rounding by the condition number of L11: on ill-conditioned
+//    RBF instances its log-determinant erred ~10x more than this panel
+//    form.)
 //  * Inverse: M = L^-1 by the recursion's merge step, post-order over the
 //    tree with 128 leaves and left child h = 128 * ceil(sz / 256):
 //    T = L21 M11, M21 = -M22 T (node_up), every thread on the same path.
 template <int BK>
 __device__ void chol_inv(const Slot& S, int ld, int np, int* info, float* smem) {
   for (int o = 0; o < np; o += TT) {
+    if (o > 0) {  // block column o minus the products of the panels to its left
+      const float* Lr = S.L + (int64_t)o * ld;  // rows o.. of L, columns < o
+      float* Ac = S.A + (int64_t)o * ld + o;
+      // the accumulator starts at -A and takes the panels in order, so
+      // every rounding is relative to the partly reduced entry as in the
+      // right-looking order (summing the panels first and subtracting once
+      // lost a factor ~6 of log-determinant accuracy on an n = 1500 RBF
+      // instance)
+      product_from<BK, false, false, true>(
+          (np - o) / TT, 1, false, Lr, ld, Lr, ld,
+          [&](int, int, int& klo, int& khi) { klo = 0; khi = o; },
+          [&](int i0, int j0, float(&acc)[8][4]) {
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+              const float4 c = *reinterpret_cast<const float4*>(
+                  Ac + (int64_t)(i0 + tile_row(u)) * ld + j0 + tile_col(0));
+              acc[u][0] = -c.x;
+              acc[u][1] = -c.y;
+              acc[u][2] = -c.z;
+              acc[u][3] = -c.w;
+            }
+          },
+          [&](int i0, int j0, const float (&acc)[8][4], float*) {
+            put_tile(Ac, ld, i0, j0, acc, -1.f, false);
+          },
+          smem);
+    }
+    __syncthreads();  // the column and track_rows' dtrack writes before the leaf reads them
     leaf_chol_inv_body(S.A, ld, o, S.dtrack, S.logdiag, info, LeafOutPlain{S.M, ld, o}, smem);
     __syncthreads();
     const int R = np - o - TT;
@@ -706,15 +772,6 @@ __device__ void chol_inv(const Slot& S, int ld, int np, int* info, float* smem) 
     panel_solve(S.A + (int64_t)(o + TT) * ld + o, Lp, ld, R, smem);
     __syncthreads();
     track_rows(S.L, ld, o + TT, R, o, TT, S.dtrack);
-    float* A22 = S.A + (int64_t)(o + TT) * ld + o + TT;
-    product<BK, false, false>(
-        R / TT, R / TT, true, Lp, ld, Lp, ld,
-        [&](int, int, int& klo, int& khi) { klo = 0; khi = TT; },
-        [&](int i0, int j0, const float (&acc)[8][4], float*) {
-          put_tile(A22, ld, i0, j0, acc, -1.f, true);
-        },
-        smem);
-    __syncthreads();  // track_rows' dtrack writes before the next leaf reads them
   }
   constexpr int DEPTH = 8;  // np <= 4096: at most 6 levels
   int so[DEPTH], ss[DEPTH], sst[DEPTH];
