@@ -806,8 +806,8 @@ __device__ __forceinline__ float dot4(float4 m, float4 v, float s) {
 
 // z = M r (lower), one warp per row, float accumulation.  The two GEMVs of a
 // solve read M from memory (np^2 / 2 floats each) with one CTA per SM, so
-// they are written for bytes in flight: four independent 16-byte loads per
-// lane before the first FMA.
+// they are written for bytes in flight: eight (then four) independent
+// 16-byte loads per lane before the first FMA.
 __device__ void gemv_lower(const float* M, int ld, int np, const float* r, float* z) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int i = warp; i < np; i += BNT / 32) {
@@ -816,6 +816,18 @@ __device__ void gemv_lower(const float* M, int ld, int np, const float* r, float
     int k = lane * 4;
     // entries past i inside the float4 that holds i are zeros of M's
     // diagonal block; every load starts at k <= i
+    for (; k + 896 <= i; k += 1024) {
+      float4 m[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) m[q] = *reinterpret_cast<const float4*>(row + k + 128 * q);
+#pragma unroll
+      for (int q = 0; q < 8; q += 4) {
+        s0 = dot4(m[q], *reinterpret_cast<const float4*>(r + k + 128 * q), s0);
+        s1 = dot4(m[q + 1], *reinterpret_cast<const float4*>(r + k + 128 * (q + 1)), s1);
+        s2 = dot4(m[q + 2], *reinterpret_cast<const float4*>(r + k + 128 * (q + 2)), s2);
+        s3 = dot4(m[q + 3], *reinterpret_cast<const float4*>(r + k + 128 * (q + 3)), s3);
+      }
+    }
     for (; k + 384 <= i; k += 512) {
       const float4 m0 = *reinterpret_cast<const float4*>(row + k);
       const float4 m1 = *reinterpret_cast<const float4*>(row + k + 128);
@@ -846,6 +858,22 @@ __device__ void gemv_upper_t(const float* M, int ld, int np, const float* z, dou
     const float* col = M + c0 + 4 * lane;
     float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f), a1 = a0;
     int i = c0 + warp;
+    for (; i + 7 * NW < np; i += 8 * NW) {
+      float4 m[8];
+      float zz[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        m[q] = *reinterpret_cast<const float4*>(col + (int64_t)(i + q * NW) * ld);
+        zz[q] = z[i + q * NW];
+      }
+#pragma unroll
+      for (int q = 0; q < 8; q += 2) {
+        a0.x = fmaf(m[q].x, zz[q], a0.x); a0.y = fmaf(m[q].y, zz[q], a0.y);
+        a0.z = fmaf(m[q].z, zz[q], a0.z); a0.w = fmaf(m[q].w, zz[q], a0.w);
+        a1.x = fmaf(m[q + 1].x, zz[q + 1], a1.x); a1.y = fmaf(m[q + 1].y, zz[q + 1], a1.y);
+        a1.z = fmaf(m[q + 1].z, zz[q + 1], a1.z); a1.w = fmaf(m[q + 1].w, zz[q + 1], a1.w);
+      }
+    }
     for (; i + 3 * NW < np; i += 4 * NW) {
       const float4 m0 = *reinterpret_cast<const float4*>(col + (int64_t)i * ld);
       const float4 m1 = *reinterpret_cast<const float4*>(col + (int64_t)(i + NW) * ld);
