@@ -1190,29 +1190,46 @@ __device__ bool instance_front(const BatchArgs& a, const BatchInst& I, const Slo
     S.M[(int64_t)i * ld + (i / TT) * TT + c] = 0.f;
   }
   __syncthreads();
-  // Gram: lower 128-blocks (diagonal blocks in full), identity past n
+  // Gram: lower 128-blocks (diagonal blocks in full), identity past n.  The
+  // block's row and column inputs are staged in shared memory with an odd
+  // row stride (a warp reads 32 consecutive columns' coordinates without
+  // bank conflicts); the kernel kind is resolved outside the loops.
   {
     const int nb = np / TT, nt = nb * (nb + 1) / 2;
-    for (int t = 0; t < nt; ++t) {
-      int bi, bj;
-      tri_index(t, bi, bj);
-      for (int e = threadIdx.x; e < TT * TT; e += BNT) {
-        const int i = bi * TT + e / TT, j = bj * TT + e % TT;
-        float v;
-        if (i >= n || j >= n) {
-          v = i == j ? 1.f : 0.f;
-        } else {
-          float sq = 0.f;
-          for (int k = 0; k < d; ++k) {
-            const float df = S.xs[i * d + k] - S.xs[j * d + k];
-            sq = fmaf(df, df, sq);
-          }
-          v = kval<float>(I.kind, sq, s2, ka);
-          if (i == j) v = (float)((double)v + noise_diag);
+    const int sd = d | 1;
+    float* gxi = smem;              // [TT][sd]
+    float* gxj = smem + TT * (BDM + 1);
+    with_kind(I.kind, [&](auto kind_c) {
+      constexpr int KIND = decltype(kind_c)::value;
+      for (int t = 0; t < nt; ++t) {
+        int bi, bj;
+        tri_index(t, bi, bj);
+        for (int e = threadIdx.x; e < TT * d; e += BNT) {
+          const int r = e / d, k = e % d;
+          gxi[r * sd + k] = bi * TT + r < n ? S.xs[(bi * TT + r) * d + k] : 0.f;
+          gxj[r * sd + k] = bj * TT + r < n ? S.xs[(bj * TT + r) * d + k] : 0.f;
         }
-        S.A[(int64_t)i * ld + j] = v;
+        __syncthreads();
+        for (int e = threadIdx.x; e < TT * TT; e += BNT) {
+          const int il = e / TT, jl = e % TT;
+          const int i = bi * TT + il, j = bj * TT + jl;
+          float v;
+          if (i >= n || j >= n) {
+            v = i == j ? 1.f : 0.f;
+          } else {
+            float sq = 0.f;
+            for (int k = 0; k < d; ++k) {
+              const float df = gxi[il * sd + k] - gxj[jl * sd + k];
+              sq = fmaf(df, df, sq);
+            }
+            v = kval<float>(KIND, sq, s2, ka);
+            if (i == j) v = (float)((double)v + noise_diag);
+          }
+          S.A[(int64_t)i * ld + j] = v;
+        }
+        __syncthreads();
       }
-    }
+    });
   }
   __syncthreads();
   chol_inv<BK>(S, ld, np, I.info, smem);
