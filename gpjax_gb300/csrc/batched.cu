@@ -935,41 +935,55 @@ __device__ __forceinline__ void ff_add_b(float& hi, float& lo, float a) {
 
 // r = diff - Sigma alpha for rows < n (zeros past n) into rres (float64),
 // Sigma regenerated from the scaled inputs, products summed in float-float.
-// ah / al: alpha split into float hi / lo parts (shared memory).
+// ah / al: alpha split into float hi / lo parts (shared memory).  The
+// columns go by chunks of RCH inputs staged in shared memory (gx, odd row
+// stride); a warp takes a row, its lanes the chunk's columns, and each
+// row's chunk sums add up in float64 in rres.
+constexpr int RCH = 512;
 __device__ void residual(const BatchInst& I, const Slot& S, int np, float s2, float ka,
-                         double noise_diag, const float* ah, const float* al, double* rres) {
+                         double noise_diag, const float* ah, const float* al, double* rres,
+                         float* gx) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int n = I.n, d = I.d;
-  for (int i = warp; i < np; i += BNT / 32) {
-    if (i >= n) {
-      if (lane == 0) rres[i] = 0.0;
-      continue;
-    }
-    float xi[BDM];
+  const int n = I.n, d = I.d, sd = d | 1;
+  for (int i = threadIdx.x; i < np; i += BNT) rres[i] = 0.0;
+  with_kind(I.kind, [&](auto kind_c) {
+    constexpr int KIND = decltype(kind_c)::value;
+    for (int c0 = 0; c0 < n; c0 += RCH) {
+      const int cn = min(RCH, n - c0);
+      __syncthreads();  // the previous chunk is done with gx (and rres is zeroed)
+      for (int e = threadIdx.x; e < cn * d; e += BNT)
+        gx[(e / d) * sd + e % d] = S.xs[c0 * d + e];
+      __syncthreads();
+      for (int i = warp; i < n; i += BNT / 32) {
+        float xi[BDM];
 #pragma unroll
-    for (int k = 0; k < BDM; ++k) xi[k] = k < d ? S.xs[i * d + k] : 0.f;
-    float sh = 0.f, sl = 0.f;
-    for (int j = lane; j < n; j += 32) {
-      float sq = 0.f;
+        for (int k = 0; k < BDM; ++k) xi[k] = k < d ? S.xs[i * d + k] : 0.f;
+        float sh = 0.f, sl = 0.f;
+        for (int jl = lane; jl < cn; jl += 32) {
+          const float* xj = gx + jl * sd;
+          float sq = 0.f;
 #pragma unroll
-      for (int k = 0; k < BDM; ++k) {
-        if (k < d) {
-          const float df = xi[k] - S.xs[j * d + k];
-          sq = fmaf(df, df, sq);
+          for (int k = 0; k < BDM; ++k) {
+            if (k < d) {
+              const float df = xi[k] - xj[k];
+              sq = fmaf(df, df, sq);
+            }
+          }
+          const float kv = kval<float>(KIND, sq, s2, ka);
+          const int j = c0 + jl;
+          const float p = kv * ah[j];
+          const float pe = fmaf(kv, ah[j], -p);
+          ff_add_b(sh, sl, p);
+          sl = fmaf(kv, al[j], sl + pe);
         }
+        const double t = warp_sum((double)sh + (double)sl);
+        if (lane == 0) rres[i] += t;
       }
-      const float kv = kval<float>(I.kind, sq, s2, ka);
-      const float p = kv * ah[j];
-      const float pe = fmaf(kv, ah[j], -p);
-      ff_add_b(sh, sl, p);
-      sl = fmaf(kv, al[j], sl + pe);
     }
-    double s = warp_sum((double)sh + (double)sl);
-    if (lane == 0) {
-      s += noise_diag * S.alpha[i];  // the noise and jitter on the diagonal
-      rres[i] = S.diff[i] - s;
-    }
-  }
+  });
+  __syncthreads();
+  for (int i = threadIdx.x; i < np; i += BNT)
+    rres[i] = i < n ? S.diff[i] - (rres[i] + noise_diag * S.alpha[i]) : 0.0;
 }
 
 // One W tile (shared memory, row stride WLD) contracted against dK/dtheta:
@@ -1244,7 +1258,8 @@ __device__ bool instance_front(const BatchArgs& a, const BatchInst& I, const Slo
   float* ah = smem;          // [np] alpha hi
   float* al = smem + np;     // [np] alpha lo
   double* rres = reinterpret_cast<double*>(smem + 2 * np);  // [np]
-  float* red = smem + 4 * np;  // [16][128] GEMV partial sums
+  float* red = smem + 4 * np;  // [16][128] GEMV partial sums, then the residual's
+                               // staged inputs [RCH][BDM + 1]
   solve_apply(S, ld, np, S.diff, false, red);
   for (int it = 0; it < 2; ++it) {
     for (int i = threadIdx.x; i < np; i += BNT) {
@@ -1254,7 +1269,7 @@ __device__ bool instance_front(const BatchArgs& a, const BatchInst& I, const Slo
       al[i] = (float)(v - (double)hi);
     }
     __syncthreads();
-    residual(I, S, np, s2, ka, noise_diag, ah, al, rres);
+    residual(I, S, np, s2, ka, noise_diag, ah, al, rres, red + 16 * TT);
     __syncthreads();
     solve_apply(S, ld, np, rres, true, red);
   }
@@ -1398,8 +1413,8 @@ size_t batch_smem_bytes(int np_max) {
   // leaf, the refinement vectors
   const size_t prod = std::max((size_t)prod_floats() * sizeof(float), tc_region_bytes());
   const size_t leaf = leaf_smem_bytes();
-  const size_t refine =
-      (size_t)np_max * (2 * sizeof(float) + sizeof(double)) + (size_t)16 * TT * sizeof(float);
+  const size_t refine = (size_t)np_max * (2 * sizeof(float) + sizeof(double)) +
+                        (size_t)(16 * TT + RCH * (BDM + 1)) * sizeof(float);
   return std::max(std::max(prod, leaf), refine);
 }
 
