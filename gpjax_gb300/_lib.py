@@ -66,6 +66,7 @@ SIGNATURES = {
     "gpk_batch_plan_config": (_c_int, [_c_ptr, _c_i64]),
     "gpk_batch_plan_config_count": (_c_int, []),
     "gpk_batch_plan_force_config": (_c_int, [_c_ptr, _c_int]),
+    "gpk_batch_plan_selftest_stall": (_c_int, [_c_ptr, ctypes.c_longlong]),
     "gpk_batch_plan_execute": (_c_int, [_c_ptr, _c_ptr, _c_size, _c_ptr]),
     "gpk_batch_plan_destroy": (_c_int, [_c_ptr]),
     "gpk_conjugate_loocv_workspace_bytes": (_c_size, [_c_i64, _c_int]),

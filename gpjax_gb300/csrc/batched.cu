@@ -88,6 +88,7 @@ struct BatchArgs {
   double jitter;
   int force_cfg;     // >= 0: every instance with this configuration (autotuner trials)
   long long wait_cycles;  // bound on an idle CTA's wait for published tiles
+  long long tc_stall;     // self-test (0: off), see tc_wait
 };
 
 struct Slot {
@@ -238,10 +239,13 @@ constexpr long long kTcWait = 4000000000LL;
 
 struct TcState {
   uint64_t bar[2];  // MMA completion, one per accumulator
+  uint64_t never;   // self-test: a barrier nothing arrives on
+  long long stall;  // self-test: > 0 makes the CTA's first MMA wait also wait on `never`
   uint32_t n[2];    // completions consumed so far (parity = n & 1)
   uint32_t issued[2];  // commits made
   uint32_t tmem;    // base of 256 TMEM columns (two 128-column accumulators)
   int err;          // a wait timed out
+  int stalled;      // the self-test wait ran out
 };
 __device__ __forceinline__ TcState& tc_state() {
   __shared__ TcState st;
@@ -318,11 +322,22 @@ __device__ __forceinline__ void tc_split(const float* raw, char* hi, char* lo) {
   }
 }
 
-// Wait for the n-th completion (from 0) of accumulator b's barrier.
+// Wait for the n-th completion (from 0) of accumulator b's barrier.  With
+// the self-test on, the CTA's first wait first waits (st.stall cycles) on a
+// barrier that nothing arrives on and records that it ran out; the MMAs are
+// still waited for, so none is in flight when the CTA moves on.
 __device__ __forceinline__ void tc_wait(int b, uint32_t n) {
   TcState& st = tc_state();
   if (*(volatile int*)&st.err) return;
+  if (st.stall > 0 && !*(volatile int*)&st.stalled) {
+    if (!tc::mbar_wait_own(&st.never, 0u, st.stall)) st.stalled = 1;
+  }
   if (!tc::mbar_wait_own(&st.bar[b], n & 1u, kTcWait)) st.err = 1;
+}
+
+__device__ __forceinline__ bool tc_failed() {
+  TcState& st = tc_state();
+  return *(volatile int*)&st.err || *(volatile int*)&st.stalled;
 }
 
 // The tensor-core staging region: the start of the dynamic shared memory,
@@ -335,14 +350,17 @@ __host__ __device__ constexpr size_t tc_region_bytes() {
 }
 
 // Kernel start (every thread): barriers, counters, 256 TMEM columns.
-__device__ void tc_setup() {
+__device__ void tc_setup(long long stall) {
   TcState& st = tc_state();
   if (threadIdx.x == 0) {
     tc::mbar_init(&st.bar[0], 1);
     tc::mbar_init(&st.bar[1], 1);
+    tc::mbar_init(&st.never, 1);
+    st.stall = stall;
     st.n[0] = st.n[1] = 0;
     st.issued[0] = st.issued[1] = 0;
     st.err = 0;
+    st.stalled = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if ((threadIdx.x >> 5) == 0) {
@@ -1299,7 +1317,7 @@ __global__ void __launch_bounds__(BNT, 1) batch_mll_kernel(const __grid_constant
     s_own = -1;
     s_wait0 = -1;
   }
-  tc_setup();
+  tc_setup(a.tc_stall);
   for (;;) {
     if (threadIdx.x == 0) {
       int mode = 0, id = -1, tile = -1;
@@ -1372,7 +1390,7 @@ __global__ void __launch_bounds__(BNT, 1) batch_mll_kernel(const __grid_constant
       bool failed = cfg == 0   ? instance_front<16>(a, s_inst, s_slot, smem)
                     : cfg == 1 ? instance_front<32>(a, s_inst, s_slot, smem)
                                : instance_front<TC_BK>(a, s_inst, s_slot, smem);
-      if (tc_state().err) {  // a tensor-core wait timed out: the instance fails
+      if (tc_failed()) {  // a tensor-core wait timed out: the instance fails
         __syncthreads();
         if (threadIdx.x == 0) *s_inst.info = -1;
         failed = true;
@@ -1390,7 +1408,7 @@ __global__ void __launch_bounds__(BNT, 1) batch_mll_kernel(const __grid_constant
           cfg == 0   ? adjoint_tile<16>(a, id, s_inst, s_slot, s_tile, smem, s_red)
           : cfg == 1 ? adjoint_tile<32>(a, id, s_inst, s_slot, s_tile, smem, s_red)
                      : adjoint_tile<TC_BK>(a, id, s_inst, s_slot, s_tile, smem, s_red);
-      if (tc_state().err && threadIdx.x == 0) atomicExch(s_inst.info, -1);
+      if (tc_failed() && threadIdx.x == 0) atomicExch(s_inst.info, -1);
       if (last) finish_instance(a, s_inst, s_slot, false, s_red + GPK_MAX_D + 2 + 16 * 18);
     }
     __syncthreads();  // everyone is done with the shared descriptors before thread 0 rewrites them
@@ -1440,6 +1458,7 @@ struct gpk_batch_plan_s {
   int* d_state = nullptr;       // head, published[count], next_tile[count], tiles_done[count]
   double* d_tpart = nullptr;    // per-tile gradient partials
   int force_cfg = -1;           // >= 0: every instance runs this configuration
+  long long tc_stall = 0;       // self-test of the bounded tensor-core waits (0: off)
 };
 
 namespace {
@@ -1467,6 +1486,7 @@ cudaError_t launch_batch(const gpk_batch_plan_s& P, void* ws, int force_cfg, int
   a.jitter = P.jitter;
   a.force_cfg = force_cfg;
   a.wait_cycles = kIdleWaitCycles;
+  a.tc_stall = P.tc_stall;
   // instances outside the queue (autotuner trials) count as published with
   // no tiles: 1 in published[], a huge next_tile
   cudaError_t e = cudaMemsetAsync(P.d_state, 0, sizeof(int) * (1 + 3 * (size_t)P.count), s);
@@ -1672,6 +1692,12 @@ extern "C" int gpk_batch_plan_config_count(void) { return NCFG; }
 extern "C" gpk_status gpk_batch_plan_force_config(gpk_batch_plan plan, int cfg) {
   if (!plan || cfg < -1 || cfg >= NCFG) return GPK_ERR_BAD_ARG;
   plan->force_cfg = cfg;
+  return GPK_OK;
+}
+
+extern "C" gpk_status gpk_batch_plan_selftest_stall(gpk_batch_plan plan, long long cycles) {
+  if (!plan || cycles < 0 || cycles > kIdleWaitCycles) return GPK_ERR_BAD_ARG;
+  plan->tc_stall = cycles;
   return GPK_OK;
 }
 

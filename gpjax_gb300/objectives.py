@@ -337,6 +337,13 @@ class BatchPlan:
         (``-1``: the tuned configurations again)."""
         _lib.call("gpk_batch_plan_force_config", self._handle, int(cfg))
 
+    def selftest_stall(self, cycles: int):
+        """Self-test of the tensor-core configuration's bounded waits: with
+        ``cycles > 0`` the first MMA wait of every CTA also waits that many SM
+        clocks on a barrier nothing arrives on, and its instances report
+        ``info = -1`` (``0`` turns it off)."""
+        _lib.call("gpk_batch_plan_selftest_stall", self._handle, int(cycles))
+
     def execute(self):
         """One launch over all instances; returns (mll, grads, info)."""
         _lib.call("gpk_batch_plan_execute", self._handle, self.workspace.data_ptr(),

@@ -317,6 +317,13 @@ size_t gpk_batch_plan_workspace_bytes(gpk_batch_plan plan);
 int gpk_batch_plan_config(gpk_batch_plan plan, int64_t n);
 int gpk_batch_plan_config_count(void);
 gpk_status gpk_batch_plan_force_config(gpk_batch_plan plan, int cfg);
+/* Self-test of the bounded waits of the tensor-core configuration: with
+ * cycles > 0, the first MMA wait of every CTA in later executions also waits
+ * up to `cycles` SM clocks on a barrier that nothing arrives on, records that
+ * it ran out, and the instances that CTA runs report info = -1 with NaN
+ * outputs (the MMAs themselves are still waited for).  0 turns it off;
+ * GPK_ERR_BAD_ARG for a null plan or cycles outside [0, 4e9]. */
+gpk_status gpk_batch_plan_selftest_stall(gpk_batch_plan plan, long long cycles);
 gpk_status gpk_batch_plan_execute(gpk_batch_plan plan, void* workspace, size_t workspace_bytes,
                                   cudaStream_t stream);
 gpk_status gpk_batch_plan_destroy(gpk_batch_plan plan);

@@ -207,3 +207,28 @@ def test_plan_rational_quadratic_and_value_only(cuda_lib):
                 gk = grads[k].cpu().numpy()[:len(gref)]
                 assert np.linalg.norm(gk - gref) <= GRAD_RTOL * np.linalg.norm(gref)
         plan.close()
+
+
+def test_tensor_core_wait_timeout_is_reported(cuda_lib):
+    """A bounded wait that runs out (the self-test makes each CTA's first MMA
+    wait also wait ~10 ms on a barrier nothing arrives on) is reported as
+    info = -1 with NaN outputs; the context stays usable and the next
+    execution without it is correct."""
+    insts = [_instance(s, 300 + k) for k, s in enumerate(SPECS[:4])]
+    plan = _plan(insts, autotune=False)
+    plan.force_config(2)
+    plan.selftest_stall(20_000_000)
+    mll, grads, info = plan.execute()
+    torch.cuda.synchronize()
+    assert np.all(info.cpu().numpy() == -1), info
+    assert np.all(np.isnan(mll.cpu().numpy()))
+    plan.selftest_stall(0)
+    mll, grads, info = plan.execute()
+    torch.cuda.synchronize()
+    assert np.all(info.cpu().numpy() == 0)
+    for k, inst in enumerate(insts):
+        ref, _ = _oracle(inst)
+        assert abs(float(mll[k]) - ref) <= MLL_RTOL * abs(ref), (k, float(mll[k]), ref)
+    with pytest.raises(_lib.GPKError):
+        plan.selftest_stall(-1)
+    plan.close()

@@ -156,6 +156,7 @@ def test_batch_plan_rejects_bad_arguments(built_lib):
     assert lib.gpk_batch_plan_destroy(None) == 0
     assert lib.gpk_batch_plan_config_count() == 3
     assert lib.gpk_batch_plan_force_config(None, 0) == 1
+    assert lib.gpk_batch_plan_selftest_stall(None, 0) == 1
 
 
 # ---------------------------------------------------------------------------
