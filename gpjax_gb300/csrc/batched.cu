@@ -21,7 +21,8 @@
 //     one product over all earlier panels, its diagonal block factored and
 //     inverted by leaf_chol_inv_body, the panel below solved by substitution;
 //   inverse: M = L^-1 by the recursive merge M21 = -M22 (L21 M11);
-//   alpha = M^T M diff, refined twice against float-float residuals;
+//   alpha = M^T M diff, refined against float-float residuals (twice, or
+//     once when the first correction is below 1e-5 of alpha);
 //   W = M^T M tile by tile, reduced at once against dK/dtheta (adjoint).
 // Every product runs on the CUDA cores as 128 x 128 output tiles, one at a
 // time on the whole CTA (512 threads, 8 x 4 outputs per thread, K slices
@@ -1193,7 +1194,7 @@ __device__ void transpose_m(const Slot& S, int ld, int np, float* smem) {
 }
 
 // Everything of an instance before its adjoint, on the CTA that took it from
-// the queue: Gram, factor and inverse, alpha refined twice.  Returns true if
+// the queue: Gram, factor and inverse, alpha refined.  Returns true if
 // the factorisation failed.
 template <int BK>
 __device__ bool instance_front(const BatchArgs& a, const BatchInst& I, const Slot& S,
@@ -1272,13 +1273,14 @@ __device__ bool instance_front(const BatchArgs& a, const BatchInst& I, const Slo
   if constexpr (BK == TC_BK) {
     if (a.want_grad) transpose_m(S, ld, np, smem);
   }
-  // alpha = Sigma^-1 diff, refined twice
+  // alpha = Sigma^-1 diff, refined (twice, or once: see below)
   float* ah = smem;          // [np] alpha hi
   float* al = smem + np;     // [np] alpha lo
   double* rres = reinterpret_cast<double*>(smem + 2 * np);  // [np]
   float* red = smem + 4 * np;  // [16][128] GEMV partial sums, then the residual's
                                // staged inputs [RCH][BDM + 1]
   solve_apply(S, ld, np, S.diff, false, red);
+  __shared__ double s_cmax[BNT / 32], s_amax[BNT / 32];
   for (int it = 0; it < 2; ++it) {
     for (int i = threadIdx.x; i < np; i += BNT) {
       const double v = S.alpha[i];
@@ -1290,6 +1292,35 @@ __device__ bool instance_front(const BatchArgs& a, const BatchInst& I, const Slo
     residual(I, S, np, s2, ka, noise_diag, ah, al, rres, red + 16 * TT);
     __syncthreads();
     solve_apply(S, ld, np, rres, true, red);
+    if (it == 0) {
+      // Refinement contracts the error by about the size of its first
+      // correction relative to alpha; below 1e-5 the second correction would
+      // be below ~1e-10 of alpha, under the float32 factor's own effect on
+      // the MLL, and is skipped (most instances of a batch).
+      double cm = 0.0, am = 0.0;
+      for (int i = threadIdx.x; i < np; i += BNT) {
+        const double v = S.alpha[i];
+        cm = fmax(cm, fabs(v - ((double)ah[i] + (double)al[i])));
+        am = fmax(am, fabs(v));
+      }
+      for (int off = 16; off > 0; off >>= 1) {
+        cm = fmax(cm, __shfl_xor_sync(0xffffffffu, cm, off));
+        am = fmax(am, __shfl_xor_sync(0xffffffffu, am, off));
+      }
+      if ((threadIdx.x & 31) == 0) {
+        s_cmax[threadIdx.x >> 5] = cm;
+        s_amax[threadIdx.x >> 5] = am;
+      }
+      __syncthreads();
+      cm = 0.0;
+      am = 0.0;
+      for (int w = 0; w < BNT / 32; ++w) {
+        cm = fmax(cm, s_cmax[w]);
+        am = fmax(am, s_amax[w]);
+      }
+      __syncthreads();
+      if (cm <= 1e-5 * am) break;
+    }
   }
   for (int i = threadIdx.x; i < np; i += BNT) S.ahf[i] = (float)S.alpha[i];
   __syncthreads();
