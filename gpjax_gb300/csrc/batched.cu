@@ -3,8 +3,8 @@
 // hyperparameter fits) in ONE launch.  Per instance the quantity is the one of
 // mll.cu -- conjugate_mll (gpjax/objectives.py:36-107) and its gradient
 // 1/2 tr((alpha alpha^T - Sigma^-1) dSigma/dtheta) -- in float32 with float64
-// pivots (a float-float diagonal track), float-float residuals for two rounds
-// of refinement of alpha and float64 sums.
+// pivots (a float-float diagonal track), float-float residuals for the
+// refinement of alpha and float64 sums.
 //
 // Schedule.  A plan (built once, outside any stream capture) holds the
 // instance descriptors on the device, a queue of instance indices sorted by n
@@ -24,10 +24,11 @@
 //   alpha = M^T M diff, refined against float-float residuals (twice, or
 //     once when the first correction is below 1e-5 of alpha);
 //   W = M^T M tile by tile, reduced at once against dK/dtheta (adjoint).
-// Every product runs on the CUDA cores as 128 x 128 output tiles, one at a
-// time on the whole CTA (512 threads, 8 x 4 outputs per thread, K slices
-// double-buffered through shared memory); the autotuner picks the K-slice
-// depth per n range.
+// Every product runs as 128 x 128 output tiles, one at a time on the whole
+// CTA, in the configuration the autotuner picks per n range: on the CUDA
+// cores (512 threads, 8 x 4 outputs per thread, K slices of 16 or 32
+// double-buffered through shared memory) or on the tcgen05 tensor cores
+// (split TF32, TMEM accumulators; tile_mma_tc).
 #include <algorithm>
 #include <climits>
 #include <map>
