@@ -620,7 +620,7 @@ struct LeafOutPlain {
 
 // dtrack[o + r] -= sum_k L[o + r][c0 + k]^2 (k < w) for rows r < rows: one
 // warp per row, float-float squares, float64 total.
-__device__ void track_rows(const float* L, int ld, int o, int rows, int c0, int w,
+__device__ __noinline__ void track_rows(const float* L, int ld, int o, int rows, int c0, int w,
                            double* dtrack) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int r = warp; r < rows; r += BNT / 32) {
@@ -683,7 +683,7 @@ __device__ void node_up(const Slot& S, int ld, int o, int h, int h2, float* smem
 // backward stable; X = A_panel M_kk^T with the leaf's inverse is not, and on
 // a smooth RBF instance (n = 1068, d = 2, condition number 8.8e6) the
 // product form drove a later pivot negative.
-__device__ void panel_solve(const float* __restrict__ Ap, float* __restrict__ Xp, int ld, int R,
+__device__ __noinline__ void panel_solve(const float* __restrict__ Ap, float* __restrict__ Xp, int ld, int R,
                             const float* leaf_smem) {
   constexpr int LDT = LEAF_LDT, PB = 32;
   const float* LT = leaf_smem;
@@ -736,6 +736,15 @@ __device__ void panel_solve(const float* __restrict__ Ap, float* __restrict__ Xp
   }
 }
 
+// The leaf, the substitution, the GEMVs, the residual, the transpose and the
+// finalisation are kept out of line (__noinline__): with everything inlined,
+// one register allocation serves the whole kernel and the tile loops paid for
+// the other phases' live ranges (the tensor-core configuration ran 2.8%
+// faster with them out of line, results unchanged bit for bit).
+__device__ __noinline__ void leaf_call(const Slot& S, int ld, int o, int* info, float* smem) {
+  leaf_chol_inv_body(S.A, ld, o, S.dtrack, S.logdiag, info, LeafOutPlain{S.M, ld, o}, smem);
+}
+
 // Cholesky + inverse of the padded matrix.
 //  * Factor: left-looking over 128-wide block columns.  Block column o is
 //    brought up to date by ONE product, A[o:, o:o+128] -= L[o:, :o]
@@ -784,7 +793,7 @@ __device__ void chol_inv(const Slot& S, int ld, int np, int* info, float* smem) 
           smem);
     }
     __syncthreads();  // the column and track_rows' dtrack writes before the leaf reads them
-    leaf_chol_inv_body(S.A, ld, o, S.dtrack, S.logdiag, info, LeafOutPlain{S.M, ld, o}, smem);
+    leaf_call(S, ld, o, info, smem);
     __syncthreads();
     const int R = np - o - TT;
     if (R <= 0) break;
@@ -828,7 +837,7 @@ __device__ __forceinline__ float dot4(float4 m, float4 v, float s) {
 // solve read M from memory (np^2 / 2 floats each) with one CTA per SM, so
 // they are written for bytes in flight: eight (then four) independent
 // 16-byte loads per lane before the first FMA.
-__device__ void gemv_lower(const float* M, int ld, int np, const float* r, float* z) {
+__device__ __noinline__ void gemv_lower(const float* M, int ld, int np, const float* r, float* z) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int i = warp; i < np; i += BNT / 32) {
     const float* row = M + (int64_t)i * ld;
@@ -870,7 +879,7 @@ __device__ void gemv_lower(const float* M, int ld, int np, const float* r, float
 // 16, ... (a float4 of 4 columns per lane, four rows in flight), the 16
 // warps' partial sums meet in shared memory (red: 16 x 128 floats).  Rows of
 // the diagonal block reach past the diagonal into its zeros.
-__device__ void gemv_upper_t(const float* M, int ld, int np, const float* z, double* alpha,
+__device__ __noinline__ void gemv_upper_t(const float* M, int ld, int np, const float* z, double* alpha,
                              bool accumulate, float* red) {
   constexpr int NW = BNT / 32;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -960,7 +969,7 @@ __device__ __forceinline__ void ff_add_b(float& hi, float& lo, float a) {
 // stride); a warp takes a row, its lanes the chunk's columns, and each
 // row's chunk sums add up in float64 in rres.
 constexpr int RCH = 512;
-__device__ void residual(const BatchInst& I, const Slot& S, int np, float s2, float ka,
+__device__ __noinline__ void residual(const BatchInst& I, const Slot& S, int np, float s2, float ka,
                          double noise_diag, const float* ah, const float* al, double* rres,
                          float* gx) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1138,7 +1147,7 @@ __device__ bool adjoint_tile(const BatchArgs& a, int id, const BatchInst& I, con
 // The outputs of an instance from its slot (any CTA): log-determinant,
 // quadratic form and alpha sum in compensated float64, the gradient slots
 // summed over the tiles' partials in tile order.
-__device__ void finish_instance(const BatchArgs& a, const BatchInst& I, const Slot& S,
+__device__ __noinline__ void finish_instance(const BatchArgs& a, const BatchInst& I, const Slot& S,
                                 bool failed, double* sg) {
   const int n = I.n, d = I.d;
   const bool grad = a.want_grad && !failed;
@@ -1167,7 +1176,7 @@ __device__ void finish_instance(const BatchArgs& a, const BatchInst& I, const Sl
 // transposing each K slice.  One block at a time through shared memory
 // (rows of 129 floats: both the row-wise writes and the column-wise reads
 // are free of bank conflicts).
-__device__ void transpose_m(const Slot& S, int ld, int np, float* smem) {
+__device__ __noinline__ void transpose_m(const Slot& S, int ld, int np, float* smem) {
   constexpr int TLD = TT + 1;
   const int nb = np / TT, nt = nb * (nb + 1) / 2;
   for (int t = 0; t < nt; ++t) {
