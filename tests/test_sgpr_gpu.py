@@ -247,7 +247,7 @@ def test_sharded_elbo_two_ranks_match_single(cuda_lib, precision, vtol, gtol):
                     slots[r] = view.cpu().numpy()          # waits for this rank's stream
                     barrier.wait()
                     tot = slots[0] + slots[1]
-                    barrier.wait()                          # both have read before the next round
+                    barrier.wait()                          # both have read before the next exchange
                     view.copy_(torch.as_tensor(tot, device=dev))
                     return 0
                 cb = _lib.ALLREDUCE_FN(hostsum)
