@@ -242,6 +242,7 @@ constexpr long long kTcWait = 4000000000LL;
 struct TcState {
   uint64_t bar[2];  // MMA completion, one per accumulator
   uint64_t never;   // self-test: a barrier nothing arrives on
+  uint64_t fin;     // kernel end after a timeout: every MMA issued has completed
   long long stall;  // self-test: > 0 makes the CTA's first MMA wait also wait on `never`
   uint32_t n[2];    // completions consumed so far (parity = n & 1)
   uint32_t issued[2];  // commits made
@@ -358,6 +359,7 @@ __device__ void tc_setup(long long stall) {
     tc::mbar_init(&st.bar[0], 1);
     tc::mbar_init(&st.bar[1], 1);
     tc::mbar_init(&st.never, 1);
+    tc::mbar_init(&st.fin, 1);
     st.stall = stall;
     st.n[0] = st.n[1] = 0;
     st.issued[0] = st.issued[1] = 0;
@@ -377,15 +379,17 @@ __device__ void tc_setup(long long stall) {
   tc::tc_fence_after();
 }
 
-// Kernel end (every thread): after a timeout, the commits not yet seen are
-// waited for (bounded) before the TMEM columns are released.
+// Kernel end (every thread): after a timeout (when later waits were skipped
+// and the counters no longer tell which MMAs were seen to complete), thread
+// 0, which issued every MMA, commits once more to `fin` -- it arrives when
+// all of them have completed -- and waits for that (bounded) before the TMEM
+// columns are released.
 __device__ void tc_teardown() {
   TcState& st = tc_state();
   __syncthreads();
-  if (threadIdx.x == 0 && st.err) {
-    for (int b = 0; b < 2; ++b)
-      while (st.n[b] < st.issued[b] && tc::mbar_wait_own(&st.bar[b], st.n[b] & 1u, kTcWait))
-        st.n[b] += 1;
+  if (threadIdx.x == 0 && st.err && (st.issued[0] | st.issued[1])) {
+    tc::mma_commit(&st.fin);
+    tc::mbar_wait_own(&st.fin, 0u, kTcWait);
   }
   tc::tc_fence_before();
   __syncthreads();
