@@ -1552,8 +1552,10 @@ cudaError_t launch_batch(const gpk_batch_plan_s& P, void* ws, int force_cfg, int
 
 // Times every configuration on up to one grid of the plan's instances of
 // each n_pad (their outputs are overwritten by the next execution) and
-// keeps the faster per (device, n_pad).
-gpk_status autotune(gpk_batch_plan_s& P, const std::vector<int>& np_of, const std::vector<int>& order) {
+// keeps, per (device, n_pad), the fastest of those that fail the fewest of
+// the trial's instances.
+gpk_status autotune(gpk_batch_plan_s& P, const std::vector<int>& np_of, const std::vector<int>& order,
+                    const int* d_info) {
   std::map<int, std::vector<int>> by_np;
   for (int i : order) by_np[np_of[i]].push_back(i);
   std::vector<int> todo;
@@ -1563,6 +1565,7 @@ gpk_status autotune(gpk_batch_plan_s& P, const std::vector<int>& np_of, const st
       if (!g_tune.count({P.device, kv.first})) todo.push_back(kv.first);
   }
   if (todo.empty()) return GPK_OK;
+  std::vector<int> hinfo(P.count);
   const size_t ws_bytes = P.ws_bytes;
   void* ws = nullptr;
   int* dq = nullptr;
@@ -1581,7 +1584,7 @@ gpk_status autotune(gpk_batch_plan_s& P, const std::vector<int>& np_of, const st
       break;
     }
     float best = 0.f;
-    int best_cfg = 0;
+    int best_cfg = 0, best_fail = INT_MAX;
     for (int cfg = 0; cfg < NCFG && st == GPK_OK; ++cfg) {
       float ms = 0.f;
       for (int rep = 0; rep < 2; ++rep) {  // the first run warms up
@@ -1592,9 +1595,21 @@ gpk_status autotune(gpk_batch_plan_s& P, const std::vector<int>& np_of, const st
           break;
         }
       }
-      if (st == GPK_OK && (cfg == 0 || ms < best)) {
+      // failed instances of the trial (a configuration must not lose an
+      // instance that another one factors)
+      int fails = 0;
+      if (st == GPK_OK) {
+        if (cudaMemcpy(hinfo.data(), d_info, sizeof(int) * P.count, cudaMemcpyDeviceToHost) !=
+            cudaSuccess) {
+          st = GPK_ERR_CUDA;
+          break;
+        }
+        for (int q = 0; q < m; ++q) fails += hinfo[ids[q]] != 0;
+      }
+      if (st == GPK_OK && (fails < best_fail || (fails == best_fail && ms < best))) {
         best = ms;
         best_cfg = cfg;
+        best_fail = fails;
       }
     }
     if (st == GPK_OK) {
@@ -1697,7 +1712,7 @@ extern "C" gpk_status gpk_batch_plan_create(int count, const int* kind, const in
           cudaSuccess)
     return fail(GPK_ERR_CUDA);
   if (autotune_flag) {
-    const gpk_status st = autotune(*P, np_of, order);
+    const gpk_status st = autotune(*P, np_of, order, info);
     if (st != GPK_OK) return fail(st);
   }
   // configurations per instance from the tuned table (K slices of 32 where untuned)

@@ -292,7 +292,8 @@ gpk_status gpk_conjugate_mll_batched(int count, const int* kind, const int64_t* 
  * execution, so their contents may change between executions), sorts them
  * by n (largest first) into a device queue and, when autotune != 0, times the
  * tile configurations on the plan's own instances for every n_pad not yet
- * tuned on this device (results kept for the process).  It allocates a few
+ * tuned on this device and keeps the fastest of those that fail the fewest
+ * of the trial's instances (results kept for the process).  It allocates a few
  * bytes per instance of device memory and synchronises the device: call it
  * outside stream capture.  gpk_batch_plan_execute zeroes the queue head and
  * launches ONE persistent kernel (one CTA per SM pulls instances from the
