@@ -88,7 +88,8 @@ struct BatchArgs {
   char* ws;          // one slot per instance
   int want_grad;
   double jitter;
-  int force_cfg;     // >= 0: every instance with this configuration (autotuner trials)
+  int force_cfg;     // >= 0: every instance with this configuration (autotuner trials,
+                     // gpk_batch_plan_force_config)
   long long wait_cycles;  // bound on an idle CTA's wait for published tiles
   long long tc_stall;     // self-test (0: off), see tc_wait
 };
