@@ -741,8 +741,8 @@ __device__ __noinline__ void panel_solve(const float* __restrict__ Ap, float* __
   }
 }
 
-// The leaf, the substitution, the GEMVs, the residual, the transpose and the
-// finalisation are kept out of line (__noinline__): with everything inlined,
+// The leaf, the substitution, the GEMVs, the residual and the finalisation
+// are kept out of line (__noinline__): with everything inlined,
 // one register allocation serves the whole kernel and the tile loops paid for
 // the other phases' live ranges (the tensor-core configuration ran 2.8%
 // faster with them out of line, results unchanged bit for bit).
@@ -1099,10 +1099,7 @@ __device__ bool adjoint_tile(const BatchArgs& a, int id, const BatchInst& I, con
   for (int u = 0; u < 8; ++u)
 #pragma unroll
     for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
-  if constexpr (BK == TC_BK)  // MT = M^T in the slot's A: K along rows
-    tile_mma<BK, false, false>(S.A, ld, S.A, ld, i0, j0, i0, np, smem, acc);
-  else
-    tile_mma<BK, true, true>(S.M, ld, S.M, ld, i0, j0, i0, np, smem, acc);
+  tile_mma<BK, true, true>(S.M, ld, S.M, ld, i0, j0, i0, np, smem, acc);
   float* Ws = smem;                          // [TT][WLD]
   float* sxi = smem + stage_floats();        // [TT][XLD]
   float* sxj = sxi + TT * XLD;
@@ -1172,40 +1169,6 @@ __device__ __noinline__ void finish_instance(const BatchArgs& a, const BatchInst
     finalize_outputs(n, d, I.theta, I.n_ls, a.jitter, logdet, quad, asum, sg, a.want_grad,
                      I.info, I.out_mll, a.want_grad ? I.out_grad : nullptr);
   __syncthreads();
-}
-
-// MT = M^T into the slot's A (dead after the factorisation): the lower
-// 128-blocks of M become the upper blocks of MT, diagonal blocks with their
-// zeros.  The tensor-core adjoint then reads both operands of W = M^T M
-// along rows (K-major in memory, 16-byte stores while staging) instead of
-// transposing each K slice.  One block at a time through shared memory
-// (rows of 129 floats: both the row-wise writes and the column-wise reads
-// are free of bank conflicts).
-__device__ __noinline__ void transpose_m(const Slot& S, int ld, int np, float* smem) {
-  constexpr int TLD = TT + 1;
-  const int nb = np / TT, nt = nb * (nb + 1) / 2;
-  for (int t = 0; t < nt; ++t) {
-    int bi, bj;
-    tri_index(t, bi, bj);
-    const float* src = S.M + (int64_t)bi * TT * ld + bj * TT;
-    for (int e = threadIdx.x; e < TT * TT / 4; e += BNT) {
-      const int r = e / (TT / 4), c = 4 * (e % (TT / 4));
-      const float4 v = *reinterpret_cast<const float4*>(src + (int64_t)r * ld + c);
-      smem[r * TLD + c] = v.x;
-      smem[r * TLD + c + 1] = v.y;
-      smem[r * TLD + c + 2] = v.z;
-      smem[r * TLD + c + 3] = v.w;
-    }
-    __syncthreads();
-    float* dst = S.A + (int64_t)bj * TT * ld + bi * TT;
-    for (int e = threadIdx.x; e < TT * TT / 4; e += BNT) {
-      const int c = e / (TT / 4), r = 4 * (e % (TT / 4));
-      *reinterpret_cast<float4*>(dst + (int64_t)c * ld + r) =
-          make_float4(smem[r * TLD + c], smem[(r + 1) * TLD + c], smem[(r + 2) * TLD + c],
-                      smem[(r + 3) * TLD + c]);
-    }
-    __syncthreads();
-  }
 }
 
 // Everything of an instance before its adjoint, on the CTA that took it from
@@ -1285,9 +1248,6 @@ __device__ bool instance_front(const BatchArgs& a, const BatchInst& I, const Slo
   const bool failed = *(volatile int*)I.info != INT_MAX;
   __syncthreads();
   if (failed) return true;
-  if constexpr (BK == TC_BK) {
-    if (a.want_grad) transpose_m(S, ld, np, smem);
-  }
   // alpha = Sigma^-1 diff, refined (twice, or once: see below)
   float* ah = smem;          // [np] alpha hi
   float* al = smem + np;     // [np] alpha lo
