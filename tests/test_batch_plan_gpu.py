@@ -7,7 +7,8 @@ Tolerances of the float32 form (float64 pivots, float-float refinement of
 alpha): 1e-4 relative on the MLL, 2e-3 relative on the gradient norm.  The
 float32 rounding of Sigma's entries alone moves the log-determinant of the
 Matern-5/2 n = 2048, d = 4 case (condition number 1.6e5) by 4.8e-5 of the MLL
-(LAPACK's float32 Cholesky of the same matrix); this path measures 7.3e-5."""
+(LAPACK's float32 Cholesky of the same matrix).  The same bounds hold for every
+tile configuration (CUDA-core and tcgen05 split-TF32) forced in turn."""
 import numpy as np
 import pytest
 import torch
